@@ -1,0 +1,186 @@
+"""ctypes binding of ``libmtgb.so`` (the C ABI in ``include/meshtryoshka_gb300.h``).
+
+This module is the only place Python touches the native library. It
+
+* loads the library (building it first with nvcc if it is missing or stale),
+* declares every entry point's argument types,
+* turns a non-zero ``mt_status`` into ``RuntimeError`` (the library's
+  equivalent of the reference's ``TORCH_CHECK`` failures), and
+* owns the per-device scratch workspaces the library asks callers to supply.
+
+There is no fallback: if the CUDA library cannot be loaded, importing the
+render path fails.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from ctypes import c_float, c_int32, c_int64, c_size_t, c_uint64, c_void_p
+
+import torch
+
+from . import build as _build
+
+P = c_void_p
+I32 = c_int32
+I64 = c_int64
+
+# name -> (restype, argtypes)
+_SIGNATURES: dict[str, tuple[object, list[object]]] = {
+    "mt_status_string": (ctypes.c_char_p, [I32]),
+    "mt_version": (I32, []),
+    "mt_scan_workspace_bytes": (c_size_t, [I64]),
+    "mt_exclusive_scan_i32": (I32, [P, I64, P, c_size_t, P]),
+    "mt_exclusive_scan_i64": (I32, [P, I64, P, c_size_t, P]),
+    "mt_inclusive_scan_i32_to_i64": (I32, [P, P, I64, P, c_size_t, P]),
+    "mt_compute_vertex_occupancy": (I32, [P, I32, I32, I32, P, P, P]),
+    "mt_count_occupancy": (I32, [P, I32, I32, I32, P, P]),
+    "mt_create_voxels": (I32, [P, P, P, P, I32, I32, I32, I64, I64, P, P, P, P, P, P]),
+    "mt_dilate_occupancy": (I32, [P, I32, I32, I32, I32, P, P]),
+    "mt_count_triangle_vertices": (I32, [P, P, I64, P, I32, P, P]),
+    "mt_create_triangle_vertices": (
+        I32,
+        [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P],
+    ),
+    "mt_create_triangle_vertices_backward": (
+        I32,
+        [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P],
+    ),
+    "mt_count_triangle_faces": (I32, [P, P, I64, P, I64, P, I32, P, P, P]),
+    "mt_create_triangle_faces": (
+        I32,
+        [P, P, I64, I64, P, P, P, I32, P, I64, P, P, P],
+    ),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIBRARY
+        if not path.exists() or _build._stale(path, _build.sources() + _build.headers()):
+            _build.build()
+        lib = ctypes.CDLL(str(path))
+        for name, (restype, argtypes) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        _lib = lib
+        return lib
+
+
+def library():
+    """The loaded ctypes library (loads / builds on first use)."""
+    return _load()
+
+
+def library_path() -> str:
+    return str(_build.LIBRARY)
+
+
+def call(name: str, *args) -> None:
+    """Call an entry point and raise RuntimeError on a non-zero status."""
+    lib = _load()
+    status = getattr(lib, name)(*args)
+    if status != 0:
+        msg = lib.mt_status_string(status).decode()
+        raise RuntimeError(f"{name} failed: {msg} (status {status})")
+
+
+def ptr(t: torch.Tensor | None) -> int | None:
+    """Device pointer of a contiguous tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_contiguous():
+        raise ValueError("meshtryoshka_gb300 kernels require contiguous tensors")
+    return t.data_ptr() if t.numel() > 0 else None
+
+
+def stream(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def require_cuda(*tensors: torch.Tensor) -> torch.device:
+    device = None
+    for t in tensors:
+        if t is None:
+            continue
+        if t.device.type != "cuda":
+            raise ValueError(
+                "meshtryoshka_gb300 runs on CUDA tensors only (got a tensor on "
+                f"{t.device}); there is no CPU path"
+            )
+        if device is None:
+            device = t.device
+        elif t.device != device:
+            raise ValueError("all tensors must be on the same CUDA device")
+    if device is None:
+        raise ValueError("no CUDA tensor given")
+    return device
+
+
+class Workspace:
+    """Growable per-device scratch buffer handed to the library.
+
+    Byte 0 holds the library's device status word, zeroed on allocation.
+    Calls that use a workspace are stream-ordered, so one workspace per device
+    is shared by all calls on that device's current stream.
+    """
+
+    def __init__(self, device: torch.device):
+        self.device = device
+        self.buffer = torch.zeros(0, dtype=torch.uint8, device=device)
+
+    def get(self, nbytes: int) -> tuple[int, int]:
+        nbytes = max(int(nbytes), 256)
+        if self.buffer.numel() < nbytes:
+            grow = max(nbytes, int(self.buffer.numel() * 1.5))
+            grow = (grow + 4095) // 4096 * 4096
+            self.buffer = torch.zeros(grow, dtype=torch.uint8, device=self.device)
+        return self.buffer.data_ptr(), self.buffer.numel()
+
+    def status(self) -> int:
+        """Device status word (synchronizes the current stream)."""
+        if self.buffer.numel() < 4:
+            return 0
+        return int(self.buffer[:4].view(torch.int32).item())
+
+    def check(self) -> None:
+        code = self.status()
+        if code != 0:
+            self.buffer[:4].zero_()
+            msg = _load().mt_status_string(code).decode()
+            raise RuntimeError(f"device-side failure: {msg} (status {code})")
+
+
+_workspaces: dict[tuple[int, int], Workspace] = {}
+
+
+def workspace(device: torch.device) -> Workspace:
+    index = device.index if device.index is not None else torch.cuda.current_device()
+    key = (index, torch.cuda.current_stream(device).cuda_stream)
+    ws = _workspaces.get(key)
+    if ws is None:
+        ws = Workspace(device)
+        _workspaces[key] = ws
+    return ws
+
+
+__all__ = [
+    "library",
+    "library_path",
+    "call",
+    "ptr",
+    "stream",
+    "require_cuda",
+    "workspace",
+    "Workspace",
+    "c_float",
+    "c_uint64",
+]

@@ -1,0 +1,684 @@
+// Sparse-voxel extraction and per-step marching cubes for sm_103a.
+//
+// Voxel topology (extract_voxels) follows triangle_extraction/
+// compute_vertex_occupancy.slang, count_occupancy.slang, create_voxels.slang
+// and dilate_occupancy.slang; per-step tessellation follows
+// count_triangle_vertices.slang, create_triangle_vertices.slang,
+// count_triangle_faces.slang and create_triangle_faces.slang.
+//
+// Layout choices: every per-word kernel indexes the packed k axis fastest so
+// a warp reads consecutive words; create_voxels runs one warp per packed word
+// with lane = bit, turning the reference's serial 32-bit walk into warp-ballot
+// stream compaction (popcount of the lanes below); all [*, G] / [*, Nv] tables
+// are read one row at a time so every row read is coalesced.
+
+#include "mc_tables.h"
+#include "mt_common.cuh"
+
+namespace mt {
+namespace {
+
+__constant__ uint8_t c_mc_count[256] = {MT_MC_CASE_COUNT_VALUES};
+__constant__ uint64_t c_mc_edges[256] = {MT_MC_CASE_EDGES_VALUES};
+__constant__ int8_t c_mc_owner[12] = {MT_MC_EDGE_OWNER_VALUES};
+__constant__ uint8_t c_mc_axis[12] = {MT_MC_EDGE_AXIS_VALUES};
+
+// ---------------------------------------------------------------------------
+// compute_vertex_occupancy.slang:9-68
+// ---------------------------------------------------------------------------
+__global__ void vertex_occupancy_kernel(const int32_t* __restrict__ occ, int I, int J, int KP,
+                                        int32_t* __restrict__ vocc, int32_t* __restrict__ vcounts) {
+  const int64_t total = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    const int kp = (int)(w % (KP + 1));
+    const int64_t ij = w / (KP + 1);
+    const int j = (int)(ij % (J + 1));
+    const int i = (int)(ij / (J + 1));
+    uint32_t result = 0;
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+#pragma unroll
+      for (int dj = 0; dj < 2; ++dj) {
+        if ((i == 0 && di == 1) || (j == 0 && dj == 1)) continue;
+        if ((i == I && di == 0) || (j == J && dj == 0)) continue;
+        const int64_t row = ((int64_t)(i - di) * J + (j - dj)) * KP;
+        const uint32_t cur = (kp == KP) ? 0u : (uint32_t)occ[row + kp];
+        const uint32_t prev_packed = (kp == 0) ? 0u : (uint32_t)occ[row + kp - 1];
+        result |= cur | ((prev_packed >> 31) | (cur << 1));
+      }
+    }
+    vocc[w] = (int32_t)result;
+    vcounts[w] = __popc(result);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) vcounts[total] = 0;
+}
+
+// count_occupancy.slang:3-20 plus the zero fill of count_occupancy.py:30.
+__global__ void count_occupancy_kernel(const int32_t* __restrict__ occ, int I, int J, int KP,
+                                       int32_t* __restrict__ counts) {
+  const int64_t total = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    const int kp = (int)(w % (KP + 1));
+    const int64_t ij = w / (KP + 1);
+    const int j = (int)(ij % (J + 1));
+    const int i = (int)(ij / (J + 1));
+    int c = 0;
+    if (i < I && j < J && kp < KP) c = __popc((uint32_t)occ[((int64_t)i * J + j) * KP + kp]);
+    counts[w] = c;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) counts[total] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// create_voxels.slang:3-276, one warp per vertex-grid word, lane = bit.
+// ---------------------------------------------------------------------------
+struct VoxelGrid {
+  const int32_t* occ;   // [I, J, KP]
+  const int32_t* xoff;  // [I+1, J+1, KP+1] voxel offsets
+  const int32_t* vocc;  // [I+1, J+1, KP+1]
+  const int32_t* voff;  // [I+1, J+1, KP+1] vertex offsets
+  int I, J, KP;
+  int64_t Nv;
+
+  __device__ __forceinline__ int64_t vw(int i, int j, int kp) const {
+    return ((int64_t)i * (J + 1) + j) * (KP + 1) + kp;
+  }
+  // Voxel occupancy word; 0 outside the voxel grid.
+  __device__ __forceinline__ uint32_t vx(int i, int j, int kp) const {
+    if (i >= I || j >= J || kp >= KP) return 0u;
+    return (uint32_t)occ[((int64_t)i * J + j) * KP + kp];
+  }
+};
+
+// Per-neighbour-word state at a given bit: the reference's local_* arrays.
+struct WordState {
+  int32_t vidx, xidx, sidx;  // indices of the entry at this bit (-64 when out of range)
+  uint32_t vo, vx, so;       // vertex / voxel / subvoxel occupancy words
+};
+
+__device__ __forceinline__ WordState word_state(const VoxelGrid& g, int i, int j, int kp, uint32_t below) {
+  WordState s;
+  if (i > g.I || j > g.J) {
+    s.vidx = s.xidx = s.sidx = -64;
+    s.vo = s.vx = s.so = 0u;
+    return s;
+  }
+  const int64_t w = g.vw(i, j, kp);
+  s.vo = (uint32_t)g.vocc[w];
+  s.vx = g.vx(i, j, kp);
+  s.so = s.vo & ~s.vx;
+  const int32_t xo = g.xoff[w], vo = g.voff[w];
+  s.vidx = vo + __popc(s.vo & below);
+  s.xidx = xo + __popc(s.vx & below);
+  s.sidx = (int32_t)g.Nv + (vo - xo) + __popc(s.so & below);
+  return s;
+}
+
+__device__ __forceinline__ int32_t pick_diag(bool diag_sub, bool side_sub, const WordState& s) {
+  // Neighbour one step along +x from a side neighbour (see create_voxels.slang:164-172).
+  return diag_sub ? (side_sub ? s.sidx + 1 : s.sidx) : (side_sub ? s.xidx : s.xidx + 1);
+}
+
+__global__ void create_voxels_kernel(VoxelGrid g, float* __restrict__ vertices, int32_t* __restrict__ neighbors,
+                                     int32_t* __restrict__ lower, int32_t* __restrict__ upper,
+                                     int32_t* __restrict__ indices, int64_t G) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps_total = (int64_t)(g.I + 1) * (g.J + 1) * (g.KP + 1);
+  const int64_t warp_global = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t warp_stride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t below = (1u << lane) - 1u;
+  const uint32_t bit = 1u << lane;
+  const int64_t Nv = g.Nv;
+  const float inv_i = 1.0f / (float)g.I;
+  const float inv_j = 1.0f / (float)g.J;
+  const float inv_k = 1.0f / (float)(32 * g.KP);
+  const int32_t k_max = 32 * g.KP;
+
+  for (int64_t w = warp_global; w < warps_total; w += warp_stride) {
+    const int kp = (int)(w % (g.KP + 1));
+    const int64_t ij = w / (g.KP + 1);
+    const int j = (int)(ij % (g.J + 1));
+    const int i = (int)(ij / (g.J + 1));
+    const uint32_t vo00 = (uint32_t)g.vocc[w];
+    if (vo00 == 0u) continue;  // warp-uniform
+    const int k = 32 * kp + lane;
+
+    const WordState s00 = word_state(g, i, j, kp, below);
+    const WordState s01 = word_state(g, i, j + 1, kp, below);
+    const WordState s10 = word_state(g, i + 1, j, kp, below);
+    const WordState s11 = word_state(g, i + 1, j + 1, kp, below);
+
+    // Vertices (create_voxels.slang:37-53).
+    if (vo00 & bit) {
+      float* v = vertices + (int64_t)s00.vidx * 3;
+      v[0] = (float)k * inv_k;
+      v[1] = (float)j * inv_j;
+      v[2] = (float)i * inv_i;
+    }
+
+    const bool is_voxel = (s00.vx & bit) != 0u;
+    const bool is_sub = (s00.so & bit) != 0u;
+    if (!is_voxel && !is_sub) continue;
+
+    // Lower corners (create_voxels.slang:108-127, last bit fixed up at :201-206).
+    const int32_t chosen = is_voxel ? s00.xidx : s00.sidx;
+    bool x_valid;
+    if (lane < 31) {
+      x_valid = is_voxel || ((s00.vo >> (lane + 1)) & 1u);
+    } else {
+      x_valid = is_voxel || (kp < g.KP && (g.vocc[g.vw(i, j, kp + 1)] & 1));
+    }
+    const bool y_valid = is_voxel || (s01.vo & bit);
+    const bool z_valid = is_voxel || (s10.vo & bit);
+    lower[chosen] = s00.vidx;
+    lower[G + chosen] = x_valid ? s00.vidx + 1 : -64;
+    lower[2 * G + chosen] = y_valid ? s01.vidx : -64;
+    lower[3 * G + chosen] = z_valid ? s10.vidx : -64;
+
+    if (!is_voxel) continue;
+    const int32_t vi = s00.xidx;
+
+    // Upper corners and linear index (create_voxels.slang:129-136).
+    upper[vi] = s11.vidx + 1;
+    upper[Nv + vi] = s11.vidx;
+    upper[2 * Nv + vi] = s10.vidx + 1;
+    upper[3 * Nv + vi] = s01.vidx + 1;
+    indices[vi] = k_max * (g.J * i + j) + k;
+
+    // Neighbours (create_voxels.slang:138-193 for bits 0..30, :211-275 for bit 31).
+    bool x_sub, y_sub, z_sub, xy_sub, yz_sub, xz_sub, xyz_sub;
+    if (lane < 31) {
+      const uint32_t nb = bit << 1;
+      x_sub = (s00.so & nb) != 0u;
+      y_sub = (s01.so & bit) != 0u;
+      z_sub = (s10.so & bit) != 0u;
+      xy_sub = (s01.so & nb) != 0u;
+      yz_sub = (s11.so & bit) != 0u;
+      xz_sub = (s10.so & nb) != 0u;
+      xyz_sub = (s11.so & nb) != 0u;
+    } else {
+      const bool cx = kp < g.KP - 1, cy = j < g.J - 1, cz = i < g.I - 1;
+      const uint32_t top = 1u << 31;
+      x_sub = cx ? ((g.vx(i, j, kp + 1) & 1u) == 0u) : true;
+      y_sub = cy ? ((g.vx(i, j + 1, kp) & top) == 0u) : true;
+      z_sub = cz ? ((g.vx(i + 1, j, kp) & top) == 0u) : true;
+      xy_sub = (cx && cy) ? ((g.vx(i, j + 1, kp + 1) & 1u) == 0u) : true;
+      yz_sub = (cy && cz) ? ((g.vx(i + 1, j + 1, kp) & top) == 0u) : true;
+      xz_sub = (cx && cz) ? ((g.vx(i + 1, j, kp + 1) & 1u) == 0u) : true;
+      xyz_sub = (cx && cy && cz) ? ((g.vx(i + 1, j + 1, kp + 1) & 1u) == 0u) : true;
+    }
+    neighbors[vi] = x_sub ? s00.sidx : s00.xidx + 1;
+    neighbors[Nv + vi] = y_sub ? s01.sidx : s01.xidx;
+    neighbors[2 * Nv + vi] = z_sub ? s10.sidx : s10.xidx;
+    neighbors[3 * Nv + vi] = pick_diag(xy_sub, y_sub, s01);
+    neighbors[4 * Nv + vi] = yz_sub ? s11.sidx : s11.xidx;
+    neighbors[5 * Nv + vi] = pick_diag(xz_sub, z_sub, s10);
+    neighbors[6 * Nv + vi] = pick_diag(xyz_sub, yz_sub, s11);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dilate_occupancy.slang:9-94 (box dilation, 0 < d < 32).
+// ---------------------------------------------------------------------------
+__global__ void dilate_kernel(const int32_t* __restrict__ occ, int I, int J, int KP, int d,
+                              int32_t* __restrict__ out) {
+  const int64_t total = (int64_t)I * J * KP;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    const int kp = (int)(w % KP);
+    const int64_t ij = w / KP;
+    const int j = (int)(ij % J);
+    const int i = (int)(ij / J);
+    uint32_t prev = 0, cur = 0, next = 0;
+    const int i0 = max(i - d, 0), i1 = min(i + d, I - 1);
+    const int j0 = max(j - d, 0), j1 = min(j + d, J - 1);
+    for (int ii = i0; ii <= i1; ++ii) {
+      for (int jj = j0; jj <= j1; ++jj) {
+        const int32_t* row = occ + ((int64_t)ii * J + jj) * KP;
+        cur |= (uint32_t)row[kp];
+        if (kp > 0) prev |= (uint32_t)row[kp - 1];
+        if (kp < KP - 1) next |= (uint32_t)row[kp + 1];
+      }
+    }
+    uint32_t result = cur;
+    // Bits that spill in from the previous word (dilate_occupancy.slang:41-44).
+    if (kp > 0) {
+      uint32_t p = prev >> (32 - d);
+      for (int b = 0; b < d; ++b) {
+        result |= p;
+        p >>= 1;
+      }
+    }
+    uint32_t l = cur, r = cur;
+    for (int b = 0; b < d; ++b) {
+      r >>= 1;
+      l <<= 1;
+      result |= l | r;
+    }
+    if (kp < KP - 1) {
+      uint32_t n = next << (32 - d);
+      for (int b = 0; b < d; ++b) {
+        result |= n;
+        n <<= 1;
+      }
+    }
+    out[w] = (int32_t)result;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// count_triangle_vertices.slang:3-37
+// ---------------------------------------------------------------------------
+struct Corners4 {
+  float d0, d[3];
+  int32_t idx[3];  // lower_corners[1..3], may be negative
+};
+
+__device__ __forceinline__ Corners4 load_corners(const float* __restrict__ sdf, const int32_t* __restrict__ lower,
+                                                 int64_t G, int64_t g) {
+  Corners4 c;
+  const int32_t i0 = __ldg(lower + g);
+  c.d0 = __ldg(sdf + i0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int32_t ia = __ldg(lower + (a + 1) * G + g);
+    c.idx[a] = ia;
+    c.d[a] = (ia >= 0) ? __ldg(sdf + ia) : c.d0;
+  }
+  return c;
+}
+
+__global__ void count_vertices_kernel(const float* __restrict__ sdf, const int32_t* __restrict__ lower, int64_t G,
+                                      const float* __restrict__ level_sets, int S, int32_t* __restrict__ counts) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+    const Corners4 c = load_corners(sdf, lower, G, g);
+    for (int s = 0; s < S; ++s) {
+      const float iso = __ldg(level_sets + s);
+      const bool b0 = c.d0 < iso;
+      counts[(int64_t)s * G + g] = (b0 != (c.d[0] < iso)) + (b0 != (c.d[1] < iso)) + (b0 != (c.d[2] < iso));
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) counts[(int64_t)S * G] = 0;
+}
+
+// Bit a of the result: edge `a` of entry g crosses level set `iso`. The same
+// predicate sizes the outputs (count) and places vertices (create), so the
+// writes always stay inside the counted range.
+__device__ __forceinline__ uint32_t crossing_mask(const Corners4& c, float iso) {
+  const bool b0 = c.d0 < iso;
+  return (uint32_t)(b0 != (c.d[0] < iso)) | ((uint32_t)(b0 != (c.d[1] < iso)) << 1) |
+         ((uint32_t)(b0 != (c.d[2] < iso)) << 2);
+}
+
+// create_triangle_vertices.slang:87-133: t is detached, positions / SH / sdf
+// are linear in the corner values with weights (1 - t, t).
+__device__ __forceinline__ float mc_weight(float d0, float d1, float iso) {
+  if (d0 == d1) return 0.5f;
+  const float t = (iso - d0) / (d1 - d0);
+  return fminf(fmaxf(t, 0.0f), 1.0f);
+}
+
+// ---------------------------------------------------------------------------
+// create_triangle_vertices.slang:145-199 (forward)
+// ---------------------------------------------------------------------------
+__global__ void create_vertices_kernel(const float* __restrict__ gv, const float* __restrict__ gsdf,
+                                       const float* __restrict__ gsh, int C, const int32_t* __restrict__ lower,
+                                       int64_t G, const float* __restrict__ level_sets, int S,
+                                       const int32_t* __restrict__ voff, int64_t V, float* __restrict__ out_v,
+                                       float* __restrict__ out_sdf, float* __restrict__ out_sh,
+                                       uint8_t* __restrict__ out_type) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+    const Corners4 c = load_corners(gsdf, lower, G, g);
+    const int32_t i0 = __ldg(lower + g);
+    // Which axes cross at least one level set: only those corners' data is read.
+    uint32_t any = 0;
+    for (int s = 0; s < S; ++s) any |= crossing_mask(c, __ldg(level_sets + s));
+    if (any == 0) continue;
+    const float v0x = __ldg(gv + 3 * (int64_t)i0), v0y = __ldg(gv + 3 * (int64_t)i0 + 1),
+                v0z = __ldg(gv + 3 * (int64_t)i0 + 2);
+    for (int a = 0; a < 3; ++a) {
+      if (!((any >> a) & 1u)) continue;
+      const int32_t i1 = c.idx[a];
+      const float d1 = c.d[a];
+      const float v1x = __ldg(gv + 3 * (int64_t)i1), v1y = __ldg(gv + 3 * (int64_t)i1 + 1),
+                  v1z = __ldg(gv + 3 * (int64_t)i1 + 2);
+      const uint32_t below_a = (1u << a) - 1u;
+      for (int s = 0; s < S; ++s) {
+        const float iso = __ldg(level_sets + s);
+        const uint32_t m = crossing_mask(c, iso);
+        if (!((m >> a) & 1u)) continue;
+        const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
+        const float t = mc_weight(c.d0, d1, iso);
+        out_v[3 * vi + 0] = __fmaf_rn(t, v1x - v0x, v0x);
+        out_v[3 * vi + 1] = __fmaf_rn(t, v1y - v0y, v0y);
+        out_v[3 * vi + 2] = __fmaf_rn(t, v1z - v0z, v0z);
+        out_sdf[vi] = __fmaf_rn(t, d1 - c.d0, c.d0);
+        out_type[vi] = (uint8_t)a;
+        for (int k = 0; k < C; ++k) {
+          const float* p0 = gsh + ((int64_t)k * G + i0) * 3;
+          const float* p1 = gsh + ((int64_t)k * G + i1) * 3;
+          float* q = out_sh + ((int64_t)k * V + vi) * 3;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            const float s0 = __ldg(p0 + ch), s1 = __ldg(p1 + ch);
+            q[ch] = __fmaf_rn(t, s1 - s0, s0);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// create_triangle_vertices.slang:201-291 (backward). The detached weight t
+// routes d(vertex) to the origin with (1 - t) and to the axis corner with t.
+// Per entry, the origin's gradient is summed over shells/axes in registers
+// and written with one atomic per scalar; axis corners get one atomic per
+// scalar per crossing axis. Entries and axes without any crossing contribute
+// exact zeros and are skipped.
+// ---------------------------------------------------------------------------
+__global__ void create_vertices_backward_kernel(const float* __restrict__ gsdf, int C,
+                                                const int32_t* __restrict__ lower, int64_t G,
+                                                const float* __restrict__ level_sets, int S,
+                                                const int32_t* __restrict__ voff,
+                                                const float* __restrict__ dv, const float* __restrict__ dsdf,
+                                                const float* __restrict__ dsh, int64_t V, float* __restrict__ gdv,
+                                                float* __restrict__ gdsdf, float* __restrict__ gdsh) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
+    const Corners4 c = load_corners(gsdf, lower, G, g);
+    const int32_t i0 = __ldg(lower + g);
+    uint32_t any = 0;
+    for (int s = 0; s < S; ++s) any |= crossing_mask(c, __ldg(level_sets + s));
+    if (any == 0) continue;
+
+    // Scalar (sdf) and position gradients first.
+    float o_d = 0.f, o_vx = 0.f, o_vy = 0.f, o_vz = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      if (!((any >> a) & 1u)) continue;
+      const int32_t i1 = c.idx[a];
+      float a_d = 0.f, a_vx = 0.f, a_vy = 0.f, a_vz = 0.f;
+      const uint32_t below_a = (1u << a) - 1u;
+      for (int s = 0; s < S; ++s) {
+        const float iso = __ldg(level_sets + s);
+        const uint32_t m = crossing_mask(c, iso);
+        if (!((m >> a) & 1u)) continue;
+        const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
+        const float t = mc_weight(c.d0, c.d[a], iso);
+        const float gd = dsdf ? __ldg(dsdf + vi) : 0.f;
+        o_d += gd - t * gd;
+        a_d += t * gd;
+        if (dv) {
+          const float gx = __ldg(dv + 3 * vi), gy = __ldg(dv + 3 * vi + 1), gz = __ldg(dv + 3 * vi + 2);
+          o_vx += gx - t * gx;
+          o_vy += gy - t * gy;
+          o_vz += gz - t * gz;
+          a_vx += t * gx;
+          a_vy += t * gy;
+          a_vz += t * gz;
+        }
+      }
+      atomicAdd(gdsdf + i1, a_d);
+      if (dv) {
+        atomicAdd(gdv + 3 * (int64_t)i1, a_vx);
+        atomicAdd(gdv + 3 * (int64_t)i1 + 1, a_vy);
+        atomicAdd(gdv + 3 * (int64_t)i1 + 2, a_vz);
+      }
+    }
+    atomicAdd(gdsdf + i0, o_d);
+    if (dv) {
+      atomicAdd(gdv + 3 * (int64_t)i0, o_vx);
+      atomicAdd(gdv + 3 * (int64_t)i0 + 1, o_vy);
+      atomicAdd(gdv + 3 * (int64_t)i0 + 2, o_vz);
+    }
+
+    // Spherical harmonics, one coefficient row at a time.
+    if (dsh == nullptr) continue;
+    for (int k = 0; k < C; ++k) {
+      float o[3] = {0.f, 0.f, 0.f};
+      for (int a = 0; a < 3; ++a) {
+        if (!((any >> a) & 1u)) continue;
+        const int32_t i1 = c.idx[a];
+        float acc[3] = {0.f, 0.f, 0.f};
+        const uint32_t below_a = (1u << a) - 1u;
+        for (int s = 0; s < S; ++s) {
+          const float iso = __ldg(level_sets + s);
+          const uint32_t m = crossing_mask(c, iso);
+          if (!((m >> a) & 1u)) continue;
+          const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
+          const float t = mc_weight(c.d0, c.d[a], iso);
+          const float* q = dsh + ((int64_t)k * V + vi) * 3;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            const float gq = __ldg(q + ch);
+            o[ch] += gq - t * gq;
+            acc[ch] += t * gq;
+          }
+        }
+        float* dst = gdsh + ((int64_t)k * G + i1) * 3;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) atomicAdd(dst + ch, acc[ch]);
+      }
+      float* dst = gdsh + ((int64_t)k * G + i0) * 3;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) atomicAdd(dst + ch, o[ch]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// count_triangle_faces.slang:15-50: cube code bit i <=> corner i >= iso with
+// corner order (origin, +x, +xy, +y, +z, +xz, +xyz, +yz).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load_cube(const float* __restrict__ sdf, const int32_t* __restrict__ lower, int64_t G,
+                                          const int32_t* __restrict__ upper, int64_t Nv, int64_t v, float (&cube)[8]) {
+  cube[0] = __ldg(sdf + __ldg(lower + v));
+  cube[1] = __ldg(sdf + __ldg(lower + G + v));
+  cube[2] = __ldg(sdf + __ldg(upper + 3 * Nv + v));
+  cube[3] = __ldg(sdf + __ldg(lower + 2 * G + v));
+  cube[4] = __ldg(sdf + __ldg(lower + 3 * G + v));
+  cube[5] = __ldg(sdf + __ldg(upper + 2 * Nv + v));
+  cube[6] = __ldg(sdf + __ldg(upper + v));
+  cube[7] = __ldg(sdf + __ldg(upper + Nv + v));
+}
+
+__global__ void count_faces_kernel(const float* __restrict__ sdf, const int32_t* __restrict__ lower, int64_t G,
+                                   const int32_t* __restrict__ upper, int64_t Nv,
+                                   const float* __restrict__ level_sets, int S, int32_t* __restrict__ counts,
+                                   uint8_t* __restrict__ codes) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
+    float cube[8];
+    load_cube(sdf, lower, G, upper, Nv, v, cube);
+    for (int s = 0; s < S; ++s) {
+      const float iso = __ldg(level_sets + s);
+      uint32_t code = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) code |= (uint32_t)(cube[q] >= iso) << q;
+      codes[(int64_t)s * Nv + v] = (uint8_t)code;
+      counts[(int64_t)s * Nv + v] = c_mc_count[code];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) counts[(int64_t)S * Nv] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// create_triangle_faces.slang:5-78. Edge id -> owning entry (self or upper
+// neighbour) -> that entry's vertices at this level set -> the one whose
+// type is the edge's axis. Triangles are written in reversed slot order.
+// ---------------------------------------------------------------------------
+__global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const int32_t* __restrict__ indices,
+                                    int64_t Nv, int64_t G, const int32_t* __restrict__ voff,
+                                    const uint8_t* __restrict__ types, const uint8_t* __restrict__ codes, int S,
+                                    const int32_t* __restrict__ foff, int32_t* __restrict__ faces,
+                                    int32_t* __restrict__ voxel_indices) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t linear = __ldg(indices + v);
+    for (int s = 0; s < S; ++s) {
+      const uint32_t code = codes[(int64_t)s * Nv + v];
+      const int n = c_mc_count[code];
+      if (n == 0) continue;
+      const uint64_t edges = c_mc_edges[code];
+      const int64_t ctr = __ldg(foff + (int64_t)s * Nv + v);
+      for (int e = 0; e < n; ++e) {
+        const int eid = (int)((edges >> (4 * e)) & 15u);
+        const int owner = c_mc_owner[eid];
+        const uint8_t axis = c_mc_axis[eid];
+        const int64_t nb = (owner < 0) ? v : (int64_t)__ldg(neighbors + (int64_t)owner * Nv + v);
+        const int64_t vo = (int64_t)s * G + nb;
+        const int32_t start = __ldg(voff + vo);
+        const int32_t count = __ldg(voff + vo + 1) - start;
+        int32_t target = -1;
+        for (int q = 0; q < count; ++q) {
+          if (types[start + q] == axis) {
+            target = start + q;
+            break;
+          }
+        }
+        const int64_t slot = ctr + e;
+        const int64_t tri = slot / 3;
+        const int corner = 2 - (int)(slot % 3);
+        faces[tri * 3 + corner] = target;
+        if (corner == 0) voxel_indices[tri] = linear;
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace mt
+
+using namespace mt;
+
+extern "C" {
+
+int mt_compute_vertex_occupancy(const int32_t* occupancy, int32_t I, int32_t J, int32_t KP, int32_t* vertex_occupancy,
+                                int32_t* vertex_counts, mt_stream_t stream) {
+  MT_REQUIRE(I >= 0 && J >= 0 && KP >= 0);
+  MT_REQUIRE(vertex_occupancy && vertex_counts);
+  MT_REQUIRE(occupancy || (int64_t)I * J * KP == 0);
+  const int64_t total = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+  vertex_occupancy_kernel<<<grid_stride_blocks(total, 256), 256, 0, as_stream(stream)>>>(
+      occupancy, I, J, KP, vertex_occupancy, vertex_counts);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_count_occupancy(const int32_t* occupancy, int32_t I, int32_t J, int32_t KP, int32_t* voxel_counts,
+                       mt_stream_t stream) {
+  MT_REQUIRE(I >= 0 && J >= 0 && KP >= 0);
+  MT_REQUIRE(voxel_counts);
+  MT_REQUIRE(occupancy || (int64_t)I * J * KP == 0);
+  const int64_t total = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+  count_occupancy_kernel<<<grid_stride_blocks(total, 256), 256, 0, as_stream(stream)>>>(occupancy, I, J, KP,
+                                                                                       voxel_counts);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_create_voxels(const int32_t* occupancy, const int32_t* voxel_offsets, const int32_t* vertex_occupancy,
+                     const int32_t* vertex_offsets, int32_t I, int32_t J, int32_t KP, int64_t num_voxels,
+                     int64_t num_vertices, float* vertices, int32_t* neighbors, int32_t* lower_corners,
+                     int32_t* upper_corners, int32_t* indices, mt_stream_t stream) {
+  MT_REQUIRE(I >= 0 && J >= 0 && KP >= 0 && num_voxels >= 0 && num_vertices >= num_voxels);
+  if (num_vertices == 0) return MT_OK;
+  MT_REQUIRE(I > 0 && J > 0 && KP > 0);
+  MT_REQUIRE(occupancy && voxel_offsets && vertex_occupancy && vertex_offsets && vertices && lower_corners);
+  MT_REQUIRE(num_voxels == 0 || (neighbors && upper_corners && indices));
+  MT_REQUIRE((int64_t)32 * KP * J * I < ((int64_t)1 << 31));
+  VoxelGrid g{occupancy, voxel_offsets, vertex_occupancy, vertex_offsets, I, J, KP, num_voxels};
+  const int64_t words = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+  const int threads = 256;
+  const int64_t want = (words * 32 + threads - 1) / threads;
+  const unsigned blocks = (unsigned)(want < (int64_t)kSmCount * 16 ? want : (int64_t)kSmCount * 16);
+  create_voxels_kernel<<<blocks, threads, 0, as_stream(stream)>>>(g, vertices, neighbors, lower_corners,
+                                                                  upper_corners, indices, num_vertices);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_dilate_occupancy(const int32_t* occupancy, int32_t I, int32_t J, int32_t KP, int32_t dilation, int32_t* out,
+                        mt_stream_t stream) {
+  MT_REQUIRE(I >= 0 && J >= 0 && KP >= 0);
+  MT_REQUIRE(dilation > 0 && dilation < 32);
+  const int64_t total = (int64_t)I * J * KP;
+  if (total == 0) return MT_OK;
+  MT_REQUIRE(occupancy && out && occupancy != out);
+  dilate_kernel<<<grid_stride_blocks(total, 256), 256, 0, as_stream(stream)>>>(occupancy, I, J, KP, dilation, out);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_count_triangle_vertices(const float* signed_distances, const int32_t* lower_corners, int64_t G,
+                               const float* level_sets, int32_t S, int32_t* counts, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && S >= 0 && counts);
+  MT_REQUIRE(G == 0 || (signed_distances && lower_corners));
+  MT_REQUIRE(S == 0 || level_sets);
+  count_vertices_kernel<<<grid_stride_blocks(G, 256), 256, 0, as_stream(stream)>>>(signed_distances, lower_corners, G,
+                                                                                  level_sets, S, counts);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_signed_distances,
+                                const float* grid_spherical_harmonics, int32_t C, const int32_t* lower_corners,
+                                int64_t G, const float* level_sets, int32_t S, const int32_t* vertex_offsets,
+                                int64_t V, float* vertices, float* signed_distances, float* spherical_harmonics,
+                                uint8_t* vertex_types, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
+  if (G == 0 || S == 0 || V == 0) return MT_OK;
+  MT_REQUIRE(grid_vertices && grid_signed_distances && grid_spherical_harmonics && lower_corners && level_sets &&
+             vertex_offsets && vertices && signed_distances && spherical_harmonics && vertex_types);
+  create_vertices_kernel<<<grid_stride_blocks(G, 128), 128, 0, as_stream(stream)>>>(
+      grid_vertices, grid_signed_distances, grid_spherical_harmonics, C, lower_corners, G, level_sets, S,
+      vertex_offsets, V, vertices, signed_distances, spherical_harmonics, vertex_types);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_create_triangle_vertices_backward(const float* grid_signed_distances, int32_t C, const int32_t* lower_corners,
+                                         int64_t G, const float* level_sets, int32_t S,
+                                         const int32_t* vertex_offsets, const float* grad_vertices,
+                                         const float* grad_signed_distances, const float* grad_spherical_harmonics,
+                                         int64_t V, float* grad_grid_vertices, float* grad_grid_signed_distances,
+                                         float* grad_grid_spherical_harmonics, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
+  if (G == 0 || S == 0 || V == 0) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && lower_corners && level_sets && vertex_offsets);
+  MT_REQUIRE(grad_grid_signed_distances && grad_grid_spherical_harmonics);
+  MT_REQUIRE(grad_vertices == nullptr || grad_grid_vertices != nullptr);
+  create_vertices_backward_kernel<<<grid_stride_blocks(G, 128), 128, 0, as_stream(stream)>>>(
+      grid_signed_distances, C, lower_corners, G, level_sets, S, vertex_offsets, grad_vertices,
+      grad_signed_distances, grad_spherical_harmonics, V, grad_grid_vertices, grad_grid_signed_distances,
+      grad_grid_spherical_harmonics);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_count_triangle_faces(const float* signed_distances, const int32_t* lower_corners, int64_t G,
+                            const int32_t* upper_corners, int64_t Nv, const float* level_sets, int32_t S,
+                            int32_t* face_counts, uint8_t* cell_codes, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && Nv >= 0 && S >= 0 && face_counts);
+  MT_REQUIRE(Nv == 0 || (signed_distances && lower_corners && upper_corners && cell_codes));
+  MT_REQUIRE(S == 0 || level_sets);
+  count_faces_kernel<<<grid_stride_blocks(Nv, 256), 256, 0, as_stream(stream)>>>(
+      signed_distances, lower_corners, G, upper_corners, Nv, level_sets, S, face_counts, cell_codes);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, int64_t Nv, int64_t G,
+                             const int32_t* vertex_offsets, const uint8_t* vertex_types, const uint8_t* cell_codes,
+                             int32_t S, const int32_t* face_offsets, int64_t F, int32_t* faces,
+                             int32_t* voxel_indices, mt_stream_t stream) {
+  MT_REQUIRE(Nv >= 0 && G >= 0 && S >= 0 && F >= 0);
+  if (Nv == 0 || S == 0 || F == 0) return MT_OK;
+  MT_REQUIRE(neighbors && indices && vertex_offsets && vertex_types && cell_codes && face_offsets && faces &&
+             voxel_indices);
+  create_faces_kernel<<<grid_stride_blocks(Nv, 128), 128, 0, as_stream(stream)>>>(
+      neighbors, indices, Nv, G, vertex_offsets, vertex_types, cell_codes, S, face_offsets, faces, voxel_indices);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+}  // extern "C"

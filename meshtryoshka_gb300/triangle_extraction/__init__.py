@@ -1,0 +1,459 @@
+"""GB300 drop-in for the reference's ``triangle_extraction`` package.
+
+Same public names, argument meanings, return types and autograd behaviour as
+``triangle_extraction/__init__.py`` of dcharatan/meshtryoshka; every kernel is
+a hand-written sm_103a CUDA kernel behind the C ABI (``libmtgb.so``).
+
+Differences that do not change results:
+
+* ``tessellate_voxels`` runs the vertex and face counting passes before any
+  output is allocated and reads both totals in one device->host copy (the
+  reference synchronises four times, ``__init__.py:93-142``).
+* Scans are single-pass decoupled look-back kernels on caller-owned scratch.
+"""
+
+from __future__ import annotations
+
+import logging
+from typing import NamedTuple
+
+import torch
+from torch import Tensor
+from torch.profiler import record_function
+
+from .. import _native as nt
+
+__all__ = [
+    "Voxels",
+    "Triangles",
+    "extract_voxels",
+    "tessellate_voxels",
+    "pack_occupancy",
+    "unpack_occupancy",
+    "dilate_occupancy",
+    "compute_exclusive_cumsum",
+    "compute_vertex_occupancy",
+    "count_occupancy",
+    "create_voxels",
+    "count_triangle_vertices",
+    "create_triangle_vertices",
+    "count_triangle_faces",
+    "create_triangle_faces",
+    "CreateTriangleVertices",
+    "CreateTriangleVerticesResult",
+    "CountTriangleFacesResult",
+    "CreateTriangleFacesResult",
+    "VertexOccupancyFnResult",
+]
+
+
+def _i32(t: Tensor, name: str) -> Tensor:
+    if t.dtype != torch.int32:
+        raise TypeError(f"{name} must be int32, got {t.dtype}")
+    return t.contiguous()
+
+
+def _f32(t: Tensor, name: str) -> Tensor:
+    if t.dtype != torch.float32:
+        raise TypeError(f"{name} must be float32, got {t.dtype}")
+    return t.contiguous()
+
+
+# ---------------------------------------------------------------------------
+# Packed occupancy (triangle_extraction/common.py:17-35). Elementwise tensor
+# reshuffles; they are not on the per-step path.
+# ---------------------------------------------------------------------------
+def pack_occupancy(occupancy: Tensor) -> Tensor:
+    """bool [i, j, k] -> int32 [i, j, k // 32]; bit b of word kp is voxel 32*kp + b."""
+    assert occupancy.shape[-1] % 32 == 0
+    i, j, k = occupancy.shape
+    occupancy = occupancy.reshape(i, j, k // 32, 32)
+    powers = 1 << torch.arange(32, device=occupancy.device, dtype=torch.int64)
+    return (occupancy * powers).sum(dim=-1).type(torch.uint32).view(torch.int32)
+
+
+def unpack_occupancy(packed_occupancy: Tensor) -> Tensor:
+    """int32 [i, j, kp] -> bool [i, j, 32 * kp]."""
+    occupancy = packed_occupancy.view(torch.int32)
+    powers = 1 << torch.arange(32, device=occupancy.device, dtype=torch.int32)
+    occupancy = occupancy[..., None] & powers
+    i, j, kp, _ = occupancy.shape
+    return occupancy.reshape(i, j, kp * 32).type(torch.bool)
+
+
+# ---------------------------------------------------------------------------
+# Scan (triangle_extraction/compute_exclusive_cumsum.py:19-21).
+# ---------------------------------------------------------------------------
+@record_function("compute_exclusive_cumsum")
+def compute_exclusive_cumsum(x: Tensor) -> None:
+    """In-place exclusive prefix sum of a contiguous int32 CUDA tensor."""
+    if x.dtype != torch.int32 or not x.is_contiguous():
+        raise TypeError("compute_exclusive_cumsum expects a contiguous int32 tensor")
+    device = nt.require_cuda(x)
+    n = x.numel()
+    if n == 0:
+        return
+    ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_scan_workspace_bytes(n))
+    nt.call("mt_exclusive_scan_i32", x.data_ptr(), n, ws_ptr, ws_bytes, nt.stream(device))
+
+
+# ---------------------------------------------------------------------------
+# Voxel extraction (triangle_extraction/__init__.py:31-62 and helpers).
+# ---------------------------------------------------------------------------
+class VertexOccupancyFnResult(NamedTuple):
+    vertex_occupancy: Tensor  # [i+1, j+1, kp+1] int32
+    vertex_counts: Tensor  # [(i+1)(j+1)(kp+1)+1] int32
+
+
+class Voxels(NamedTuple):
+    vertices: Tensor  # [vertex, 3] float32 in [0, 1]^3, ordered (k, j, i) / extent
+    neighbors: Tensor  # [7, voxel] int32 (+x, +y, +z, +xy, +yz, +xz, +xyz)
+    lower_corners: Tensor  # [4, voxel_and_subvoxel] int32 (origin, +x, +y, +z); -64 = invalid
+    upper_corners: Tensor  # [4, voxel] int32 (+xyz, +yz, +xz, +xy)
+    indices: Tensor  # [voxel] int32 linear grid index
+    grid_shape: tuple[int, int, int]
+
+    @property
+    def num_vertices(self) -> int:
+        return self.vertices.shape[0]
+
+    @property
+    def num_voxels(self) -> int:
+        return self.upper_corners.shape[1]
+
+    @property
+    def num_subvoxels(self) -> int:
+        return self.lower_corners.shape[1] - self.upper_corners.shape[1]
+
+
+@record_function("compute_vertex_occupancy")
+def compute_vertex_occupancy(occupancy: Tensor) -> VertexOccupancyFnResult:
+    occupancy = _i32(occupancy, "occupancy")
+    device = nt.require_cuda(occupancy)
+    i, j, kp = occupancy.shape
+    shape = (i + 1, j + 1, kp + 1)
+    vertex_occupancy = torch.empty(shape, dtype=torch.int32, device=device)
+    vertex_counts = torch.empty(((i + 1) * (j + 1) * (kp + 1) + 1,), dtype=torch.int32, device=device)
+    nt.call(
+        "mt_compute_vertex_occupancy",
+        nt.ptr(occupancy), i, j, kp,
+        vertex_occupancy.data_ptr(), vertex_counts.data_ptr(), nt.stream(device),
+    )
+    return VertexOccupancyFnResult(vertex_occupancy, vertex_counts)
+
+
+@record_function("count_occupancy")
+def count_occupancy(occupancy: Tensor) -> Tensor:
+    occupancy = _i32(occupancy, "occupancy")
+    device = nt.require_cuda(occupancy)
+    i, j, kp = occupancy.shape
+    counts = torch.empty(((i + 1) * (j + 1) * (kp + 1) + 1,), dtype=torch.int32, device=device)
+    nt.call("mt_count_occupancy", nt.ptr(occupancy), i, j, kp, counts.data_ptr(), nt.stream(device))
+    return counts
+
+
+@record_function("create_voxels")
+def create_voxels(
+    occupancy: Tensor,
+    voxel_offsets: Tensor,
+    num_voxels: int,
+    vertex_occupancy: Tensor,
+    vertex_offsets: Tensor,
+    num_vertices: int,
+) -> Voxels:
+    occupancy = _i32(occupancy, "occupancy")
+    device = nt.require_cuda(occupancy)
+    i, j, kp = occupancy.shape
+    kw = dict(device=device)
+    vertices = torch.empty((num_vertices, 3), dtype=torch.float32, **kw)
+    neighbors = torch.empty((7, num_voxels), dtype=torch.int32, **kw)
+    lower_corners = torch.empty((4, num_vertices), dtype=torch.int32, **kw)
+    upper_corners = torch.empty((4, num_voxels), dtype=torch.int32, **kw)
+    indices = torch.empty((num_voxels,), dtype=torch.int32, **kw)
+    if num_voxels > 0:
+        nt.call(
+            "mt_create_voxels",
+            occupancy.data_ptr(),
+            _i32(voxel_offsets, "voxel_offsets").data_ptr(),
+            _i32(vertex_occupancy, "vertex_occupancy").data_ptr(),
+            _i32(vertex_offsets, "vertex_offsets").data_ptr(),
+            i, j, kp, num_voxels, num_vertices,
+            vertices.data_ptr(), neighbors.data_ptr(), lower_corners.data_ptr(),
+            upper_corners.data_ptr(), indices.data_ptr(), nt.stream(device),
+        )
+    return Voxels(vertices, neighbors, lower_corners, upper_corners, indices, (i, j, kp * 32))
+
+
+@record_function("extract_voxels")
+def extract_voxels(occupancy: Tensor) -> Voxels:
+    """Packed occupancy [i, j, kp] -> sparse voxel topology (one host sync)."""
+    occupancy = _i32(occupancy, "occupancy")
+    i, j, kp = occupancy.shape
+    logging.debug(f"Extracting voxels for grid with shape ({i}, {j}, {kp * 32}).")
+    vertex_occupancy, vertex_counts = compute_vertex_occupancy(occupancy)
+    voxel_counts = count_occupancy(occupancy)
+    compute_exclusive_cumsum(vertex_counts)
+    compute_exclusive_cumsum(voxel_counts)
+    totals = torch.stack((vertex_counts[-1], voxel_counts[-1])).cpu()
+    num_vertices, num_voxels = int(totals[0]), int(totals[1])
+    shape = vertex_occupancy.shape
+    return create_voxels(
+        occupancy,
+        voxel_counts[:-1].view(shape),
+        num_voxels,
+        vertex_occupancy,
+        vertex_counts[:-1].view(shape),
+        num_vertices,
+    )
+
+
+@record_function("dilate_occupancy")
+def dilate_occupancy(occupancy: Tensor, dilation: int) -> Tensor:
+    if dilation == 0:
+        return occupancy.clone()
+    assert 0 < dilation < 32
+    occupancy = _i32(occupancy, "occupancy")
+    device = nt.require_cuda(occupancy)
+    out = torch.empty_like(occupancy)
+    i, j, kp = occupancy.shape
+    if out.numel() > 0:
+        nt.call("mt_dilate_occupancy", occupancy.data_ptr(), i, j, kp, dilation, out.data_ptr(), nt.stream(device))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Per-step marching cubes.
+# ---------------------------------------------------------------------------
+@record_function("count_triangle_vertices")
+def count_triangle_vertices(signed_distances: Tensor, lower_corners: Tensor, level_sets: Tensor) -> Tensor:
+    signed_distances = _f32(signed_distances, "signed_distances")
+    lower_corners = _i32(lower_corners, "lower_corners")
+    level_sets = _f32(level_sets, "level_sets")
+    device = nt.require_cuda(signed_distances, lower_corners, level_sets)
+    (s,) = level_sets.shape
+    _, g = lower_corners.shape
+    counts = torch.empty((s * g + 1,), dtype=torch.int32, device=device)
+    nt.call(
+        "mt_count_triangle_vertices",
+        nt.ptr(signed_distances), nt.ptr(lower_corners), g, nt.ptr(level_sets), s,
+        counts.data_ptr(), nt.stream(device),
+    )
+    return counts
+
+
+class CreateTriangleVerticesResult(NamedTuple):
+    vertices: Tensor
+    signed_distances: Tensor
+    spherical_harmonics: Tensor
+    vertex_types: Tensor
+
+
+class CreateTriangleVertices(torch.autograd.Function):
+    """create_triangle_vertices.py:30-170: vertices on crossing edges, with the
+    MC weight t detached (gradients reach both edge corners with (1-t, t))."""
+
+    @staticmethod
+    def forward(ctx, grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners,
+                level_sets, vertex_offsets, num_vertices=None):
+        with record_function("create_triangle_vertices_forward"):
+            grid_vertices = _f32(grid_vertices, "grid_vertices")
+            grid_signed_distances = _f32(grid_signed_distances, "grid_signed_distances")
+            grid_spherical_harmonics = _f32(grid_spherical_harmonics, "grid_spherical_harmonics")
+            voxel_lower_corners = _i32(voxel_lower_corners, "voxel_lower_corners")
+            level_sets = _f32(level_sets, "level_sets")
+            vertex_offsets = _i32(vertex_offsets, "vertex_offsets")
+            device = nt.require_cuda(grid_vertices, grid_signed_distances, grid_spherical_harmonics,
+                                     voxel_lower_corners, level_sets, vertex_offsets)
+            (s,) = level_sets.shape
+            _, g = voxel_lower_corners.shape
+            c = grid_spherical_harmonics.shape[0]
+            v = int(vertex_offsets[-1].item()) if num_vertices is None else int(num_vertices)
+            kw = dict(dtype=torch.float32, device=device)
+            vertices = torch.empty((v, 3), **kw)
+            sdf = torch.empty((v,), **kw)
+            sh = torch.empty((c, v, 3), **kw)
+            types = torch.empty((v,), dtype=torch.uint8, device=device)
+            nt.call(
+                "mt_create_triangle_vertices",
+                nt.ptr(grid_vertices), nt.ptr(grid_signed_distances), nt.ptr(grid_spherical_harmonics), c,
+                nt.ptr(voxel_lower_corners), g, nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v,
+                nt.ptr(vertices), nt.ptr(sdf), nt.ptr(sh), nt.ptr(types), nt.stream(device),
+            )
+            ctx.save_for_backward(grid_signed_distances, voxel_lower_corners, level_sets, vertex_offsets)
+            ctx.shapes = (grid_vertices.shape, grid_spherical_harmonics.shape, v)
+            ctx.mark_non_differentiable(types)
+            ctx.set_materialize_grads(False)
+            return vertices, sdf, sh, types
+
+    @staticmethod
+    def backward(ctx, grad_vertices, grad_signed_distances, grad_spherical_harmonics, grad_types):
+        with record_function("create_triangle_vertices_backward"):
+            grid_signed_distances, lower_corners, level_sets, vertex_offsets = ctx.saved_tensors
+            gv_shape, gsh_shape, v = ctx.shapes
+            device = grid_signed_distances.device
+            g = lower_corners.shape[1]
+            (s,) = level_sets.shape
+            c = gsh_shape[0]
+            grad_grid_vertices = torch.zeros(gv_shape, dtype=torch.float32, device=device)
+            grad_grid_sdf = torch.zeros_like(grid_signed_distances)
+            grad_grid_sh = torch.zeros(gsh_shape, dtype=torch.float32, device=device)
+            gv = grad_vertices.contiguous() if grad_vertices is not None else None
+            gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
+            gs = grad_spherical_harmonics.contiguous() if grad_spherical_harmonics is not None else None
+            nt.call(
+                "mt_create_triangle_vertices_backward",
+                nt.ptr(grid_signed_distances), c, nt.ptr(lower_corners), g, nt.ptr(level_sets), s,
+                nt.ptr(vertex_offsets), nt.ptr(gv), nt.ptr(gd), nt.ptr(gs), v,
+                nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), nt.stream(device),
+            )
+            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None
+
+
+def create_triangle_vertices(
+    grid_vertices: Tensor,
+    grid_signed_distances: Tensor,
+    grid_spherical_harmonics: Tensor,
+    voxel_lower_corners: Tensor,
+    level_sets: Tensor,
+    vertex_offsets: Tensor,
+    num_vertices: int | None = None,
+) -> CreateTriangleVerticesResult:
+    """``num_vertices`` (optional, not in the reference signature) skips the
+    device->host read of ``vertex_offsets[-1]`` when the caller knows it."""
+    result = CreateTriangleVertices.apply(
+        grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners, level_sets,
+        vertex_offsets, num_vertices,
+    )
+    return CreateTriangleVerticesResult(*result)
+
+
+class CountTriangleFacesResult(NamedTuple):
+    # Field names and positional order are kept as in the reference
+    # (count_triangle_faces.py:23-25, filled positionally at :63): the first
+    # field holds the face counts, the second the cube codes.
+    cell_codes: Tensor
+    face_counts: Tensor
+
+
+@record_function("count_triangle_faces")
+def count_triangle_faces(
+    signed_distances: Tensor, lower_corners: Tensor, upper_corners: Tensor, level_sets: Tensor
+) -> CountTriangleFacesResult:
+    signed_distances = _f32(signed_distances, "signed_distances")
+    lower_corners = _i32(lower_corners, "lower_corners")
+    upper_corners = _i32(upper_corners, "upper_corners")
+    level_sets = _f32(level_sets, "level_sets")
+    device = nt.require_cuda(signed_distances, lower_corners, upper_corners, level_sets)
+    _, nv = upper_corners.shape
+    _, g = lower_corners.shape
+    (s,) = level_sets.shape
+    codes = torch.empty((s, nv), dtype=torch.uint8, device=device)
+    counts = torch.empty((s * nv + 1,), dtype=torch.int32, device=device)
+    nt.call(
+        "mt_count_triangle_faces",
+        nt.ptr(signed_distances), nt.ptr(lower_corners), g, nt.ptr(upper_corners), nv, nt.ptr(level_sets), s,
+        counts.data_ptr(), nt.ptr(codes), nt.stream(device),
+    )
+    return CountTriangleFacesResult(counts, codes)
+
+
+class CreateTriangleFacesResult(NamedTuple):
+    faces: Tensor
+    voxel_indices: Tensor | None
+
+
+@record_function("create_triangle_faces")
+def create_triangle_faces(
+    signed_distances: Tensor,
+    neighbors: Tensor,
+    indices: Tensor,
+    vertex_offsets: Tensor,
+    triangle_vertex_types: Tensor,
+    voxel_cell_codes: Tensor,
+    level_sets: Tensor,
+    face_offsets: Tensor,
+    num_faces: int | None = None,
+) -> CreateTriangleFacesResult:
+    device = nt.require_cuda(signed_distances, neighbors, indices, vertex_offsets, face_offsets)
+    _, nv = neighbors.shape
+    (s,) = level_sets.shape
+    g = (vertex_offsets.shape[0] - 1) // s if s > 0 else 0
+    f = int(face_offsets[-1].item()) // 3 if num_faces is None else int(num_faces)
+    faces = torch.empty((f, 3), dtype=torch.int32, device=device)
+    voxel_indices = torch.empty((f,), dtype=torch.int32, device=device)
+    nt.call(
+        "mt_create_triangle_faces",
+        nt.ptr(_i32(neighbors, "neighbors")), nt.ptr(_i32(indices, "indices")), nv, g,
+        nt.ptr(_i32(vertex_offsets, "vertex_offsets")), nt.ptr(triangle_vertex_types.contiguous()),
+        nt.ptr(voxel_cell_codes.contiguous()), s, nt.ptr(_i32(face_offsets, "face_offsets")), f,
+        nt.ptr(faces), nt.ptr(voxel_indices), nt.stream(device),
+    )
+    return CreateTriangleFacesResult(faces, voxel_indices)
+
+
+class Triangles(NamedTuple):
+    vertices: Tensor  # [vertex, 3]
+    signed_distances: Tensor  # [vertex]
+    spherical_harmonics: Tensor  # [sh, vertex, 3]
+    faces: Tensor  # [face, 3] int32
+    voxel_indices: Tensor  # [face] int32
+    vertex_boundaries: Tensor  # [level_set] int32 (cumulative ends)
+    face_boundaries: Tensor  # [level_set] int32 (cumulative ends)
+
+
+@record_function("tessellate_voxels")
+def tessellate_voxels(
+    signed_distances: Tensor,
+    vertices: Tensor,
+    spherical_harmonics: Tensor,
+    neighbors: Tensor,
+    lower_corners: Tensor,
+    upper_corners: Tensor,
+    indices: Tensor,
+    level_sets: Tensor,
+) -> Triangles:
+    """Marching cubes over every level set (triangle_extraction/__init__.py:75-157).
+
+    Differentiable with respect to ``signed_distances`` and
+    ``spherical_harmonics`` (and ``vertices``) through the triangle vertices'
+    signed distances / colours, exactly as the reference.
+    """
+    (num_level_sets,) = level_sets.shape
+    device = nt.require_cuda(signed_distances, lower_corners, level_sets)
+    logging.debug(f"Tessellating {neighbors.shape[1]} voxels with {num_level_sets} level sets.")
+    _, g = lower_corners.shape
+    _, nv = upper_corners.shape
+
+    with torch.no_grad():
+        vertex_offsets = count_triangle_vertices(signed_distances, lower_corners, level_sets)
+        compute_exclusive_cumsum(vertex_offsets)
+        face_offsets, voxel_cell_codes = count_triangle_faces(signed_distances, lower_corners, upper_corners,
+                                                              level_sets)
+        compute_exclusive_cumsum(face_offsets)
+        # One device->host read for both totals (and the scan status word).
+        totals = torch.stack((vertex_offsets[-1], face_offsets[-1])).cpu()
+        nt.workspace(device).check()
+    num_vertices = int(totals[0])
+    num_faces = int(totals[1]) // 3
+
+    triangle_vertices, triangle_sdf, triangle_sh, triangle_types = create_triangle_vertices(
+        vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets, num_vertices,
+    )
+
+    with torch.no_grad():
+        faces, voxel_indices = create_triangle_faces(
+            signed_distances, neighbors, indices, vertex_offsets, triangle_types, voxel_cell_codes, level_sets,
+            face_offsets, num_faces,
+        )
+        if g > 0 and num_level_sets > 0:
+            vertex_boundaries = vertex_offsets[1:].view(num_level_sets, -1)[:, -1].clone()
+        else:
+            vertex_boundaries = torch.zeros((num_level_sets,), dtype=torch.int32, device=device)
+        if nv > 0 and num_level_sets > 0:
+            face_boundaries = face_offsets[1:].view(num_level_sets, -1)[:, -1].clone() // 3
+        else:
+            face_boundaries = torch.zeros((num_level_sets,), dtype=torch.int32, device=device)
+
+    logging.debug(f"Created {num_vertices} vertices and {num_faces} faces.")
+    return Triangles(triangle_vertices, triangle_sdf, triangle_sh, faces, voxel_indices, vertex_boundaries,
+                     face_boundaries)
