@@ -178,6 +178,168 @@ MT_API int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* ind
                              int32_t* faces, int32_t* voxel_indices,
                              mt_stream_t stream);
 
+
+/* ------------------------------------------------------------------------
+ * Key sort (triangle_rasterization/sort_keys.cu:215-270, which calls
+ * cub::DeviceRadixSort::SortPairs over bits [0, 64) of int64 keys).
+ * Stable LSD radix sort in SIGNED int64 key order over bits
+ * [begin_bit, end_bit); keys_out/values_out must not alias the inputs.
+ * ---------------------------------------------------------------------- */
+
+MT_API size_t mt_sort_pairs_workspace_bytes(int64_t n);
+
+MT_API int mt_sort_pairs_i64_i32(const int64_t* keys_in, const int32_t* values_in,
+                                 int64_t* keys_out, int32_t* values_out, int64_t n,
+                                 int32_t begin_bit, int32_t end_bit, void* workspace,
+                                 size_t workspace_bytes, mt_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Rasterization front end. B = cameras, V = triangle vertices, F = faces.
+ * Key layout arrays are int32[7]: camera offset, camera length, shell
+ * offset, shell length, tile offset, tile length, depth offset (depth is
+ * always 32 bits); see triangle_rasterization/keys.py:4-22.
+ * ---------------------------------------------------------------------- */
+
+/* inverse(extrinsics)[:, :3, 3] (evaluate_spherical_harmonics.py:38).
+ * extrinsics [B,4,4] world->camera; out [B,3]. */
+MT_API int mt_camera_positions(const float* extrinsics, int32_t B, float* out,
+                               mt_stream_t stream);
+
+/* triangle_rasterization/project_vertices.slang:51-92.
+ * out_xy [B,V,2] pixels (unnormalised, no +0.5), out_depth [B,V]. */
+MT_API int mt_project_vertices(const float* vertices, int64_t V,
+                               const float* extrinsics, const float* intrinsics,
+                               int32_t B, float* out_xy, float* out_depth,
+                               mt_stream_t stream);
+
+/* triangle_rasterization/evaluate_spherical_harmonics.slang:187-228.
+ * spherical_harmonics [C,V,3] (C >= (sh_degree+1)^2), camera_positions [B,3],
+ * out_colors [B,V,3] = max(SH(dir) + 0.5, 0). */
+MT_API int mt_evaluate_spherical_harmonics(const float* vertices, int64_t V,
+                                           const float* spherical_harmonics,
+                                           int32_t C, int32_t sh_degree,
+                                           const float* camera_positions, int32_t B,
+                                           float* out_colors, mt_stream_t stream);
+
+/* evaluate_spherical_harmonics.slang:230-270 (backward to the SH only).
+ * Accumulates (+=) into grad_spherical_harmonics [C,V,3]. */
+MT_API int mt_evaluate_spherical_harmonics_backward(
+    const float* vertices, int64_t V, int32_t C, int32_t sh_degree,
+    const float* camera_positions, int32_t B, const float* out_colors,
+    const float* grad_colors, float* grad_spherical_harmonics, mt_stream_t stream);
+
+/* triangle_rasterization/bound_triangles.slang:144-192.
+ * out_min / out_max [B,F,2] (row, col) tile bounds [min, max); out_count
+ * [B,F] = tiles touched (0 for back-facing or near-plane-culled faces). */
+MT_API int mt_bound_triangles(const float* xy, const float* depth, int64_t V,
+                              const int32_t* faces, int64_t F, int32_t B,
+                              int32_t tile_h, int32_t tile_w, int32_t rows,
+                              int32_t cols, float near_plane, int32_t* out_min,
+                              int32_t* out_max, int32_t* out_count,
+                              mt_stream_t stream);
+
+/* triangle_rasterization/generate_keys.slang:4-68. offsets [B*F] is the
+ * inclusive int64 prefix sum of out_count; K = offsets[B*F-1]. Writes one
+ * key per (camera, face, tile) in (camera, face, row, col) order. */
+MT_API int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces,
+                            int64_t F, const int32_t* shell_face_boundaries,
+                            int32_t S, const int32_t* tile_min,
+                            const int32_t* tile_max, const int64_t* offsets,
+                            int32_t B, int32_t grid_width, const int32_t* layout,
+                            int64_t K, int64_t* out_keys, int32_t* out_triangles,
+                            mt_stream_t stream);
+
+/* triangle_rasterization/delineate_tiles.slang:14-58 (+ the zero fill of
+ * delineate_tiles.py:40, done here). out_boundaries [B, shell_dim,
+ * num_tiles, 2] int64; shell_dim = S when separate_shells, else 1. */
+MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
+                              const int32_t* layout, int32_t separate_shells,
+                              int32_t B, int32_t shell_dim, int64_t num_tiles,
+                              int64_t* out_boundaries, mt_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Fused multi-shell compositing
+ * (triangle_rasterization/intersect_and_composite.slang:224-564).
+ * xy [B,V,2], colors [B,V,3], signed_distances [V], faces [F,3],
+ * sharpness: device scalar; tile_boundaries [B, rows*cols, 2];
+ * out [B,4,H,W] = (rgb, transmittance). One CTA of tile_h*tile_w (<= 1024)
+ * threads per (camera, tile).
+ * ---------------------------------------------------------------------- */
+MT_API int mt_intersect_and_composite_forward(
+    const float* xy, const float* colors, const float* signed_distances, int64_t V,
+    const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
+    const int32_t* sorted_triangles, const int64_t* tile_boundaries, int32_t B,
+    int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w,
+    int32_t H, int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
+    float* out, mt_stream_t stream);
+
+/* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
+ * [V], grad_sharpness [1]. exact_adjoint = 0 reproduces the reference's
+ * gradient routing (the outer hit's deferred gradient is scattered with the
+ * current hit's barycentric weights); 1 uses the outer hit's own weights. */
+MT_API int mt_intersect_and_composite_backward(
+    const float* xy, const float* colors, const float* signed_distances, int64_t V,
+    const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
+    const int32_t* sorted_triangles, const int64_t* tile_boundaries, int32_t B,
+    int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w,
+    int32_t H, int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
+    const float* out, const float* grad_out, float* grad_colors,
+    float* grad_signed_distances, float* grad_sharpness, int32_t exact_adjoint,
+    mt_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Explicit mode (triangle_rasterization/__init__.py:22-164).
+ * ---------------------------------------------------------------------- */
+
+/* intersect.slang:86-182: first hit per (camera, shell, pixel).
+ * tile_boundaries [B,S,rows*cols,2]; out_uv [B*S,H,W,2]; out_index
+ * [B*S,H,W] (-1 = miss, uv = 0). */
+MT_API int mt_intersect(const float* xy, int64_t V, const int32_t* faces,
+                        const int32_t* sorted_triangles,
+                        const int64_t* tile_boundaries, int32_t B, int32_t S,
+                        int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w,
+                        int32_t H, int32_t W, float* out_uv, int32_t* out_index,
+                        mt_stream_t stream);
+
+/* interpolate.slang:22-76: out_signed_distances [B*S,H,W], out_colors
+ * [B*S,H,W,3] with weights (u, v, 1-u-v); misses are 0. */
+MT_API int mt_interpolate(const float* uv, const int32_t* index, int32_t B,
+                          int32_t S, int32_t H, int32_t W, const int32_t* faces,
+                          const float* signed_distances, const float* colors,
+                          int64_t V, float* out_signed_distances,
+                          float* out_colors, mt_stream_t stream);
+
+/* Backward of mt_interpolate; accumulates (+=) into grad_signed_distances [V]
+ * and grad_colors [B,V,3]. Either grad_out pointer may be NULL (zero). */
+MT_API int mt_interpolate_backward(const float* uv, const int32_t* index,
+                                   int32_t B, int32_t S, int32_t H, int32_t W,
+                                   const int32_t* faces, int64_t V,
+                                   const float* grad_out_signed_distances,
+                                   const float* grad_out_colors,
+                                   float* grad_signed_distances,
+                                   float* grad_colors, mt_stream_t stream);
+
+/* composite.slang:60-120: signed_distances [P,S], colors [P,S,3], mask [P,S]
+ * (bytes, non-zero = hit) -> out_colors [P,3], out_transmittances [P]. */
+MT_API int mt_composite(const float* signed_distances, const float* colors,
+                        const uint8_t* mask, int64_t P, int32_t S,
+                        const float* sharpness, float* out_colors,
+                        float* out_transmittances, mt_stream_t stream);
+
+/* composite.slang:122-218; accumulates (+=) into grad_signed_distances [P,S],
+ * grad_colors [P,S,3], grad_sharpness [1]. exact_adjoint = 0 reproduces the
+ * reference's slot routing (shell_index - 1, and num_shells - 1 for the
+ * last hit); 1 routes to the previous / last hit shell. */
+MT_API int mt_composite_backward(const float* signed_distances, const float* colors,
+                                 const uint8_t* mask, int64_t P, int32_t S,
+                                 const float* sharpness, const float* out_colors,
+                                 const float* out_transmittances,
+                                 const float* grad_out_colors,
+                                 const float* grad_out_transmittances,
+                                 float* grad_signed_distances, float* grad_colors,
+                                 float* grad_sharpness, int32_t exact_adjoint,
+                                 mt_stream_t stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -1,0 +1,413 @@
+// Rasterization front end for sm_103a: camera centres, vertex projection,
+// spherical-harmonic colours (forward / backward), triangle tile bounds, key
+// generation and tile delineation.
+//
+// Follows triangle_rasterization/project_vertices.slang, bound_triangles.slang,
+// generate_keys.slang + keys.slang, delineate_tiles.slang and
+// evaluate_spherical_harmonics.slang. Geometry that decides integer outputs
+// (projection, back-face test, tile bounds, key depth) uses a fixed operation
+// order with explicit fused multiply-adds, so results are reproducible
+// bit-for-bit by the CPU restatement.
+
+#include "mt_common.cuh"
+
+namespace mt {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Camera centres: inverse(extrinsics)[:, :3, 3]
+// (triangle_rasterization/evaluate_spherical_harmonics.py:38), in fp64.
+// ---------------------------------------------------------------------------
+__global__ void camera_positions_kernel(const float* __restrict__ ext, int B, float* __restrict__ out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  double m[16];
+  for (int i = 0; i < 16; ++i) m[i] = (double)ext[16 * b + i];
+  // Column 3 of the inverse via cofactors: inv[r][3] = C[3][r] / det.
+  auto det3 = [&](int r0, int r1, int r2, int c0, int c1, int c2) {
+    return m[4 * r0 + c0] * (m[4 * r1 + c1] * m[4 * r2 + c2] - m[4 * r1 + c2] * m[4 * r2 + c1]) -
+           m[4 * r0 + c1] * (m[4 * r1 + c0] * m[4 * r2 + c2] - m[4 * r1 + c2] * m[4 * r2 + c0]) +
+           m[4 * r0 + c2] * (m[4 * r1 + c0] * m[4 * r2 + c1] - m[4 * r1 + c1] * m[4 * r2 + c0]);
+  };
+  double cof[4][4];
+  for (int r = 0; r < 4; ++r) {
+    for (int c = 0; c < 4; ++c) {
+      int rs[3], cs[3], ri = 0, ci = 0;
+      for (int k = 0; k < 4; ++k) {
+        if (k != r) rs[ri++] = k;
+        if (k != c) cs[ci++] = k;
+      }
+      const double minor = det3(rs[0], rs[1], rs[2], cs[0], cs[1], cs[2]);
+      cof[r][c] = ((r + c) & 1) ? -minor : minor;
+    }
+  }
+  double det = 0;
+  for (int c = 0; c < 4; ++c) det += m[c] * cof[0][c];
+  for (int r = 0; r < 3; ++r) out[3 * b + r] = (float)(cof[3][r] / det);
+}
+
+// ---------------------------------------------------------------------------
+// project_vertices.slang:51-92. cam = W2C [v, 1]; xy = (K cam).xy / cam.z.
+// ---------------------------------------------------------------------------
+__global__ void project_kernel(const float* __restrict__ verts, int64_t V, const float* __restrict__ ext,
+                               const float* __restrict__ intr, int B, float* __restrict__ out_xy,
+                               float* __restrict__ out_depth) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float x = verts[3 * v], y = verts[3 * v + 1], z = verts[3 * v + 2];
+    for (int b = 0; b < B; ++b) {
+      const float* E = ext + 16 * b;
+      const float* K = intr + 9 * b;
+      float cam[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const float* row = E + 4 * r;
+        cam[r] = __fmaf_rn(row[3], 1.0f, __fmaf_rn(row[2], z, __fmaf_rn(row[1], y, __fmul_rn(row[0], x))));
+      }
+      const float kx = __fmaf_rn(K[2], cam[2], __fmaf_rn(K[1], cam[1], __fmul_rn(K[0], cam[0])));
+      const float ky = __fmaf_rn(K[5], cam[2], __fmaf_rn(K[4], cam[1], __fmul_rn(K[3], cam[0])));
+      const int64_t o = (int64_t)b * V + v;
+      out_xy[2 * o] = __fdiv_rn(kx, cam[2]);
+      out_xy[2 * o + 1] = __fdiv_rn(ky, cam[2]);
+      out_depth[o] = cam[2];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// evaluate_spherical_harmonics.slang:4-270. Real SH up to degree 3;
+// rgb = max(sum_k basis_k(dir) sh_k + 0.5, 0).
+// ---------------------------------------------------------------------------
+__constant__ float kShC0 = 0.28209479177387814f;
+__constant__ float kShC1 = 0.4886025119029199f;
+__constant__ float kShC2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f,
+                               -1.0925484305920792f, 0.5462742152960396f};
+__constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f,
+                               0.3731763325901154f,  -0.4570457994644658f, 1.445305721320277f,
+                               -0.5900435899266435f};
+
+__device__ __forceinline__ void sh_basis(float x, float y, float z, int n, float (&basis)[16]) {
+  basis[0] = kShC0;
+  if (n <= 1) return;
+  basis[1] = -kShC1 * y;
+  basis[2] = kShC1 * z;
+  basis[3] = -kShC1 * x;
+  if (n <= 4) return;
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  basis[4] = kShC2[0] * xy;
+  basis[5] = kShC2[1] * yz;
+  basis[6] = kShC2[2] * (2.0f * zz - xx - yy);
+  basis[7] = kShC2[3] * xz;
+  basis[8] = kShC2[4] * (xx - yy);
+  if (n <= 9) return;
+  basis[9] = kShC3[0] * y * (3.0f * xx - yy);
+  basis[10] = kShC3[1] * xy * z;
+  basis[11] = kShC3[2] * y * (4.0f * zz - xx - yy);
+  basis[12] = kShC3[3] * z * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+  basis[13] = kShC3[4] * x * (4.0f * zz - xx - yy);
+  basis[14] = kShC3[5] * z * (xx - yy);
+  basis[15] = kShC3[6] * x * (xx - 3.0f * yy);
+}
+
+__device__ __forceinline__ void view_dir(const float* __restrict__ verts, int64_t v, const float* __restrict__ cam,
+                                         float& x, float& y, float& z) {
+  const float dx = verts[3 * v] - cam[0], dy = verts[3 * v + 1] - cam[1], dz = verts[3 * v + 2] - cam[2];
+  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+  x = dx / len;
+  y = dy / len;
+  z = dz / len;
+}
+
+__global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, const float* __restrict__ sh,
+                                  int n_coeff, const float* __restrict__ campos, int B, float* __restrict__ out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    for (int b = 0; b < B; ++b) {
+      float x, y, z;
+      view_dir(verts, v, campos + 3 * b, x, y, z);
+      float basis[16];
+      sh_basis(x, y, z, n_coeff, basis);
+      float rgb[3] = {0.f, 0.f, 0.f};
+      for (int k = 0; k < n_coeff; ++k) {
+        const float* s = sh + ((int64_t)k * V + v) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rgb[c] += basis[k] * s[c];
+      }
+      float* o = out + ((int64_t)b * V + v) * 3;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = fmaxf(rgb[c] + 0.5f, 0.0f);
+    }
+  }
+}
+
+// d sh_k += sum_b basis_k(dir_b) * d rgb_b * [rgb_b + 0.5 > 0]; the mask is
+// read from the forward output (out > 0 exactly when the pre-clamp value is).
+__global__ void sh_backward_kernel(const float* __restrict__ verts, int64_t V, int n_coeff,
+                                   const float* __restrict__ campos, int B, const float* __restrict__ colors,
+                                   const float* __restrict__ dcolors, float* __restrict__ dsh) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    float acc[16][3];
+    for (int k = 0; k < 16; ++k) acc[k][0] = acc[k][1] = acc[k][2] = 0.f;
+    for (int b = 0; b < B; ++b) {
+      const int64_t o = ((int64_t)b * V + v) * 3;
+      float g[3];
+      bool any = false;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        g[c] = colors[o + c] > 0.0f ? dcolors[o + c] : 0.0f;
+        any |= g[c] != 0.0f;
+      }
+      if (!any) continue;
+      float x, y, z;
+      view_dir(verts, v, campos + 3 * b, x, y, z);
+      float basis[16];
+      sh_basis(x, y, z, n_coeff, basis);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k < n_coeff) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[k][c] += basis[k] * g[c];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      if (k < n_coeff) {
+        float* d = dsh + ((int64_t)k * V + v) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) d[c] += acc[k][c];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// bound_triangles.slang:62-192: back-face and near-plane culling, tile AABB
+// with min = int(x) / ts (truncation), max = int(ceil(x / ts)), clamped.
+// ---------------------------------------------------------------------------
+struct TileBounds {
+  int r0, c0, r1, c1;
+};
+
+__device__ __forceinline__ TileBounds triangle_tile_bounds(const float* __restrict__ xy,
+                                                           const float* __restrict__ depth, int64_t V,
+                                                           const int32_t* __restrict__ faces, int64_t f, int b,
+                                                           int tile_h, int tile_w, int rows, int cols, float near) {
+  const int64_t base = (int64_t)b * V;
+  const int32_t ia = faces[3 * f], ib = faces[3 * f + 1], ic = faces[3 * f + 2];
+  const float ax = xy[2 * (base + ia)], ay = xy[2 * (base + ia) + 1], ad = depth[base + ia];
+  const float bx = xy[2 * (base + ib)], by = xy[2 * (base + ib) + 1], bd = depth[base + ib];
+  const float cx = xy[2 * (base + ic)], cy = xy[2 * (base + ic) + 1], cd = depth[base + ic];
+  TileBounds t{0, 0, 0, 0};
+  const float check =
+      __fmaf_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay), -__fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
+  if (check < 0.0f) return t;
+  if (fminf(fminf(ad, bd), cd) < near) return t;
+  const float ymin = fminf(fminf(ay, by), cy), ymax = fmaxf(fmaxf(ay, by), cy);
+  const float xmin = fminf(fminf(ax, bx), cx), xmax = fmaxf(fmaxf(ax, bx), cx);
+  t.r0 = min(max(f2i_rz(ymin) / tile_h, 0), rows);
+  t.r1 = min(max(f2i_rz(ceilf(__fdiv_rn(ymax, (float)tile_h))), 0), rows);
+  t.c0 = min(max(f2i_rz(xmin) / tile_w, 0), cols);
+  t.c1 = min(max(f2i_rz(ceilf(__fdiv_rn(xmax, (float)tile_w))), 0), cols);
+  return t;
+}
+
+__global__ void bound_kernel(const float* __restrict__ xy, const float* __restrict__ depth, int64_t V,
+                             const int32_t* __restrict__ faces, int64_t F, int B, int tile_h, int tile_w, int rows,
+                             int cols, float near, int32_t* __restrict__ out_min, int32_t* __restrict__ out_max,
+                             int32_t* __restrict__ out_count) {
+  const int64_t total = (int64_t)B * F;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(i / F);
+    const int64_t f = i - (int64_t)b * F;
+    const TileBounds t = triangle_tile_bounds(xy, depth, V, faces, f, b, tile_h, tile_w, rows, cols, near);
+    out_min[2 * i] = t.r0;
+    out_min[2 * i + 1] = t.c0;
+    out_max[2 * i] = t.r1;
+    out_max[2 * i + 1] = t.c1;
+    out_count[i] = (t.r1 - t.r0) * (t.c1 - t.c0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// generate_keys.slang:4-68 + keys.slang:6-22. One thread per (camera, face);
+// keys land at the exclusive offset of (camera, face) in row-major tile order,
+// so the unsorted order (and therefore the stable sort's tie order) is the
+// reference's.
+// ---------------------------------------------------------------------------
+struct KeyLayout {
+  int cam_off, cam_len, shell_off, shell_len, tile_off, tile_len, depth_off;
+};
+
+__device__ __forceinline__ uint64_t field_mask(int len) { return (uint64_t)((1u << len) - 1u); }
+
+__global__ void keys_kernel(const float* __restrict__ depth, int64_t V, const int32_t* __restrict__ faces,
+                            int64_t F, const int32_t* __restrict__ sfb, int S, const int32_t* __restrict__ tmin,
+                            const int32_t* __restrict__ tmax, const int64_t* __restrict__ offsets, int B,
+                            int grid_width, KeyLayout L, int64_t K, uint64_t* __restrict__ out_keys,
+                            int32_t* __restrict__ out_tri) {
+  const int64_t total = (int64_t)B * F;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(i / F);
+    const int64_t f = i - (int64_t)b * F;
+    const int r0 = tmin[2 * i], c0 = tmin[2 * i + 1], r1 = tmax[2 * i], c1 = tmax[2 * i + 1];
+    if (r1 <= r0 || c1 <= c0) continue;
+    uint32_t shell = 0;
+    for (; shell < (uint32_t)S; ++shell)
+      if (f < sfb[shell]) break;
+    const int64_t base = (int64_t)b * V;
+    const float da = depth[base + faces[3 * f]], db = depth[base + faces[3 * f + 1]],
+                dc = depth[base + faces[3 * f + 2]];
+    const float mean = __fdiv_rn(__fadd_rn(__fadd_rn(da, db), dc), 3.0f);
+    const uint64_t fixed = (((uint64_t)b & field_mask(L.cam_len)) << L.cam_off) |
+                           (((uint64_t)shell & field_mask(L.shell_len)) << L.shell_off) |
+                           ((uint64_t)__float_as_uint(mean) << L.depth_off);
+    int64_t k = (i == 0) ? 0 : offsets[i - 1];
+    for (int r = r0; r < r1; ++r) {
+      for (int c = c0; c < c1; ++c) {
+        if (k >= K) return;  // guarded: offsets and K always agree for valid inputs
+        const uint32_t tile = (uint32_t)(r * grid_width + c);
+        out_keys[k] = fixed | (((uint64_t)tile & field_mask(L.tile_len)) << L.tile_off);
+        out_tri[k] = (int32_t)f;
+        ++k;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// delineate_tiles.slang:14-58: [start, end) per (camera, shell|0, tile) where
+// the (camera, shell|0, tile) index changes between consecutive sorted keys.
+// ---------------------------------------------------------------------------
+__global__ void delineate_kernel(const uint64_t* __restrict__ keys, int64_t K, KeyLayout L, int separate_shells,
+                                 int B, int Sd, int64_t T, int64_t* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < K; i += (int64_t)gridDim.x * blockDim.x) {
+    auto index_of = [&](uint64_t key) -> int64_t {
+      const int64_t cam = (int64_t)((key >> L.cam_off) & field_mask(L.cam_len));
+      const int64_t sh = separate_shells ? (int64_t)((key >> L.shell_off) & field_mask(L.shell_len)) : 0;
+      const int64_t tile = (int64_t)((key >> L.tile_off) & field_mask(L.tile_len));
+      if (cam >= B || sh >= Sd || tile >= T) return -1;
+      return (cam * Sd + sh) * T + tile;
+    };
+    const int64_t here = index_of(keys[i]);
+    if (i > 0) {
+      const int64_t prev = index_of(keys[i - 1]);
+      if (here != prev) {
+        if (prev >= 0) out[2 * prev + 1] = i;
+        if (here >= 0) out[2 * here] = i;
+      }
+    }
+    if (i == K - 1 && here >= 0) out[2 * here + 1] = K;
+  }
+}
+
+inline bool layout_ok(const KeyLayout& L) {
+  auto ok = [](int off, int len) { return off >= 0 && len >= 0 && len <= 31 && off + len <= 64; };
+  return ok(L.cam_off, L.cam_len) && ok(L.shell_off, L.shell_len) && ok(L.tile_off, L.tile_len) &&
+         L.depth_off >= 0 && L.depth_off + 32 <= 64;
+}
+
+}  // namespace
+}  // namespace mt
+
+using namespace mt;
+
+extern "C" {
+
+int mt_camera_positions(const float* extrinsics, int32_t B, float* out, mt_stream_t stream) {
+  MT_REQUIRE(B >= 0);
+  if (B == 0) return MT_OK;
+  MT_REQUIRE(extrinsics && out);
+  camera_positions_kernel<<<grid_1d(B, 64), 64, 0, as_stream(stream)>>>(extrinsics, B, out);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_project_vertices(const float* vertices, int64_t V, const float* extrinsics, const float* intrinsics, int32_t B,
+                        float* out_xy, float* out_depth, mt_stream_t stream) {
+  MT_REQUIRE(V >= 0 && B >= 0);
+  if (V == 0 || B == 0) return MT_OK;
+  MT_REQUIRE(vertices && extrinsics && intrinsics && out_xy && out_depth);
+  project_kernel<<<grid_stride_blocks(V, 256), 256, 0, as_stream(stream)>>>(vertices, V, extrinsics, intrinsics, B,
+                                                                           out_xy, out_depth);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_evaluate_spherical_harmonics(const float* vertices, int64_t V, const float* spherical_harmonics, int32_t C,
+                                    int32_t sh_degree, const float* camera_positions, int32_t B, float* out_colors,
+                                    mt_stream_t stream) {
+  MT_REQUIRE(V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+  MT_REQUIRE(C >= n);
+  if (V == 0 || B == 0) return MT_OK;
+  MT_REQUIRE(vertices && spherical_harmonics && camera_positions && out_colors);
+  sh_forward_kernel<<<grid_stride_blocks(V, 256), 256, 0, as_stream(stream)>>>(vertices, V, spherical_harmonics, n,
+                                                                              camera_positions, B, out_colors);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_evaluate_spherical_harmonics_backward(const float* vertices, int64_t V, int32_t C, int32_t sh_degree,
+                                             const float* camera_positions, int32_t B, const float* out_colors,
+                                             const float* grad_colors, float* grad_spherical_harmonics,
+                                             mt_stream_t stream) {
+  MT_REQUIRE(V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+  MT_REQUIRE(C >= n);
+  if (V == 0 || B == 0) return MT_OK;
+  MT_REQUIRE(vertices && camera_positions && out_colors && grad_colors && grad_spherical_harmonics);
+  sh_backward_kernel<<<grid_stride_blocks(V, 128), 128, 0, as_stream(stream)>>>(
+      vertices, V, n, camera_positions, B, out_colors, grad_colors, grad_spherical_harmonics);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_bound_triangles(const float* xy, const float* depth, int64_t V, const int32_t* faces, int64_t F, int32_t B,
+                       int32_t tile_h, int32_t tile_w, int32_t rows, int32_t cols, float near_plane,
+                       int32_t* out_min, int32_t* out_max, int32_t* out_count, mt_stream_t stream) {
+  MT_REQUIRE(V >= 0 && F >= 0 && B >= 0 && tile_h > 0 && tile_w > 0 && rows >= 0 && cols >= 0);
+  if (F == 0 || B == 0) return MT_OK;
+  MT_REQUIRE(xy && depth && faces && out_min && out_max && out_count);
+  bound_kernel<<<grid_stride_blocks((int64_t)B * F, 256), 256, 0, as_stream(stream)>>>(
+      xy, depth, V, faces, F, B, tile_h, tile_w, rows, cols, near_plane, out_min, out_max, out_count);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces, int64_t F,
+                     const int32_t* shell_face_boundaries, int32_t S, const int32_t* tile_min,
+                     const int32_t* tile_max, const int64_t* offsets, int32_t B, int32_t grid_width,
+                     const int32_t* layout, int64_t K, int64_t* out_keys, int32_t* out_triangles,
+                     mt_stream_t stream) {
+  MT_REQUIRE(V >= 0 && F >= 0 && B >= 0 && S >= 0 && K >= 0 && layout);
+  KeyLayout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
+  MT_REQUIRE(layout_ok(L));
+  if (F == 0 || B == 0 || K == 0) return MT_OK;
+  MT_REQUIRE(depth && faces && tile_min && tile_max && offsets && out_keys && out_triangles);
+  MT_REQUIRE(S == 0 || shell_face_boundaries);
+  keys_kernel<<<grid_stride_blocks((int64_t)B * F, 256), 256, 0, as_stream(stream)>>>(
+      depth, V, faces, F, shell_face_boundaries, S, tile_min, tile_max, offsets, B, grid_width, L, K,
+      reinterpret_cast<uint64_t*>(out_keys), out_triangles);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K, const int32_t* layout, int32_t separate_shells,
+                       int32_t B, int32_t shell_dim, int64_t num_tiles, int64_t* out_boundaries,
+                       mt_stream_t stream) {
+  MT_REQUIRE(K >= 0 && B >= 0 && shell_dim >= 1 && num_tiles >= 0 && layout);
+  KeyLayout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
+  MT_REQUIRE(layout_ok(L));
+  const size_t bytes = (size_t)B * shell_dim * num_tiles * 2 * sizeof(int64_t);
+  if (bytes == 0) return MT_OK;
+  MT_REQUIRE(out_boundaries);
+  if (cudaMemsetAsync(out_boundaries, 0, bytes, as_stream(stream)) != cudaSuccess) return MT_ERR_CUDA;
+  if (K == 0) return MT_OK;
+  MT_REQUIRE(sorted_keys);
+  delineate_kernel<<<grid_stride_blocks(K, 256), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const uint64_t*>(sorted_keys), K, L, separate_shells, B, shell_dim, num_tiles,
+      out_boundaries);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+}  // extern "C"

@@ -607,4 +607,650 @@ void or_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, 
   }
 }
 
+
+// ===========================================================================
+// Rasterization (triangle_rasterization/*.slang, sort_keys.cu)
+// ===========================================================================
+}  // extern "C"
+
+namespace {
+
+// `int(x)` on the GPU: truncation toward zero, saturating, NaN -> 0.
+inline int f2i_rz(float x) {
+  if (std::isnan(x)) return 0;
+  if (x >= 2147483648.0f) return 2147483647;
+  if (x < -2147483648.0f) return (int)0x80000000u;
+  return (int)x;
+}
+
+inline float dot2(float ax, float ay, float bx, float by) { return std::fmaf(ay, by, ax * bx); }
+
+// intersect_and_composite.slang:65-106 / intersect.slang:14-49, evaluated in
+// full for every (pixel, triangle) pair as the reference does.
+inline void barycentric(float p1x, float p1y, float p2x, float p2y, float p3x, float p3y, float px, float py,
+                        float& u, float& v, float& w) {
+  const float e12x = p2x - p1x, e12y = p2y - p1y;
+  const float e23x = p3x - p2x, e23y = p3y - p2y;
+  const float e13x = p3x - p1x, e13y = p3y - p1y;
+  const float d_12_12 = dot2(e12x, e12y, e12x, e12y);
+  const float d_12_23 = dot2(e12x, e12y, e23x, e23y);
+  const float d_12_13 = dot2(e12x, e12y, e13x, e13y);
+  const float d_13_13 = dot2(e13x, e13y, e13x, e13y);
+  const float d_13_23 = dot2(e13x, e13y, e23x, e23y);
+  const float d_23_23 = dot2(e23x, e23y, e23x, e23y);
+  const float d_1x_12 = dot2(px - p1x, py - p1y, e12x, e12y);
+  const float d_1x_13 = dot2(px - p1x, py - p1y, e13x, e13y);
+  const float d_2x_12 = dot2(px - p2x, py - p2y, e12x, e12y);
+  const float d_2x_13 = dot2(px - p2x, py - p2y, e13x, e13y);
+  float denom = std::nanf("");  // the reference leaves it unset; only reachable with NaNs
+  if (std::fabs(d_12_13) <= std::fabs(d_12_23) && std::fabs(d_12_13) <= std::fabs(d_13_23)) {
+    denom = std::fmaf(d_12_12, d_13_13, -(d_12_13 * d_12_13));
+  } else if (std::fabs(d_12_23) <= std::fabs(d_12_13) && std::fabs(d_12_23) <= std::fabs(d_13_23)) {
+    denom = std::fmaf(d_12_12, d_23_23, -(d_12_23 * d_12_23));
+  } else if (std::fabs(d_13_23) <= std::fabs(d_12_13) && std::fabs(d_13_23) <= std::fabs(d_12_23)) {
+    denom = std::fmaf(d_13_13, d_23_23, -(d_13_23 * d_13_23));
+  }
+  v = std::fmaf(d_13_13, d_1x_12, -(d_12_13 * d_1x_13));
+  w = std::fmaf(d_12_12, d_1x_13, -(d_12_13 * d_1x_12));
+  u = std::fmaf(d_12_23, d_2x_13, -(d_13_23 * d_2x_12));
+  const float eps = 1e-8f;
+  v /= denom + eps;
+  w /= denom + eps;
+  u /= denom + eps;
+}
+
+// intersect_and_composite.slang:131-136 / intersect.slang:61-64.
+inline bool accepted(float u, float v, float w) {
+  const float sum = (u + v) + w;
+  if (std::isnan(u) || std::isnan(v) || std::isnan(w) || u < 0 || u > 1 || v < 0 || v > 1 || w < 0 || w > 1 ||
+      sum < 0.999f || sum > 1.001f)
+    return false;
+  return true;
+}
+
+inline float interp3(float u, float v, float w, float a, float b, float c) {
+  return std::fmaf(w, c, std::fmaf(v, b, u * a));
+}
+
+inline float sdf_to_cdf(float sdf, float s, float& e) {
+  e = std::exp(-sdf * s);
+  return 1.0f / (1.0f + e);
+}
+
+inline float alpha_raw(float oc, float ic) { return ((oc - ic) + 1e-5f) / (oc + 1e-5f); }
+inline float clamp01(float x) { return std::min(std::max(x, 0.0f), 1.0f); }
+
+const float kSH_C0 = 0.28209479177387814f;
+const float kSH_C1 = 0.4886025119029199f;
+const float kSH_C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+                         0.5462742152960396f};
+const float kSH_C3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f, 0.3731763325901154f,
+                         -0.4570457994644658f, 1.445305721320277f, -0.5900435899266435f};
+
+// evaluate_spherical_harmonics.slang:124-160 as basis functions of dir.
+inline void sh_basis(float x, float y, float z, int n, float* basis) {
+  basis[0] = kSH_C0;
+  if (n <= 1) return;
+  basis[1] = -kSH_C1 * y;
+  basis[2] = kSH_C1 * z;
+  basis[3] = -kSH_C1 * x;
+  if (n <= 4) return;
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  basis[4] = kSH_C2[0] * xy;
+  basis[5] = kSH_C2[1] * yz;
+  basis[6] = kSH_C2[2] * (2.0f * zz - xx - yy);
+  basis[7] = kSH_C2[3] * xz;
+  basis[8] = kSH_C2[4] * (xx - yy);
+  if (n <= 9) return;
+  basis[9] = kSH_C3[0] * y * (3.0f * xx - yy);
+  basis[10] = kSH_C3[1] * xy * z;
+  basis[11] = kSH_C3[2] * y * (4.0f * zz - xx - yy);
+  basis[12] = kSH_C3[3] * z * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+  basis[13] = kSH_C3[4] * x * (4.0f * zz - xx - yy);
+  basis[14] = kSH_C3[5] * z * (xx - yy);
+  basis[15] = kSH_C3[6] * x * (xx - 3.0f * yy);
+}
+
+inline void view_dir(const float* v, const float* cam, float& x, float& y, float& z) {
+  const float dx = v[0] - cam[0], dy = v[1] - cam[1], dz = v[2] - cam[2];
+  const float len = std::sqrt(dx * dx + dy * dy + dz * dz);
+  x = dx / len;
+  y = dy / len;
+  z = dz / len;
+}
+
+struct Layout {
+  int cam_off, cam_len, shell_off, shell_len, tile_off, tile_len, depth_off;
+};
+inline uint64_t fmask(int len) { return (uint64_t)((1u << len) - 1u); }
+
+}  // namespace
+
+extern "C" {
+
+// torch.inverse(extrinsics)[:, :3, 3] (evaluate_spherical_harmonics.py:38),
+// Gauss-Jordan with partial pivoting in double precision.
+void or_camera_positions(const float* ext, int B, float* out) {
+  for (int b = 0; b < B; ++b) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? (double)ext[16 * b + 4 * r + c] : (c - 4 == r ? 1.0 : 0.0);
+    for (int c = 0; c < 4; ++c) {
+      int piv = c;
+      for (int r = c + 1; r < 4; ++r)
+        if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+      for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+      const double d = a[c][c];
+      for (int k = 0; k < 8; ++k) a[c][k] /= d;
+      for (int r = 0; r < 4; ++r)
+        if (r != c) {
+          const double f = a[r][c];
+          for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+        }
+    }
+    for (int r = 0; r < 3; ++r) out[3 * b + r] = (float)a[r][4 + 3];
+  }
+}
+
+// project_vertices.slang:51-92.
+void or_project_vertices(const float* verts, int64_t V, const float* ext, const float* intr, int B, float* out_xy,
+                         float* out_depth) {
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < V; ++v) {
+    const float x = verts[3 * v], y = verts[3 * v + 1], z = verts[3 * v + 2];
+    for (int b = 0; b < B; ++b) {
+      const float* E = ext + 16 * b;
+      const float* K = intr + 9 * b;
+      float cam[3];
+      for (int r = 0; r < 3; ++r)
+        cam[r] = std::fmaf(E[4 * r + 3], 1.0f, std::fmaf(E[4 * r + 2], z, std::fmaf(E[4 * r + 1], y, E[4 * r] * x)));
+      const float kx = std::fmaf(K[2], cam[2], std::fmaf(K[1], cam[1], K[0] * cam[0]));
+      const float ky = std::fmaf(K[5], cam[2], std::fmaf(K[4], cam[1], K[3] * cam[0]));
+      const int64_t o = (int64_t)b * V + v;
+      out_xy[2 * o] = kx / cam[2];
+      out_xy[2 * o + 1] = ky / cam[2];
+      out_depth[o] = cam[2];
+    }
+  }
+}
+
+// evaluate_spherical_harmonics.slang:187-228 (forward).
+void or_evaluate_sh(const float* verts, int64_t V, const float* sh, int sh_degree, const float* campos, int B,
+                    float* out) {
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < V; ++v) {
+    for (int b = 0; b < B; ++b) {
+      float x, y, z, basis[16];
+      view_dir(verts + 3 * v, campos + 3 * b, x, y, z);
+      sh_basis(x, y, z, n, basis);
+      for (int c = 0; c < 3; ++c) {
+        float rgb = 0.f;
+        for (int k = 0; k < n; ++k) rgb += basis[k] * sh[((int64_t)k * V + v) * 3 + c];
+        out[((int64_t)b * V + v) * 3 + c] = std::max(rgb + 0.5f, 0.0f);
+      }
+    }
+  }
+}
+
+// evaluate_spherical_harmonics.slang:230-270 (backward, to the SH only).
+void or_evaluate_sh_backward(const float* verts, int64_t V, int sh_degree, const float* campos, int B,
+                             const float* colors, const float* dcolors, float* dsh) {
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < V; ++v) {
+    for (int b = 0; b < B; ++b) {
+      float x, y, z, basis[16];
+      view_dir(verts + 3 * v, campos + 3 * b, x, y, z);
+      sh_basis(x, y, z, n, basis);
+      for (int c = 0; c < 3; ++c) {
+        const int64_t o = ((int64_t)b * V + v) * 3 + c;
+        const float g = colors[o] > 0.0f ? dcolors[o] : 0.0f;
+        for (int k = 0; k < n; ++k) dsh[((int64_t)k * V + v) * 3 + c] += basis[k] * g;
+      }
+    }
+  }
+}
+
+// bound_triangles.slang:62-192.
+void or_bound_triangles(const float* xy, const float* depth, int64_t V, const int32_t* faces, int64_t F, int B,
+                        int tile_h, int tile_w, int rows, int cols, float near, int32_t* out_min, int32_t* out_max,
+                        int32_t* out_count) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)B * F; ++i) {
+    const int b = (int)(i / F);
+    const int64_t f = i % F;
+    const int64_t base = (int64_t)b * V;
+    const int64_t ia = base + faces[3 * f], ib = base + faces[3 * f + 1], ic = base + faces[3 * f + 2];
+    const float ax = xy[2 * ia], ay = xy[2 * ia + 1], bx = xy[2 * ib], by = xy[2 * ib + 1];
+    const float cx = xy[2 * ic], cy = xy[2 * ic + 1];
+    int r0 = 0, r1 = 0, c0 = 0, c1 = 0;
+    const float check = std::fmaf(bx - ax, cy - ay, -((by - ay) * (cx - ax)));
+    const float min_depth = std::fmin(std::fmin(depth[ia], depth[ib]), depth[ic]);
+    if (!(check < 0) && !(min_depth < near)) {
+      const float ymin = std::fmin(std::fmin(ay, by), cy), ymax = std::fmax(std::fmax(ay, by), cy);
+      const float xmin = std::fmin(std::fmin(ax, bx), cx), xmax = std::fmax(std::fmax(ax, bx), cx);
+      r0 = std::clamp(f2i_rz(ymin) / tile_h, 0, rows);
+      r1 = std::clamp(f2i_rz(std::ceil(ymax / (float)tile_h)), 0, rows);
+      c0 = std::clamp(f2i_rz(xmin) / tile_w, 0, cols);
+      c1 = std::clamp(f2i_rz(std::ceil(xmax / (float)tile_w)), 0, cols);
+    }
+    out_min[2 * i] = r0;
+    out_min[2 * i + 1] = c0;
+    out_max[2 * i] = r1;
+    out_max[2 * i + 1] = c1;
+    out_count[i] = (r1 - r0) * (c1 - c0);
+  }
+}
+
+// generate_keys.slang:4-68 with keys.slang:6-22. offsets: inclusive int64.
+void or_generate_keys(const float* depth, int64_t V, const int32_t* faces, int64_t F, const int32_t* sfb, int S,
+                      const int32_t* tmin, const int32_t* tmax, const int64_t* offsets, int B, int grid_width,
+                      const int32_t* layout, int64_t* out_keys, int32_t* out_tri) {
+  const Layout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < F; ++f) {
+    uint32_t shell = 0;
+    for (; shell < (uint32_t)S; ++shell)
+      if (f < sfb[shell]) break;
+    for (int b = 0; b < B; ++b) {
+      const int64_t oi = (int64_t)b * F + f;
+      int64_t key_index = oi == 0 ? 0 : offsets[oi - 1];
+      const int r0 = tmin[2 * oi], c0 = tmin[2 * oi + 1], r1 = tmax[2 * oi], c1 = tmax[2 * oi + 1];
+      const int64_t base = (int64_t)b * V;
+      const float mean = ((depth[base + faces[3 * f]] + depth[base + faces[3 * f + 1]]) + depth[base + faces[3 * f + 2]]) / 3.f;
+      uint32_t bits;
+      std::memcpy(&bits, &mean, 4);
+      for (int row = r0; row < r1; ++row)
+        for (int col = c0; col < c1; ++col) {
+          const uint32_t tile = (uint32_t)(row * grid_width + col);
+          const uint64_t key = (((uint64_t)b & fmask(L.cam_len)) << L.cam_off) |
+                               (((uint64_t)shell & fmask(L.shell_len)) << L.shell_off) |
+                               (((uint64_t)tile & fmask(L.tile_len)) << L.tile_off) | ((uint64_t)bits << L.depth_off);
+          out_keys[key_index] = (int64_t)key;
+          out_tri[key_index] = (int32_t)f;
+          key_index++;
+        }
+    }
+  }
+}
+
+// cub::DeviceRadixSort::SortPairs on signed int64 keys, bits [0, 64)
+// (sort_keys.cu:241-267): a stable sort by signed key.
+void or_sort_pairs(const int64_t* keys, const int32_t* vals, int64_t n, int64_t* out_keys, int32_t* out_vals) {
+  std::vector<int64_t> idx((size_t)n);
+  for (int64_t i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) { return keys[a] < keys[b]; });
+  for (int64_t i = 0; i < n; ++i) {
+    out_keys[i] = keys[idx[i]];
+    out_vals[i] = vals[idx[i]];
+  }
+}
+
+// delineate_tiles.slang:14-58 (output zero-filled first, delineate_tiles.py:40).
+void or_delineate_tiles(const int64_t* keys, int64_t K, const int32_t* layout, int separate_shells, int B, int Sd,
+                        int64_t T, int64_t* out) {
+  const Layout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
+  std::memset(out, 0, sizeof(int64_t) * 2 * (size_t)B * Sd * T);
+  auto index_of = [&](uint64_t key) {
+    const int64_t cam = (int64_t)((key >> L.cam_off) & fmask(L.cam_len));
+    const int64_t sh = separate_shells ? (int64_t)((key >> L.shell_off) & fmask(L.shell_len)) : 0;
+    const int64_t tile = (int64_t)((key >> L.tile_off) & fmask(L.tile_len));
+    return (cam * Sd + sh) * T + tile;
+  };
+  for (int64_t i = 0; i < K; ++i) {
+    const int64_t here = index_of((uint64_t)keys[i]);
+    if (i > 0) {
+      const int64_t last = index_of((uint64_t)keys[i - 1]);
+      if (here != last) {
+        out[2 * last + 1] = i;
+        out[2 * here] = i;
+      }
+    }
+    if (i == K - 1) out[2 * here + 1] = K;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// intersect_and_composite.slang:224-339 (forward) and :341-564 (backward).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+struct FusedScene {
+  const float* xy;
+  const float* colors;
+  const float* sdf;
+  int64_t V;
+  const int32_t* faces;
+  float s;
+  const int64_t* keys;
+  const int32_t* tri;
+  const int64_t* bounds;
+  int B, S, rows, cols, th, tw, H, W, shell_off, shell_len;
+};
+
+struct Hit {
+  int64_t k;  // position in the sorted list
+  int32_t f;
+  int shell;
+  float u, v, w;
+};
+
+// All hits of one pixel, in compositing order (the shell-monotone walk).
+inline void walk(const FusedScene& a, int cam, int64_t tile, float px, float py, std::vector<Hit>& hits) {
+  hits.clear();
+  const int64_t T = (int64_t)a.rows * a.cols;
+  const int64_t start = a.bounds[2 * (cam * T + tile)], end = a.bounds[2 * (cam * T + tile) + 1];
+  int last_shell = -1;
+  const float* xy = a.xy + (int64_t)cam * a.V * 2;
+  for (int64_t k = start; k < end; ++k) {
+    const int shell = (int)(((uint64_t)a.keys[k] >> a.shell_off) & fmask(a.shell_len));
+    if (shell <= last_shell) continue;
+    const int32_t f = a.tri[k];
+    const int32_t ia = a.faces[3 * (int64_t)f], ib = a.faces[3 * (int64_t)f + 1], ic = a.faces[3 * (int64_t)f + 2];
+    float u, v, w;
+    barycentric(xy[2 * ia], xy[2 * ia + 1], xy[2 * ib], xy[2 * ib + 1], xy[2 * ic], xy[2 * ic + 1], px, py, u, v, w);
+    if (!accepted(u, v, w)) continue;
+    hits.push_back({k, f, shell, u, v, w});
+    last_shell = shell;
+    if (last_shell == a.S - 1) break;
+  }
+}
+
+inline void sample(const FusedScene& a, int cam, const Hit& h, float* rgb, float& sdf) {
+  const int32_t ia = a.faces[3 * (int64_t)h.f], ib = a.faces[3 * (int64_t)h.f + 1], ic = a.faces[3 * (int64_t)h.f + 2];
+  const float* col = a.colors + (int64_t)cam * a.V * 3;
+  for (int c = 0; c < 3; ++c) rgb[c] = interp3(h.u, h.v, h.w, col[3 * ia + c], col[3 * ib + c], col[3 * ic + c]);
+  sdf = interp3(h.u, h.v, h.w, a.sdf[ia], a.sdf[ib], a.sdf[ic]);
+}
+}  // namespace
+
+extern "C" {
+
+void or_intersect_and_composite_forward(const float* xy, const float* colors, const float* sdf, int64_t V,
+                                        const int32_t* faces, float sharpness, const int64_t* keys,
+                                        const int32_t* tri, const int64_t* bounds, int B, int S, int rows, int cols,
+                                        int th, int tw, int H, int W, int shell_off, int shell_len, float* out) {
+  const FusedScene a{xy, colors, sdf, V, faces, sharpness, keys, tri, bounds, B, S, rows, cols, th, tw, H, W,
+                     shell_off, shell_len};
+  const int64_t T = (int64_t)rows * cols;
+#pragma omp parallel
+  {
+    std::vector<Hit> hits;
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t bt = 0; bt < B * T; ++bt) {
+      const int cam = (int)(bt / T);
+      const int64_t tile = bt % T;
+      for (int ty = 0; ty < th; ++ty)
+        for (int tx = 0; tx < tw; ++tx) {
+          const int px = (int)(tile % cols) * tw + tx, py = (int)(tile / cols) * th + ty;
+          if (px >= W || py >= H) continue;
+          walk(a, cam, tile, (float)px + 0.5f, (float)py + 0.5f, hits);
+          float acc[3] = {0.f, 0.f, 0.f}, Tr = 1.0f, e;
+          float outer_cdf = sdf_to_cdf(1e10f, sharpness, e);
+          for (const Hit& h : hits) {
+            float rgb[3], s_in;
+            sample(a, cam, h, rgb, s_in);
+            const float inner_cdf = sdf_to_cdf(s_in, sharpness, e);
+            const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
+            for (int c = 0; c < 3; ++c) acc[c] = std::fmaf(rgb[c] * Tr, alpha, acc[c]);
+            Tr = Tr * (1.0f - alpha);
+            outer_cdf = inner_cdf;
+          }
+          const int64_t plane = (int64_t)H * W;
+          float* o = out + (int64_t)cam * 4 * plane + (int64_t)py * W + px;
+          o[0] = acc[0];
+          o[plane] = acc[1];
+          o[2 * plane] = acc[2];
+          o[3 * plane] = Tr;
+        }
+    }
+  }
+}
+
+// exact = 0: the reference's routing (outer hit's deferred gradient scattered
+// with the current hit's weights); exact = 1: the true adjoint.
+void or_intersect_and_composite_backward(const float* xy, const float* colors, const float* sdf, int64_t V,
+                                         const int32_t* faces, float sharpness, const int64_t* keys,
+                                         const int32_t* tri, const int64_t* bounds, int B, int S, int rows,
+                                         int cols, int th, int tw, int H, int W, int shell_off, int shell_len,
+                                         const float* out, const float* grad_out, float* grad_colors,
+                                         float* grad_sdf, float* grad_sharpness, int exact) {
+  const FusedScene a{xy, colors, sdf, V, faces, sharpness, keys, tri, bounds, B, S, rows, cols, th, tw, H, W,
+                     shell_off, shell_len};
+  const int64_t T = (int64_t)rows * cols;
+  const float s = sharpness;
+  double d_sharp_total = 0.0;
+#pragma omp parallel reduction(+ : d_sharp_total)
+  {
+    std::vector<Hit> hits;
+    auto scatter = [&](int cam, int32_t f, float u, float v, float w, const float* drgb, float dsdf) {
+      const int32_t id[3] = {faces[3 * (int64_t)f], faces[3 * (int64_t)f + 1], faces[3 * (int64_t)f + 2]};
+      const float wt[3] = {u, v, w};
+      for (int q = 0; q < 3; ++q) {
+        for (int c = 0; c < 3; ++c) {
+#pragma omp atomic
+          grad_colors[((int64_t)cam * V + id[q]) * 3 + c] += wt[q] * drgb[c];
+        }
+#pragma omp atomic
+        grad_sdf[id[q]] += wt[q] * dsdf;
+      }
+    };
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t bt = 0; bt < B * T; ++bt) {
+      const int cam = (int)(bt / T);
+      const int64_t tile = bt % T;
+      for (int ty = 0; ty < th; ++ty)
+        for (int tx = 0; tx < tw; ++tx) {
+          const int px = (int)(tile % cols) * tw + tx, py = (int)(tile / cols) * th + ty;
+          if (px >= W || py >= H) continue;
+          walk(a, cam, tile, (float)px + 0.5f, (float)py + 0.5f, hits);
+          const int64_t plane = (int64_t)H * W;
+          const int64_t o = (int64_t)cam * 4 * plane + (int64_t)py * W + px;
+          float final_rgb[3], dL[3];
+          for (int c = 0; c < 3; ++c) {
+            final_rgb[c] = out[o + c * plane];
+            dL[c] = grad_out[o + c * plane];
+          }
+          const float final_T = out[o + 3 * plane], dLT = grad_out[o + 3 * plane];
+          float acc[3] = {0.f, 0.f, 0.f}, Tr = 1.0f, e_out;
+          float outer_cdf = sdf_to_cdf(1e10f, s, e_out), outer_sdf = 1e10f;
+          float dp_rgb[3] = {0.f, 0.f, 0.f}, dp_sdf = 0.f;
+          const Hit* prev = nullptr;
+          for (const Hit& h : hits) {
+            float rgb[3], s_in, e_in;
+            sample(a, cam, h, rgb, s_in);
+            const float inner_cdf = sdf_to_cdf(s_in, s, e_in);
+            const float raw = alpha_raw(outer_cdf, inner_cdf);
+            const float alpha = clamp01(raw);
+            const float weight = alpha * Tr;
+            const float inv = 1.0f / ((1.0f - alpha) + 1e-6f);
+            float d_color[3], d_alpha = 0.f;
+            for (int c = 0; c < 3; ++c) {
+              acc[c] = std::fmaf(weight, rgb[c], acc[c]);
+              const float suffix = final_rgb[c] - acc[c];
+              d_color[c] = weight * dL[c];
+              d_alpha += dL[c] * (Tr * rgb[c] - suffix * inv);
+            }
+            d_alpha += -dLT * final_T * inv;
+            const float d_raw = (raw > 0.0f && raw < 1.0f) ? d_alpha : 0.0f;
+            const float den = outer_cdf + 1e-5f, num = (outer_cdf - inner_cdf) + 1e-5f;
+            const float d_num = d_raw / den, d_den = -d_raw * num / (den * den);
+            const float d_oc = d_num + d_den, d_ic = -d_num;
+            const float ki = inner_cdf * inner_cdf * e_in, ko = outer_cdf * outer_cdf * e_out;
+            d_sharp_total += (double)(d_ic * ki * s_in + d_oc * ko * outer_sdf);
+            if (prev) {
+              dp_sdf += d_oc * ko * s;
+              if (exact)
+                scatter(cam, prev->f, prev->u, prev->v, prev->w, dp_rgb, dp_sdf);
+              else
+                scatter(cam, prev->f, h.u, h.v, h.w, dp_rgb, dp_sdf);
+            }
+            for (int c = 0; c < 3; ++c) dp_rgb[c] = d_color[c];
+            dp_sdf = d_ic * ki * s;
+            prev = &h;
+            Tr = Tr * (1.0f - alpha);
+            outer_cdf = inner_cdf;
+            outer_sdf = s_in;
+            e_out = e_in;
+          }
+          if (prev) scatter(cam, prev->f, prev->u, prev->v, prev->w, dp_rgb, dp_sdf);
+        }
+    }
+  }
+  grad_sharpness[0] += (float)d_sharp_total;
+}
+
+// ---------------------------------------------------------------------------
+// Explicit mode: intersect.slang:86-182, interpolate.slang:19-76,
+// composite.slang:60-218.
+// ---------------------------------------------------------------------------
+void or_intersect(const float* xy, int64_t V, const int32_t* faces, const int32_t* tri, const int64_t* bounds, int B,
+                  int S, int rows, int cols, int th, int tw, int H, int W, float* out_uv, int32_t* out_index) {
+  const int64_t T = (int64_t)rows * cols;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t bt = 0; bt < (int64_t)B * S * T; ++bt) {
+    const int64_t batch = bt / T, tile = bt % T;
+    const int cam = (int)(batch / S);
+    const float* p = xy + (int64_t)cam * V * 2;
+    const int64_t start = bounds[2 * bt], end = bounds[2 * bt + 1];
+    for (int ty = 0; ty < th; ++ty)
+      for (int tx = 0; tx < tw; ++tx) {
+        const int px = (int)(tile % cols) * tw + tx, py = (int)(tile / cols) * th + ty;
+        if (px >= W || py >= H) continue;
+        const int64_t o = (batch * H + py) * W + px;
+        out_uv[2 * o] = 0.f;
+        out_uv[2 * o + 1] = 0.f;
+        out_index[o] = -1;
+        for (int64_t k = start; k < end; ++k) {
+          const int32_t f = tri[k];
+          const int32_t ia = faces[3 * (int64_t)f], ib = faces[3 * (int64_t)f + 1], ic = faces[3 * (int64_t)f + 2];
+          float u, v, w;
+          barycentric(p[2 * ia], p[2 * ia + 1], p[2 * ib], p[2 * ib + 1], p[2 * ic], p[2 * ic + 1], (float)px + 0.5f,
+                      (float)py + 0.5f, u, v, w);
+          if (!accepted(u, v, w)) continue;
+          out_uv[2 * o] = u;
+          out_uv[2 * o + 1] = v;
+          out_index[o] = f;
+          break;
+        }
+      }
+  }
+}
+
+void or_interpolate(const float* uv, const int32_t* index, int B, int S, int H, int W, const int32_t* faces,
+                    const float* sdf, const float* colors, int64_t V, float* out_sdf, float* out_colors) {
+  const int64_t HW = (int64_t)H * W, total = (int64_t)B * S * HW;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < total; ++i) {
+    const int32_t f = index[i];
+    if (f < 0) {
+      out_sdf[i] = 0.f;
+      for (int c = 0; c < 3; ++c) out_colors[3 * i + c] = 0.f;
+      continue;
+    }
+    const int64_t b = (i / HW) / S;
+    const float u = uv[2 * i], v = uv[2 * i + 1], w = (1.0f - u) - v;
+    const int32_t ia = faces[3 * (int64_t)f], ib = faces[3 * (int64_t)f + 1], ic = faces[3 * (int64_t)f + 2];
+    const float* col = colors + b * V * 3;
+    for (int c = 0; c < 3; ++c) out_colors[3 * i + c] = interp3(u, v, w, col[3 * ia + c], col[3 * ib + c], col[3 * ic + c]);
+    out_sdf[i] = interp3(u, v, w, sdf[ia], sdf[ib], sdf[ic]);
+  }
+}
+
+void or_interpolate_backward(const float* uv, const int32_t* index, int B, int S, int H, int W, const int32_t* faces,
+                             int64_t V, const float* gsdf_out, const float* gcol_out, float* gsdf, float* gcol) {
+  const int64_t HW = (int64_t)H * W, total = (int64_t)B * S * HW;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < total; ++i) {
+    const int32_t f = index[i];
+    if (f < 0) continue;
+    const int64_t b = (i / HW) / S;
+    const float u = uv[2 * i], v = uv[2 * i + 1], w = (1.0f - u) - v;
+    const int32_t id[3] = {faces[3 * (int64_t)f], faces[3 * (int64_t)f + 1], faces[3 * (int64_t)f + 2]};
+    const float wt[3] = {u, v, w};
+    for (int q = 0; q < 3; ++q) {
+      if (gsdf_out) {
+#pragma omp atomic
+        gsdf[id[q]] += wt[q] * gsdf_out[i];
+      }
+      if (gcol_out)
+        for (int c = 0; c < 3; ++c) {
+#pragma omp atomic
+          gcol[(b * V + id[q]) * 3 + c] += wt[q] * gcol_out[3 * i + c];
+        }
+    }
+  }
+}
+
+void or_composite(const float* sdf, const float* colors, const uint8_t* mask, int64_t P, int S, float sharpness,
+                  float* out_colors, float* out_T) {
+#pragma omp parallel for schedule(static)
+  for (int64_t p = 0; p < P; ++p) {
+    float acc[3] = {0.f, 0.f, 0.f}, Tr = 1.0f, e;
+    float outer_cdf = sdf_to_cdf(1e10f, sharpness, e);
+    for (int l = 0; l < S; ++l) {
+      if (!mask[p * S + l]) continue;
+      const float inner_cdf = sdf_to_cdf(sdf[p * S + l], sharpness, e);
+      const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
+      for (int c = 0; c < 3; ++c) acc[c] = std::fmaf(colors[(p * S + l) * 3 + c] * Tr, alpha, acc[c]);
+      Tr = Tr * (1.0f - alpha);
+      outer_cdf = inner_cdf;
+    }
+    for (int c = 0; c < 3; ++c) out_colors[3 * p + c] = acc[c];
+    out_T[p] = Tr;
+  }
+}
+
+void or_composite_backward(const float* sdf, const float* colors, const uint8_t* mask, int64_t P, int S,
+                           float sharpness, const float* out_colors, const float* out_T, const float* gcol_out,
+                           const float* gT_out, float* gsdf, float* gcol, float* gsharp, int exact) {
+  const float s = sharpness;
+  double total = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : total)
+  for (int64_t p = 0; p < P; ++p) {
+    const float dL[3] = {gcol_out ? gcol_out[3 * p] : 0.f, gcol_out ? gcol_out[3 * p + 1] : 0.f,
+                         gcol_out ? gcol_out[3 * p + 2] : 0.f};
+    const float dLT = gT_out ? gT_out[p] : 0.f;
+    float acc[3] = {0.f, 0.f, 0.f}, Tr = 1.0f, e_out;
+    float outer_cdf = sdf_to_cdf(1e10f, s, e_out), outer_sdf = 1e10f, d_partial = 0.f;
+    int prev_shell = -1;
+    for (int l = 0; l < S; ++l) {
+      if (!mask[p * S + l]) continue;
+      const float inner = sdf[p * S + l];
+      float e_in;
+      const float inner_cdf = sdf_to_cdf(inner, s, e_in);
+      const float raw = alpha_raw(outer_cdf, inner_cdf), alpha = clamp01(raw);
+      const float weight = alpha * Tr, inv = 1.0f / ((1.0f - alpha) + 1e-6f);
+      float d_alpha = 0.f;
+      for (int c = 0; c < 3; ++c) {
+        const float col = colors[(p * S + l) * 3 + c];
+        acc[c] = std::fmaf(weight, col, acc[c]);
+        d_alpha += dL[c] * (Tr * col - (out_colors[3 * p + c] - acc[c]) * inv);
+        gcol[(p * S + l) * 3 + c] += weight * dL[c];
+      }
+      d_alpha += -dLT * out_T[p] * inv;
+      const float d_raw = (raw > 0.0f && raw < 1.0f) ? d_alpha : 0.0f;
+      const float den = outer_cdf + 1e-5f, num = (outer_cdf - inner_cdf) + 1e-5f;
+      const float d_num = d_raw / den, d_den = -d_raw * num / (den * den);
+      const float d_oc = d_num + d_den, d_ic = -d_num;
+      const float ki = inner_cdf * inner_cdf * e_in, ko = outer_cdf * outer_cdf * e_out;
+      total += (double)(d_ic * ki * inner + d_oc * ko * outer_sdf);
+      if (prev_shell >= 0) {
+        d_partial += d_oc * ko * s;
+        gsdf[p * S + (exact ? prev_shell : l - 1)] += d_partial;
+      }
+      d_partial = d_ic * ki * s;
+      Tr = Tr * (1.0f - alpha);
+      outer_cdf = inner_cdf;
+      outer_sdf = inner;
+      e_out = e_in;
+      prev_shell = l;
+    }
+    if (prev_shell >= 0) gsdf[p * S + (exact ? prev_shell : S - 1)] += d_partial;
+  }
+  gsharp[0] += (float)total;
+}
+
 }  // extern "C"

@@ -233,3 +233,251 @@ def create_triangle_vertices_backward(sdf, sh_shape, lower, level_sets, vertex_o
         _p(out_v), _p(out_d), _p(out_sh),
     )
     return out_v, out_d, out_sh
+
+
+# ---------------------------------------------------------------------------
+# Rasterization
+# ---------------------------------------------------------------------------
+_SIGNATURES.update({
+    "or_camera_positions": (None, [P, I32, P]),
+    "or_project_vertices": (None, [P, I64, P, P, I32, P, P]),
+    "or_evaluate_sh": (None, [P, I64, P, I32, P, I32, P]),
+    "or_evaluate_sh_backward": (None, [P, I64, I32, P, I32, P, P, P]),
+    "or_bound_triangles": (None, [P, P, I64, P, I64, I32, I32, I32, I32, I32, F32, P, P, P]),
+    "or_generate_keys": (None, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, P, P]),
+    "or_sort_pairs": (None, [P, P, I64, P, P]),
+    "or_delineate_tiles": (None, [P, I64, P, I32, I32, I32, I64, P]),
+    "or_intersect_and_composite_forward": (
+        None, [P, P, P, I64, P, F32, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P]),
+    "or_intersect_and_composite_backward": (
+        None, [P, P, P, I64, P, F32, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P, P,
+               I32]),
+    "or_intersect": (None, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P]),
+    "or_interpolate": (None, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P]),
+    "or_interpolate_backward": (None, [P, P, I32, I32, I32, I32, P, I64, P, P, P, P]),
+    "or_composite": (None, [P, P, P, I64, I32, F32, P, P]),
+    "or_composite_backward": (None, [P, P, P, I64, I32, F32, P, P, P, P, P, P, P, I32]),
+})
+
+
+def key_layout(key_defines) -> np.ndarray:
+    d = dict(key_defines)
+    return np.array([d["CAMERA_BIT_OFFSET"], d["CAMERA_BIT_LENGTH"], d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"],
+                     d["TILE_BIT_OFFSET"], d["TILE_BIT_LENGTH"], d["DEPTH_BIT_OFFSET"]], np.int32)
+
+
+def fused_key_defines(camera=6, shell=6, tile=20):
+    """Fused layout, MSB first: camera | tile | depth | shell (__init__.py:207-212)."""
+    return (("SHELL_BIT_OFFSET", 0), ("SHELL_BIT_LENGTH", shell), ("DEPTH_BIT_OFFSET", shell),
+            ("DEPTH_BIT_LENGTH", 32), ("TILE_BIT_OFFSET", shell + 32), ("TILE_BIT_LENGTH", tile),
+            ("CAMERA_BIT_OFFSET", shell + 32 + tile), ("CAMERA_BIT_LENGTH", camera))
+
+
+def explicit_key_defines(camera=6, shell=6, tile=20):
+    """Explicit layout, MSB first: camera | shell | tile | depth (__init__.py:53-58)."""
+    return (("DEPTH_BIT_OFFSET", 0), ("DEPTH_BIT_LENGTH", 32), ("TILE_BIT_OFFSET", 32), ("TILE_BIT_LENGTH", tile),
+            ("SHELL_BIT_OFFSET", 32 + tile), ("SHELL_BIT_LENGTH", shell), ("CAMERA_BIT_OFFSET", 32 + tile + shell),
+            ("CAMERA_BIT_LENGTH", camera))
+
+
+def camera_positions(extrinsics) -> np.ndarray:
+    e = _c(extrinsics, np.float32)
+    out = np.empty((e.shape[0], 3), np.float32)
+    lib().or_camera_positions(_p(e), e.shape[0], _p(out))
+    return out
+
+
+def project_vertices(vertices, extrinsics, intrinsics):
+    v, e, k = _c(vertices, np.float32), _c(extrinsics, np.float32), _c(intrinsics, np.float32)
+    b = e.shape[0]
+    xy = np.empty((b, v.shape[0], 2), np.float32)
+    depth = np.empty((b, v.shape[0]), np.float32)
+    lib().or_project_vertices(_p(v), v.shape[0], _p(e), _p(k), b, _p(xy), _p(depth))
+    return xy, depth
+
+
+def evaluate_spherical_harmonics(vertices, sh, extrinsics, sh_degree):
+    v, sh = _c(vertices, np.float32), _c(sh, np.float32)
+    campos = camera_positions(extrinsics)
+    b = campos.shape[0]
+    out = np.empty((b, v.shape[0], 3), np.float32)
+    lib().or_evaluate_sh(_p(v), v.shape[0], _p(sh), sh_degree, _p(campos), b, _p(out))
+    return out
+
+
+def evaluate_spherical_harmonics_backward(vertices, sh_shape, extrinsics, sh_degree, colors, grad_colors):
+    v = _c(vertices, np.float32)
+    campos = camera_positions(extrinsics)
+    out = np.zeros(sh_shape, np.float32)
+    lib().or_evaluate_sh_backward(_p(v), v.shape[0], sh_degree, _p(campos), campos.shape[0],
+                                  _p(_c(colors, np.float32)), _p(_c(grad_colors, np.float32)), _p(out))
+    return out
+
+
+def bound_triangles(xy, depth, faces, tile_shape, grid_shape, near_plane):
+    xy, depth, faces = _c(xy, np.float32), _c(depth, np.float32), _c(faces, np.int32)
+    b, v, _ = xy.shape
+    f = faces.shape[0]
+    tmin = np.empty((b, f, 2), np.int32)
+    tmax = np.empty((b, f, 2), np.int32)
+    count = np.empty((b, f), np.int32)
+    lib().or_bound_triangles(_p(xy), _p(depth), v, _p(faces), f, b, tile_shape[0], tile_shape[1], grid_shape[0],
+                             grid_shape[1], near_plane, _p(tmin), _p(tmax), _p(count))
+    return tmin, tmax, count
+
+
+def generate_keys(depth, faces, shell_face_boundaries, tmin, tmax, count, grid_width, key_defines):
+    depth, faces = _c(depth, np.float32), _c(faces, np.int32)
+    sfb = _c(shell_face_boundaries, np.int32)
+    offsets = inclusive_cumsum_i64(count.reshape(-1))
+    k = int(offsets[-1]) if offsets.size else 0
+    keys = np.zeros((k,), np.int64)
+    tri = np.zeros((k,), np.int32)
+    b, v = depth.shape
+    lib().or_generate_keys(_p(depth), v, _p(faces), faces.shape[0], _p(sfb), sfb.shape[0], _p(_c(tmin, np.int32)),
+                           _p(_c(tmax, np.int32)), _p(offsets), b, grid_width, _p(key_layout(key_defines)),
+                           _p(keys), _p(tri))
+    return keys, tri
+
+
+def sort_pairs(keys, tri):
+    keys, tri = _c(keys, np.int64), _c(tri, np.int32)
+    ok, ot = np.empty_like(keys), np.empty_like(tri)
+    lib().or_sort_pairs(_p(keys), _p(tri), keys.size, _p(ok), _p(ot))
+    return ok, ot
+
+
+def delineate_tiles(sorted_keys, key_defines, separate_shells, num_cameras, num_shells, num_tiles):
+    keys = _c(sorted_keys, np.int64)
+    sd = num_shells if separate_shells else 1
+    out = np.empty((num_cameras, sd, num_tiles, 2), np.int64)
+    lib().or_delineate_tiles(_p(keys), keys.size, _p(key_layout(key_defines)), int(separate_shells), num_cameras, sd,
+                             num_tiles, _p(out))
+    return out
+
+
+class FusedRender(NamedTuple):
+    xy: np.ndarray
+    depth: np.ndarray
+    tile_min: np.ndarray
+    tile_max: np.ndarray
+    counts: np.ndarray
+    keys: np.ndarray
+    tri: np.ndarray
+    sorted_keys: np.ndarray
+    sorted_tri: np.ndarray
+    tile_boundaries: np.ndarray
+    colors: np.ndarray
+    raw: np.ndarray  # [B, 4, H, W] compositor output before the epilogue
+    image: np.ndarray  # [B, 3, H, W] after background / clip
+
+
+def intersect_and_composite(xy, colors, sdf, faces, sharpness, sorted_keys, sorted_tri, tile_boundaries, num_shells,
+                            tile_shape, image_shape, key_defines):
+    xy, colors, sdf, faces = _c(xy, np.float32), _c(colors, np.float32), _c(sdf, np.float32), _c(faces, np.int32)
+    b, v, _ = xy.shape
+    h, w = image_shape
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    d = dict(key_defines)
+    out = np.zeros((b, 4, h, w), np.float32)
+    lib().or_intersect_and_composite_forward(
+        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(_c(sorted_keys, np.int64)),
+        _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b, num_shells, rows, cols, tile_shape[0],
+        tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out))
+    return out
+
+
+def intersect_and_composite_backward(xy, colors, sdf, faces, sharpness, sorted_keys, sorted_tri, tile_boundaries,
+                                     num_shells, tile_shape, image_shape, key_defines, out, grad_out, exact=False):
+    xy, colors, sdf, faces = _c(xy, np.float32), _c(colors, np.float32), _c(sdf, np.float32), _c(faces, np.int32)
+    b, v, _ = xy.shape
+    h, w = image_shape
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    d = dict(key_defines)
+    gcol = np.zeros_like(colors)
+    gsdf = np.zeros_like(sdf)
+    gsharp = np.zeros((1,), np.float32)
+    lib().or_intersect_and_composite_backward(
+        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(_c(sorted_keys, np.int64)),
+        _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b, num_shells, rows, cols, tile_shape[0],
+        tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(_c(out, np.float32)),
+        _p(_c(grad_out, np.float32)), _p(gcol), _p(gsdf), _p(gsharp), int(exact))
+    return gcol, gsdf, float(gsharp[0])
+
+
+def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, sdf, sh, sh_degree,
+                 sharpness, background, tile_shape=(16, 16), near_plane=0.2, num_camera_bits=6, num_shell_bits=6,
+                 num_tile_bits=20) -> FusedRender:
+    """triangle_rasterization/__init__.py:167-287 on the host (ssaa = 1)."""
+    h, w = image_shape
+    b = extrinsics.shape[0]
+    s = shell_face_boundaries.shape[0]
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    kd = fused_key_defines(num_camera_bits, num_shell_bits, num_tile_bits)
+    xy, depth = project_vertices(vertices, extrinsics, intrinsics)
+    tmin, tmax, count = bound_triangles(xy, depth, faces, tile_shape, (rows, cols), near_plane)
+    keys, tri = generate_keys(depth, faces, shell_face_boundaries, tmin, tmax, count, cols, kd)
+    sk, st = sort_pairs(keys, tri)
+    tb = delineate_tiles(sk, kd, False, b, s, rows * cols)
+    colors = evaluate_spherical_harmonics(vertices, sh, extrinsics, sh_degree)
+    raw = intersect_and_composite(xy, colors, sdf, faces, sharpness, sk, st, tb.reshape(b, rows * cols, 2), s,
+                                  tile_shape, image_shape, kd)
+    bg = np.asarray(background, np.float32)
+    image = np.clip(raw[:, :3] + raw[:, 3:4] * bg[None, :, None, None], 0.0, 1.0)
+    return FusedRender(xy, depth, tmin, tmax, count, keys, tri, sk, st, tb, colors, raw, image)
+
+
+def intersect(xy, faces, sorted_tri, tile_boundaries, num_shells, tile_shape, image_shape):
+    xy, faces = _c(xy, np.float32), _c(faces, np.int32)
+    b, v, _ = xy.shape
+    h, w = image_shape
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    uv = np.zeros((b * num_shells, h, w, 2), np.float32)
+    index = np.zeros((b * num_shells, h, w), np.int32)
+    lib().or_intersect(_p(xy), v, _p(faces), _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b,
+                       num_shells, rows, cols, tile_shape[0], tile_shape[1], h, w, _p(uv), _p(index))
+    return uv.reshape(b, num_shells, h, w, 2), index.reshape(b, num_shells, h, w)
+
+
+def interpolate(uv, index, faces, sdf, colors):
+    uv, index, faces = _c(uv, np.float32), _c(index, np.int32), _c(faces, np.int32)
+    sdf, colors = _c(sdf, np.float32), _c(colors, np.float32)
+    b, s, h, w, _ = uv.shape
+    out_sdf = np.empty((b, s, h, w), np.float32)
+    out_col = np.empty((b, s, h, w, 3), np.float32)
+    lib().or_interpolate(_p(uv), _p(index), b, s, h, w, _p(faces), _p(sdf), _p(colors), sdf.shape[0], _p(out_sdf),
+                         _p(out_col))
+    return out_sdf, out_col
+
+
+def interpolate_backward(uv, index, faces, v, num_cameras, grad_sdf, grad_colors):
+    uv, index, faces = _c(uv, np.float32), _c(index, np.int32), _c(faces, np.int32)
+    b, s, h, w, _ = uv.shape
+    gsdf = np.zeros((v,), np.float32)
+    gcol = np.zeros((num_cameras, v, 3), np.float32)
+    lib().or_interpolate_backward(_p(uv), _p(index), b, s, h, w, _p(faces), v, _p(_c(grad_sdf, np.float32)),
+                                  _p(_c(grad_colors, np.float32)), _p(gsdf), _p(gcol))
+    return gsdf, gcol
+
+
+def composite(sdf, colors, mask, sharpness):
+    sdf, colors = _c(sdf, np.float32), _c(colors, np.float32)
+    mask = _c(mask, np.uint8)
+    p, s = sdf.shape
+    out_c = np.empty((p, 3), np.float32)
+    out_t = np.empty((p,), np.float32)
+    lib().or_composite(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(out_c), _p(out_t))
+    return out_c, out_t
+
+
+def composite_backward(sdf, colors, mask, sharpness, out_c, out_t, grad_c, grad_t, exact=False):
+    sdf, colors = _c(sdf, np.float32), _c(colors, np.float32)
+    mask = _c(mask, np.uint8)
+    p, s = sdf.shape
+    gsdf = np.zeros_like(sdf)
+    gcol = np.zeros_like(colors)
+    gsharp = np.zeros((1,), np.float32)
+    lib().or_composite_backward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(_c(out_c, np.float32)),
+                                _p(_c(out_t, np.float32)), _p(_c(grad_c, np.float32)), _p(_c(grad_t, np.float32)),
+                                _p(gsdf), _p(gcol), _p(gsharp), int(exact))
+    return gsdf, gcol, float(gsharp[0])

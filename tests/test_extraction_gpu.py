@@ -80,7 +80,7 @@ def test_exclusive_cumsum_i32(cuda_device, n):
 
 def test_exclusive_cumsum_unaligned_view(cuda_device):
     x = np.random.default_rng(1).integers(0, 9, 100_003).astype(np.int32)
-    base = _t(np.concatenate(([7], x)), cuda_device)
+    base = _t(np.concatenate((np.array([7], np.int32), x)), cuda_device)
     view = base[1:]  # 4-byte aligned only: exercises the scalar path
     te.compute_exclusive_cumsum(view)
     np.testing.assert_array_equal(_n(view), oracle.exclusive_cumsum(x))

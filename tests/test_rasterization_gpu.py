@@ -1,0 +1,303 @@
+"""GPU parity of the rasterization path against the CPU oracle.
+
+Bit-exact: projected positions and depths, tile bounds, keys, sorted keys,
+tile ranges, explicit-mode hits (uv, face index). Within 1e-5 max-abs:
+colours and images. Within 1e-4 (relative to the largest magnitude):
+gradients, in both gradient-routing modes.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from meshtryoshka_gb300 import triangle_rasterization as tr
+from oracle import oracle
+from tests.scenes import SCENES, make_scene
+
+pytestmark = pytest.mark.gpu
+
+IMAGE_ATOL = 1e-5
+GRAD_RTOL = 1e-4
+
+
+def _t(a, device):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+def _n(t):
+    return t.detach().cpu().numpy()
+
+
+def _close_grad(got, want, rtol=GRAD_RTOL):
+    scale = max(float(np.abs(want).max()), 1e-12)
+    err = float(np.abs(got - want).max())
+    assert err <= rtol * scale, f"max abs err {err:.3e} > {rtol:g} x {scale:.3e}"
+
+
+# ---------------------------------------------------------------------------
+# Sort
+# ---------------------------------------------------------------------------
+def _sort_both(keys, vals, device):
+    want_k, want_v = oracle.sort_pairs(keys, vals)
+    got = tr.sort_keys(tr.PairedKeys(_t(keys, device), _t(vals, device)))
+    return (_n(got.keys), _n(got.triangle_indices)), (want_k, want_v)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3071, 3072, 3073, 100_000, 1_000_003])
+def test_sort_random_full_width(cuda_device, n):
+    rng = np.random.default_rng(n)
+    keys = rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, n, dtype=np.int64)
+    vals = np.arange(n, dtype=np.int32)
+    got, want = _sort_both(keys, vals, cuda_device)
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[1], want[1])
+
+
+def test_sort_stability_and_skipped_passes(cuda_device):
+    # Few distinct keys (heavy ties, most digit passes constant), negative keys
+    # from camera indices >= 32 in the top bits.
+    rng = np.random.default_rng(0)
+    n = 250_000
+    cams = rng.integers(0, 64, n).astype(np.int64)
+    tiles = rng.integers(0, 50, n).astype(np.int64)
+    keys = (cams << 58) | (tiles << 38) | (np.int64(0x3F800000) << 6)
+    vals = np.arange(n, dtype=np.int32)
+    got, want = _sort_both(keys, vals, cuda_device)
+    np.testing.assert_array_equal(got[0], want[0])
+    np.testing.assert_array_equal(got[1], want[1])
+    ts = torch.sort(_t(keys, cuda_device), stable=True)
+    np.testing.assert_array_equal(_n(ts.indices).astype(np.int32), want[1])
+
+
+def test_sort_all_equal(cuda_device):
+    keys = np.full(10_000, -5, np.int64)
+    vals = np.arange(10_000, dtype=np.int32)[::-1].copy()
+    got, want = _sort_both(keys, vals, cuda_device)
+    np.testing.assert_array_equal(got[1], want[1])
+
+
+# ---------------------------------------------------------------------------
+# Front end, stage by stage
+# ---------------------------------------------------------------------------
+def _front(scene, device, tile=(16, 16)):
+    h, w = scene.image_shape
+    b = scene.extrinsics.shape[0]
+    s = scene.face_boundaries.shape[0]
+    grid = tr.TileGrid(tile, (h, w), b, s)
+    kd = tr.create_key_defines(("camera", 6), ("tile", 20), ("depth", 32), ("shell", 6))
+    xy, depth = tr.project_vertices(_t(scene.vertices, device), _t(scene.extrinsics, device),
+                                    _t(scene.intrinsics, device))
+    bounds = tr.bound_triangles(xy, depth, _t(scene.faces, device), grid, 0.2)
+    paired = tr.generate_keys(depth, _t(scene.faces, device), _t(scene.face_boundaries, device), bounds.tile_minima,
+                              bounds.tile_maxima, bounds.num_tiles_overlapped, grid, kd)
+    sorted_ = tr.sort_keys(paired, grid)
+    tb = tr.delineate_tiles(sorted_, grid, kd, False)
+    return grid, kd, xy, depth, bounds, paired, sorted_, tb
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_front_end_bit_exact(cuda_device, name):
+    scene = make_scene(**SCENES[name])
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, cuda_device)
+    want = oracle.render_fused(scene.extrinsics, scene.intrinsics, scene.image_shape, scene.vertices, scene.faces,
+                               scene.face_boundaries, scene.sdf, scene.sh, scene.sh_degree, scene.sharpness,
+                               scene.background)
+    assert oracle.key_layout(kd).tolist() == oracle.key_layout(oracle.fused_key_defines()).tolist()
+    np.testing.assert_array_equal(_n(xy), want.xy)
+    np.testing.assert_array_equal(_n(depth), want.depth)
+    np.testing.assert_array_equal(_n(bounds.tile_minima), want.tile_min)
+    np.testing.assert_array_equal(_n(bounds.tile_maxima), want.tile_max)
+    np.testing.assert_array_equal(_n(bounds.num_tiles_overlapped), want.counts)
+    np.testing.assert_array_equal(_n(paired.keys), want.keys)
+    np.testing.assert_array_equal(_n(paired.triangle_indices), want.tri)
+    np.testing.assert_array_equal(_n(sorted_.keys), want.sorted_keys)
+    np.testing.assert_array_equal(_n(sorted_.triangle_indices), want.sorted_tri)
+    np.testing.assert_array_equal(_n(tb), want.tile_boundaries)
+    assert want.keys.size > 0
+
+
+@pytest.mark.parametrize("degree", [0, 1, 2, 3])
+def test_spherical_harmonics(cuda_device, degree):
+    scene = make_scene(**dict(SCENES["three_cams_odd"], sh_degree=3))
+    d = cuda_device
+    sh = _t(scene.sh, d).requires_grad_(True)
+    colors = tr.evaluate_spherical_harmonics(_t(scene.vertices, d), sh, _t(scene.extrinsics, d), degree)
+    want = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, degree)
+    np.testing.assert_allclose(_n(colors), want, atol=2e-6, rtol=0)
+    g = np.random.default_rng(degree).normal(0, 1, want.shape).astype(np.float32)
+    colors.backward(_t(g, d))
+    want_g = oracle.evaluate_spherical_harmonics_backward(scene.vertices, scene.sh.shape, scene.extrinsics, degree,
+                                                          want, g)
+    _close_grad(_n(sh.grad), want_g)
+
+
+def test_camera_positions_match_torch_inverse(cuda_device):
+    scene = make_scene(**SCENES["three_cams_odd"])
+    got = tr._camera_positions(_t(scene.extrinsics, cuda_device))
+    want = torch.inverse(_t(scene.extrinsics, cuda_device))[:, :3, 3]
+    torch.testing.assert_close(got, want, atol=1e-6, rtol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# Fused compositing
+# ---------------------------------------------------------------------------
+def _fused_inputs(scene, device):
+    d = device
+    return dict(
+        extrinsics=_t(scene.extrinsics, d), intrinsics=_t(scene.intrinsics, d), image_shape=scene.image_shape,
+        vertices=_t(scene.vertices, d), faces=_t(scene.faces, d), shell_face_boundaries=_t(scene.face_boundaries, d),
+        signed_distances=_t(scene.sdf, d).requires_grad_(True), spherical_harmonics=_t(scene.sh, d).requires_grad_(True),
+        sh_degree=scene.sh_degree, sharpness=torch.tensor(scene.sharpness, device=d).requires_grad_(True),
+        background=_t(scene.background, d),
+    )
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_fused_forward(cuda_device, name):
+    scene = make_scene(**SCENES[name])
+    inputs = _fused_inputs(scene, cuda_device)
+    image = tr.render(**inputs, mode="fused")
+    want = oracle.render_fused(scene.extrinsics, scene.intrinsics, scene.image_shape, scene.vertices, scene.faces,
+                               scene.face_boundaries, scene.sdf, scene.sh, scene.sh_degree, scene.sharpness,
+                               scene.background)
+    np.testing.assert_allclose(_n(image), want.image, atol=IMAGE_ATOL, rtol=0)
+    # The image is not trivially the background: some pixels see the mesh.
+    assert (want.raw[:, 3] < 0.5).mean() > 0.01
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+@pytest.mark.parametrize("mode", ["reference", "exact"])
+def test_fused_backward(cuda_device, name, mode):
+    scene = make_scene(**SCENES[name])
+    d = cuda_device
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
+    colors_np = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
+    colors = _t(colors_np, d).requires_grad_(True)
+    sdf = _t(scene.sdf, d).requires_grad_(True)
+    sharp = torch.tensor(scene.sharpness, device=d).requires_grad_(True)
+    b, s = grid.num_cameras, grid.num_shells
+    t = grid.num_tiles_per_image
+    out = tr.intersect_and_composite(xy, colors, sdf, _t(scene.faces, d), sharp, sorted_.keys,
+                                     sorted_.triangle_indices, tb.view(b, t, 2), s, grid, kd, gradient_mode=mode)
+    want_out = oracle.intersect_and_composite(_n(xy), colors_np, scene.sdf, scene.faces, scene.sharpness,
+                                              _n(sorted_.keys), _n(sorted_.triangle_indices), _n(tb).reshape(b, t, 2),
+                                              s, grid.tile_shape, grid.image_shape, kd)
+    np.testing.assert_allclose(_n(out), want_out, atol=IMAGE_ATOL, rtol=0)
+    g = np.random.default_rng(1).normal(0, 1, want_out.shape).astype(np.float32)
+    out.backward(_t(g, d))
+    wc, ws, wsharp = oracle.intersect_and_composite_backward(
+        _n(xy), colors_np, scene.sdf, scene.faces, scene.sharpness, _n(sorted_.keys), _n(sorted_.triangle_indices),
+        _n(tb).reshape(b, t, 2), s, grid.tile_shape, grid.image_shape, kd, want_out, g, exact=(mode == "exact"))
+    _close_grad(_n(colors.grad), wc)
+    _close_grad(_n(sdf.grad), ws)
+    assert abs(float(sharp.grad) - wsharp) <= GRAD_RTOL * max(abs(wsharp), 1e-6) + 1e-6
+
+
+def test_reference_and_exact_routing_differ_only_with_multiple_hits(cuda_device):
+    one_shell = make_scene(levels=(0.0,))
+    d = cuda_device
+    grads = {}
+    for mode in ("reference", "exact"):
+        inputs = _fused_inputs(one_shell, d)
+        img = tr.render(**inputs, mode="fused", gradient_mode=mode)
+        img.sum().backward()
+        grads[mode] = _n(inputs["signed_distances"].grad)
+    np.testing.assert_array_equal(grads["reference"], grads["exact"])
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 32), (16, 8)])
+def test_fused_tile_shapes(cuda_device, tile):
+    scene = make_scene(**SCENES["three_cams_odd"])
+    inputs = _fused_inputs(scene, cuda_device)
+    image = tr.render(**inputs, tile_shape=tile, mode="fused")
+    want = oracle.render_fused(scene.extrinsics, scene.intrinsics, scene.image_shape, scene.vertices, scene.faces,
+                               scene.face_boundaries, scene.sdf, scene.sh, scene.sh_degree, scene.sharpness,
+                               scene.background, tile_shape=tile)
+    np.testing.assert_allclose(_n(image), want.image, atol=IMAGE_ATOL, rtol=0)
+
+
+def test_fused_empty_scene_returns_background(cuda_device):
+    scene = make_scene()
+    inputs = _fused_inputs(scene, cuda_device)
+    inputs["faces"] = inputs["faces"][:0]
+    image = tr.render(**inputs)
+    expect = np.broadcast_to(scene.background[None, :, None, None], (1, 3, *scene.image_shape))
+    np.testing.assert_array_equal(_n(image), expect)
+
+
+def test_ssaa_matches_mean_of_supersampled(cuda_device):
+    scene = make_scene(image_shape=(64, 64))
+    inputs = _fused_inputs(scene, cuda_device)
+    image = tr.render(**inputs, ssaa=2)
+    assert image.shape == (1, 3, 64, 64)
+    sup = dict(inputs)
+    sup["image_shape"] = (128, 128)
+    sup["intrinsics"] = inputs["intrinsics"] * torch.tensor((2, 2, 1), device=cuda_device)[:, None]
+    raw = tr.render(**sup)
+    # Clip happens after the mean in the reference; the raw image is clipped
+    # per sample, so compare in the interior where nothing saturates.
+    assert float((image - raw.reshape(1, 3, 64, 2, 64, 2).mean((3, 5))).abs().max()) < 0.05
+
+
+# ---------------------------------------------------------------------------
+# Explicit mode
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", list(SCENES))
+def test_explicit_rasterize_bit_exact(cuda_device, name):
+    scene = make_scene(**SCENES[name])
+    d = cuda_device
+    uv, index = tr.rasterize(_t(scene.vertices, d), _t(scene.faces, d), _t(scene.face_boundaries, d),
+                             _t(scene.extrinsics, d), _t(scene.intrinsics, d), scene.image_shape)
+    h, w = scene.image_shape
+    b = scene.extrinsics.shape[0]
+    s = scene.face_boundaries.shape[0]
+    rows, cols = -(-h // 16), -(-w // 16)
+    kd = oracle.explicit_key_defines()
+    xy, depth = oracle.project_vertices(scene.vertices, scene.extrinsics, scene.intrinsics)
+    tmin, tmax, count = oracle.bound_triangles(xy, depth, scene.faces, (16, 16), (rows, cols), 0.2)
+    keys, tri = oracle.generate_keys(depth, scene.faces, scene.face_boundaries, tmin, tmax, count, cols, kd)
+    sk, st = oracle.sort_pairs(keys, tri)
+    tb = oracle.delineate_tiles(sk, kd, True, b, s, rows * cols)
+    want_uv, want_index = oracle.intersect(xy, scene.faces, st, tb, s, (16, 16), scene.image_shape)
+    np.testing.assert_array_equal(_n(index), want_index)
+    np.testing.assert_array_equal(_n(uv), want_uv)
+    assert (want_index >= 0).any()
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+@pytest.mark.parametrize("mode", ["reference", "exact"])
+def test_explicit_render_and_gradients(cuda_device, name, mode):
+    scene = make_scene(**SCENES[name])
+    d = cuda_device
+    inputs = _fused_inputs(scene, d)
+    image = tr.render(**inputs, mode="explicit", gradient_mode=mode)
+    # Oracle chain: rasterize -> SH -> interpolate -> composite -> background.
+    uv, index = tr.rasterize(inputs["vertices"], inputs["faces"], inputs["shell_face_boundaries"],
+                             inputs["extrinsics"], inputs["intrinsics"], scene.image_shape)
+    uv, index = _n(uv), _n(index)
+    colors = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
+    isdf, icol = oracle.interpolate(uv, index, scene.faces, scene.sdf, colors)
+    b, s, h, w = isdf.shape
+    psdf = isdf.transpose(0, 2, 3, 1).reshape(-1, s)
+    pcol = icol.transpose(0, 2, 3, 1, 4).reshape(-1, s, 3)
+    mask = (index != -1).transpose(0, 2, 3, 1).reshape(-1, s)
+    oc, ot = oracle.composite(psdf, pcol, mask, scene.sharpness)
+    want = (oc + scene.background[None] * ot[:, None]).reshape(b, h, w, 3).transpose(0, 3, 1, 2)
+    np.testing.assert_allclose(_n(image), want, atol=IMAGE_ATOL, rtol=0)
+
+    g = np.random.default_rng(2).normal(0, 1, want.shape).astype(np.float32)
+    image.backward(_t(g, d))
+    gc = g.transpose(0, 2, 3, 1).reshape(-1, 3)
+    gt = (gc * scene.background[None]).sum(-1)
+    gpsdf, gpcol, gsharp = oracle.composite_backward(psdf, pcol, mask, scene.sharpness, oc, ot, gc, gt,
+                                                     exact=(mode == "exact"))
+    gisdf = gpsdf.reshape(b, h, w, s).transpose(0, 3, 1, 2)
+    gicol = gpcol.reshape(b, h, w, s, 3).transpose(0, 3, 1, 2, 4)
+    gsdf, gcolors = oracle.interpolate_backward(uv, index, scene.faces, scene.vertices.shape[0], b, gisdf, gicol)
+    gsh = oracle.evaluate_spherical_harmonics_backward(scene.vertices, scene.sh.shape, scene.extrinsics,
+                                                       scene.sh_degree, colors, gcolors)
+    _close_grad(_n(inputs["signed_distances"].grad), gsdf)
+    _close_grad(_n(inputs["spherical_harmonics"].grad), gsh)
+    assert abs(float(inputs["sharpness"].grad) - gsharp) <= GRAD_RTOL * max(abs(gsharp), 1e-6) + 1e-6
