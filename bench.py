@@ -1,0 +1,401 @@
+"""Benchmark of the per-step render path (one JSON line on stdout).
+
+Workload: the 256^3 training step — a sparse band around the union of 8
+spheres, SH degree 3, 8 shells, 4 cameras at 800x800 (synthetic stand-in for
+the reference's datasets). A step is tessellation of all shells + fused render
+of all cameras + MSE + backward into the grid SDF and SH, through the
+package's public API.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is the device time of one step (CUDA events on the launching
+stream, inputs resident in HBM, L2 flushed between steps); ``e2e`` is the same
+step with the inputs copied from pinned host memory and the loss copied back
+inside the timed region. ``--impl reference`` times the CPU restatement of the
+reference algorithm (the reference's Slang kernels cannot run here) on the
+host cores.
+
+With N > 1 (torchrun), every rank runs an independent replica of the step on
+its own GPU (the path needs no exchange); the reported time is the maximum
+over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "fwd+bwd step ms & HBM GB/s at 256³×8 shells×4×800²; serve p99 ms vs plain"
+CONFIG_NAME = "mid"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    p.add_argument("--config", default=CONFIG_NAME)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(n):
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle (restatement of the reference algorithm) on host cores.
+# ---------------------------------------------------------------------------
+def cpu_sample(w, camera: int):
+    """Tessellation of the whole grid plus fused render fwd+bwd of one camera on
+    the host cores; returns (tessellate_s, render_s)."""
+    import numpy as np
+
+    from oracle import oracle
+
+    vox = w.voxels
+    np_vox = [t.detach().cpu().numpy() for t in (vox.vertices, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                                 vox.indices)]
+    sdf = w.grid_sdf.detach().cpu().numpy()
+    sh = w.grid_sh.detach().cpu().numpy()
+    ls = w.level_sets.cpu().numpy()
+    t0 = time.perf_counter()
+    tri = oracle.tessellate_voxels(sdf, np_vox[0], sh, np_vox[1], np_vox[2], np_vox[3], np_vox[4], ls)
+    rng = np.random.default_rng(0)
+    g_sdf = rng.normal(0, 1e-3, tri.signed_distances.shape).astype(np.float32)
+    g_sh = rng.normal(0, 1e-3, tri.spherical_harmonics.shape).astype(np.float32)
+    oracle.create_triangle_vertices_backward(sdf, sh.shape, np_vox[2], ls, tri.vertex_offsets, None, g_sdf, g_sh)
+    t1 = time.perf_counter()
+    ext = w.extrinsics[camera:camera + 1].cpu().numpy()
+    intr = w.intrinsics[camera:camera + 1].cpu().numpy()
+    verts = (2.0 * tri.vertices - 1.0).astype(np.float32)
+    r = oracle.render_fused(ext, intr, w.image_shape, verts, tri.faces, tri.face_boundaries, tri.signed_distances,
+                            tri.spherical_harmonics, w.sh_degree, float(w.sharpness), w.background.cpu().numpy())
+    grad = (2.0 / r.image.size) * (r.image - w.target[camera:camera + 1].cpu().numpy())
+    h, wd = w.image_shape
+    rows, cols = -(-h // 16), -(-wd // 16)
+    kd = oracle.fused_key_defines()
+    graw = np.zeros_like(r.raw)
+    graw[:, :3] = grad
+    graw[:, 3] = (grad * w.background.cpu().numpy()[None, :, None, None]).sum(1)
+    gcol, gsdf, _ = oracle.intersect_and_composite_backward(
+        r.xy, r.colors, tri.signed_distances, tri.faces, float(w.sharpness), r.sorted_keys, r.sorted_tri,
+        r.tile_boundaries.reshape(1, rows * cols, 2), tri.face_boundaries.shape[0], (16, 16), w.image_shape, kd,
+        r.raw, graw)
+    oracle.evaluate_spherical_harmonics_backward(verts, tri.spherical_harmonics.shape, ext, w.sh_degree, r.colors,
+                                                 gcol)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
+
+
+def cpu_threads():
+    return int(os.environ.get("OMP_NUM_THREADS") or os.cpu_count() or 1)
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference path on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import torch
+
+    from meshtryoshka_gb300 import pipeline
+
+    device = torch.device("cuda", 0) if torch.cuda.is_available() else None
+    if device is None:
+        print(json.dumps({"impl": "reference", "unavailable": "needs the GPU-built scene inputs (no CUDA device)"}))
+        return
+    w = pipeline.build_workload(args.config, device)
+    b = w.extrinsics.shape[0]
+    times = []
+    for i in range(args.warmup + args.steps):
+        tess_s, render_s = cpu_sample(w, i % b)
+        if i >= args.warmup:
+            times.append(tess_s + b * render_s)
+    ms = 1000.0 * statistics.mean(times)
+    h, wd = w.image_shape
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{args.config}: {w.config.resolution}^3 band, {w.config.num_spheres} spheres, "
+                               f"SH deg {w.sh_degree}, {w.level_sets.numel()} shells, {b}x{h}x{wd} fused fwd+bwd",
+                   "parallelism": "host threads"},
+        "impl": "reference",
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": cpu_threads(), "kind": "port",
+                         "sample": f"per step: full tessellation fwd+bwd + fused render fwd+bwd of 1 of {b} cameras "
+                                   f"(round robin), render time x{b}"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+
+    from meshtryoshka_gb300 import _native, pipeline
+
+    device = torch.device("cuda", local)
+    torch.manual_seed(0)
+    w = pipeline.build_workload(args.config, device)
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)  # > L2 (129 MB)
+
+    def step():
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+        loss, stats = pipeline.forward(w)
+        loss.backward()
+        return loss, stats
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(device)
+
+    # Timed device region: per-step events, L2 flushed between steps (outside
+    # the step's events), library launches counted and timed per entry point.
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize(device)
+    clocks = ClockSampler(local) if rank == 0 else None
+    wall0 = time.perf_counter()
+    with _native.record_launches(timed=True) as rec:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            loss, stats = step()
+            ev[i][1].record(stream)
+    torch.cuda.synchronize(device)
+    wall = time.perf_counter() - wall0
+    barrier(world)
+    clock_info = clocks.stop() if clocks else None
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = max_over_ranks(statistics.mean(step_ms), world)
+    per_call = rec.times_ms()
+    launches_per_step = rec.launches / args.steps
+
+    # End to end through the public API: inputs from pinned host memory,
+    # loss read back, every step.
+    host = {k: v.detach().cpu().pin_memory() for k, v in
+            (("sdf", w.grid_sdf), ("sh", w.grid_sh), ("target", w.target), ("ext", w.extrinsics),
+             ("intr", w.intrinsics))}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+
+    def e2e_step():
+        sdf = host["sdf"].to(device, non_blocking=True).requires_grad_(True)
+        sh = host["sh"].to(device, non_blocking=True).requires_grad_(True)
+        target = host["target"].to(device, non_blocking=True)
+        w.extrinsics.copy_(host["ext"], non_blocking=True)
+        w.intrinsics.copy_(host["intr"], non_blocking=True)
+        loss, _ = pipeline.forward(w, grid_sdf=sdf, grid_sh=sh, target=target)
+        loss.backward()
+        return float(loss.detach().cpu())
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize(device)
+    barrier(world)
+    e_ms = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize(device)
+        e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_value = max_over_ranks(statistics.mean(e_ms), world)
+
+    if rank != 0:
+        return
+
+    # Roofline of the dominant kernel (largest share of device time).
+    peak, peak_kind = measured_peaks()
+    bytes_by_stage = pipeline.algorithmic_bytes(stats)
+    stage_of = {
+        "mt_intersect_and_composite_backward": "composite_bwd",
+        "mt_intersect_and_composite_forward": "composite_fwd",
+        "mt_sort_pairs_i64_i32": "sort",
+        "mt_create_triangle_vertices_backward": "create_vertices_bwd",
+        "mt_create_triangle_vertices": "create_vertices",
+        "mt_evaluate_spherical_harmonics_backward": "sh_bwd",
+    }
+    totals = {k: sum(v) for k, v in per_call.items()}
+    dominant = max(totals, key=totals.get)
+    dom_ms = statistics.mean(per_call[dominant])
+    dom_bytes = bytes_by_stage.get(stage_of.get(dominant, ""), None)
+    achieved = (dom_bytes / (dom_ms * 1e-3) / 1e9) if dom_bytes else None
+    total_bytes = sum(bytes_by_stage.values())
+    traffic = None
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as f:
+            traffic = json.load(f).get(dominant)
+
+    b = stats["B"]
+    h, wd = w.image_shape
+    line = {
+        "metric": METRIC,
+        "value": ms,
+        "unit": "ms",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": f"{args.config}: {w.config.resolution}^3 band around {w.config.num_spheres} spheres, "
+                        f"SH deg {w.sh_degree}, {stats['S']} shells, {b}x{h}x{wd}, fused fwd+bwd training step",
+            "sizes": {k: stats[k] for k in ("G", "Nv", "V", "F", "K", "P")},
+            "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "hbm_gbs": total_bytes / (ms * 1e-3) / 1e9,
+        "step_ms_median": statistics.median(step_ms),
+        "step_ms_p90": sorted(step_ms)[int(0.9 * (len(step_ms) - 1))],
+        "wall_s_timed_region": wall,
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "gpu_launches_per_step": launches_per_step,
+        "kernel_ms": {k: statistics.mean(v) for k, v in sorted(per_call.items(), key=lambda kv: -sum(kv[1]))},
+        "roofline": {
+            "kernel": dominant,
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "peak_kind": peak_kind,
+            "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "traffic": traffic,
+            "algorithmic_bytes_per_launch": dom_bytes,
+            "launch_ms": dom_ms,
+        },
+        "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
+        "clocks": clock_info,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        tess_s, render_s = cpu_sample(w, 0)
+        cpu_ms = 1000.0 * (tess_s + b * render_s)
+        line["cpu_baseline"] = {
+            "value": cpu_ms, "unit": "ms", "cores": cpu_threads(), "kind": "port",
+            "sample": f"full tessellation fwd+bwd + fused render fwd+bwd of 1 of {b} cameras, render time x{b}",
+        }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

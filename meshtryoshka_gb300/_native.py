@@ -14,6 +14,7 @@ render path fails.
 
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import threading
 from ctypes import c_float, c_int32, c_int64, c_size_t, c_uint64, c_void_p
@@ -106,10 +107,57 @@ def library_path() -> str:
     return str(_build.LIBRARY)
 
 
+# Kernels each entry point enqueues (memsets excluded); used to count this
+# library's launches, e.g. inside a benchmark's timed region.
+KERNELS_PER_CALL = {
+    "mt_sort_pairs_i64_i32": 11,  # histogram, plan, 8 digit passes, copy
+    "mt_create_voxels": 1,
+}
+
+
+class LaunchRecorder:
+    """Counts library kernel launches and optionally times every entry point
+    with CUDA events on the stream it was enqueued on."""
+
+    def __init__(self, timed: bool = False):
+        self.launches = 0
+        self.calls: dict[str, int] = {}
+        self.timed = timed
+        self.events: dict[str, list[tuple[torch.cuda.Event, torch.cuda.Event]]] = {}
+
+    def times_ms(self) -> dict[str, list[float]]:
+        return {k: [a.elapsed_time(b) for a, b in v] for k, v in self.events.items()}
+
+
+_recorder: LaunchRecorder | None = None
+
+
+@contextlib.contextmanager
+def record_launches(timed: bool = False):
+    global _recorder
+    previous = _recorder
+    _recorder = LaunchRecorder(timed)
+    try:
+        yield _recorder
+    finally:
+        _recorder = previous
+
+
 def call(name: str, *args) -> None:
     """Call an entry point and raise RuntimeError on a non-zero status."""
     lib = _load()
+    rec = _recorder
+    if rec is not None:
+        rec.launches += KERNELS_PER_CALL.get(name, 1)
+        rec.calls[name] = rec.calls.get(name, 0) + 1
+        if rec.timed:
+            start = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            start.record()
     status = getattr(lib, name)(*args)
+    if rec is not None and rec.timed:
+        end.record()
+        rec.events.setdefault(name, []).append((start, end))
     if status != 0:
         msg = lib.mt_status_string(status).decode()
         raise RuntimeError(f"{name} failed: {msg} (status {status})")

@@ -61,6 +61,10 @@ __all__ = [
 
 _GRADIENT_MODE = "reference"
 
+# Sizes of the most recent render (host integers already known to the
+# wrapper; no extra synchronisation).
+LAST_RENDER_STATS: dict[str, int] = {}
+
 
 def set_gradient_mode(mode: Literal["reference", "exact"]) -> None:
     """Select the compositors' gradient routing (see the module docstring)."""
@@ -572,6 +576,7 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
     paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
                            bounds.num_tiles_overlapped, grid, key_defines)
     del bounds, depths
+    LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.num_tiles_per_image)
     paired = sort_keys(paired, grid)
     tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)

@@ -125,7 +125,7 @@ def test_tessellate_bit_exact(cuda_device, n, levels, c):
 
 
 def test_tessellate_stages_bit_exact(cuda_device):
-    occ, vox, sdf, sh, ls = _sphere_scene(48, (0.03, 0.01, -0.01, -0.03), 4)
+    occ, vox, sdf, sh, ls = _sphere_scene(64, (0.03, 0.01, -0.01, -0.03), 4)
     d = cuda_device
     counts = te.count_triangle_vertices(_t(sdf, d), _t(vox.lower_corners, d), _t(ls, d))
     np.testing.assert_array_equal(_n(counts), oracle.count_triangle_vertices(sdf, vox.lower_corners, ls))
@@ -164,7 +164,7 @@ def test_tessellate_empty_level_set_and_empty_voxels(cuda_device):
 
 @pytest.mark.parametrize("c", [1, 16])
 def test_create_triangle_vertices_backward(cuda_device, c):
-    occ, vox, sdf, sh, ls = _sphere_scene(48, (0.02, 0.0, -0.02), c, seed=3)
+    occ, vox, sdf, sh, ls = _sphere_scene(64, (0.02, 0.0, -0.02), c, seed=3)
     d = cuda_device
     sdf_t = _t(sdf, d).requires_grad_(True)
     sh_t = _t(sh, d).requires_grad_(True)
