@@ -107,3 +107,76 @@ __device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f),
 
 
 }  // namespace mt
+
+namespace mt {
+
+// ---------------------------------------------------------------------------
+// Warp-level culling.
+//
+// A pixel centre p can only be accepted by hit_test if none of the three
+// numerators falls below the fast-reject threshold. For a well-conditioned
+// triangle (every angle's sine^2 >= 1e-4, positive finite denominator above
+// 2^-20, extent below 8192 px) the numerators are affine functions of p whose
+// rounding error is bounded by a few ulps of |coefficients| x |p - p_i|;
+// outside the triangle's bounding box grown by 1 px + 1e-3 x extent, one of
+// them is negative by orders of magnitude more than that error, so
+// hit_test's exact fast reject fires. Such a box is therefore a conservative
+// superset of the accepted pixels, and a warp whose pixel rectangle misses it
+// skips the triangle without changing any decision. Triangles that are not
+// well-conditioned get an infinite box (never culled).
+// ---------------------------------------------------------------------------
+struct CullBox {
+  float x0, x1, y0, y1;
+};
+
+__device__ __forceinline__ CullBox cull_box(const TriGeom& g, float p1x, float p1y, float p2x, float p2y, float p3x,
+                                            float p3y) {
+  const float inf = __int_as_float(0x7f800000);
+  CullBox open{-inf, inf, -inf, inf};
+  const float xmin = fminf(fminf(p1x, p2x), p3x), xmax = fmaxf(fmaxf(p1x, p2x), p3x);
+  const float ymin = fminf(fminf(p1y, p2y), p3y), ymax = fmaxf(fmaxf(p1y, p2y), p3y);
+  const float ext = fmaxf(xmax - xmin, ymax - ymin);
+  if (!(ext < 8192.0f) || !(fabsf(xmin) < 1e6f && fabsf(xmax) < 1e6f && fabsf(ymin) < 1e6f && fabsf(ymax) < 1e6f))
+    return open;
+  if (!(g.thr > -inf)) return open;  // fast reject unavailable: no culling
+  const float e23x = p3x - p2x, e23y = p3y - p2y;
+  const float l12 = g.d1212, l13 = g.d1313, l23 = e23x * e23x + e23y * e23y;
+  const float worst = fmaxf(fmaxf(l12 * l13, l12 * l23), l13 * l23);
+  if (!(g.dd >= 1e-4f * worst)) return open;
+  const float m = 1.0f + 1e-3f * ext;
+  return CullBox{xmin - m, xmax + m, ymin - m, ymax + m};
+}
+
+__device__ __forceinline__ bool box_overlaps(const CullBox& b, float rx0, float rx1, float ry0, float ry1) {
+  return !(b.x1 < rx0 || b.x0 > rx1 || b.y1 < ry0 || b.y0 > ry1);
+}
+
+// Pixel of thread `tid` inside its tile. When the tile is a whole number of
+// 8x4 blocks each warp covers one 8x4 block (compact warp footprint, so a
+// small triangle overlaps few warps); otherwise row-major.
+__device__ __forceinline__ void tile_pixel(int tid, int tile_w, int tile_h, int& lx, int& ly) {
+  if ((tile_w & 7) == 0 && (tile_h & 3) == 0) {
+    const int warp = tid >> 5, lane = tid & 31;
+    const int per_row = tile_w >> 3;
+    lx = (warp % per_row) * 8 + (lane & 7);
+    ly = (warp / per_row) * 4 + (lane >> 3);
+  } else {
+    lx = tid % tile_w;
+    ly = tid / tile_w;
+  }
+}
+
+// Bounding rectangle of the warp's pixel centres.
+__device__ __forceinline__ void warp_rect(float fx, float fy, float& x0, float& x1, float& y0, float& y1) {
+  x0 = x1 = fx;
+  y0 = y1 = fy;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+    x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+    y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+    y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+  }
+}
+
+}  // namespace mt

@@ -171,12 +171,16 @@ def create_voxels(
     upper_corners = torch.empty((4, num_voxels), dtype=torch.int32, **kw)
     indices = torch.empty((num_voxels,), dtype=torch.int32, **kw)
     if num_voxels > 0:
+        # Converted inputs are bound to names so they outlive the launch.
+        voxel_offsets = _i32(voxel_offsets, "voxel_offsets")
+        vertex_occupancy = _i32(vertex_occupancy, "vertex_occupancy")
+        vertex_offsets = _i32(vertex_offsets, "vertex_offsets")
         nt.call(
             "mt_create_voxels",
             occupancy.data_ptr(),
-            _i32(voxel_offsets, "voxel_offsets").data_ptr(),
-            _i32(vertex_occupancy, "vertex_occupancy").data_ptr(),
-            _i32(vertex_offsets, "vertex_offsets").data_ptr(),
+            voxel_offsets.data_ptr(),
+            vertex_occupancy.data_ptr(),
+            vertex_offsets.data_ptr(),
             i, j, kp, num_voxels, num_vertices,
             vertices.data_ptr(), neighbors.data_ptr(), lower_corners.data_ptr(),
             upper_corners.data_ptr(), indices.data_ptr(), nt.stream(device),
@@ -381,12 +385,13 @@ def create_triangle_faces(
     f = int(face_offsets[-1].item()) // 3 if num_faces is None else int(num_faces)
     faces = torch.empty((f, 3), dtype=torch.int32, device=device)
     voxel_indices = torch.empty((f,), dtype=torch.int32, device=device)
+    neighbors, indices = _i32(neighbors, "neighbors"), _i32(indices, "indices")
+    vertex_offsets, face_offsets = _i32(vertex_offsets, "vertex_offsets"), _i32(face_offsets, "face_offsets")
+    types, codes = triangle_vertex_types.contiguous(), voxel_cell_codes.contiguous()
     nt.call(
         "mt_create_triangle_faces",
-        nt.ptr(_i32(neighbors, "neighbors")), nt.ptr(_i32(indices, "indices")), nv, g,
-        nt.ptr(_i32(vertex_offsets, "vertex_offsets")), nt.ptr(triangle_vertex_types.contiguous()),
-        nt.ptr(voxel_cell_codes.contiguous()), s, nt.ptr(_i32(face_offsets, "face_offsets")), f,
-        nt.ptr(faces), nt.ptr(voxel_indices), nt.stream(device),
+        nt.ptr(neighbors), nt.ptr(indices), nv, g, nt.ptr(vertex_offsets), nt.ptr(types), nt.ptr(codes), s,
+        nt.ptr(face_offsets), f, nt.ptr(faces), nt.ptr(voxel_indices), nt.stream(device),
     )
     return CreateTriangleFacesResult(faces, voxel_indices)
 

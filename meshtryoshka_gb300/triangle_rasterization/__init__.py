@@ -241,8 +241,9 @@ def generate_keys(depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor, 
     keys = torch.zeros(num_keys, dtype=torch.int64, device=device)
     tri = torch.zeros(num_keys, dtype=torch.int32, device=device)
     b, v = depths.shape
+    tile_minima, tile_maxima = _i32(tile_minima), _i32(tile_maxima)
     nt.call("mt_generate_keys", nt.ptr(depths), v, nt.ptr(faces), faces.shape[0], nt.ptr(sfb), sfb.shape[0],
-            nt.ptr(_i32(tile_minima)), nt.ptr(_i32(tile_maxima)), nt.ptr(offsets), b, grid.grid_shape[1],
+            nt.ptr(tile_minima), nt.ptr(tile_maxima), nt.ptr(offsets), b, grid.grid_shape[1],
             _layout(key_defines), num_keys, nt.ptr(keys), nt.ptr(tri), nt.stream(device))
     return PairedKeys(keys, tri)
 
@@ -409,7 +410,8 @@ def intersect(vertices: Tensor, faces: Tensor, sorted_triangle_indices: Tensor, 
     uv = torch.empty((*out_shape, 2), dtype=torch.float32, device=device)
     index = torch.empty(out_shape, dtype=torch.int32, device=device)
     rows, cols = grid.grid_shape
-    nt.call("mt_intersect", nt.ptr(xy), xy.shape[1], nt.ptr(faces), nt.ptr(tri), nt.ptr(tile_boundaries.contiguous()),
+    tile_boundaries = tile_boundaries.contiguous()
+    nt.call("mt_intersect", nt.ptr(xy), xy.shape[1], nt.ptr(faces), nt.ptr(tri), nt.ptr(tile_boundaries),
             grid.num_cameras, grid.num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w,
             nt.ptr(uv), nt.ptr(index), nt.stream(device))
     shape = (grid.num_cameras, grid.num_shells, h, w)

@@ -309,8 +309,9 @@ def evaluate_spherical_harmonics_backward(vertices, sh_shape, extrinsics, sh_deg
     v = _c(vertices, np.float32)
     campos = camera_positions(extrinsics)
     out = np.zeros(sh_shape, np.float32)
+    colors, grad_colors = _c(colors, np.float32), _c(grad_colors, np.float32)
     lib().or_evaluate_sh_backward(_p(v), v.shape[0], sh_degree, _p(campos), campos.shape[0],
-                                  _p(_c(colors, np.float32)), _p(_c(grad_colors, np.float32)), _p(out))
+                                  _p(colors), _p(grad_colors), _p(out))
     return out
 
 
@@ -334,9 +335,9 @@ def generate_keys(depth, faces, shell_face_boundaries, tmin, tmax, count, grid_w
     keys = np.zeros((k,), np.int64)
     tri = np.zeros((k,), np.int32)
     b, v = depth.shape
-    lib().or_generate_keys(_p(depth), v, _p(faces), faces.shape[0], _p(sfb), sfb.shape[0], _p(_c(tmin, np.int32)),
-                           _p(_c(tmax, np.int32)), _p(offsets), b, grid_width, _p(key_layout(key_defines)),
-                           _p(keys), _p(tri))
+    tmin, tmax, layout = _c(tmin, np.int32), _c(tmax, np.int32), key_layout(key_defines)
+    lib().or_generate_keys(_p(depth), v, _p(faces), faces.shape[0], _p(sfb), sfb.shape[0], _p(tmin), _p(tmax),
+                           _p(offsets), b, grid_width, _p(layout), _p(keys), _p(tri))
     return keys, tri
 
 
@@ -351,8 +352,9 @@ def delineate_tiles(sorted_keys, key_defines, separate_shells, num_cameras, num_
     keys = _c(sorted_keys, np.int64)
     sd = num_shells if separate_shells else 1
     out = np.empty((num_cameras, sd, num_tiles, 2), np.int64)
-    lib().or_delineate_tiles(_p(keys), keys.size, _p(key_layout(key_defines)), int(separate_shells), num_cameras, sd,
-                             num_tiles, _p(out))
+    layout = key_layout(key_defines)
+    lib().or_delineate_tiles(_p(keys), keys.size, _p(layout), int(separate_shells), num_cameras, sd, num_tiles,
+                             _p(out))
     return out
 
 
@@ -380,10 +382,10 @@ def intersect_and_composite(xy, colors, sdf, faces, sharpness, sorted_keys, sort
     rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
     d = dict(key_defines)
     out = np.zeros((b, 4, h, w), np.float32)
+    sk, st, tb = _c(sorted_keys, np.int64), _c(sorted_tri, np.int32), _c(tile_boundaries, np.int64)
     lib().or_intersect_and_composite_forward(
-        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(_c(sorted_keys, np.int64)),
-        _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b, num_shells, rows, cols, tile_shape[0],
-        tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out))
+        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(sk), _p(st), _p(tb), b, num_shells, rows,
+        cols, tile_shape[0], tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out))
     return out
 
 
@@ -397,11 +399,12 @@ def intersect_and_composite_backward(xy, colors, sdf, faces, sharpness, sorted_k
     gcol = np.zeros_like(colors)
     gsdf = np.zeros_like(sdf)
     gsharp = np.zeros((1,), np.float32)
+    sk, st, tb = _c(sorted_keys, np.int64), _c(sorted_tri, np.int32), _c(tile_boundaries, np.int64)
+    out, grad_out = _c(out, np.float32), _c(grad_out, np.float32)
     lib().or_intersect_and_composite_backward(
-        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(_c(sorted_keys, np.int64)),
-        _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b, num_shells, rows, cols, tile_shape[0],
-        tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(_c(out, np.float32)),
-        _p(_c(grad_out, np.float32)), _p(gcol), _p(gsdf), _p(gsharp), int(exact))
+        _p(xy), _p(colors), _p(sdf), v, _p(faces), float(sharpness), _p(sk), _p(st), _p(tb), b, num_shells, rows,
+        cols, tile_shape[0], tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out),
+        _p(grad_out), _p(gcol), _p(gsdf), _p(gsharp), int(exact))
     return gcol, gsdf, float(gsharp[0])
 
 
@@ -434,7 +437,8 @@ def intersect(xy, faces, sorted_tri, tile_boundaries, num_shells, tile_shape, im
     rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
     uv = np.zeros((b * num_shells, h, w, 2), np.float32)
     index = np.zeros((b * num_shells, h, w), np.int32)
-    lib().or_intersect(_p(xy), v, _p(faces), _p(_c(sorted_tri, np.int32)), _p(_c(tile_boundaries, np.int64)), b,
+    st, tb = _c(sorted_tri, np.int32), _c(tile_boundaries, np.int64)
+    lib().or_intersect(_p(xy), v, _p(faces), _p(st), _p(tb), b,
                        num_shells, rows, cols, tile_shape[0], tile_shape[1], h, w, _p(uv), _p(index))
     return uv.reshape(b, num_shells, h, w, 2), index.reshape(b, num_shells, h, w)
 
@@ -455,8 +459,9 @@ def interpolate_backward(uv, index, faces, v, num_cameras, grad_sdf, grad_colors
     b, s, h, w, _ = uv.shape
     gsdf = np.zeros((v,), np.float32)
     gcol = np.zeros((num_cameras, v, 3), np.float32)
-    lib().or_interpolate_backward(_p(uv), _p(index), b, s, h, w, _p(faces), v, _p(_c(grad_sdf, np.float32)),
-                                  _p(_c(grad_colors, np.float32)), _p(gsdf), _p(gcol))
+    grad_sdf, grad_colors = _c(grad_sdf, np.float32), _c(grad_colors, np.float32)
+    lib().or_interpolate_backward(_p(uv), _p(index), b, s, h, w, _p(faces), v, _p(grad_sdf), _p(grad_colors),
+                                  _p(gsdf), _p(gcol))
     return gsdf, gcol
 
 
@@ -477,7 +482,8 @@ def composite_backward(sdf, colors, mask, sharpness, out_c, out_t, grad_c, grad_
     gsdf = np.zeros_like(sdf)
     gcol = np.zeros_like(colors)
     gsharp = np.zeros((1,), np.float32)
-    lib().or_composite_backward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(_c(out_c, np.float32)),
-                                _p(_c(out_t, np.float32)), _p(_c(grad_c, np.float32)), _p(_c(grad_t, np.float32)),
-                                _p(gsdf), _p(gcol), _p(gsharp), int(exact))
+    out_c, out_t = _c(out_c, np.float32), _c(out_t, np.float32)
+    grad_c, grad_t = _c(grad_c, np.float32), _c(grad_t, np.float32)
+    lib().or_composite_backward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(out_c), _p(out_t),
+                                _p(grad_c), _p(grad_t), _p(gsdf), _p(gcol), _p(gsharp), int(exact))
     return gsdf, gcol, float(gsharp[0])
