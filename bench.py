@@ -261,9 +261,11 @@ def run_ours(args, rank, world, local):
     with _native.record_launches(timed=True) as rec:
         for i in range(args.steps):
             flush.fill_(float(i))
+            torch.cuda.nvtx.range_push("step")
             ev[i][0].record(stream)
             loss, stats = step()
             ev[i][1].record(stream)
+            torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize(device)
     wall = time.perf_counter() - wall0
     barrier(world)

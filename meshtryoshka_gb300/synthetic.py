@@ -101,15 +101,17 @@ def make_occupancy(cfg: SceneConfig, device: torch.device | str = "cpu") -> torc
     coords = (-1.0 + (torch.arange(n, device=device, dtype=torch.float32) + 0.5) * width)
     powers = (1 << torch.arange(32, device=device, dtype=torch.int64))
     packed = torch.empty((n, n, n // 32), dtype=torch.int32, device=device)
-    # One i-slab at a time keeps memory bounded at 512^3.
-    for i in range(n):
-        z = coords[i].expand(n, n)
-        y = coords[:, None].expand(n, n)
-        x = coords[None, :].expand(n, n)
+    # Slabs of i keep memory bounded at 512^3 with few launches.
+    slab = max(1, (1 << 22) // (n * n))
+    for i0 in range(0, n, slab):
+        i1 = min(n, i0 + slab)
+        z = coords[i0:i1, None, None].expand(i1 - i0, n, n)
+        y = coords[None, :, None].expand(i1 - i0, n, n)
+        x = coords[None, None, :].expand(i1 - i0, n, n)
         pts = torch.stack((x, y, z), dim=-1)
         d = analytic_sdf(pts, centres_t, radii_t, cfg.background_radius)
-        occ = (d.abs() < cfg.band_voxels * width).reshape(n, n // 32, 32)
-        packed[i] = (occ.to(torch.int64) * powers).sum(-1).to(torch.uint32).view(torch.int32)
+        occ = (d.abs() < cfg.band_voxels * width).reshape(i1 - i0, n, n // 32, 32)
+        packed[i0:i1] = (occ.to(torch.int64) * powers).sum(-1).to(torch.uint32).view(torch.int32)
     return packed
 
 
