@@ -46,7 +46,8 @@ enum mt_status {
   MT_ERR_WORKSPACE_TOO_SMALL = 3,
   MT_ERR_KEY_OVERFLOW = 4,      /* a key field does not fit its bit budget */
   MT_ERR_DEVICE_TIMEOUT = 5,    /* a bounded device spin-wait gave up */
-  MT_ERR_CAPACITY = 6           /* an output buffer is smaller than needed */
+  MT_ERR_CAPACITY = 6,          /* an output buffer is smaller than needed */
+  MT_ERR_TOO_LARGE = 7          /* size exceeds a fixed static-scratch limit */
 };
 
 /* Human-readable name of a status code (static string, never NULL). */
@@ -78,6 +79,23 @@ MT_API int mt_exclusive_scan_i64(int64_t* data, int64_t n, void* workspace,
 MT_API int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n,
                                  void* workspace, size_t workspace_bytes,
                                  mt_stream_t stream);
+
+/* Allocation-free exclusive scan (no counterpart in the reference). Same
+ * result as mt_exclusive_scan_i32, for callers that cannot allocate device
+ * memory for scratch: a plain C/C++ host with no device allocator of its own,
+ * or code whose host framework forbids new device allocations. Its scratch is
+ * a fixed 131,328-byte __device__ array inside this library, resident on
+ * every GPU that loads it until the process exits. Limits: n <=
+ * mt_exclusive_scan_i32_static_max_elements() (2^26); larger n returns
+ * MT_ERR_TOO_LARGE. All calls on a device share the array, so calls whose
+ * work overlaps on the GPU race; issue them on one stream. The first call on
+ * a device (with that device current) looks up the array's address; make it
+ * before any stream capture on that device. data must live on the current
+ * device. */
+MT_API int mt_exclusive_scan_i32_static(int32_t* data, int64_t n, mt_stream_t stream);
+
+/* Largest n accepted by mt_exclusive_scan_i32_static. */
+MT_API int64_t mt_exclusive_scan_i32_static_max_elements(void);
 
 /* ------------------------------------------------------------------------
  * Voxel extraction (triangle_extraction/__init__.py:31-62 extract_voxels).

@@ -20,6 +20,8 @@ const char* mt_status_string(int status) {
       return "device spin-wait timed out";
     case MT_ERR_CAPACITY:
       return "output capacity exceeded";
+    case MT_ERR_TOO_LARGE:
+      return "size exceeds the static scratch limit";
     default:
       return "unknown status";
   }

@@ -13,6 +13,9 @@
 // Workspace layout: [0,4) status, [4,8) tile counter, [256, 256+8*tiles)
 // tile descriptors. Descriptor = (inclusive-or-aggregate value << 2) | flag.
 
+#include <atomic>
+#include <mutex>
+
 #include "mt_common.cuh"
 
 namespace mt {
@@ -235,6 +238,84 @@ int mt_exclusive_scan_i64(int64_t* data, int64_t n, void* ws, size_t ws_bytes, m
 int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, void* ws, size_t ws_bytes,
                                  mt_stream_t stream) {
   return mt::launch_scan<int32_t, int64_t, true>(in, out, n, ws, ws_bytes, mt::as_stream(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free exclusive scan.
+//
+// Some callers cannot allocate device memory for the scan's scratch: a plain
+// C or C++ host that links this library without any device allocator of its
+// own, or code running under a host framework whose memory policy forbids
+// new device allocations (or where a cudaMalloc would synchronise the device
+// in the middle of its work). For them, this variant keeps its scratch in a
+// file-scope __device__ array of fixed size, so a call needs nothing but the
+// data pointer and a stream.
+//
+// Limits and sharing rules:
+//   * at most kStaticScanMaxElements (2^26 = 67,108,864) elements per call;
+//     larger sizes are rejected with MT_ERR_TOO_LARGE before any work;
+//   * the array (131,328 bytes) is resident on every GPU that loads this
+//     library, until the process exits;
+//   * every call on a device shares the same array and re-initialises the
+//     parts that must start at zero, so calls whose work overlaps on the GPU
+//     (two streams at once) race and must not be issued;
+//   * the first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress, with that device current, and caches it; make
+//     that first call before any stream capture on that device.
+// ---------------------------------------------------------------------------
+namespace mt {
+namespace {
+
+constexpr int64_t kStaticScanMaxElements = (int64_t)1 << 26;
+constexpr size_t kStaticScanBytes =
+    kScanHeader + (size_t)((kStaticScanMaxElements + kScanTile - 1) / kScanTile) * 8;
+constexpr int kStaticScanMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scan_scratch[kStaticScanBytes];
+
+// Host-side cache of each device's address of the array above. The symbol
+// itself is only a host-side stand-in and must never be passed to a kernel.
+std::atomic<void*> g_static_scan_address[kStaticScanMaxDevices];
+std::mutex g_static_scan_setup;
+
+int static_scan_scratch(void** out) {
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return MT_ERR_CUDA;
+  if (device < 0 || device >= kStaticScanMaxDevices) return MT_ERR_INVALID_ARGUMENT;
+  void* p = g_static_scan_address[device].load(std::memory_order_acquire);
+  if (p == nullptr) {
+    std::lock_guard<std::mutex> lock(g_static_scan_setup);
+    p = g_static_scan_address[device].load(std::memory_order_relaxed);
+    if (p == nullptr) {
+      if (cudaGetSymbolAddress(&p, g_static_scan_scratch) != cudaSuccess || p == nullptr) return MT_ERR_CUDA;
+      g_static_scan_address[device].store(p, std::memory_order_release);
+    }
+  }
+  *out = p;
+  return MT_OK;
+}
+
+}  // namespace
+}  // namespace mt
+
+extern "C" {
+
+int64_t mt_exclusive_scan_i32_static_max_elements(void) { return mt::kStaticScanMaxElements; }
+
+int mt_exclusive_scan_i32_static(int32_t* data, int64_t n, mt_stream_t stream) {
+  MT_REQUIRE(n >= 0);
+  if (n > mt::kStaticScanMaxElements) return MT_ERR_TOO_LARGE;
+  if (n == 0) return MT_OK;
+  MT_REQUIRE(data != nullptr);
+  void* scratch = nullptr;
+  const int rc = mt::static_scan_scratch(&scratch);
+  if (rc != MT_OK) return rc;
+  // The status word is cleared too: calls share the array.
+  if (cudaMemsetAsync(scratch, 0, 4, mt::as_stream(stream)) != cudaSuccess) return MT_ERR_CUDA;
+  return mt::launch_scan<int32_t, int32_t, false>(data, data, n, scratch, mt::kStaticScanBytes,
+                                                  mt::as_stream(stream));
 }
 
 }  // extern "C"
