@@ -279,31 +279,35 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
  * Fused multi-shell compositing
  * (triangle_rasterization/intersect_and_composite.slang:224-564).
  * xy [B,V,2], colors [B,V,3], signed_distances [V], faces [F,3],
- * sharpness: device scalar; tile_boundaries [B, rows*cols, 2];
+ * sharpness: device scalar; sorted keys / triangles [K]; tile_boundaries
+ * [B, rows*cols, 2]; layout: host int32[7] key layout (as mt_generate_keys);
  * out [B,4,H,W] = (rgb, transmittance). One CTA of tile_h*tile_w (<= 1024)
- * threads per (camera, tile).
+ * threads per (camera, tile); its warps work independently.
+ * warp_masks [K] uint32 is scratch written by the forward (per key, the warps
+ * of its tile the triangle can cover) and read by the backward.
  * ---------------------------------------------------------------------- */
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
     const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
-    const int32_t* sorted_triangles, const int64_t* tile_boundaries, int32_t B,
-    int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w,
-    int32_t H, int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
-    float* out, mt_stream_t stream);
+    const int32_t* sorted_triangles, int64_t K, const int64_t* tile_boundaries,
+    int32_t B, int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
+    int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
+    uint32_t* warp_masks, float* out, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
- * [V], grad_sharpness [1]. exact_adjoint = 0 reproduces the reference's
- * gradient routing (the outer hit's deferred gradient is scattered with the
- * current hit's barycentric weights); 1 uses the outer hit's own weights. */
+ * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
+ * same keys. exact_adjoint = 0 reproduces the reference's gradient routing
+ * (the outer hit's deferred gradient is scattered with the current hit's
+ * barycentric weights); 1 uses the outer hit's own weights. */
 MT_API int mt_intersect_and_composite_backward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
     const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
-    const int32_t* sorted_triangles, const int64_t* tile_boundaries, int32_t B,
-    int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w,
-    int32_t H, int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
-    const float* out, const float* grad_out, float* grad_colors,
-    float* grad_signed_distances, float* grad_sharpness, int32_t exact_adjoint,
-    mt_stream_t stream);
+    const int32_t* sorted_triangles, int64_t K, const int64_t* tile_boundaries,
+    int32_t B, int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
+    int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
+    const uint32_t* warp_masks, const float* out, const float* grad_out,
+    float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
+    int32_t exact_adjoint, mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Explicit mode (triangle_rasterization/__init__.py:22-164).

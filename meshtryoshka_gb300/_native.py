@@ -66,11 +66,11 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_delineate_tiles": (I32, [P, I64, P, I32, I32, I32, I64, P, P]),
     "mt_intersect_and_composite_forward": (
         I32,
-        [P, P, P, I64, P, P, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P, P],
+        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P],
     ),
     "mt_intersect_and_composite_backward": (
         I32,
-        [P, P, P, I64, P, P, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P, P, I32, P],
+        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P, P, P, P, I32, P],
     ),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),

@@ -1,31 +1,38 @@
 // Fused multi-shell intersect + composite, forward and backward, for sm_103a.
 //
 // Follows triangle_rasterization/intersect_and_composite.slang:1-564. One CTA
-// per (camera, tile), one thread per pixel. Each tile's depth-sorted triangle
-// list is staged through shared memory in chunks of up to 256 triangles; the
-// staging thread computes the triangle-only part of the barycentric solve
-// (edge vectors, the six edge dot products, the chosen denominator) once,
-// with the same operations the per-pixel formula uses, so every per-pixel
-// result is bit-identical to evaluating the full formula per pixel.
+// per (camera, tile) and one thread per pixel, as in the reference, but the
+// warps of a CTA never wait for each other:
 //
-// Work reduction without changing any decision:
-//   * warps cover compact 8x4 pixel blocks and build, per chunk, a compacted
-//     list (ballot + popcount) of the triangles whose conservative accept box
-//     overlaps their pixels (bary.cuh: cull_box);
-//   * per pixel, the three barycentric numerators reject most remaining
-//     triangles before any division (bary.cuh: hit_test).
+//   * a pre-pass (warp_mask_kernel) gives every sorted key a bitmask of the
+//     warps of its tile whose pixels the triangle can cover. Warps own compact
+//     8x4 pixel blocks, and the bit is set unless the triangle's conservative
+//     accept box (bary.cuh: cull_box) misses the block, so culling changes
+//     no hit decision;
+//   * each warp walks its tile's key list on its own: it scans 32 masks per
+//     step (one coalesced load + ballot), queues the keys that concern it,
+//     and whenever 32 are queued its lanes gather those triangles (one each)
+//     into the warp's private shared memory, computing the triangle-only part
+//     of the barycentric solve with the same operations the per-pixel formula
+//     uses (bit-identical results), then composites them in depth order;
+//   * a warp stops as soon as all its pixels are done, without any CTA-wide
+//     barrier.
 //
-// Backward re-walks the list, recomputes hits and applies the suffix trick
-// of the reference. Per-triangle gradients are summed in shared memory per
-// chunk (12 floats per staged triangle) and flushed with one global atomic
-// per non-zero scalar; gradients for triangles of an earlier chunk go to
-// global memory directly. Two routings:
+// Per pixel, the three barycentric numerators reject most triangles before
+// any division (bary.cuh: hit_test).
+//
+// Backward re-walks the same way, recomputes hits and applies the suffix
+// trick of the reference. Per-triangle gradient sums live in a per-warp ring
+// of 64 shared-memory slots (the current and the previous batch); a slot is
+// flushed to global memory with one atomic per non-zero scalar when its batch
+// retires, and gradients for older triangles go to global memory directly.
+// Two routings:
 //   reference (exact_adjoint = 0): the deferred gradient of the previous
 //     (outer) hit is scattered to the previous triangle's vertices with the
 //     *current* hit's barycentric weights (intersect_and_composite.slang:
 //     487-509), as the reference does;
 //   exact (exact_adjoint = 1): with the previous hit's own weights.
-// The sharpness gradient is reduced per CTA before one global atomic.
+// The sharpness gradient is warp-reduced before one global atomic per warp.
 
 #include "bary.cuh"
 #include "mt_common.cuh"
@@ -33,7 +40,9 @@
 namespace mt {
 namespace {
 
-constexpr int kMaxChunk = 256;
+constexpr int kBatch = 32;   // triangles gathered per warp batch
+constexpr int kQueue = 64;   // queued key offsets per warp
+constexpr int kRing = 64;    // gradient slots per warp (two batches)
 
 struct TriAttr {
   float ca[3], cb[3], cc[3];
@@ -51,7 +60,7 @@ struct CompositeArgs {
   const int32_t* tri;     // sorted triangle indices
   const int64_t* bounds;  // [B, T, 2]
   int B, S, rows, cols, tile_h, tile_w, H, W;
-  int shell_off, shell_len;
+  int shell_off, shell_len, cam_off, cam_len, tile_off, tile_len;
   const float* out;  // forward output [B, 4, H, W] (input to backward)
 };
 
@@ -63,45 +72,85 @@ struct CompositeGrads {
   int exact;
 };
 
-// Shared-memory carve-up for one chunk of `chunk` staged triangles.
-struct Smem {
-  TriGeom* geo;
-  TriAttr* attr;
-  CullBox* box;
-  int3* vids;        // backward only
-  float* gslot;      // backward only: [chunk][12]
-  uint8_t* wlist;    // [warps][chunk]
+// Per-warp shared-memory region.
+struct WarpForward {
+  TriGeom geo[kBatch];
+  TriAttr attr[kBatch];
+  int queue[kQueue];
 };
 
-__device__ __forceinline__ Smem carve(void* base, int chunk, int warps, bool backward) {
-  char* p = static_cast<char*>(base);
-  Smem s;
-  s.geo = reinterpret_cast<TriGeom*>(p);
-  p += sizeof(TriGeom) * chunk;
-  s.attr = reinterpret_cast<TriAttr*>(p);
-  p += sizeof(TriAttr) * chunk;
-  s.box = reinterpret_cast<CullBox*>(p);
-  p += sizeof(CullBox) * chunk;
-  s.vids = nullptr;
-  s.gslot = nullptr;
-  if (backward) {
-    s.vids = reinterpret_cast<int3*>(p);
-    p += sizeof(int3) * chunk;
-    s.gslot = reinterpret_cast<float*>(p);
-    p += sizeof(float) * 12 * chunk;
+struct WarpBackward {
+  TriGeom geo[kBatch];
+  TriAttr attr[kBatch];
+  int3 vids[kRing];
+  float gslot[kRing][13];  // 12 used; stride 13 keeps lanes on distinct banks
+  int queue[kQueue];
+};
+
+__device__ __forceinline__ uint64_t field(uint64_t key, int off, int len) {
+  return (key >> off) & (uint64_t)((1u << len) - 1u);
+}
+
+// Pixel rectangle (pixel centres) of warp `w` inside tile (tx, ty); matches
+// tile_pixel().
+__device__ __forceinline__ void warp_block_rect(int w, int tile_w, int tile_h, int tx, int ty, float& x0, float& x1,
+                                                float& y0, float& y1) {
+  int lx0, lx1, ly0, ly1;
+  if ((tile_w & 7) == 0 && (tile_h & 3) == 0) {
+    const int per_row = tile_w >> 3;
+    lx0 = (w % per_row) * 8;
+    lx1 = lx0 + 7;
+    ly0 = (w / per_row) * 4;
+    ly1 = ly0 + 3;
+  } else {
+    const int numel = tile_w * tile_h;
+    const int t0 = 32 * w, t1 = min(32 * w + 31, numel - 1);
+    ly0 = t0 / tile_w;
+    ly1 = t1 / tile_w;
+    if (ly0 == ly1) {
+      lx0 = t0 % tile_w;
+      lx1 = t1 % tile_w;
+    } else {
+      lx0 = 0;
+      lx1 = tile_w - 1;
+    }
   }
-  s.wlist = reinterpret_cast<uint8_t*>(p);
-  return s;
+  x0 = (float)(tx * tile_w + lx0) + 0.5f;
+  x1 = (float)(tx * tile_w + lx1) + 0.5f;
+  y0 = (float)(ty * tile_h + ly0) + 0.5f;
+  y1 = (float)(ty * tile_h + ly1) + 0.5f;
 }
 
-size_t smem_bytes(int chunk, int warps, bool backward) {
-  size_t b = (sizeof(TriGeom) + sizeof(TriAttr) + sizeof(CullBox)) * (size_t)chunk;
-  if (backward) b += (sizeof(int3) + 12 * sizeof(float)) * (size_t)chunk;
-  return b + (size_t)warps * chunk;
+// One mask per sorted key: bit w = warp w of the key's tile may be covered.
+__global__ void warp_mask_kernel(CompositeArgs a, int64_t K, uint32_t* __restrict__ masks) {
+  const int warps = (a.tile_h * a.tile_w + 31) / 32;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
+    const int cam = (int)field(key, a.cam_off, a.cam_len);
+    const int tile = (int)field(key, a.tile_off, a.tile_len);
+    uint32_t m = 0;
+    if (cam < a.B && tile < a.rows * a.cols) {
+      const int32_t f = __ldg(a.tri + k);
+      const float2* xy = reinterpret_cast<const float2*>(a.xy) + (int64_t)cam * a.V;
+      const float2 pa = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f)), pb = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f + 1)),
+                   pc = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f + 2));
+      TriGeom g;
+      setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
+      const CullBox box = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
+      const int tx = tile % a.cols, ty = tile / a.cols;
+      for (int w = 0; w < warps; ++w) {
+        float x0, x1, y0, y1;
+        warp_block_rect(w, a.tile_w, a.tile_h, tx, ty, x0, x1, y0, y1);
+        if (box_overlaps(box, x0, x1, y0, y1)) m |= 1u << w;
+      }
+    }
+    masks[k] = m;
+  }
 }
 
-// Stages triangle `k` of the sorted list into slot `slot`.
-__device__ __forceinline__ void stage(const CompositeArgs& a, int cam, int64_t k, const Smem& sm, int slot) {
+// Gathers triangle `k` of the sorted list into batch slot `slot`.
+__device__ __forceinline__ int3 gather(const CompositeArgs& a, int cam, int64_t k, TriGeom* geo, TriAttr* attr,
+                                       int slot) {
   const int32_t f = __ldg(a.tri + k);
   const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
   const int32_t ia = __ldg(a.faces + 3 * (int64_t)f), ib = __ldg(a.faces + 3 * (int64_t)f + 1),
@@ -110,9 +159,8 @@ __device__ __forceinline__ void stage(const CompositeArgs& a, int cam, int64_t k
   const float2 pa = __ldg(xy + ia), pb = __ldg(xy + ib), pc = __ldg(xy + ic);
   TriGeom g;
   setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
-  g.shell = (int)((key >> a.shell_off) & (uint64_t)((1u << a.shell_len) - 1u));
-  sm.geo[slot] = g;
-  sm.box[slot] = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
+  g.shell = (int)field(key, a.shell_off, a.shell_len);
+  geo[slot] = g;
   const float* col = a.colors + (int64_t)cam * a.V * 3;
   TriAttr t;
 #pragma unroll
@@ -124,64 +172,67 @@ __device__ __forceinline__ void stage(const CompositeArgs& a, int cam, int64_t k
   t.sa = __ldg(a.sdf + ia);
   t.sb = __ldg(a.sdf + ib);
   t.sc = __ldg(a.sdf + ic);
-  sm.attr[slot] = t;
-  if (sm.vids) sm.vids[slot] = make_int3(ia, ib, ic);
+  attr[slot] = t;
+  return make_int3(ia, ib, ic);
 }
 
-// Builds this warp's list of staged triangles whose accept box overlaps the
-// warp's pixels; returns its length.
-__device__ __forceinline__ int build_warp_list(const Smem& sm, int n, int chunk, int warp, int lane, float rx0,
-                                               float rx1, float ry0, float ry1) {
-  uint8_t* list = sm.wlist + warp * chunk;
-  int count = 0;
-  for (int base = 0; base < n; base += 32) {
-    const int i = base + lane;
-    const bool keep = i < n && box_overlaps(sm.box[i], rx0, rx1, ry0, ry1);
-    const uint32_t m = __ballot_sync(0xffffffffu, keep);
-    if (keep) list[count + __popc(m & lanemask_lt())] = (uint8_t)i;
-    count += __popc(m);
+// Fills the warp's queue with offsets (relative to `start`) of keys whose
+// mask has this warp's bit, until 32 are queued or the list ends. Returns the
+// number queued; `next` advances through the list 32 keys at a time.
+__device__ __forceinline__ int refill(const uint32_t* __restrict__ masks, int64_t start, int64_t end, int64_t& next,
+                                      int queued, int* queue, int warp, int lane) {
+  const uint32_t lt = lanemask_lt();
+  while (queued < kBatch && next < end) {
+    const int64_t k = next + lane;
+    const bool keep = k < end && ((__ldg(masks + k) >> warp) & 1u);
+    const uint32_t sel = __ballot_sync(0xffffffffu, keep);
+    if (keep) queue[queued + __popc(sel & lt)] = (int)(k - start);
+    queued += __popc(sel);
+    next += 32;
   }
   __syncwarp();
-  return count;
+  return queued;
 }
 
-struct PixelSetup {
+// Drops the first `nb` queue entries.
+__device__ __forceinline__ void pop(int* queue, int queued, int nb, int lane) {
+  const int rest = queued - nb;  // <= 31
+  const int v = lane < rest ? queue[nb + lane] : 0;
+  __syncwarp();
+  if (lane < rest) queue[lane] = v;
+  __syncwarp();
+}
+
+struct Pixel {
   int cam;
   int64_t tile;
   int px, py;
   bool in_image;
   float fx, fy;
-  float rx0, rx1, ry0, ry1;
 };
 
-__device__ __forceinline__ PixelSetup setup_pixel(const CompositeArgs& a) {
-  PixelSetup p;
+__device__ __forceinline__ Pixel pixel_of(const CompositeArgs& a) {
+  Pixel p;
   const int64_t T = (int64_t)a.rows * a.cols;
   p.tile = blockIdx.x % T;
   p.cam = (int)(blockIdx.x / T);
-  const int tid = threadIdx.x;
-  const int numel = a.tile_h * a.tile_w;
   int lx = 0, ly = 0;
-  tile_pixel(tid, a.tile_w, a.tile_h, lx, ly);
-  const bool in_tile = tid < numel;
+  tile_pixel(threadIdx.x, a.tile_w, a.tile_h, lx, ly);
   p.px = (int)(p.tile % a.cols) * a.tile_w + lx;
   p.py = (int)(p.tile / a.cols) * a.tile_h + ly;
-  p.in_image = in_tile && p.px < a.W && p.py < a.H;
+  p.in_image = (int)threadIdx.x < a.tile_h * a.tile_w && p.px < a.W && p.py < a.H;
   p.fx = (float)p.px + 0.5f;
   p.fy = (float)p.py + 0.5f;
-  const float nan = __int_as_float(0x7fffffff);
-  warp_rect(in_tile ? p.fx : nan, in_tile ? p.fy : nan, p.rx0, p.rx1, p.ry0, p.ry1);
   return p;
 }
 
 template <int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads) composite_forward_kernel(CompositeArgs a, float* __restrict__ out) {
+__global__ void __launch_bounds__(kMaxThreads)
+    composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out) {
   extern __shared__ float4 smem_f4[];
-  const int bs = blockDim.x;
-  const int chunk = bs < kMaxChunk ? bs : kMaxChunk;
-  const Smem sm = carve(smem_f4, chunk, bs >> 5, false);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const PixelSetup px = setup_pixel(a);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[warp];
+  const Pixel px = pixel_of(a);
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -194,21 +245,22 @@ __global__ void __launch_bounds__(kMaxThreads) composite_forward_kernel(Composit
 
   const int64_t start = a.bounds[2 * ((int64_t)px.cam * T + px.tile)];
   const int64_t end = a.bounds[2 * ((int64_t)px.cam * T + px.tile) + 1];
-  for (int64_t c0 = start; c0 < end; c0 += chunk) {
-    if (__syncthreads_count(active) == 0) break;
-    const int n = (int)min((int64_t)chunk, end - c0);
-    if (tid < n) stage(a, px.cam, c0 + tid, sm, tid);
-    __syncthreads();
-    const int len = build_warp_list(sm, n, chunk, warp, lane, px.rx0, px.rx1, px.ry0, px.ry1);
+  int64_t next = start;
+  int queued = 0;
+  while (__any_sync(0xffffffffu, active)) {
+    queued = refill(masks, start, end, next, queued, ws.queue, warp, lane);
+    const int nb = min(queued, kBatch);
+    if (nb == 0) break;
+    if (lane < nb) gather(a, px.cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
+    pop(ws.queue, queued, nb, lane);
+    queued -= nb;
     if (active) {
-      const uint8_t* list = sm.wlist + warp * chunk;
-      for (int j = 0; j < len; ++j) {
-        const int i = list[j];
-        const TriGeom& g = sm.geo[i];
+      for (int i = 0; i < nb; ++i) {
+        const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
         if (!hit_test(g, px.fx, px.fy, u, v, w)) continue;
-        const TriAttr& t = sm.attr[i];
+        const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
         const float inner_cdf = sdf_to_cdf(sdf_in, s, e_in);
@@ -227,6 +279,7 @@ __global__ void __launch_bounds__(kMaxThreads) composite_forward_kernel(Composit
         }
       }
     }
+    __syncwarp();
   }
   if (px.in_image) {
     const int64_t plane = (int64_t)a.H * a.W;
@@ -262,15 +315,37 @@ __device__ __forceinline__ void scatter_slot(float* slot, float u, float v, floa
   }
 }
 
+// Flushes and clears the 32 ring slots of batch parity `half` (lane i owns
+// slot half * 32 + i).
+__device__ __forceinline__ void flush_half(const CompositeArgs& a, const CompositeGrads& gr, int cam, WarpBackward& ws,
+                                           int half, int lane) {
+  const int slot = half * kBatch + lane;
+  float* g = ws.gslot[slot];
+  const int3 vid = ws.vids[slot];
+  const int id[3] = {vid.x, vid.y, vid.z};
+  float* gc = gr.grad_colors + (int64_t)cam * a.V * 3;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float x = g[4 * q + c];
+      if (x != 0.f) atomicAdd(gc + 3 * (int64_t)id[q] + c, x);
+      g[4 * q + c] = 0.f;
+    }
+    const float y = g[4 * q + 3];
+    if (y != 0.f) atomicAdd(gr.grad_sdf + id[q], y);
+    g[4 * q + 3] = 0.f;
+  }
+  __syncwarp();
+}
+
 template <int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads) composite_backward_kernel(CompositeArgs a, CompositeGrads gr) {
+__global__ void __launch_bounds__(kMaxThreads)
+    composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr) {
   extern __shared__ float4 smem_f4[];
-  __shared__ float s_red[32];
-  const int bs = blockDim.x;
-  const int chunk = bs < kMaxChunk ? bs : kMaxChunk;
-  const Smem sm = carve(smem_f4, chunk, bs >> 5, true);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const PixelSetup px = setup_pixel(a);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[warp];
+  const Pixel px = pixel_of(a);
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -288,7 +363,10 @@ __global__ void __launch_bounds__(kMaxThreads) composite_backward_kernel(Composi
     final_T = a.out[o + 3 * plane];
     dL_T = gr.grad_out[o + 3 * plane];
   }
-  for (int i = tid; i < chunk * 12; i += bs) sm.gslot[i] = 0.f;
+  for (int i = lane; i < kRing * 13; i += 32) (&ws.gslot[0][0])[i] = 0.f;
+  ws.vids[lane] = make_int3(0, 0, 0);
+  ws.vids[kBatch + lane] = make_int3(0, 0, 0);
+  __syncwarp();
 
   float acc[3] = {0.f, 0.f, 0.f};
   float T_ = 1.0f;
@@ -300,27 +378,32 @@ __global__ void __launch_bounds__(kMaxThreads) composite_backward_kernel(Composi
   float d_sharp = 0.f;
   float dp_rgb[3] = {0.f, 0.f, 0.f};
   float dp_sdf = 0.f;
-  int64_t prev_k = -1;
+  int prev_batch = -2, prev_slot = 0;  // ring slot of the previous hit (valid while its batch is live)
   int3 prev_vid = make_int3(0, 0, 0);
   float pu = 0.f, pv = 0.f, pw = 0.f;
 
   const int64_t start = a.bounds[2 * ((int64_t)cam * T + px.tile)];
   const int64_t end = a.bounds[2 * ((int64_t)cam * T + px.tile) + 1];
-  for (int64_t c0 = start; c0 < end; c0 += chunk) {
-    if (__syncthreads_count(active) == 0) break;
-    const int n = (int)min((int64_t)chunk, end - c0);
-    if (tid < n) stage(a, cam, c0 + tid, sm, tid);
-    __syncthreads();
-    const int len = build_warp_list(sm, n, chunk, warp, lane, px.rx0, px.rx1, px.ry0, px.ry1);
+  int64_t next = start;
+  int queued = 0;
+  int batch = 0;
+  while (__any_sync(0xffffffffu, active)) {
+    queued = refill(masks, start, end, next, queued, ws.queue, warp, lane);
+    const int nb = min(queued, kBatch);
+    if (nb == 0) break;
+    const int half = batch & 1;
+    // The half being overwritten held batch - 2: flush it first.
+    if (batch >= 2) flush_half(a, gr, cam, ws, half, lane);
+    if (lane < nb) ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
+    pop(ws.queue, queued, nb, lane);
+    queued -= nb;
     if (active) {
-      const uint8_t* list = sm.wlist + warp * chunk;
-      for (int j = 0; j < len; ++j) {
-        const int i = list[j];
-        const TriGeom& g = sm.geo[i];
+      for (int i = 0; i < nb; ++i) {
+        const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
         if (!hit_test(g, px.fx, px.fy, u, v, w)) continue;
-        const TriAttr& t = sm.attr[i];
+        const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
         const float inner_cdf = sdf_to_cdf(sdf_in, s, e_in);
@@ -358,16 +441,17 @@ __global__ void __launch_bounds__(kMaxThreads) composite_backward_kernel(Composi
         if (last_shell != -1) {
           dp_sdf += d_oc * ko * s;
           const float su = gr.exact ? pu : u, sv = gr.exact ? pv : v, sw = gr.exact ? pw : w;
-          if (prev_k >= c0)
-            scatter_slot(sm.gslot + 12 * (prev_k - c0), su, sv, sw, dp_rgb, dp_sdf);
+          if (prev_batch >= batch - 1)
+            scatter_slot(ws.gslot[prev_slot], su, sv, sw, dp_rgb, dp_sdf);
           else
             scatter_global(a, gr, cam, prev_vid, su, sv, sw, dp_rgb, dp_sdf);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) dp_rgb[c] = d_color[c];
         dp_sdf = d_ic * ki * s;
-        prev_k = c0 + i;
-        prev_vid = sm.vids[i];
+        prev_batch = batch;
+        prev_slot = half * kBatch + i;
+        prev_vid = ws.vids[prev_slot];
         pu = u;
         pv = v;
         pw = w;
@@ -383,42 +467,25 @@ __global__ void __launch_bounds__(kMaxThreads) composite_backward_kernel(Composi
         }
       }
     }
-    // Flush this chunk's per-triangle sums (thread t owns slot t).
-    __syncthreads();
-    if (tid < n) {
-      float* slot = sm.gslot + 12 * tid;
-      const int3 vid = sm.vids[tid];
-      const int id[3] = {vid.x, vid.y, vid.z};
-      float* gc = gr.grad_colors + (int64_t)cam * a.V * 3;
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float x = slot[4 * q + c];
-          if (x != 0.f) atomicAdd(gc + 3 * (int64_t)id[q] + c, x);
-          slot[4 * q + c] = 0.f;
-        }
-        const float y = slot[4 * q + 3];
-        if (y != 0.f) atomicAdd(gr.grad_sdf + id[q], y);
-        slot[4 * q + 3] = 0.f;
-      }
-    }
+    __syncwarp();
+    ++batch;
   }
-  if (px.in_image && last_shell != -1) scatter_global(a, gr, cam, prev_vid, pu, pv, pw, dp_rgb, dp_sdf);
+  // The last hit's deferred gradient, with its own weights.
+  if (px.in_image && last_shell != -1) {
+    if (prev_batch >= batch - 2)
+      scatter_slot(ws.gslot[prev_slot], pu, pv, pw, dp_rgb, dp_sdf);
+    else
+      scatter_global(a, gr, cam, prev_vid, pu, pv, pw, dp_rgb, dp_sdf);
+  }
+  __syncwarp();
+  flush_half(a, gr, cam, ws, 0, lane);
+  flush_half(a, gr, cam, ws, 1, lane);
 
-  // Block reduction of the sharpness gradient, one atomic per CTA.
+  // Sharpness gradient: one atomic per warp.
   float x = px.in_image ? d_sharp : 0.f;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  if (lane == 0) s_red[warp] = x;
-  __syncthreads();
-  if (tid < 32) {
-    const int nw = bs >> 5;
-    float y = tid < nw ? s_red[tid] : 0.f;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
-    if (tid == 0 && y != 0.f) atomicAdd(gr.grad_sharpness, y);
-  }
+  if (lane == 0 && x != 0.f) atomicAdd(gr.grad_sharpness, x);
 }
 
 int check_args(const CompositeArgs& a) {
@@ -426,7 +493,8 @@ int check_args(const CompositeArgs& a) {
     return MT_ERR_INVALID_ARGUMENT;
   if ((int64_t)a.tile_h * a.tile_w > 1024) return MT_ERR_INVALID_ARGUMENT;
   if ((int64_t)a.rows * a.tile_h < a.H || (int64_t)a.cols * a.tile_w < a.W) return MT_ERR_INVALID_ARGUMENT;
-  if (a.shell_len < 1 || a.shell_len > 31 || a.shell_off < 0 || a.shell_off + a.shell_len > 64)
+  auto ok = [](int off, int len) { return off >= 0 && len >= 1 && len <= 31 && off + len <= 64; };
+  if (!ok(a.shell_off, a.shell_len) || !ok(a.cam_off, a.cam_len) || !ok(a.tile_off, a.tile_len))
     return MT_ERR_INVALID_ARGUMENT;
   return MT_OK;
 }
@@ -442,6 +510,38 @@ int set_smem(K kernel, size_t bytes) {
   return MT_OK;
 }
 
+CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, int64_t V, const int32_t* faces,
+                        const float* sharpness, const int64_t* keys, const int32_t* tri, const int64_t* bounds,
+                        int32_t B, int32_t S, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
+                        int32_t W, const int32_t* layout, const float* out) {
+  CompositeArgs a{};
+  a.xy = xy;
+  a.colors = colors;
+  a.sdf = sdf;
+  a.V = V;
+  a.faces = faces;
+  a.sharpness = sharpness;
+  a.keys = reinterpret_cast<const uint64_t*>(keys);
+  a.tri = tri;
+  a.bounds = bounds;
+  a.B = B;
+  a.S = S;
+  a.rows = rows;
+  a.cols = cols;
+  a.tile_h = tile_h;
+  a.tile_w = tile_w;
+  a.H = H;
+  a.W = W;
+  a.cam_off = layout ? layout[0] : -1;
+  a.cam_len = layout ? layout[1] : 0;
+  a.shell_off = layout ? layout[2] : -1;
+  a.shell_len = layout ? layout[3] : 0;
+  a.tile_off = layout ? layout[4] : -1;
+  a.tile_len = layout ? layout[5] : 0;
+  a.out = out;
+  return a;
+}
+
 }  // namespace
 }  // namespace mt
 
@@ -451,31 +551,36 @@ extern "C" {
 
 int mt_intersect_and_composite_forward(const float* xy, const float* colors, const float* signed_distances,
                                        int64_t V, const int32_t* faces, const float* sharpness,
-                                       const int64_t* sorted_keys, const int32_t* sorted_triangles,
+                                       const int64_t* sorted_keys, const int32_t* sorted_triangles, int64_t K,
                                        const int64_t* tile_boundaries, int32_t B, int32_t num_shells,
                                        int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
-                                       int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
-                                       float* out, mt_stream_t stream) {
-  CompositeArgs a{xy, colors, signed_distances, V, faces, sharpness,
-                  reinterpret_cast<const uint64_t*>(sorted_keys), sorted_triangles, tile_boundaries,
-                  B, num_shells, rows, cols, tile_h, tile_w, H, W, shell_bit_offset, shell_bit_length, nullptr};
+                                       int32_t W, const int32_t* layout, uint32_t* warp_masks, float* out,
+                                       mt_stream_t stream) {
+  MT_REQUIRE(layout != nullptr && K >= 0);
+  CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
+                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
   const int64_t blocks = (int64_t)B * rows * cols;
   if (blocks == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out);
+  MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
   MT_REQUIRE(blocks < ((int64_t)1 << 31));
+  cudaStream_t s = as_stream(stream);
+  if (K > 0) {
+    warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, warp_masks);
+    MT_CHECK_LAUNCH();
+  }
   const int bs = block_threads(a);
-  const int chunk = bs < kMaxChunk ? bs : kMaxChunk;
-  const size_t smem = smem_bytes(chunk, bs / 32, false);
+  const size_t smem = sizeof(WarpForward) * (bs / 32);
   if (bs <= 256) {
     rc = set_smem(composite_forward_kernel<256>, smem);
     if (rc != MT_OK) return rc;
-    composite_forward_kernel<256><<<(unsigned)blocks, bs, smem, as_stream(stream)>>>(a, out);
+    composite_forward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
   } else {
     rc = set_smem(composite_forward_kernel<1024>, smem);
     if (rc != MT_OK) return rc;
-    composite_forward_kernel<1024><<<(unsigned)blocks, bs, smem, as_stream(stream)>>>(a, out);
+    composite_forward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
   }
   MT_CHECK_LAUNCH();
   return MT_OK;
@@ -483,35 +588,36 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
 
 int mt_intersect_and_composite_backward(const float* xy, const float* colors, const float* signed_distances,
                                         int64_t V, const int32_t* faces, const float* sharpness,
-                                        const int64_t* sorted_keys, const int32_t* sorted_triangles,
+                                        const int64_t* sorted_keys, const int32_t* sorted_triangles, int64_t K,
                                         const int64_t* tile_boundaries, int32_t B, int32_t num_shells,
                                         int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
-                                        int32_t W, int32_t shell_bit_offset, int32_t shell_bit_length,
+                                        int32_t W, const int32_t* layout, const uint32_t* warp_masks,
                                         const float* out, const float* grad_out, float* grad_colors,
                                         float* grad_signed_distances, float* grad_sharpness, int32_t exact_adjoint,
                                         mt_stream_t stream) {
-  CompositeArgs a{xy, colors, signed_distances, V, faces, sharpness,
-                  reinterpret_cast<const uint64_t*>(sorted_keys), sorted_triangles, tile_boundaries,
-                  B, num_shells, rows, cols, tile_h, tile_w, H, W, shell_bit_offset, shell_bit_length, out};
+  MT_REQUIRE(layout != nullptr && K >= 0);
+  CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
+                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
   const int64_t blocks = (int64_t)B * rows * cols;
   if (blocks == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && grad_out);
   MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness);
+  MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
   MT_REQUIRE(blocks < ((int64_t)1 << 31));
   CompositeGrads gr{grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
   const int bs = block_threads(a);
-  const int chunk = bs < kMaxChunk ? bs : kMaxChunk;
-  const size_t smem = smem_bytes(chunk, bs / 32, true);
+  const size_t smem = sizeof(WarpBackward) * (bs / 32);
+  cudaStream_t s = as_stream(stream);
   if (bs <= 256) {
     rc = set_smem(composite_backward_kernel<256>, smem);
     if (rc != MT_OK) return rc;
-    composite_backward_kernel<256><<<(unsigned)blocks, bs, smem, as_stream(stream)>>>(a, gr);
+    composite_backward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
   } else {
     rc = set_smem(composite_backward_kernel<1024>, smem);
     if (rc != MT_OK) return rc;
-    composite_backward_kernel<1024><<<(unsigned)blocks, bs, smem, as_stream(stream)>>>(a, gr);
+    composite_backward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
   }
   MT_CHECK_LAUNCH();
   return MT_OK;

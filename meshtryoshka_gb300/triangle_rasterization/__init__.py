@@ -332,11 +332,6 @@ def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, 
 # ---------------------------------------------------------------------------
 # Fused compositing (intersect_and_composite.py:24-175)
 # ---------------------------------------------------------------------------
-def _shell_bits(key_defines) -> tuple[int, int]:
-    d = dict(key_defines)
-    return d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"]
-
-
 class IntersectAndComposite(torch.autograd.Function):
     @staticmethod
     def forward(ctx, vertices, colors, signed_distances, faces, sharpness, sorted_keys, sorted_triangle_indices,
@@ -348,15 +343,16 @@ class IntersectAndComposite(torch.autograd.Function):
             keys, tri = sorted_keys.contiguous(), _i32(sorted_triangle_indices)
             bounds = tile_boundaries.contiguous()
             b, v, _ = xy.shape
+            k = keys.numel()
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
-            soff, slen = _shell_bits(key_defines)
+            masks = torch.empty((k,), dtype=torch.int32, device=device)
             out = torch.empty((b, 4, h, w), dtype=torch.float32, device=device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
-                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), nt.ptr(bounds), b, int(num_shells),
-                    rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, soff, slen, nt.ptr(out),
-                    nt.stream(device))
-            ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, out)
+                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(bounds), b, int(num_shells),
+                    rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines), nt.ptr(masks),
+                    nt.ptr(out), nt.stream(device))
+            ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness))
             return out
@@ -364,7 +360,7 @@ class IntersectAndComposite(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         with record_function("intersect_and_composite_backward"):
-            xy, colors, sdf, faces, sharp, keys, tri, bounds, out = ctx.saved_tensors
+            xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out = ctx.saved_tensors
             num_shells, grid, key_defines, mode, sharp_is_tensor = ctx.meta
             device = xy.device
             grad_out = grad_out.contiguous()
@@ -374,12 +370,11 @@ class IntersectAndComposite(torch.autograd.Function):
             b, v, _ = xy.shape
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
-            soff, slen = _shell_bits(key_defines)
             nt.call("mt_intersect_and_composite_backward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
-                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), nt.ptr(bounds), b, num_shells,
-                    rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, soff, slen, nt.ptr(out),
-                    nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp),
-                    int(mode == "exact"), nt.stream(device))
+                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
+                    num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
+                    nt.ptr(masks), nt.ptr(out), nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf),
+                    nt.ptr(grad_sharp), int(mode == "exact"), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None)
 
