@@ -38,6 +38,13 @@ NVCC_FLAGS = [
     "-diag-suppress=177",
 ]
 
+# Translation units whose floating-point results must equal the reference
+# kernels' source evaluated operation by operation: no multiply-add
+# contraction anywhere in them. The compositing kernels keep contraction for
+# speed and spell every result-defining operation with explicit
+# __fmul_rn / __fadd_rn intrinsics instead.
+UNCONTRACTED = {"extraction", "raster_front", "explicit"}
+
 
 def find_nvcc() -> str:
     for candidate in (
@@ -59,7 +66,8 @@ def sources() -> list[Path]:
 
 
 def headers() -> list[Path]:
-    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+    # This file is a dependency too: a change of flags rebuilds everything.
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h")) + [Path(__file__)]
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:
@@ -89,8 +97,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD_DIR / (src.stem + ".o")
         objects.append(obj)
         if force or _stale(obj, [src, *hdrs]):
+            fmad = ["-fmad=false"] if src.stem in UNCONTRACTED else []
             jobs.append(
-                [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
+                [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, *fmad, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)]
             )
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as pool:

@@ -3,9 +3,10 @@
 // identical intersect.slang:14-67), plus the NeuS alpha helpers
 // (intersect_and_composite.slang:153-163, composite.slang:33-46).
 //
-// The operation order is fixed (explicit __fmaf_rn / __fmul_rn / __fdiv_rn,
-// so nvcc cannot re-contract), which lets the CPU restatement reproduce every
-// hit decision bit for bit.
+// Every operation is the reference source's, in its order and without
+// contraction (explicit __fmul_rn / __fadd_rn / __fsub_rn / __fdiv_rn, which
+// nvcc never fuses), so hit decisions equal the reference kernel evaluated
+// operation by operation in IEEE-754 single precision.
 #pragma once
 
 #include "mt_common.cuh"
@@ -21,7 +22,12 @@ struct TriGeom {
 };
 
 __device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) {
-  return __fmaf_rn(ay, by, __fmul_rn(ax, bx));
+  return __fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by));
+}
+
+// a * b - c * d, both products rounded.
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) {
+  return __fsub_rn(__fmul_rn(a, b), __fmul_rn(c, d));
 }
 
 // intersect_and_composite.slang:65-106 (triangle-only part) for one staged
@@ -40,11 +46,11 @@ __device__ __forceinline__ void setup_geometry(float p1x, float p1y, float p2x, 
   const float a = fabsf(d1213), b = fabsf(d1223), c = fabsf(d1323);
   float denom;
   if (a <= b && a <= c) {
-    denom = __fmaf_rn(d1212, d1313, -__fmul_rn(d1213, d1213));
+    denom = diff_of_products(d1212, d1313, d1213, d1213);
   } else if (b <= a && b <= c) {
-    denom = __fmaf_rn(d1212, d2323, -__fmul_rn(d1223, d1223));
+    denom = diff_of_products(d1212, d2323, d1223, d1223);
   } else if (c <= a && c <= b) {
-    denom = __fmaf_rn(d1313, d2323, -__fmul_rn(d1323, d1323));
+    denom = diff_of_products(d1313, d2323, d1323, d1323);
   } else {
     denom = __int_as_float(0x7fffffff);  // only reachable with a NaN product: the sample is rejected anyway
   }
@@ -75,9 +81,9 @@ __device__ __forceinline__ bool hit_test(const TriGeom& g, float px, float py, f
   const float d1x13 = dot2(q1x, q1y, g.e13x, g.e13y);
   const float d2x12 = dot2(q2x, q2y, g.e12x, g.e12y);
   const float d2x13 = dot2(q2x, q2y, g.e13x, g.e13y);
-  const float vn = __fmaf_rn(g.d1313, d1x12, -__fmul_rn(g.d1213, d1x13));
-  const float wn = __fmaf_rn(g.d1212, d1x13, -__fmul_rn(g.d1213, d1x12));
-  const float un = __fmaf_rn(g.d1223, d2x13, -__fmul_rn(g.d1323, d2x12));
+  const float vn = diff_of_products(g.d1313, d1x12, g.d1213, d1x13);
+  const float wn = diff_of_products(g.d1212, d1x13, g.d1213, d1x12);
+  const float un = diff_of_products(g.d1223, d2x13, g.d1323, d2x12);
   if (un < g.thr || vn < g.thr || wn < g.thr) return false;
   u = __fdiv_rn(un, g.dd);
   v = __fdiv_rn(vn, g.dd);
@@ -89,8 +95,14 @@ __device__ __forceinline__ bool hit_test(const TriGeom& g, float px, float py, f
   return true;
 }
 
+// u * a + v * b + w * c, left to right (intersect_and_composite.slang:141-146).
 __device__ __forceinline__ float interp(float u, float v, float w, float a, float b, float c) {
-  return __fmaf_rn(w, c, __fmaf_rn(v, b, __fmul_rn(u, a)));
+  return __fadd_rn(__fadd_rn(__fmul_rn(u, a), __fmul_rn(v, b)), __fmul_rn(w, c));
+}
+
+// acc + rgb * T * alpha (intersect_and_composite.slang:171-172).
+__device__ __forceinline__ float over(float acc, float rgb, float T, float alpha) {
+  return __fadd_rn(acc, __fmul_rn(__fmul_rn(rgb, T), alpha));
 }
 
 // sdf_to_cdf (intersect_and_composite.slang:153-156); also returns exp(-sdf s).

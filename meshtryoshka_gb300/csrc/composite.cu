@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kMaxThreads)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float rgb = interp(u, v, w, t.ca[c], t.cb[c], t.cc[c]);
-          acc[c] = __fmaf_rn(__fmul_rn(rgb, T_), alpha, acc[c]);
+          acc[c] = over(acc[c], rgb, T_, alpha);
         }
         T_ = __fmul_rn(T_, __fsub_rn(1.0f, alpha));
         outer_cdf = inner_cdf;
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kMaxThreads)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float rgb = interp(u, v, w, t.ca[c], t.cb[c], t.cc[c]);
-          acc[c] = __fmaf_rn(weight, rgb, acc[c]);
+          acc[c] = __fadd_rn(acc[c], __fmul_rn(weight, rgb));
           const float suffix = final_rgb[c] - acc[c];
           d_color[c] = weight * dL_rgb[c];
           d_alpha += dL_rgb[c] * (T_ * rgb - suffix * inv);

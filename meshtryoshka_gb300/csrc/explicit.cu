@@ -152,7 +152,7 @@ __global__ void shell_composite_forward_kernel(const float* __restrict__ sdf, co
       const float inner_cdf = sdf_to_cdf(inner, s, e);
       const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
 #pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] = __fmaf_rn(__fmul_rn(colors[(p * S + l) * 3 + c], T), alpha, acc[c]);
+      for (int c = 0; c < 3; ++c) acc[c] = over(acc[c], colors[(p * S + l) * 3 + c], T, alpha);
       T = __fmul_rn(T, __fsub_rn(1.0f, alpha));
       outer_cdf = inner_cdf;
     }
@@ -203,7 +203,7 @@ __global__ void shell_composite_backward_kernel(const float* __restrict__ sdf, c
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float col = colors[(p * S + l) * 3 + c];
-        acc[c] = __fmaf_rn(weight, col, acc[c]);
+        acc[c] = __fadd_rn(acc[c], __fmul_rn(weight, col));
         const float suffix = final_rgb[c] - acc[c];
         d_alpha += dL[c] * (T * col - suffix * inv);
         grad_colors[(p * S + l) * 3 + c] += weight * dL[c];

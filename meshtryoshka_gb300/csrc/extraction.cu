@@ -312,12 +312,18 @@ __device__ __forceinline__ uint32_t crossing_mask(const Corners4& c, float iso) 
          ((uint32_t)(b0 != (c.d[2] < iso)) << 2);
 }
 
-// create_triangle_vertices.slang:87-133: t is detached, positions / SH / sdf
+// create_triangle_vertices.slang:87-96: t is detached; positions / SH / sdf
 // are linear in the corner values with weights (1 - t, t).
 __device__ __forceinline__ float mc_weight(float d0, float d1, float iso) {
   if (d0 == d1) return 0.5f;
   const float t = (iso - d0) / (d1 - d0);
   return fminf(fmaxf(t, 0.0f), 1.0f);
+}
+
+// a + t * (b - a), rounded after each operation as the reference source
+// writes it (create_triangle_vertices.slang:105-127).
+__device__ __forceinline__ float lerp_ref(float a, float b, float t) {
+  return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a)));
 }
 
 // ---------------------------------------------------------------------------
@@ -351,10 +357,10 @@ __global__ void create_vertices_kernel(const float* __restrict__ gv, const float
         if (!((m >> a) & 1u)) continue;
         const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
         const float t = mc_weight(c.d0, d1, iso);
-        out_v[3 * vi + 0] = __fmaf_rn(t, v1x - v0x, v0x);
-        out_v[3 * vi + 1] = __fmaf_rn(t, v1y - v0y, v0y);
-        out_v[3 * vi + 2] = __fmaf_rn(t, v1z - v0z, v0z);
-        out_sdf[vi] = __fmaf_rn(t, d1 - c.d0, c.d0);
+        out_v[3 * vi + 0] = lerp_ref(v0x, v1x, t);
+        out_v[3 * vi + 1] = lerp_ref(v0y, v1y, t);
+        out_v[3 * vi + 2] = lerp_ref(v0z, v1z, t);
+        out_sdf[vi] = lerp_ref(c.d0, d1, t);
         out_type[vi] = (uint8_t)a;
         for (int k = 0; k < C; ++k) {
           const float* p0 = gsh + ((int64_t)k * G + i0) * 3;
@@ -363,7 +369,7 @@ __global__ void create_vertices_kernel(const float* __restrict__ gv, const float
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
             const float s0 = __ldg(p0 + ch), s1 = __ldg(p1 + ch);
-            q[ch] = __fmaf_rn(t, s1 - s0, s0);
+            q[ch] = lerp_ref(s0, s1, t);
           }
         }
       }

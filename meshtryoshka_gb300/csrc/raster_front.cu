@@ -4,10 +4,11 @@
 //
 // Follows triangle_rasterization/project_vertices.slang, bound_triangles.slang,
 // generate_keys.slang + keys.slang, delineate_tiles.slang and
-// evaluate_spherical_harmonics.slang. Geometry that decides integer outputs
-// (projection, back-face test, tile bounds, key depth) uses a fixed operation
-// order with explicit fused multiply-adds, so results are reproducible
-// bit-for-bit by the CPU restatement.
+// evaluate_spherical_harmonics.slang. Arithmetic follows the reference
+// source's operations in their order, without contraction (explicit
+// __fmul_rn / __fadd_rn, never fused by nvcc), so projected positions, tile
+// bounds, key depths and colours equal the reference kernels evaluated
+// operation by operation in IEEE-754 single precision.
 
 #include "mt_common.cuh"
 
@@ -57,14 +58,18 @@ __global__ void project_kernel(const float* __restrict__ verts, int64_t V, const
     for (int b = 0; b < B; ++b) {
       const float* E = ext + 16 * b;
       const float* K = intr + 9 * b;
+      // mul(W2C, float4(v, 1)) and mul(K, cam.xyz): row sums left to right.
       float cam[3];
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         const float* row = E + 4 * r;
-        cam[r] = __fmaf_rn(row[3], 1.0f, __fmaf_rn(row[2], z, __fmaf_rn(row[1], y, __fmul_rn(row[0], x))));
+        cam[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(row[0], x), __fmul_rn(row[1], y)), __fmul_rn(row[2], z)),
+                           __fmul_rn(row[3], 1.0f));
       }
-      const float kx = __fmaf_rn(K[2], cam[2], __fmaf_rn(K[1], cam[1], __fmul_rn(K[0], cam[0])));
-      const float ky = __fmaf_rn(K[5], cam[2], __fmaf_rn(K[4], cam[1], __fmul_rn(K[3], cam[0])));
+      const float kx =
+          __fadd_rn(__fadd_rn(__fmul_rn(K[0], cam[0]), __fmul_rn(K[1], cam[1])), __fmul_rn(K[2], cam[2]));
+      const float ky =
+          __fadd_rn(__fadd_rn(__fmul_rn(K[3], cam[0]), __fmul_rn(K[4], cam[1])), __fmul_rn(K[5], cam[2]));
       const int64_t o = (int64_t)b * V + v;
       out_xy[2 * o] = __fdiv_rn(kx, cam[2]);
       out_xy[2 * o + 1] = __fdiv_rn(ky, cam[2]);
@@ -110,11 +115,13 @@ __device__ __forceinline__ void sh_basis(float x, float y, float z, int n, float
 
 __device__ __forceinline__ void view_dir(const float* __restrict__ verts, int64_t v, const float* __restrict__ cam,
                                          float& x, float& y, float& z) {
-  const float dx = verts[3 * v] - cam[0], dy = verts[3 * v + 1] - cam[1], dz = verts[3 * v + 2] - cam[2];
-  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
-  x = dx / len;
-  y = dy / len;
-  z = dz / len;
+  // normalize(vertex - camera) = d / sqrt(dot(d, d))
+  const float dx = __fsub_rn(verts[3 * v], cam[0]), dy = __fsub_rn(verts[3 * v + 1], cam[1]),
+              dz = __fsub_rn(verts[3 * v + 2], cam[2]);
+  const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  x = __fdiv_rn(dx, len);
+  y = __fdiv_rn(dy, len);
+  z = __fdiv_rn(dz, len);
 }
 
 __global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, const float* __restrict__ sh,
@@ -129,11 +136,11 @@ __global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, co
       for (int k = 0; k < n_coeff; ++k) {
         const float* s = sh + ((int64_t)k * V + v) * 3;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) rgb[c] += basis[k] * s[c];
+        for (int c = 0; c < 3; ++c) rgb[c] = k == 0 ? __fmul_rn(basis[0], s[c]) : __fadd_rn(rgb[c], __fmul_rn(basis[k], s[c]));
       }
       float* o = out + ((int64_t)b * V + v) * 3;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) o[c] = fmaxf(rgb[c] + 0.5f, 0.0f);
+      for (int c = 0; c < 3; ++c) o[c] = fmaxf(__fadd_rn(rgb[c], 0.5f), 0.0f);
     }
   }
 }
@@ -197,8 +204,8 @@ __device__ __forceinline__ TileBounds triangle_tile_bounds(const float* __restri
   const float bx = xy[2 * (base + ib)], by = xy[2 * (base + ib) + 1], bd = depth[base + ib];
   const float cx = xy[2 * (base + ic)], cy = xy[2 * (base + ic) + 1], cd = depth[base + ic];
   TileBounds t{0, 0, 0, 0};
-  const float check =
-      __fmaf_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay), -__fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
+  const float check = __fsub_rn(__fmul_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay)),
+                                __fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
   if (check < 0.0f) return t;
   if (fminf(fminf(ad, bd), cd) < near) return t;
   const float ymin = fminf(fminf(ay, by), cy), ymax = fmaxf(fmaxf(ay, by), cy);

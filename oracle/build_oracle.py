@@ -2,9 +2,9 @@
 
 Compiles ``mt_oracle.cpp`` into ``oracle/liboracle.so`` with OpenMP and with
 floating-point contraction disabled (``-ffp-contract=off``), so that every
-fused multiply-add in the oracle is an explicit ``std::fmaf`` and the result
-bits do not depend on the host compiler or CPU (x86_64 here, aarch64 on the
-GPU host).
+floating-point operation is rounded once, in the reference source's order, and
+the result bits do not depend on the host compiler or CPU (x86_64 and
+aarch64 alike).
 """
 
 from __future__ import annotations

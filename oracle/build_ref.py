@@ -135,7 +135,6 @@ def translate(src: str, fname: str, drops: list[str]) -> tuple[str, list[str]]:
     src = re.sub(r"\bno_diff\s+", "", src)
     src = re.sub(r"\bgroupshared\b", "static", src)
     src = re.sub(r"typealias\s+(\w+)\s*=\s*(\w+)\[(\w+)\]\s*;", r"using \1 = std::array<\2, \3>;", src)
-    src = re.sub(r"\.(xyz|xy)\b(?!\s*\()", r".\1()", src)
     src = FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", src)
     if fname in ARRAY_VALUE_FILES:
         src = ARRAY_DECL.sub(to_std_array, src)

@@ -9,10 +9,9 @@
 // statement by statement (including the arithmetic-shift and last-bit cases of
 // create_voxels). The reference itself cannot be executed in this environment
 // (its kernels need slangtorch, which is absent), so bit patterns of the
-// floating-point kernels are defined here by an explicit operation order:
-// fused multiply-adds are written as std::fmaf where the GPU kernels use
-// __fmaf_rn, everything else is a single IEEE operation, and the file is
-// compiled with -ffp-contract=off so the host compiler adds no contraction.
+// floating-point kernels follow the reference source's operations in their
+// order, each rounded once (IEEE-754 single precision), and the file is
+// compiled with -ffp-contract=off so the host compiler fuses nothing.
 //
 // Conventions: host pointers, dense row-major arrays, the same shapes as the
 // reference tensors. OpenMP parallelises independent work items; scatters
@@ -451,14 +450,14 @@ void or_create_triangle_vertices(const float* gv, const float* gsdf, const float
       for (int a = 0; a < 3; ++a) {
         if (!should_compute_triangle_vertex(vx, a, ls)) continue;
         const float t = mc_weight(vx.d0, vx.d1[a], ls);
-        for (int c = 0; c < 3; ++c) out_v[3 * vi + c] = std::fmaf(t, vx.v1[a][c] - vx.v0[c], vx.v0[c]);
+        for (int c = 0; c < 3; ++c) out_v[3 * vi + c] = vx.v0[c] + t * (vx.v1[a][c] - vx.v0[c]);
         for (int k = 0; k < C; ++k)
           for (int ch = 0; ch < 3; ++ch) {
             const float s0 = gsh[((int64_t)k * G + vx.i0) * 3 + ch];
             const float s1 = gsh[((int64_t)k * G + vx.i1[a]) * 3 + ch];
-            out_sh[((int64_t)k * V + vi) * 3 + ch] = std::fmaf(t, s1 - s0, s0);
+            out_sh[((int64_t)k * V + vi) * 3 + ch] = s0 + t * (s1 - s0);
           }
-        out_sdf[vi] = std::fmaf(t, vx.d1[a] - vx.d0, vx.d0);
+        out_sdf[vi] = vx.d0 + t * (vx.d1[a] - vx.d0);
         out_type[vi] = (uint8_t)a;
         vi++;
       }
@@ -623,7 +622,7 @@ inline int f2i_rz(float x) {
   return (int)x;
 }
 
-inline float dot2(float ax, float ay, float bx, float by) { return std::fmaf(ay, by, ax * bx); }
+inline float dot2(float ax, float ay, float bx, float by) { return ax * bx + ay * by; }
 
 // intersect_and_composite.slang:65-106 / intersect.slang:14-49, evaluated in
 // full for every (pixel, triangle) pair as the reference does.
@@ -644,15 +643,15 @@ inline void barycentric(float p1x, float p1y, float p2x, float p2y, float p3x, f
   const float d_2x_13 = dot2(px - p2x, py - p2y, e13x, e13y);
   float denom = std::nanf("");  // the reference leaves it unset; only reachable with NaNs
   if (std::fabs(d_12_13) <= std::fabs(d_12_23) && std::fabs(d_12_13) <= std::fabs(d_13_23)) {
-    denom = std::fmaf(d_12_12, d_13_13, -(d_12_13 * d_12_13));
+    denom = d_12_12 * d_13_13 - d_12_13 * d_12_13;
   } else if (std::fabs(d_12_23) <= std::fabs(d_12_13) && std::fabs(d_12_23) <= std::fabs(d_13_23)) {
-    denom = std::fmaf(d_12_12, d_23_23, -(d_12_23 * d_12_23));
+    denom = d_12_12 * d_23_23 - d_12_23 * d_12_23;
   } else if (std::fabs(d_13_23) <= std::fabs(d_12_13) && std::fabs(d_13_23) <= std::fabs(d_12_23)) {
-    denom = std::fmaf(d_13_13, d_23_23, -(d_13_23 * d_13_23));
+    denom = d_13_13 * d_23_23 - d_13_23 * d_13_23;
   }
-  v = std::fmaf(d_13_13, d_1x_12, -(d_12_13 * d_1x_13));
-  w = std::fmaf(d_12_12, d_1x_13, -(d_12_13 * d_1x_12));
-  u = std::fmaf(d_12_23, d_2x_13, -(d_13_23 * d_2x_12));
+  v = d_13_13 * d_1x_12 - d_12_13 * d_1x_13;
+  w = d_12_12 * d_1x_13 - d_12_13 * d_1x_12;
+  u = d_12_23 * d_2x_13 - d_13_23 * d_2x_12;
   const float eps = 1e-8f;
   v /= denom + eps;
   w /= denom + eps;
@@ -668,9 +667,7 @@ inline bool accepted(float u, float v, float w) {
   return true;
 }
 
-inline float interp3(float u, float v, float w, float a, float b, float c) {
-  return std::fmaf(w, c, std::fmaf(v, b, u * a));
-}
+inline float interp3(float u, float v, float w, float a, float b, float c) { return u * a + v * b + w * c; }
 
 inline float sdf_to_cdf(float sdf, float s, float& e) {
   e = std::exp(-sdf * s);
@@ -762,10 +759,9 @@ void or_project_vertices(const float* verts, int64_t V, const float* ext, const 
       const float* E = ext + 16 * b;
       const float* K = intr + 9 * b;
       float cam[3];
-      for (int r = 0; r < 3; ++r)
-        cam[r] = std::fmaf(E[4 * r + 3], 1.0f, std::fmaf(E[4 * r + 2], z, std::fmaf(E[4 * r + 1], y, E[4 * r] * x)));
-      const float kx = std::fmaf(K[2], cam[2], std::fmaf(K[1], cam[1], K[0] * cam[0]));
-      const float ky = std::fmaf(K[5], cam[2], std::fmaf(K[4], cam[1], K[3] * cam[0]));
+      for (int r = 0; r < 3; ++r) cam[r] = E[4 * r] * x + E[4 * r + 1] * y + E[4 * r + 2] * z + E[4 * r + 3] * 1.0f;
+      const float kx = K[0] * cam[0] + K[1] * cam[1] + K[2] * cam[2];
+      const float ky = K[3] * cam[0] + K[4] * cam[1] + K[5] * cam[2];
       const int64_t o = (int64_t)b * V + v;
       out_xy[2 * o] = kx / cam[2];
       out_xy[2 * o + 1] = ky / cam[2];
@@ -785,8 +781,8 @@ void or_evaluate_sh(const float* verts, int64_t V, const float* sh, int sh_degre
       view_dir(verts + 3 * v, campos + 3 * b, x, y, z);
       sh_basis(x, y, z, n, basis);
       for (int c = 0; c < 3; ++c) {
-        float rgb = 0.f;
-        for (int k = 0; k < n; ++k) rgb += basis[k] * sh[((int64_t)k * V + v) * 3 + c];
+        float rgb = basis[0] * sh[((int64_t)0 * V + v) * 3 + c];
+        for (int k = 1; k < n; ++k) rgb += basis[k] * sh[((int64_t)k * V + v) * 3 + c];
         out[((int64_t)b * V + v) * 3 + c] = std::max(rgb + 0.5f, 0.0f);
       }
     }
@@ -825,7 +821,7 @@ void or_bound_triangles(const float* xy, const float* depth, int64_t V, const in
     const float ax = xy[2 * ia], ay = xy[2 * ia + 1], bx = xy[2 * ib], by = xy[2 * ib + 1];
     const float cx = xy[2 * ic], cy = xy[2 * ic + 1];
     int r0 = 0, r1 = 0, c0 = 0, c1 = 0;
-    const float check = std::fmaf(bx - ax, cy - ay, -((by - ay) * (cx - ax)));
+    const float check = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
     const float min_depth = std::fmin(std::fmin(depth[ia], depth[ib]), depth[ic]);
     if (!(check < 0) && !(min_depth < near)) {
       const float ymin = std::fmin(std::fmin(ay, by), cy), ymax = std::fmax(std::fmax(ay, by), cy);
@@ -994,7 +990,7 @@ void or_intersect_and_composite_forward(const float* xy, const float* colors, co
             sample(a, cam, h, rgb, s_in);
             const float inner_cdf = sdf_to_cdf(s_in, sharpness, e);
             const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
-            for (int c = 0; c < 3; ++c) acc[c] = std::fmaf(rgb[c] * Tr, alpha, acc[c]);
+            for (int c = 0; c < 3; ++c) acc[c] = acc[c] + rgb[c] * Tr * alpha;
             Tr = Tr * (1.0f - alpha);
             outer_cdf = inner_cdf;
           }
@@ -1068,7 +1064,7 @@ void or_intersect_and_composite_backward(const float* xy, const float* colors, c
             const float inv = 1.0f / ((1.0f - alpha) + 1e-6f);
             float d_color[3], d_alpha = 0.f;
             for (int c = 0; c < 3; ++c) {
-              acc[c] = std::fmaf(weight, rgb[c], acc[c]);
+              acc[c] = acc[c] + weight * rgb[c];
               const float suffix = final_rgb[c] - acc[c];
               d_color[c] = weight * dL[c];
               d_alpha += dL[c] * (Tr * rgb[c] - suffix * inv);
@@ -1194,7 +1190,7 @@ void or_composite(const float* sdf, const float* colors, const uint8_t* mask, in
       if (!mask[p * S + l]) continue;
       const float inner_cdf = sdf_to_cdf(sdf[p * S + l], sharpness, e);
       const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
-      for (int c = 0; c < 3; ++c) acc[c] = std::fmaf(colors[(p * S + l) * 3 + c] * Tr, alpha, acc[c]);
+      for (int c = 0; c < 3; ++c) acc[c] = acc[c] + colors[(p * S + l) * 3 + c] * Tr * alpha;
       Tr = Tr * (1.0f - alpha);
       outer_cdf = inner_cdf;
     }
@@ -1226,7 +1222,7 @@ void or_composite_backward(const float* sdf, const float* colors, const uint8_t*
       float d_alpha = 0.f;
       for (int c = 0; c < 3; ++c) {
         const float col = colors[(p * S + l) * 3 + c];
-        acc[c] = std::fmaf(weight, col, acc[c]);
+        acc[c] = acc[c] + weight * col;
         d_alpha += dL[c] * (Tr * col - (out_colors[3 * p + c] - acc[c]) * inv);
         gcol[(p * S + l) * 3 + c] += weight * dL[c];
       }

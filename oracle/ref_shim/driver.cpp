@@ -8,6 +8,7 @@
 // kernels with CTA barriers run one block at a time, each emulated thread on
 // its own OS thread, synchronised by a std::barrier.
 
+#include <cstdlib>
 #include <functional>
 #include <thread>
 #include <vector>
@@ -63,46 +64,51 @@ void run_grid_with_barriers(uint3 grid, uint3 block, const std::function<void()>
 // ---------------------------------------------------------------------------
 // Rewritten reference sources
 // ---------------------------------------------------------------------------
-namespace ref_vertex_occupancy {
+namespace k_vertex_occupancy {
 #include "triangle_extraction__compute_vertex_occupancy.inc"
 }
-namespace ref_count_occupancy {
+namespace k_count_occupancy {
 #include "triangle_extraction__count_occupancy.inc"
 }
-namespace ref_create_voxels {
+namespace k_create_voxels {
 #include "triangle_extraction__create_voxels.inc"
 }
-namespace ref_dilate {
+namespace k_dilate {
 #include "triangle_extraction__dilate_occupancy.inc"
 }
-namespace ref_count_vertices {
+namespace k_count_vertices {
 #include "triangle_extraction__count_triangle_vertices.inc"
 }
 #define NUM_SPHERICAL_HARMONICS 1
-namespace ref_create_vertices_1 {
+namespace k_create_vertices_1 {
 #include "triangle_extraction__create_triangle_vertices.inc"
 }
 #undef NUM_SPHERICAL_HARMONICS
 #define NUM_SPHERICAL_HARMONICS 4
-namespace ref_create_vertices_4 {
+namespace k_create_vertices_4 {
+#include "triangle_extraction__create_triangle_vertices.inc"
+}
+#undef NUM_SPHERICAL_HARMONICS
+#define NUM_SPHERICAL_HARMONICS 9
+namespace k_create_vertices_9 {
 #include "triangle_extraction__create_triangle_vertices.inc"
 }
 #undef NUM_SPHERICAL_HARMONICS
 #define NUM_SPHERICAL_HARMONICS 16
-namespace ref_create_vertices_16 {
+namespace k_create_vertices_16 {
 #include "triangle_extraction__create_triangle_vertices.inc"
 }
 #undef NUM_SPHERICAL_HARMONICS
-namespace ref_count_faces {
+namespace k_count_faces {
 #include "triangle_extraction__count_triangle_faces.inc"
 }
-namespace ref_create_faces {
+namespace k_create_faces {
 #include "triangle_extraction__create_triangle_faces.inc"
 }
-namespace ref_project {
+namespace k_project {
 #include "triangle_rasterization__project_vertices.inc"
 }
-namespace ref_bound {
+namespace k_bound {
 #include "triangle_rasterization__bound_triangles.inc"
 }
 
@@ -115,15 +121,15 @@ namespace ref_bound {
 #define DEPTH_BIT_LENGTH 32
 #define SHELL_BIT_OFFSET 0
 #define SHELL_BIT_LENGTH 6
-namespace ref_keys_fused {
+namespace k_keys_fused {
 #include "triangle_rasterization__generate_keys.inc"
 }
-namespace ref_delineate_fused {
+namespace k_delineate_fused {
 #include "triangle_rasterization__delineate_tiles.inc"
 }
 #define TILE_HEIGHT 16
 #define TILE_WIDTH 16
-namespace ref_fused_16 {
+namespace k_fused_16 {
 #include "triangle_rasterization__intersect_and_composite.inc"
 }
 #undef TILE_HEIGHT
@@ -146,44 +152,44 @@ namespace ref_fused_16 {
 #define TILE_BIT_LENGTH 20
 #define DEPTH_BIT_OFFSET 0
 #define DEPTH_BIT_LENGTH 32
-namespace ref_keys_explicit {
+namespace k_keys_explicit {
 #include "triangle_rasterization__generate_keys.inc"
 }
-namespace ref_delineate_explicit {
+namespace k_delineate_explicit {
 #include "triangle_rasterization__delineate_tiles.inc"
 }
 #define TILE_HEIGHT 16
 #define TILE_WIDTH 16
-namespace ref_intersect_16 {
+namespace k_intersect_16 {
 #include "triangle_rasterization__intersect.inc"
 }
 #undef TILE_HEIGHT
 #undef TILE_WIDTH
 
 #define SH_DEGREE 0
-namespace ref_sh_0 {
+namespace k_sh_0 {
 #include "triangle_rasterization__evaluate_spherical_harmonics.inc"
 }
 #undef SH_DEGREE
 #define SH_DEGREE 1
-namespace ref_sh_1 {
+namespace k_sh_1 {
 #include "triangle_rasterization__evaluate_spherical_harmonics.inc"
 }
 #undef SH_DEGREE
 #define SH_DEGREE 2
-namespace ref_sh_2 {
+namespace k_sh_2 {
 #include "triangle_rasterization__evaluate_spherical_harmonics.inc"
 }
 #undef SH_DEGREE
 #define SH_DEGREE 3
-namespace ref_sh_3 {
+namespace k_sh_3 {
 #include "triangle_rasterization__evaluate_spherical_harmonics.inc"
 }
 #undef SH_DEGREE
-namespace ref_interpolate {
+namespace k_interpolate {
 #include "triangle_rasterization__interpolate.inc"
 }
-namespace ref_composite {
+namespace k_composite {
 #include "triangle_rasterization__composite.inc"
 }
 
@@ -198,7 +204,7 @@ void ref_compute_vertex_occupancy(int32_t* occ, int I, int J, int KP, int32_t* v
   TensorView<int> v(vocc, {(uint64_t)I + 1, (uint64_t)J + 1, (uint64_t)KP + 1});
   TensorView<int> c(vcounts, {(uint64_t)I + 1, (uint64_t)J + 1, (uint64_t)KP + 1});
   run_grid(ceil_grid(uint3(I + 1, J + 1, KP + 1), uint3(32, 32, 1)), uint3(32, 32, 1),
-           [&] { ref_vertex_occupancy::compute_vertex_occupancy(o, v, c); });
+           [&] { k_vertex_occupancy::compute_vertex_occupancy(o, v, c); });
   vcounts[(int64_t)(I + 1) * (J + 1) * (KP + 1)] = 0;
 }
 
@@ -207,7 +213,7 @@ void ref_count_occupancy(int32_t* occ, int I, int J, int KP, int32_t* counts) {
   TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
   TensorView<int> c(counts, {(uint64_t)I + 1, (uint64_t)J + 1, (uint64_t)KP + 1});
   run_grid(ceil_grid(uint3(I, J, KP), uint3(32, 32, 1)), uint3(32, 32, 1),
-           [&] { ref_count_occupancy::count_occupancy(o, c); });
+           [&] { k_count_occupancy::count_occupancy(o, c); });
 }
 
 // create_voxels.py:66-88
@@ -222,14 +228,14 @@ void ref_create_voxels(int32_t* occ, int32_t* xoff, int32_t* vocc, int32_t* voff
   TensorView<int> nb(neighbors, {7, (uint64_t)Nv}), lc(lower, {4, (uint64_t)G}), uc(upper, {4, (uint64_t)Nv});
   TensorView<int> ix(indices, {(uint64_t)Nv});
   run_grid(ceil_grid(uint3(I + 1, J + 1, KP + 1), uint3(32, 32, 1)), uint3(32, 32, 1),
-           [&] { ref_create_voxels::create_voxels(o, xo, vo, vf, ve, nb, lc, uc, ix); });
+           [&] { k_create_voxels::create_voxels(o, xo, vo, vf, ve, nb, lc, uc, ix); });
 }
 
 // dilate_occupancy.py:36-46
 void ref_dilate_occupancy(int32_t* occ, int I, int J, int KP, int d, int32_t* out) {
   TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP}), n(out, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
   run_grid(ceil_grid(uint3(I, J, KP), uint3(32, 32, 1)), uint3(32, 32, 1),
-           [&] { ref_dilate::dilate_occupancy(o, n, d); });
+           [&] { k_dilate::dilate_occupancy(o, n, d); });
 }
 
 // count_triangle_vertices.py:31-50
@@ -237,7 +243,7 @@ void ref_count_triangle_vertices(float* sdf, int32_t* lower, int64_t G, float* l
   TensorView<float> d(sdf, {(uint64_t)G}), ls(level_sets, {(uint64_t)S});
   TensorView<int> lc(lower, {4, (uint64_t)G}), c(counts, {(uint64_t)S, (uint64_t)G});
   run_grid(uint3((G + 255) / 256, 1, 1), uint3(256, 1, 1),
-           [&] { ref_count_vertices::countTriangleVertices(d, lc, ls, c); });
+           [&] { k_count_vertices::countTriangleVertices(d, lc, ls, c); });
   counts[(int64_t)S * G] = 0;
 }
 
@@ -252,11 +258,15 @@ void ref_create_triangle_vertices(float* gv, float* gsdf, float* gsh, int C, int
   TensorView<uint8_t> ot(out_type, {(uint64_t)V});
   const uint3 grid((G + 255) / 256, 1, 1), block(256, 1, 1);
   if (C == 1)
-    run_grid(grid, block, [&] { ref_create_vertices_1::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
+    run_grid(grid, block, [&] { k_create_vertices_1::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
   else if (C == 4)
-    run_grid(grid, block, [&] { ref_create_vertices_4::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
+    run_grid(grid, block, [&] { k_create_vertices_4::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
+  else if (C == 9)
+    run_grid(grid, block, [&] { k_create_vertices_9::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
   else if (C == 16)
-    run_grid(grid, block, [&] { ref_create_vertices_16::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
+    run_grid(grid, block, [&] { k_create_vertices_16::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
+  else
+    std::abort();
 }
 
 // count_triangle_faces.py:48-61
@@ -266,7 +276,7 @@ void ref_count_triangle_faces(float* sdf, int32_t* lower, int64_t G, int32_t* up
   TensorView<int> lc(lower, {4, (uint64_t)G}), uc(upper, {4, (uint64_t)Nv}), c(counts, {(uint64_t)S, (uint64_t)Nv});
   TensorView<uint8_t> cc(codes, {(uint64_t)S, (uint64_t)Nv});
   run_grid(uint3((Nv + 255) / 256, 1, 1), uint3(256, 1, 1),
-           [&] { ref_count_faces::count_triangle_faces(d, lc, uc, ls, c, cc); });
+           [&] { k_count_faces::count_triangle_faces(d, lc, uc, ls, c, cc); });
   counts[(int64_t)S * Nv] = 0;
 }
 
@@ -280,14 +290,14 @@ void ref_create_triangle_faces(float* sdf, int64_t G, int32_t* neighbors, int32_
   TensorView<uint8_t> ty(types, {(uint64_t)V}), cc(codes, {(uint64_t)S, (uint64_t)Nv});
   TensorView<int> fo(foff, {(uint64_t)S * Nv + 1}), fa(faces, {(uint64_t)F, 3}), vi(voxel_indices, {(uint64_t)F});
   run_grid(uint3((Nv + 255) / 256, 1, 1), uint3(256, 1, 1),
-           [&] { ref_create_faces::create_triangle_faces(d, nb, ix, vo, ty, cc, ls, fa, vi, (int)G, fo); });
+           [&] { k_create_faces::create_triangle_faces(d, nb, ix, vo, ty, cc, ls, fa, vi, (int)G, fo); });
 }
 
 // project_vertices.py:44-54
 void ref_project_vertices(float* ext, float* intr, int B, float* verts, int64_t V, float* out_xy, float* out_depth) {
   TensorView<float> e(ext, {(uint64_t)B, 4, 4}), k(intr, {(uint64_t)B, 3, 3}), v(verts, {(uint64_t)V, 3});
   TensorView<float> xy(out_xy, {(uint64_t)B, (uint64_t)V, 2}), dp(out_depth, {(uint64_t)B, (uint64_t)V});
-  run_grid(uint3((V + 255) / 256, 1, 1), uint3(256, 1, 1), [&] { ref_project::project_vertices(e, k, v, xy, dp); });
+  run_grid(uint3((V + 255) / 256, 1, 1), uint3(256, 1, 1), [&] { k_project::project_vertices(e, k, v, xy, dp); });
 }
 
 // bound_triangles.py:51-69
@@ -298,7 +308,7 @@ void ref_bound_triangles(float* xy, float* depth, int B, int64_t V, int32_t* fac
   TensorView<int> mn(out_min, {(uint64_t)B, (uint64_t)F, 2}), mx(out_max, {(uint64_t)B, (uint64_t)F, 2});
   TensorView<int> ct(out_count, {(uint64_t)B, (uint64_t)F});
   run_grid(uint3((F + 255) / 256, 1, 1), uint3(256, 1, 1), [&] {
-    ref_bound::bound_triangles(v, d, f, tile_h, tile_w, 0, 0, rows, cols, near, mn, mx, ct);
+    k_bound::bound_triangles(v, d, f, tile_h, tile_w, 0, 0, rows, cols, near, mn, mx, ct);
   });
 }
 
@@ -313,9 +323,9 @@ void ref_generate_keys(int explicit_layout, float* depth, int B, int64_t V, int3
   TensorView<int> ot(out_tri, {(uint64_t)K});
   const uint3 grid((F + 255) / 256, 1, 1), block(256, 1, 1);
   if (explicit_layout)
-    run_grid(grid, block, [&] { ref_keys_explicit::generate_keys(d, f, s, mn, mx, of, grid_width, ok, ot); });
+    run_grid(grid, block, [&] { k_keys_explicit::generate_keys(d, f, s, mn, mx, of, grid_width, ok, ot); });
   else
-    run_grid(grid, block, [&] { ref_keys_fused::generate_keys(d, f, s, mn, mx, of, grid_width, ok, ot); });
+    run_grid(grid, block, [&] { k_keys_fused::generate_keys(d, f, s, mn, mx, of, grid_width, ok, ot); });
 }
 
 // delineate_tiles.py:40-53 (output zero-filled by the caller)
@@ -325,9 +335,9 @@ void ref_delineate_tiles(int explicit_layout, int64_t* keys, int64_t K, int B, i
   TensorView<int64_t> k(keys, {(uint64_t)K}), n(&num_keys, {1}), o(out, {(uint64_t)B, (uint64_t)Sd, (uint64_t)T, 2});
   const uint3 grid((K + 255) / 256, 1, 1), block(256, 1, 1);
   if (explicit_layout)
-    run_grid(grid, block, [&] { ref_delineate_explicit::delineate_tiles(k, n, o, separate != 0, 1e-8f); });
+    run_grid(grid, block, [&] { k_delineate_explicit::delineate_tiles(k, n, o, separate != 0, 1e-8f); });
   else
-    run_grid(grid, block, [&] { ref_delineate_fused::delineate_tiles(k, n, o, separate != 0, 1e-8f); });
+    run_grid(grid, block, [&] { k_delineate_fused::delineate_tiles(k, n, o, separate != 0, 1e-8f); });
 }
 
 // evaluate_spherical_harmonics.py:42-53; camera positions given.
@@ -336,10 +346,10 @@ void ref_evaluate_sh(int degree, float* verts, int64_t V, float* sh, int C, floa
   TensorView<float> o(out, {(uint64_t)B, (uint64_t)V, 3});
   const uint3 grid((V + 255) / 256, 1, 1), block(256, 1, 1);
   switch (degree) {
-    case 0: run_grid(grid, block, [&] { ref_sh_0::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
-    case 1: run_grid(grid, block, [&] { ref_sh_1::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
-    case 2: run_grid(grid, block, [&] { ref_sh_2::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
-    default: run_grid(grid, block, [&] { ref_sh_3::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
+    case 0: run_grid(grid, block, [&] { k_sh_0::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
+    case 1: run_grid(grid, block, [&] { k_sh_1::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
+    case 2: run_grid(grid, block, [&] { k_sh_2::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
+    default: run_grid(grid, block, [&] { k_sh_3::evaluate_spherical_harmonics_forward(v, s, c, o); }); break;
   }
 }
 
@@ -354,7 +364,7 @@ void ref_intersect_and_composite_forward(float* xy, float* colors, float* sdf, i
   TensorView<int64_t> k(keys, {(uint64_t)K}), bd(bounds, {(uint64_t)B, (uint64_t)rows * cols, 2});
   TensorView<float> o(out, {(uint64_t)B, 4, (uint64_t)H, (uint64_t)W});
   run_grid_with_barriers(uint3((uint)(rows * cols * B), 1, 1), uint3(256, 1, 1), [&] {
-    ref_fused_16::intersect_and_composite_forward(t, bd, v, c, d, f, s, num_shells, rows, cols, o, k);
+    k_fused_16::intersect_and_composite_forward(t, bd, v, c, d, f, s, num_shells, rows, cols, o, k);
   });
 }
 
@@ -367,7 +377,7 @@ void ref_intersect(float* xy, int B, int64_t V, int32_t* faces, int64_t F, int32
   TensorView<float> uv(out_uv, {(uint64_t)B * S, (uint64_t)H, (uint64_t)W, 2});
   TensorView<int> ix(out_index, {(uint64_t)B * S, (uint64_t)H, (uint64_t)W});
   run_grid_with_barriers(uint3((uint)(rows * cols * B * S), 1, 1), uint3(256, 1, 1), [&] {
-    ref_intersect_16::intersect(t, bd, v, f, rows, cols, H, W, uv, ix);
+    k_intersect_16::intersect(t, bd, v, f, rows, cols, H, W, uv, ix);
   });
 }
 
@@ -380,7 +390,7 @@ void ref_interpolate(float* uv, int32_t* index, int B, int S, int H, int W, int3
   TensorView<float> d(sdf, {(uint64_t)V}), c(colors, {(uint64_t)B, (uint64_t)V, 3});
   TensorView<float> od(out_sdf, {bs, (uint64_t)H, (uint64_t)W}), oc(out_colors, {bs, (uint64_t)H, (uint64_t)W, 3});
   run_grid(uint3((W + 15) / 16, (H + 15) / 16, (uint)bs), uint3(16, 16, 1),
-           [&] { ref_interpolate::interpolate(u, ix, f, d, c, od, oc, S); });
+           [&] { k_interpolate::interpolate(u, ix, f, d, c, od, oc, S); });
 }
 
 // composite.py:36-50
@@ -390,7 +400,7 @@ void ref_composite_forward(float* sdf, float* colors, uint8_t* mask, int64_t P, 
   TensorView<bool> m(reinterpret_cast<bool*>(mask), {(uint64_t)P, (uint64_t)S});
   TensorView<float> s(&sharpness, {1}), oc(out_colors, {(uint64_t)P, 3}), ot(out_T, {(uint64_t)P});
   run_grid(uint3((P + 255) / 256, 1, 1), uint3(256, 1, 1),
-           [&] { ref_composite::composite_forward(d, c, m, s, oc, ot); });
+           [&] { k_composite::composite_forward(d, c, m, s, oc, ot); });
 }
 
 }  // extern "C"

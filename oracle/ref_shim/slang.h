@@ -30,7 +30,7 @@ struct vec<T, 2> {
     struct { T x, y; };
     struct { T r, g; };
   };
-  vec() : x(), y() {}
+  vec() = default;
   template <typename A, typename B>
   vec(A a, B b) : x((T)a), y((T)b) {}
   template <typename U>
@@ -44,15 +44,15 @@ struct vec<T, 3> {
   union {
     struct { T x, y, z; };
     struct { T r, g, b; };
+    vec<T, 2> xy;  // swizzle .xy
   };
-  vec() : x(), y(), z() {}
+  vec() = default;
   template <typename A, typename B, typename C>
   vec(A a, B b, C c) : x((T)a), y((T)b), z((T)c) {}
   template <typename U>
   explicit vec(const vec<U, 3>& o) : x((T)o.x), y((T)o.y), z((T)o.z) {}
   T& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
   const T& operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
-  vec<T, 2> xy() const { return vec<T, 2>(x, y); }
 };
 
 template <typename T>
@@ -60,16 +60,16 @@ struct vec<T, 4> {
   union {
     struct { T x, y, z, w; };
     struct { T r, g, b, a; };
+    vec<T, 3> xyz;  // swizzle .xyz
+    vec<T, 2> xy;   // swizzle .xy
   };
-  vec() : x(), y(), z(), w() {}
+  vec() = default;
   template <typename A, typename B, typename C, typename D>
   vec(A a, B b, C c, D d) : x((T)a), y((T)b), z((T)c), w((T)d) {}
   template <typename U, typename D>
   vec(const vec<U, 3>& v, D d) : x((T)v.x), y((T)v.y), z((T)v.z), w((T)d) {}
   T& operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
   const T& operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
-  vec<T, 3> xyz() const { return vec<T, 3>(x, y, z); }
-  vec<T, 2> xy() const { return vec<T, 2>(x, y); }
 };
 
 using uint2 = vec<uint, 2>;

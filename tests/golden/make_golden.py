@@ -1,0 +1,201 @@
+"""Generate the golden fixtures in this folder from the reference's own kernels.
+
+Every output array is computed by the reference implementation's compute
+kernels (its Slang sources, rewritten textually to C++ and compiled on the
+host by ``oracle/build_ref.py``; see ``oracle/ref.py``). The glue between
+kernels follows the reference's Python call sites:
+
+* exclusive scans are numpy cumsums (triangle_extraction/__init__.py uses
+  torch.cumsum),
+* key sorting is a stable sort of the int64 keys (sort_keys.cu uses cub's
+  stable radix sort over all 64 bits),
+* camera centres are inverse(extrinsics)[:, :3, 3] in float64, rounded to
+  float32 (evaluate_spherical_harmonics.py:38).
+
+Inputs are seeded synthetic scenes: occupancy grids, a sphere band with a
+noisy signed distance field, cameras looking at the origin.
+
+Run from the repository root with the reference tree mounted:
+
+    python tests/golden/make_golden.py [--reference PATH]
+
+The output is deterministic; tests/test_golden_cpu.py regenerates it in
+memory when the reference is present and checks it matches the committed
+files.
+"""
+
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+NEAR_PLANE = 0.2
+TILE = (16, 16)  # the reference's compiled tile shape
+
+
+def _pack(bits: np.ndarray) -> np.ndarray:
+    from tests import semantics
+
+    return semantics.pack(bits)
+
+
+def _sphere_band(n: int, radius: float = 0.5, width: float = 2.5) -> np.ndarray:
+    c = -1 + (np.arange(n) + 0.5) * 2 / n
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    d = np.sqrt(x * x + y * y + z * z) - radius
+    return _pack(np.abs(d) < width * 2 / n)
+
+
+def _look_at(eye) -> np.ndarray:
+    from meshtryoshka_gb300 import synthetic
+
+    return synthetic.look_at(np.asarray(eye, np.float64))
+
+
+def _pinhole(h, w, fov) -> np.ndarray:
+    from meshtryoshka_gb300 import synthetic
+
+    return synthetic.pinhole(h, w, fov)
+
+
+# ---------------------------------------------------------------------------
+# Extraction: voxels, dilation, tessellation
+# ---------------------------------------------------------------------------
+def extraction_fixture(ref) -> dict[str, np.ndarray]:
+    rng = np.random.default_rng(3)
+    out: dict[str, np.ndarray] = {}
+    grids = {
+        "random": _pack(rng.random((6, 5, 96)) < 0.3),
+        "sphere": _sphere_band(32),
+        "edges": _pack((np.arange(64)[None, None, :] % 32 >= 30) & (rng.random((3, 4, 64)) < 0.7)),
+    }
+    for name, occ in grids.items():
+        vox = ref.extract_voxels(occ)
+        out[f"{name}/occupancy"] = occ
+        for field in ("vertices", "neighbors", "lower_corners", "upper_corners", "indices", "vertex_occupancy",
+                      "vertex_counts", "voxel_counts"):
+            out[f"{name}/{field}"] = vox[field]
+        for d in (1, 3):
+            out[f"{name}/dilated_{d}"] = ref.dilate_occupancy(occ, d)
+
+    vox = ref.extract_voxels(grids["sphere"])
+    p = 2 * vox["vertices"].astype(np.float64) - 1
+    sdf = (np.linalg.norm(p, axis=1) - 0.5 + rng.normal(0, 0.002, len(p))).astype(np.float32)
+    sh = rng.uniform(0, 1, (4, len(p), 3)).astype(np.float32)
+    level_sets = np.array([0.02, 0.0, -0.02], np.float32)
+    tri = ref.tessellate(sdf, vox["vertices"], sh, vox["neighbors"], vox["lower_corners"], vox["upper_corners"],
+                         vox["indices"], level_sets)
+    out["tess/signed_distances"] = sdf
+    out["tess/spherical_harmonics"] = sh
+    out["tess/level_sets"] = level_sets
+    for field, value in tri.items():
+        out[f"tess/out_{field}"] = value
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Rasterization: a tessellated sphere seen by a few cameras
+# ---------------------------------------------------------------------------
+SCENES = {
+    "two_cams": dict(n=32, levels=(0.03, 0.0, -0.03), sh_degree=2, cameras=((0.0, 0.0, 2.0), (1.2, 0.8, 1.3)),
+                     image_shape=(40, 56), fov=55.0, sharpness=40.0, seed=5),
+    "close_up": dict(n=32, levels=(0.01, -0.01), sh_degree=1, cameras=((0.3, 0.2, 0.9),), image_shape=(48, 32),
+                     fov=70.0, sharpness=80.0, seed=6),
+}
+
+
+def raster_fixture(ref, n, levels, sh_degree, cameras, image_shape, fov, sharpness, seed) -> dict[str, np.ndarray]:
+    rng = np.random.default_rng(seed)
+    vox = ref.extract_voxels(_sphere_band(n))
+    p = 2 * vox["vertices"].astype(np.float64) - 1
+    gsdf = (np.linalg.norm(p, axis=1) - 0.5 + rng.normal(0, 0.002, len(p))).astype(np.float32)
+    c = (sh_degree + 1) ** 2
+    gsh = np.empty((c, len(p), 3), np.float32)
+    gsh[0] = rng.uniform(0, 1, (len(p), 3))
+    gsh[1:] = rng.normal(0, 0.1, (c - 1, len(p), 3))
+    ls = np.array(levels, np.float32)
+    tri = ref.tessellate(gsdf, vox["vertices"], gsh, vox["neighbors"], vox["lower_corners"], vox["upper_corners"],
+                         vox["indices"], ls)
+    vertices = (2.0 * tri["vertices"] - 1.0).astype(np.float32)
+    faces = tri["faces"]
+    face_offsets = tri["face_offsets"]
+    s = len(levels)
+    # face_offsets[1:].view(S, -1)[:, -1] // 3 (triangle_extraction/__init__.py:146)
+    sfb = np.ascontiguousarray(face_offsets[1:].reshape(s, -1)[:, -1] // 3).astype(np.int32)
+    sdf = tri["signed_distances"]
+    sh = tri["spherical_harmonics"]
+
+    ext = np.stack([_look_at(cam) for cam in cameras]).astype(np.float32)
+    intr = np.stack([_pinhole(image_shape[0], image_shape[1], fov) for _ in cameras]).astype(np.float32)
+    h, w = image_shape
+    b = len(cameras)
+    rows, cols = -(-h // TILE[0]), -(-w // TILE[1])
+    t = rows * cols
+
+    xy, depth = ref.project_vertices(vertices, ext, intr)
+    tmin, tmax, count = ref.bound_triangles(xy, depth, faces, TILE, (rows, cols), NEAR_PLANE)
+    campos = np.linalg.inv(ext.astype(np.float64))[:, :3, 3].astype(np.float32)
+    colors = ref.evaluate_sh(sh_degree, vertices, sh, campos)
+
+    out = dict(vertices=vertices, faces=faces, shell_face_boundaries=sfb, signed_distances=sdf,
+               spherical_harmonics=sh, sh_degree=np.int32(sh_degree), extrinsics=ext, intrinsics=intr,
+               image_shape=np.array(image_shape, np.int32), sharpness=np.float32(sharpness),
+               near_plane=np.float32(NEAR_PLANE), xy=xy, depth=depth, tile_minima=tmin, tile_maxima=tmax,
+               num_tiles_overlapped=count, camera_positions=campos, colors=colors)
+
+    for mode, explicit in (("fused", False), ("explicit", True)):
+        keys, tri_idx = ref.generate_keys(explicit, depth, faces, sfb, tmin, tmax, count, cols)
+        order = np.argsort(keys, kind="stable")
+        sk, st = keys[order], tri_idx[order]
+        bounds = ref.delineate_tiles(explicit, sk, b, s if explicit else 1, t, explicit)
+        out.update({f"{mode}/keys": keys, f"{mode}/triangles": tri_idx, f"{mode}/sorted_keys": sk,
+                    f"{mode}/sorted_triangles": st, f"{mode}/tile_boundaries": bounds})
+
+    out["fused/image"] = ref.intersect_and_composite(xy, colors, sdf, faces, sharpness, out["fused/sorted_keys"],
+                                                     out["fused/sorted_triangles"],
+                                                     out["fused/tile_boundaries"].reshape(b, t, 2), s, (h, w))
+    uv, index = ref.intersect(xy, faces, out["explicit/sorted_triangles"], out["explicit/tile_boundaries"], s, (h, w))
+    isdf, icol = ref.interpolate(uv, index, faces, sdf, colors)
+    per_pixel_sdf = isdf.transpose(0, 2, 3, 1).reshape(-1, s)
+    per_pixel_col = icol.transpose(0, 2, 3, 1, 4).reshape(-1, s, 3)
+    mask = (index != -1).transpose(0, 2, 3, 1).reshape(-1, s)
+    ccol, ct = ref.composite(per_pixel_sdf, per_pixel_col, mask, sharpness)
+    out.update({"explicit/uv": uv, "explicit/index": index, "explicit/interp_sdf": isdf,
+                "explicit/interp_colors": icol, "explicit/composite_colors": ccol, "explicit/composite_T": ct})
+    return out
+
+
+def generate(reference: str | None = None) -> dict[str, dict[str, np.ndarray]]:
+    if reference:
+        os.environ["MESHTRYOSHKA_REFERENCE"] = reference
+    from oracle import ref
+
+    if not ref.available():
+        raise SystemExit("reference tree not found; cannot build its kernels")
+    fixtures = {"extraction": extraction_fixture(ref)}
+    for name, kw in SCENES.items():
+        fixtures[f"raster_{name}"] = raster_fixture(ref, **kw)
+    return fixtures
+
+
+def main() -> None:
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--reference", default=None)
+    args = parser.parse_args()
+    for name, arrays in generate(args.reference).items():
+        path = HERE / f"{name}.npz"
+        np.savez_compressed(path, **arrays)
+        print(f"{path.name}: {len(arrays)} arrays, {path.stat().st_size / 1024:.0f} KiB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,7 +1,8 @@
 """GPU parity of the extraction path against the CPU oracle.
 
 Topology, offsets, faces and vertex indices must be bit-exact; interpolated
-vertex attributes are bit-exact too (same operation order, explicit FMAs);
+vertex attributes are bit-exact too (the reference source's operations in
+its order, no contraction);
 gradients of the marching-cubes vertices agree within 1e-5 relative.
 """
 

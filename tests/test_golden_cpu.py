@@ -1,0 +1,122 @@
+"""Pins the CPU oracle to the reference's own kernel outputs.
+
+The fixtures in tests/golden/ were computed by the reference's compute
+kernels (compiled on the host from its sources, see tests/golden/make_golden.py).
+Every stage of the oracle must reproduce them bit for bit from the same
+inputs: voxel extraction, dilation, marching-cubes tessellation, projection,
+tile bounds, keys in both layouts, sorting, tile ranges, spherical harmonics,
+the fused intersect-and-composite image, and the explicit intersect /
+interpolate / composite chain.
+
+When the reference tree is mounted, the fixtures are also regenerated in
+memory and must equal the committed files.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import goldens
+
+
+@pytest.fixture(scope="module")
+def extraction():
+    return goldens.load("extraction")
+
+
+@pytest.mark.parametrize("grid", goldens.EXTRACTION_GRIDS)
+def test_oracle_extract_voxels_matches_reference(extraction, grid):
+    g = {k.split("/", 1)[1]: v for k, v in extraction.items() if k.startswith(grid + "/")}
+    occ = g["occupancy"]
+    vox = oracle.extract_voxels(occ)
+    for field in ("vertices", "neighbors", "lower_corners", "upper_corners", "indices"):
+        np.testing.assert_array_equal(getattr(vox, field), g[field], err_msg=field)
+    vocc, vcounts = oracle.compute_vertex_occupancy(occ)
+    np.testing.assert_array_equal(vocc, g["vertex_occupancy"])
+    np.testing.assert_array_equal(vcounts, g["vertex_counts"])
+    np.testing.assert_array_equal(oracle.count_occupancy(occ), g["voxel_counts"])
+    for d in (1, 3):
+        np.testing.assert_array_equal(oracle.dilate_occupancy(occ, d), g[f"dilated_{d}"], err_msg=f"dilation {d}")
+
+
+def test_oracle_tessellation_matches_reference(extraction):
+    e = extraction
+    tri = oracle.tessellate_voxels(e["tess/signed_distances"], e["sphere/vertices"], e["tess/spherical_harmonics"],
+                                   e["sphere/neighbors"], e["sphere/lower_corners"], e["sphere/upper_corners"],
+                                   e["sphere/indices"], e["tess/level_sets"])
+    assert e["tess/out_faces"].shape[0] > 0
+    for field in goldens.TESS_FIELDS:
+        np.testing.assert_array_equal(getattr(tri, field), e[f"tess/out_{field}"], err_msg=field)
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_oracle_raster_front_end_matches_reference(scene):
+    g = goldens.raster(scene)
+    b, s, h, w, rows, cols = goldens.grid_dims(g)
+    xy, depth = oracle.project_vertices(g["vertices"], g["extrinsics"], g["intrinsics"])
+    np.testing.assert_array_equal(xy, g["xy"])
+    np.testing.assert_array_equal(depth, g["depth"])
+    tmin, tmax, count = oracle.bound_triangles(xy, depth, g["faces"], (16, 16), (rows, cols), float(g["near_plane"]))
+    np.testing.assert_array_equal(tmin, g["tile_minima"])
+    np.testing.assert_array_equal(tmax, g["tile_maxima"])
+    np.testing.assert_array_equal(count, g["num_tiles_overlapped"])
+    np.testing.assert_array_equal(oracle.camera_positions(g["extrinsics"]), g["camera_positions"])
+    colors = oracle.evaluate_spherical_harmonics(g["vertices"], g["spherical_harmonics"], g["extrinsics"],
+                                                 int(g["sh_degree"]))
+    np.testing.assert_array_equal(colors, g["colors"])
+    for mode, kd, explicit in (("fused", oracle.fused_key_defines(), False),
+                               ("explicit", oracle.explicit_key_defines(), True)):
+        keys, tri = oracle.generate_keys(depth, g["faces"], g["shell_face_boundaries"], tmin, tmax, count, cols, kd)
+        np.testing.assert_array_equal(keys, g[f"{mode}/keys"], err_msg=mode)
+        np.testing.assert_array_equal(tri, g[f"{mode}/triangles"], err_msg=mode)
+        sk, st = oracle.sort_pairs(keys, tri)
+        np.testing.assert_array_equal(sk, g[f"{mode}/sorted_keys"], err_msg=mode)
+        np.testing.assert_array_equal(st, g[f"{mode}/sorted_triangles"], err_msg=mode)
+        bounds = oracle.delineate_tiles(sk, kd, explicit, b, s, rows * cols)
+        np.testing.assert_array_equal(bounds.reshape(g[f"{mode}/tile_boundaries"].shape),
+                                      g[f"{mode}/tile_boundaries"], err_msg=mode)
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_oracle_fused_image_matches_reference(scene):
+    g = goldens.raster(scene)
+    b, s, h, w, rows, cols = goldens.grid_dims(g)
+    image = oracle.intersect_and_composite(g["xy"], g["colors"], g["signed_distances"], g["faces"],
+                                           float(g["sharpness"]), g["fused/sorted_keys"], g["fused/sorted_triangles"],
+                                           g["fused/tile_boundaries"].reshape(b, rows * cols, 2), s, (16, 16), (h, w),
+                                           oracle.fused_key_defines())
+    np.testing.assert_array_equal(image, g["fused/image"])
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_oracle_explicit_chain_matches_reference(scene):
+    g = goldens.raster(scene)
+    b, s, h, w, rows, cols = goldens.grid_dims(g)
+    uv, index = oracle.intersect(g["xy"], g["faces"], g["explicit/sorted_triangles"], g["explicit/tile_boundaries"],
+                                 s, (16, 16), (h, w))
+    np.testing.assert_array_equal(index, g["explicit/index"])
+    np.testing.assert_array_equal(uv, g["explicit/uv"])
+    isdf, icol = oracle.interpolate(uv, index, g["faces"], g["signed_distances"], g["colors"])
+    np.testing.assert_array_equal(isdf, g["explicit/interp_sdf"])
+    np.testing.assert_array_equal(icol, g["explicit/interp_colors"])
+    sdf, col, mask = goldens.per_pixel_shells(g)
+    out_c, out_t = oracle.composite(sdf, col, mask, float(g["sharpness"]))
+    np.testing.assert_array_equal(out_c, g["explicit/composite_colors"])
+    np.testing.assert_array_equal(out_t, g["explicit/composite_T"])
+
+
+def test_fixtures_regenerate_from_reference():
+    """The committed fixtures are what the reference's kernels produce now."""
+    from oracle import ref
+
+    if not ref.available():
+        pytest.skip("reference sources not mounted; the committed fixtures stand")
+    from tests.golden import make_golden
+
+    for name, arrays in make_golden.generate().items():
+        committed = goldens.load(name)
+        assert sorted(arrays) == sorted(committed), name
+        for key, value in arrays.items():
+            np.testing.assert_array_equal(np.asarray(value), committed[key], err_msg=f"{name}:{key}")
