@@ -465,6 +465,33 @@ void or_create_triangle_vertices(const float* gv, const float* gsdf, const float
   }
 }
 
+// Where each triangle vertex comes from: origin corner, axis corner and the
+// (detached) weight t of create_triangle_vertices.slang:80-96. Used by the
+// finite-difference checks, which hold t fixed as the reference's adjoint does.
+void or_triangle_vertex_sources(const float* gsdf, const int32_t* lower, int64_t G, const float* level_sets, int S,
+                                const int32_t* voff, int32_t* out_i0, int32_t* out_i1, float* out_t) {
+#pragma omp parallel for schedule(static)
+  for (int64_t g = 0; g < G; ++g) {
+    OracleVoxel vx;
+    vx.i0 = lower[g];
+    vx.d0 = gsdf[vx.i0];
+    for (int a = 0; a < 3; ++a) {
+      vx.i1[a] = lower[(a + 1) * G + g];
+      vx.d1[a] = vx.i1[a] >= 0 ? gsdf[vx.i1[a]] : vx.d0;
+    }
+    for (int s = 0; s < S; ++s) {
+      int64_t vi = voff[(int64_t)s * G + g];
+      for (int a = 0; a < 3; ++a) {
+        if (!should_compute_triangle_vertex(vx, a, level_sets[s])) continue;
+        out_i0[vi] = vx.i0;
+        out_i1[vi] = vx.i1[a];
+        out_t[vi] = mc_weight(vx.d0, vx.d1[a], level_sets[s]);
+        vi++;
+      }
+    }
+  }
+}
+
 // create_triangle_vertices.slang:201-291 (backward). d(v0 + t(v1 - v0)) with
 // t detached: origin receives (1 - t) * grad, the axis corner t * grad; the
 // per-voxel differential is summed over level sets and axes, then scattered
@@ -1000,6 +1027,39 @@ void or_intersect_and_composite_forward(const float* xy, const float* colors, co
           o[plane] = acc[1];
           o[2 * plane] = acc[2];
           o[3 * plane] = Tr;
+        }
+    }
+  }
+}
+
+// The hits the fused walk accepts at every pixel, in compositing order
+// (at most one per shell): face index (-1 = none) and barycentrics (u, v, w).
+void or_fused_hits(const float* xy, int64_t V, const int32_t* faces, const int64_t* keys, const int32_t* tri,
+                   const int64_t* bounds, int B, int S, int rows, int cols, int th, int tw, int H, int W,
+                   int shell_off, int shell_len, int32_t* out_face, float* out_uvw) {
+  const FusedScene a{xy, nullptr, nullptr, V, faces, 0.f, keys, tri, bounds, B, S, rows, cols, th, tw, H, W,
+                     shell_off, shell_len};
+  const int64_t T = (int64_t)rows * cols;
+#pragma omp parallel
+  {
+    std::vector<Hit> hits;
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t bt = 0; bt < B * T; ++bt) {
+      const int cam = (int)(bt / T);
+      const int64_t tile = bt % T;
+      for (int ty = 0; ty < th; ++ty)
+        for (int tx = 0; tx < tw; ++tx) {
+          const int px = (int)(tile % cols) * tw + tx, py = (int)(tile / cols) * th + ty;
+          if (px >= W || py >= H) continue;
+          walk(a, cam, tile, (float)px + 0.5f, (float)py + 0.5f, hits);
+          const int64_t base = (((int64_t)cam * H + py) * W + px) * S;
+          for (int l = 0; l < S; ++l) {
+            const bool have = l < (int)hits.size();
+            out_face[base + l] = have ? hits[l].f : -1;
+            out_uvw[3 * (base + l)] = have ? hits[l].u : 0.f;
+            out_uvw[3 * (base + l) + 1] = have ? hits[l].v : 0.f;
+            out_uvw[3 * (base + l) + 2] = have ? hits[l].w : 0.f;
+          }
         }
     }
   }

@@ -36,6 +36,7 @@ _SIGNATURES = {
     "or_count_triangle_vertices": (None, [P, P, I64, P, I32, P]),
     "or_create_triangle_vertices": (None, [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P]),
     "or_create_triangle_vertices_backward": (None, [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P]),
+    "or_triangle_vertex_sources": (None, [P, P, I64, P, I32, P, P, P, P]),
     "or_count_triangle_faces": (None, [P, P, I64, P, I64, P, I32, P, P]),
     "or_create_triangle_faces": (None, [P, P, I64, I64, P, P, P, I32, P, P, P]),
 }
@@ -213,6 +214,18 @@ def tessellate_voxels(sdf, vertices, sh, neighbors, lower, upper, indices, level
     return Triangles(out_v, out_sdf, out_sh, faces, vidx, vb, fb, voff, foff, codes, types)
 
 
+def triangle_vertex_sources(sdf, lower, level_sets, vertex_offsets, num_vertices):
+    """(origin corner, axis corner, weight t) of every triangle vertex."""
+    sdf, lower = _c(sdf, np.float32), _c(lower, np.int32)
+    level_sets, voff = _c(level_sets, np.float32), _c(vertex_offsets, np.int32)
+    g, s = lower.shape[1], level_sets.shape[0]
+    i0 = np.zeros((num_vertices,), np.int32)
+    i1 = np.zeros((num_vertices,), np.int32)
+    t = np.zeros((num_vertices,), np.float32)
+    lib().or_triangle_vertex_sources(_p(sdf), _p(lower), g, _p(level_sets), s, _p(voff), _p(i0), _p(i1), _p(t))
+    return i0, i1, t
+
+
 def create_triangle_vertices_backward(sdf, sh_shape, lower, level_sets, vertex_offsets, grad_vertices,
                                       grad_sdf, grad_sh):
     """create_triangle_vertices.py:104-170: returns (d grid_vertices, d grid_sdf, d grid_sh)."""
@@ -252,6 +265,7 @@ _SIGNATURES.update({
     "or_intersect_and_composite_backward": (
         None, [P, P, P, I64, P, F32, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P, P,
                I32]),
+    "or_fused_hits": (None, [P, I64, P, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, I32, I32, P, P]),
     "or_intersect": (None, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P]),
     "or_interpolate": (None, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P]),
     "or_interpolate_backward": (None, [P, P, I32, I32, I32, I32, P, I64, P, P, P, P]),
@@ -406,6 +420,22 @@ def intersect_and_composite_backward(xy, colors, sdf, faces, sharpness, sorted_k
         cols, tile_shape[0], tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out),
         _p(grad_out), _p(gcol), _p(gsdf), _p(gsharp), int(exact))
     return gcol, gsdf, float(gsharp[0])
+
+
+def fused_hits(xy, faces, sorted_keys, sorted_tri, tile_boundaries, num_shells, tile_shape, image_shape, key_defines):
+    """Per pixel, the hits the fused walk accepts in compositing order:
+    faces [B, H, W, S] (-1 = none) and barycentrics [B, H, W, S, 3]."""
+    xy, faces = _c(xy, np.float32), _c(faces, np.int32)
+    b, v, _ = xy.shape
+    h, w = image_shape
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    d = dict(key_defines)
+    out_face = np.full((b, h, w, num_shells), -1, np.int32)
+    out_uvw = np.zeros((b, h, w, num_shells, 3), np.float32)
+    sk, st, tb = _c(sorted_keys, np.int64), _c(sorted_tri, np.int32), _c(tile_boundaries, np.int64)
+    lib().or_fused_hits(_p(xy), v, _p(faces), _p(sk), _p(st), _p(tb), b, num_shells, rows, cols, tile_shape[0],
+                        tile_shape[1], h, w, d["SHELL_BIT_OFFSET"], d["SHELL_BIT_LENGTH"], _p(out_face), _p(out_uvw))
+    return out_face, out_uvw
 
 
 def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, sdf, sh, sh_degree,
