@@ -4,11 +4,17 @@ TEST INFRASTRUCTURE ONLY. The reference's render-path kernels are Slang
 (slangtorch JIT); neither slangtorch nor slangc exists here. Most of these
 kernels use a C-like subset of Slang, so this recipe rewrites each source
 file textually (attributes dropped, ``let``/``var`` to ``auto``, ``$for`` to
-``for``, float literals suffixed, struct definitions hoisted, backward
-kernels removed), writes the result under ``oracle/_ref/`` (git-ignored, never
-committed), and compiles it with ``oracle/ref_shim/slang.h`` (host stand-ins
-for Slang types and intrinsics) and ``oracle/ref_shim/driver.cpp`` (grid
-emulation and a C ABI) into ``oracle/_ref/libref.so``.
+``for``, float literals suffixed, struct definitions hoisted), writes the
+result under ``oracle/_ref/`` (git-ignored, never committed), and compiles it
+with ``oracle/ref_shim/slang.h`` (host stand-ins for Slang types and
+intrinsics) and ``oracle/ref_shim/driver.cpp`` (grid emulation and a C ABI)
+into ``oracle/_ref/libref.so``.
+
+Backward kernels: the two hand-written ones (fused intersect-and-composite
+and explicit composite) are kept; the ``bwd_diff(helper)`` calls in them use
+adjoints of the small helpers written by hand in ``oracle/ref_shim/autodiff_*.h``.
+The backward kernels that are pure automatic differentiation (SH evaluation,
+triangle vertex creation) are dropped.
 
 The reference's module-level helpers in ``common.slang`` (64-bit indexing,
 DiffTensorView load/store) are replaced by equivalents in the shim; every
@@ -50,10 +56,18 @@ SOURCES = {
     ("triangle_rasterization", "generate_keys.slang"): [],
     ("triangle_rasterization", "delineate_tiles.slang"): [],
     ("triangle_rasterization", "evaluate_spherical_harmonics.slang"): ["evaluate_spherical_harmonics_backward"],
-    ("triangle_rasterization", "intersect_and_composite.slang"): ["intersect_and_composite_backward"],
+    ("triangle_rasterization", "intersect_and_composite.slang"): [],
     ("triangle_rasterization", "intersect.slang"): [],
     ("triangle_rasterization", "interpolate.slang"): [],
-    ("triangle_rasterization", "composite.slang"): ["composite_backward"],
+    ("triangle_rasterization", "composite.slang"): [],
+}
+
+# Hand-written backward kernels that call bwd_diff(helper)(...): the
+# adjoints of those helpers come from a shim header, included right before
+# the kernel.
+AUTODIFF = {
+    "intersect_and_composite.slang": ("intersect_and_composite_backward", "autodiff_intersect_and_composite.h"),
+    "composite.slang": ("composite_backward", "autodiff_composite.h"),
 }
 
 # Files whose local/struct arrays are copied as values (aggregate returns):
@@ -139,7 +153,13 @@ def translate(src: str, fname: str, drops: list[str]) -> tuple[str, list[str]]:
     if fname in ARRAY_VALUE_FILES:
         src = ARRAY_DECL.sub(to_std_array, src)
     src = re.sub(r",(\s*)\)", r"\1)", src)  # trailing commas in parameter / argument lists
+    src = re.sub(r"\bbwd_diff\((\w+)\)\s*\(", r"bwd_diff_\1(", src)
+    src = re.sub(r"\b(\w+)\.Differential\(", r"\1Diff(", src)
     src = hoist_structs(src)
+    if fname in AUTODIFF:
+        kernel, header = AUTODIFF[fname]
+        m = re.search(r"\bvoid\s+" + kernel + r"\s*\(", src)
+        src = src[: m.start()] + f'#include "{header}"\n' + src[m.start():]
     return src, imports
 
 
@@ -165,7 +185,7 @@ def build(root: Path | str | None = None, force: bool = False) -> Path | None:
     if not (root / "triangle_extraction").is_dir():
         return None
     driver = SHIM_DIR / "driver.cpp"
-    deps = [driver, SHIM_DIR / "slang.h", Path(__file__)]
+    deps = [driver, *sorted(SHIM_DIR.glob("*.h")), Path(__file__)]
     if not force and LIBRARY.exists() and all(d.stat().st_mtime <= LIBRARY.stat().st_mtime for d in deps):
         return LIBRARY
     generate(root)

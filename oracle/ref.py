@@ -35,6 +35,9 @@ _SIGNATURES = {
     "ref_intersect": [P, I, I64, P, I64, P, I64, P, I, I, I, I, I, P, P],
     "ref_interpolate": [P, P, I, I, I, I, P, I64, P, P, I64, P, P],
     "ref_composite_forward": [P, P, P, I64, I, F32, P, P],
+    "ref_intersect_and_composite_backward": [P, P, P, I, I64, P, I64, F32, P, P, I64, P, I, I, I, I, I, P, P, P, P,
+                                             P],
+    "ref_composite_backward": [P, P, P, I64, I, F32, P, P, P, P, P, P, P],
 }
 
 _lib = None
@@ -207,3 +210,32 @@ def composite(sdf, colors, mask, sharpness):
     oc, ot = np.zeros((p, 3), np.float32), np.zeros((p,), np.float32)
     lib().ref_composite_forward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(oc), _p(ot))
     return oc, ot
+
+
+def intersect_and_composite_backward(xy, colors, sdf, faces, sharpness, keys, tri, bounds, num_shells, image_shape,
+                                     out, grad_out):
+    """The reference's fused backward (hand-written kernel, shim adjoints for
+    its bwd_diff helpers): gradients of colours, signed distances, sharpness."""
+    xy, colors, sdf, faces = _c(xy, np.float32), _c(colors, np.float32), _c(sdf, np.float32), _c(faces, np.int32)
+    keys, tri, bounds = _c(keys, np.int64), _c(tri, np.int32), _c(bounds, np.int64)
+    out, grad_out = _c(out, np.float32), _c(grad_out, np.float32)
+    b, v, _ = xy.shape
+    h, w = image_shape
+    rows, cols = -(-h // 16), -(-w // 16)
+    gc, gs, gsh = np.zeros_like(colors), np.zeros_like(sdf), np.zeros((1,), np.float32)
+    lib().ref_intersect_and_composite_backward(_p(xy), _p(colors), _p(sdf), b, v, _p(faces), faces.shape[0],
+                                               float(sharpness), _p(keys), _p(tri), keys.size, _p(bounds),
+                                               num_shells, rows, cols, h, w, _p(out), _p(grad_out), _p(gc), _p(gs),
+                                               _p(gsh))
+    return gc, gs, float(gsh[0])
+
+
+def composite_backward(sdf, colors, mask, sharpness, out_colors, out_t, grad_colors, grad_t):
+    sdf, colors, mask = _c(sdf, np.float32), _c(colors, np.float32), _c(mask, np.uint8)
+    out_colors, out_t = _c(out_colors, np.float32), _c(out_t, np.float32)
+    grad_colors, grad_t = _c(grad_colors, np.float32), _c(grad_t, np.float32)
+    p, s = sdf.shape
+    gsdf, gcol, gsh = np.zeros_like(sdf), np.zeros_like(colors), np.zeros((1,), np.float32)
+    lib().ref_composite_backward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(out_colors), _p(out_t),
+                                 _p(grad_colors), _p(grad_t), _p(gsdf), _p(gcol), _p(gsh))
+    return gsdf, gcol, float(gsh[0])

@@ -368,6 +368,25 @@ void ref_intersect_and_composite_forward(float* xy, float* colors, float* sdf, i
   });
 }
 
+// intersect_and_composite.py:82-147 (tile 16x16, fused layout). Gradient
+// buffers are zero-filled by the caller, as torch.zeros_like there.
+void ref_intersect_and_composite_backward(float* xy, float* colors, float* sdf, int B, int64_t V, int32_t* faces,
+                                          int64_t F, float sharpness, int64_t* keys, int32_t* tri, int64_t K,
+                                          int64_t* bounds, int num_shells, int rows, int cols, int H, int W,
+                                          float* out, float* grad_out, float* grad_colors, float* grad_sdf,
+                                          float* grad_sharpness) {
+  TensorView<float> v(xy, {(uint64_t)B, (uint64_t)V, 2});
+  DiffTensorView c(TensorView<float>(colors, {(uint64_t)B, (uint64_t)V, 3}), grad_colors);
+  DiffTensorView d(TensorView<float>(sdf, {(uint64_t)V}), grad_sdf);
+  DiffTensorView s(TensorView<float>(&sharpness, {1}), grad_sharpness);
+  TensorView<int> f(faces, {(uint64_t)F, 3}), t(tri, {(uint64_t)K});
+  TensorView<int64_t> k(keys, {(uint64_t)K}), bd(bounds, {(uint64_t)B, (uint64_t)rows * cols, 2});
+  DiffTensorView o(TensorView<float>(out, {(uint64_t)B, 4, (uint64_t)H, (uint64_t)W}), grad_out);
+  run_grid_with_barriers(uint3((uint)(rows * cols * B), 1, 1), uint3(256, 1, 1), [&] {
+    k_fused_16::intersect_and_composite_backward(t, bd, v, c, d, f, s, num_shells, rows, cols, o, k);
+  });
+}
+
 // intersect.py:50-63 (tile 16x16).
 void ref_intersect(float* xy, int B, int64_t V, int32_t* faces, int64_t F, int32_t* tri, int64_t K, int64_t* bounds,
                    int S, int rows, int cols, int H, int W, float* out_uv, int32_t* out_index) {
@@ -401,6 +420,20 @@ void ref_composite_forward(float* sdf, float* colors, uint8_t* mask, int64_t P, 
   TensorView<float> s(&sharpness, {1}), oc(out_colors, {(uint64_t)P, 3}), ot(out_T, {(uint64_t)P});
   run_grid(uint3((P + 255) / 256, 1, 1), uint3(256, 1, 1),
            [&] { k_composite::composite_forward(d, c, m, s, oc, ot); });
+}
+
+// composite.py:63-99. Gradient buffers zero-filled by the caller.
+void ref_composite_backward(float* sdf, float* colors, uint8_t* mask, int64_t P, int S, float sharpness,
+                            float* out_colors, float* out_T, float* grad_colors_out, float* grad_T_out,
+                            float* grad_sdf, float* grad_colors, float* grad_sharpness) {
+  DiffTensorView d(TensorView<float>(sdf, {(uint64_t)P, (uint64_t)S}), grad_sdf);
+  DiffTensorView c(TensorView<float>(colors, {(uint64_t)P, (uint64_t)S, 3}), grad_colors);
+  TensorView<bool> m(reinterpret_cast<bool*>(mask), {(uint64_t)P, (uint64_t)S});
+  DiffTensorView s(TensorView<float>(&sharpness, {1}), grad_sharpness);
+  DiffTensorView oc(TensorView<float>(out_colors, {(uint64_t)P, 3}), grad_colors_out);
+  DiffTensorView ot(TensorView<float>(out_T, {(uint64_t)P}), grad_T_out);
+  run_grid(uint3((P + 255) / 256, 1, 1), uint3(256, 1, 1),
+           [&] { k_composite::composite_backward(d, c, m, s, oc, ot); });
 }
 
 }  // extern "C"

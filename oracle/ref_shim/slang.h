@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <barrier>
 #include <cmath>
 #include <cstdint>
@@ -272,7 +273,22 @@ struct TensorView {
     ptr[(uint64_t)idx] = value;
   }
 };
-using DiffTensorView = TensorView<float>;
+// A float tensor with an optional gradient tensor of the same shape, as
+// slangtorch passes (primal, gradient) pairs. Backward kernels read the
+// gradient of stored outputs and add into the gradient of loaded inputs.
+struct DiffTensorView : TensorView<float> {
+  float* grad = nullptr;
+  DiffTensorView() = default;
+  DiffTensorView(const TensorView<float>& t, float* g = nullptr) : TensorView<float>(t), grad(g) {}
+  template <typename... I>
+  float grad_at(I... idx) const {
+    return grad ? grad[offset(idx...)] : 0.f;
+  }
+  template <typename... I>
+  void grad_add(float value, I... idx) const {
+    if (grad) std::atomic_ref<float>(grad[offset(idx...)]).fetch_add(value, std::memory_order_relaxed);
+  }
+};
 
 // The reference's 64-bit indexing helpers (common.slang), by semantics.
 template <typename T, typename U, int N>

@@ -2,7 +2,10 @@
 
 Every output array is computed by the reference implementation's compute
 kernels (its Slang sources, rewritten textually to C++ and compiled on the
-host by ``oracle/build_ref.py``; see ``oracle/ref.py``). The glue between
+host by ``oracle/build_ref.py``; see ``oracle/ref.py``). Gradients come from
+the reference's two hand-written backward kernels (fused intersect-and-composite
+and explicit composite), whose calls to automatically differentiated helpers
+use hand-derived adjoints (``oracle/ref_shim/autodiff_*.h``). The glue between
 kernels follows the reference's Python call sites:
 
 * exclusive scans are numpy cumsums (triangle_extraction/__init__.py uses
@@ -160,9 +163,13 @@ def raster_fixture(ref, n, levels, sh_degree, cameras, image_shape, fov, sharpne
         out.update({f"{mode}/keys": keys, f"{mode}/triangles": tri_idx, f"{mode}/sorted_keys": sk,
                     f"{mode}/sorted_triangles": st, f"{mode}/tile_boundaries": bounds})
 
-    out["fused/image"] = ref.intersect_and_composite(xy, colors, sdf, faces, sharpness, out["fused/sorted_keys"],
-                                                     out["fused/sorted_triangles"],
-                                                     out["fused/tile_boundaries"].reshape(b, t, 2), s, (h, w))
+    fused_args = (xy, colors, sdf, faces, sharpness, out["fused/sorted_keys"], out["fused/sorted_triangles"],
+                  out["fused/tile_boundaries"].reshape(b, t, 2), s, (h, w))
+    out["fused/image"] = ref.intersect_and_composite(*fused_args)
+    grad_image = rng.normal(0, 1, out["fused/image"].shape).astype(np.float32)
+    gc, gs, gsh = ref.intersect_and_composite_backward(*fused_args, out["fused/image"], grad_image)
+    out.update({"fused/grad_image": grad_image, "fused/grad_colors": gc, "fused/grad_signed_distances": gs,
+                "fused/grad_sharpness": np.float32(gsh)})
     uv, index = ref.intersect(xy, faces, out["explicit/sorted_triangles"], out["explicit/tile_boundaries"], s, (h, w))
     isdf, icol = ref.interpolate(uv, index, faces, sdf, colors)
     per_pixel_sdf = isdf.transpose(0, 2, 3, 1).reshape(-1, s)
@@ -171,6 +178,12 @@ def raster_fixture(ref, n, levels, sh_degree, cameras, image_shape, fov, sharpne
     ccol, ct = ref.composite(per_pixel_sdf, per_pixel_col, mask, sharpness)
     out.update({"explicit/uv": uv, "explicit/index": index, "explicit/interp_sdf": isdf,
                 "explicit/interp_colors": icol, "explicit/composite_colors": ccol, "explicit/composite_T": ct})
+    g_col = rng.normal(0, 1, ccol.shape).astype(np.float32)
+    g_t = rng.normal(0, 1, ct.shape).astype(np.float32)
+    gs, gc, gsh = ref.composite_backward(per_pixel_sdf, per_pixel_col, mask, sharpness, ccol, ct, g_col, g_t)
+    out.update({"explicit/grad_composite_colors": g_col, "explicit/grad_composite_T": g_t,
+                "explicit/grad_shell_signed_distances": gs, "explicit/grad_shell_colors": gc,
+                "explicit/grad_sharpness": np.float32(gsh)})
     return out
 
 

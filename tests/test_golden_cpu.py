@@ -8,8 +8,13 @@ tile bounds, keys in both layouts, sorting, tile ranges, spherical harmonics,
 the fused intersect-and-composite image, and the explicit intersect /
 interpolate / composite chain.
 
+Gradients: the oracle's default ("reference") routing must reproduce the
+reference's two hand-written backward kernels (fused intersect-and-composite,
+explicit composite) within 1e-4 of the largest gradient magnitude.
+
 When the reference tree is mounted, the fixtures are also regenerated in
-memory and must equal the committed files.
+memory and must equal the committed files (gradients, which the reference
+accumulates with atomics in a thread-order-dependent sum, within 1e-5).
 """
 
 from __future__ import annotations
@@ -19,6 +24,17 @@ import pytest
 
 from oracle import oracle
 from tests import goldens
+
+GRAD_RTOL = 1e-4
+ATOMIC_OUTPUTS = ("fused/grad_colors", "fused/grad_signed_distances", "fused/grad_sharpness",
+                  "explicit/grad_shell_signed_distances", "explicit/grad_shell_colors", "explicit/grad_sharpness")
+
+
+def close_grad(got, want, rtol=GRAD_RTOL, what=""):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    scale = max(float(np.abs(want).max()), 1e-30)
+    err = float(np.abs(got - want).max())
+    assert err <= rtol * scale, f"{what}: max abs err {err:.3e} > {rtol:g} x {scale:.3e}"
 
 
 @pytest.fixture(scope="module")
@@ -107,6 +123,31 @@ def test_oracle_explicit_chain_matches_reference(scene):
     np.testing.assert_array_equal(out_t, g["explicit/composite_T"])
 
 
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_oracle_fused_backward_matches_reference(scene):
+    g = goldens.raster(scene)
+    b, s, h, w, rows, cols = goldens.grid_dims(g)
+    gc, gs, gsh = oracle.intersect_and_composite_backward(
+        g["xy"], g["colors"], g["signed_distances"], g["faces"], float(g["sharpness"]), g["fused/sorted_keys"],
+        g["fused/sorted_triangles"], g["fused/tile_boundaries"].reshape(b, rows * cols, 2), s, (16, 16), (h, w),
+        oracle.fused_key_defines(), g["fused/image"], g["fused/grad_image"], exact=False)
+    close_grad(gc, g["fused/grad_colors"], what="colours")
+    close_grad(gs, g["fused/grad_signed_distances"], what="signed distances")
+    close_grad([gsh], [g["fused/grad_sharpness"]], what="sharpness")
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_oracle_explicit_composite_backward_matches_reference(scene):
+    g = goldens.raster(scene)
+    sdf, col, mask = goldens.per_pixel_shells(g)
+    gs, gc, gsh = oracle.composite_backward(sdf, col, mask, float(g["sharpness"]), g["explicit/composite_colors"],
+                                            g["explicit/composite_T"], g["explicit/grad_composite_colors"],
+                                            g["explicit/grad_composite_T"], exact=False)
+    close_grad(gs, g["explicit/grad_shell_signed_distances"], what="signed distances")
+    close_grad(gc, g["explicit/grad_shell_colors"], what="colours")
+    close_grad([gsh], [g["explicit/grad_sharpness"]], what="sharpness")
+
+
 def test_fixtures_regenerate_from_reference():
     """The committed fixtures are what the reference's kernels produce now."""
     from oracle import ref
@@ -119,4 +160,7 @@ def test_fixtures_regenerate_from_reference():
         committed = goldens.load(name)
         assert sorted(arrays) == sorted(committed), name
         for key, value in arrays.items():
-            np.testing.assert_array_equal(np.asarray(value), committed[key], err_msg=f"{name}:{key}")
+            if key in ATOMIC_OUTPUTS:
+                close_grad(value, committed[key], rtol=1e-5, what=f"{name}:{key}")
+            else:
+                np.testing.assert_array_equal(np.asarray(value), committed[key], err_msg=f"{name}:{key}")

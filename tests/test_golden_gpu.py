@@ -9,6 +9,10 @@ Outputs that pass through exp() (the fused image, the shell compositing and
 the rendered images) agree within 1e-5 max-abs: CUDA's expf and the host
 libm's exp may differ in the last bits. The full render entry points are
 checked against the fixtures' images with the background blended in.
+
+Gradients in the default ("reference") routing must reproduce the
+reference's hand-written backward kernels within 1e-4 of the largest
+gradient magnitude.
 """
 
 from __future__ import annotations
@@ -27,6 +31,7 @@ FUSED_KEYS = (("camera", 6), ("tile", 20), ("depth", 32), ("shell", 6))
 EXPLICIT_KEYS = (("camera", 6), ("shell", 6), ("tile", 20), ("depth", 32))
 BACKGROUND = np.array([0.2, 0.4, 0.6], np.float32)
 IMAGE_ATOL = 1e-5
+GRAD_RTOL = 1e-4
 
 
 def _t(a, device):
@@ -43,6 +48,13 @@ def _eq(got, want, what):
 
 def _near(got, want, what):
     np.testing.assert_allclose(_n(got), want, atol=IMAGE_ATOL, rtol=0, err_msg=what)
+
+
+def _close_grad(got, want, what):
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    scale = max(float(np.abs(want).max()), 1e-30)
+    err = float(np.abs(got - want).max())
+    assert err <= GRAD_RTOL * scale, f"{what}: max abs err {err:.3e} > {GRAD_RTOL:g} x {scale:.3e}"
 
 
 @pytest.fixture(scope="module")
@@ -145,3 +157,37 @@ def test_render_matches_reference_images(cuda_device, scene, mode):
         rgb = g["explicit/composite_colors"] + BACKGROUND * g["explicit/composite_T"][:, None]
         want = rgb.reshape(b, h, w, 3).transpose(0, 3, 1, 2)
     np.testing.assert_allclose(_n(image), want, atol=IMAGE_ATOL, rtol=0)
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_fused_backward_matches_reference(cuda_device, scene):
+    g, d = goldens.raster(scene), cuda_device
+    b, s, h, w, rows, cols = goldens.grid_dims(g)
+    grid = tr.TileGrid((16, 16), (h, w), b, s)
+    kd = tr.create_key_defines(*FUSED_KEYS)
+    colors = _t(g["colors"], d).requires_grad_(True)
+    sdf = _t(g["signed_distances"], d).requires_grad_(True)
+    sharp = torch.tensor(float(g["sharpness"]), device=d, requires_grad=True)
+    out = tr.intersect_and_composite(_t(g["xy"], d), colors, sdf, _t(g["faces"], d), sharp,
+                                     _t(g["fused/sorted_keys"], d), _t(g["fused/sorted_triangles"], d),
+                                     _t(g["fused/tile_boundaries"].reshape(b, rows * cols, 2), d), s, grid, kd,
+                                     gradient_mode="reference")
+    out.backward(_t(g["fused/grad_image"], d))
+    _close_grad(_n(colors.grad), g["fused/grad_colors"], "colours")
+    _close_grad(_n(sdf.grad), g["fused/grad_signed_distances"], "signed distances")
+    _close_grad([float(sharp.grad)], [g["fused/grad_sharpness"]], "sharpness")
+
+
+@pytest.mark.parametrize("scene", goldens.RASTER_SCENES)
+def test_explicit_composite_backward_matches_reference(cuda_device, scene):
+    g, d = goldens.raster(scene), cuda_device
+    psdf, pcol, mask = goldens.per_pixel_shells(g)
+    sdf = _t(psdf, d).requires_grad_(True)
+    col = _t(pcol, d).requires_grad_(True)
+    sharp = torch.tensor(float(g["sharpness"]), device=d, requires_grad=True)
+    out_c, out_t = tr.Composite.apply(sdf, col, _t(mask, d), sharp, "reference")
+    torch.autograd.backward((out_c, out_t), (_t(g["explicit/grad_composite_colors"], d),
+                                             _t(g["explicit/grad_composite_T"], d)))
+    _close_grad(_n(sdf.grad), g["explicit/grad_shell_signed_distances"], "signed distances")
+    _close_grad(_n(col.grad), g["explicit/grad_shell_colors"], "colours")
+    _close_grad([float(sharp.grad)], [g["explicit/grad_sharpness"]], "sharpness")
