@@ -150,7 +150,9 @@ MT_API int mt_count_triangle_vertices(const float* signed_distances,
 /* triangle_extraction/create_triangle_vertices.slang:145-199 (forward).
  * vertex_offsets: exclusive scan of the counts above (S*G+1 entries).
  * grid_sh [C,G,3]; outputs vertices [V,3], signed_distances [V],
- * spherical_harmonics [C,V,3], vertex_types [V] (uint8 axis 0/1/2). */
+ * spherical_harmonics [C,V,3], vertex_types [V] (uint8 axis 0/1/2), and
+ * vertex_sources [3,V] int32: origin corner, axis corner and the float bits
+ * of the (detached) weight t of every vertex. */
 MT_API int mt_create_triangle_vertices(const float* grid_vertices,
                                 const float* grid_signed_distances,
                                 const float* grid_spherical_harmonics,
@@ -159,20 +161,23 @@ MT_API int mt_create_triangle_vertices(const float* grid_vertices,
                                 const int32_t* vertex_offsets, int64_t V,
                                 float* vertices, float* signed_distances,
                                 float* spherical_harmonics,
-                                uint8_t* vertex_types, mt_stream_t stream);
+                                uint8_t* vertex_types, int32_t* vertex_sources,
+                                mt_stream_t stream);
 
 /* triangle_extraction/create_triangle_vertices.slang:201-291 (backward).
- * Accumulates (+=) into grad_grid_vertices [G,3], grad_grid_signed_distances
- * [G], grad_grid_spherical_harmonics [C,G,3]; callers zero them first.
- * grad_vertices may be NULL (treated as zero). The MC weight t is detached,
- * as in the reference. */
+ * Writes (=) every entry of grad_grid_vertices [G,3] (may be NULL when
+ * grad_vertices is NULL), grad_grid_signed_distances [G] and
+ * grad_grid_spherical_harmonics [C,G,3]; no zero-filled outputs needed.
+ * corner_inverse: scratch of 4*G int32. A NULL input gradient counts as
+ * zero. The MC weight t is detached, as in the reference. */
 MT_API int mt_create_triangle_vertices_backward(
     const float* grid_signed_distances, int32_t C,
     const int32_t* lower_corners, int64_t G, const float* level_sets,
     int32_t S, const int32_t* vertex_offsets, const float* grad_vertices,
     const float* grad_signed_distances, const float* grad_spherical_harmonics,
-    int64_t V, float* grad_grid_vertices, float* grad_grid_signed_distances,
-    float* grad_grid_spherical_harmonics, mt_stream_t stream);
+    int64_t V, int32_t* corner_inverse, float* grad_grid_vertices,
+    float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
+    mt_stream_t stream);
 
 /* triangle_extraction/count_triangle_faces.slang:15-50.
  * face_counts: S*Nv+1 int32 (3 x triangles; last entry 0);
@@ -240,7 +245,8 @@ MT_API int mt_evaluate_spherical_harmonics(const float* vertices, int64_t V,
                                            float* out_colors, mt_stream_t stream);
 
 /* evaluate_spherical_harmonics.slang:230-270 (backward to the SH only).
- * Accumulates (+=) into grad_spherical_harmonics [C,V,3]. */
+ * Writes (=) every entry of grad_spherical_harmonics [C,V,3]; rows beyond
+ * (sh_degree+1)^2 are zero. */
 MT_API int mt_evaluate_spherical_harmonics_backward(
     const float* vertices, int64_t V, int32_t C, int32_t sh_degree,
     const float* camera_positions, int32_t B, const float* out_colors,

@@ -44,11 +44,11 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_count_triangle_vertices": (I32, [P, P, I64, P, I32, P, P]),
     "mt_create_triangle_vertices": (
         I32,
-        [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P],
+        [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P, P],
     ),
     "mt_create_triangle_vertices_backward": (
         I32,
-        [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P],
+        [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P, P],
     ),
     "mt_count_triangle_faces": (I32, [P, P, I64, P, I64, P, I32, P, P, P]),
     "mt_create_triangle_faces": (
@@ -114,6 +114,9 @@ def library_path() -> str:
 KERNELS_PER_CALL = {
     "mt_sort_pairs_i64_i32": 11,  # histogram, plan, 8 digit passes, copy
     "mt_create_voxels": 1,
+    "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows
+    "mt_create_triangle_vertices_backward": 2,  # corner inverse, gather
+    "mt_intersect_and_composite_forward": 2,  # warp masks, composite
 }
 
 

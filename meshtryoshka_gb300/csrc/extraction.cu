@@ -327,18 +327,24 @@ __device__ __forceinline__ float lerp_ref(float a, float b, float t) {
 }
 
 // ---------------------------------------------------------------------------
-// create_triangle_vertices.slang:145-199 (forward)
+// create_triangle_vertices.slang:145-199 (forward), in two passes.
+//
+// Pass 1, one thread per entry g: positions, signed distance and type of
+// every vertex on g's crossing edges, plus the vertex's source record
+// (origin corner, axis corner, t) in vertex order.
+// Pass 2, one thread per (coefficient row k, vertex): the SH row k of the
+// vertex from its two corners. Consecutive threads write consecutive
+// vertices of one row, so the [C, V, 3] output is written coalesced.
 // ---------------------------------------------------------------------------
 __global__ void create_vertices_kernel(const float* __restrict__ gv, const float* __restrict__ gsdf,
-                                       const float* __restrict__ gsh, int C, const int32_t* __restrict__ lower,
-                                       int64_t G, const float* __restrict__ level_sets, int S,
+                                       const int32_t* __restrict__ lower, int64_t G,
+                                       const float* __restrict__ level_sets, int S,
                                        const int32_t* __restrict__ voff, int64_t V, float* __restrict__ out_v,
-                                       float* __restrict__ out_sdf, float* __restrict__ out_sh,
-                                       uint8_t* __restrict__ out_type) {
+                                       float* __restrict__ out_sdf, uint8_t* __restrict__ out_type,
+                                       int32_t* __restrict__ sources) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
     const Corners4 c = load_corners(gsdf, lower, G, g);
     const int32_t i0 = __ldg(lower + g);
-    // Which axes cross at least one level set: only those corners' data is read.
     uint32_t any = 0;
     for (int s = 0; s < S; ++s) any |= crossing_mask(c, __ldg(level_sets + s));
     if (any == 0) continue;
@@ -362,113 +368,185 @@ __global__ void create_vertices_kernel(const float* __restrict__ gv, const float
         out_v[3 * vi + 2] = lerp_ref(v0z, v1z, t);
         out_sdf[vi] = lerp_ref(c.d0, d1, t);
         out_type[vi] = (uint8_t)a;
-        for (int k = 0; k < C; ++k) {
-          const float* p0 = gsh + ((int64_t)k * G + i0) * 3;
-          const float* p1 = gsh + ((int64_t)k * G + i1) * 3;
-          float* q = out_sh + ((int64_t)k * V + vi) * 3;
-#pragma unroll
-          for (int ch = 0; ch < 3; ++ch) {
-            const float s0 = __ldg(p0 + ch), s1 = __ldg(p1 + ch);
-            q[ch] = lerp_ref(s0, s1, t);
-          }
-        }
+        sources[vi] = i0;
+        sources[V + vi] = i1;
+        sources[2 * V + vi] = __float_as_int(t);
       }
     }
   }
 }
 
+__global__ void interpolate_vertex_sh_kernel(const float* __restrict__ gsh, int C, int64_t G,
+                                             const int32_t* __restrict__ sources, int64_t V,
+                                             float* __restrict__ out_sh) {
+  const int64_t total = (int64_t)C * V;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = o / V, vi = o - k * V;
+    const int32_t i0 = __ldg(sources + vi), i1 = __ldg(sources + V + vi);
+    const float t = __int_as_float(__ldg(sources + 2 * V + vi));
+    const float* p0 = gsh + (k * G + i0) * 3;
+    const float* p1 = gsh + (k * G + i1) * 3;
+    float* q = out_sh + o * 3;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) q[ch] = lerp_ref(__ldg(p0 + ch), __ldg(p1 + ch), t);
+  }
+}
+
 // ---------------------------------------------------------------------------
-// create_triangle_vertices.slang:201-291 (backward). The detached weight t
-// routes d(vertex) to the origin with (1 - t) and to the axis corner with t.
-// Per entry, the origin's gradient is summed over shells/axes in registers
-// and written with one atomic per scalar; axis corners get one atomic per
-// scalar per crossing axis. Entries and axes without any crossing contribute
-// exact zeros and are skipped.
+// create_triangle_vertices.slang:201-291 (backward) as a gather. The detached
+// weight t routes d(vertex) to the origin corner with (1 - t) and to the axis
+// corner with t. Grid vertex x receives from the vertices of the one entry
+// whose origin it is and from the vertices on axis a of the (at most three)
+// entries whose axis-a corner it is; `inverse` [4, G] lists those entries.
+// One thread per grid vertex writes all of x's gradients (zeros included),
+// so no atomics and no zero-filled outputs are needed.
+//
+// Crossings are packed 3 bits per shell into 64-bit masks, shells taken in
+// chunks of 21; the first chunk writes, later chunks add.
 // ---------------------------------------------------------------------------
+__global__ void invert_corners_kernel(const int32_t* __restrict__ lower, int64_t G, int32_t* __restrict__ inverse) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G; e += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int32_t x = __ldg(lower + r * G + e);
+      if (x >= 0 && x < G) inverse[r * G + x] = (int32_t)e;
+    }
+  }
+}
+
+constexpr int kShellsPerChunk = 21;
+
+__device__ __forceinline__ uint64_t crossing_bits(const Corners4& c, const float* __restrict__ level_sets, int s0,
+                                                  int s1) {
+  uint64_t bits = 0;
+  for (int s = s0; s < s1; ++s) bits |= (uint64_t)crossing_mask(c, __ldg(level_sets + s)) << (3 * (s - s0));
+  return bits;
+}
+
+// One contribution list of grid vertex x for the shells of one chunk: the
+// vertex index and weight of every triangle vertex that x feeds.
+struct GatherChunk {
+  uint64_t own;       // crossings of x's own entry (3 bits per shell)
+  uint64_t nb[3];     // crossings of the entry whose axis-a corner x is
+  int64_t e, h[3];    // those entries (-1 = none)
+  float d0, d1[3];    // own entry: origin and axis-corner signed distances
+  float nd0[3], nd1[3];  // entry h[a]: origin and axis-a corner signed distances
+};
+
+__device__ __forceinline__ int64_t vertex_of(const int32_t* __restrict__ voff, int64_t G, int64_t entry, int s,
+                                             uint64_t bits, int s0, int a) {
+  const uint32_t m = (uint32_t)(bits >> (3 * (s - s0))) & 7u;
+  return (int64_t)__ldg(voff + (int64_t)s * G + entry) + __popc(m & ((1u << a) - 1u));
+}
+
+// Calls f(vertex, weight) for each of x's contributions in this shell chunk:
+// weight (1 - t) for the vertices of x's own entry, t for the axis-a vertices
+// of the entries whose axis-a corner x is.
+template <typename F>
+__device__ __forceinline__ void for_each_contribution(const GatherChunk& q, const float* __restrict__ level_sets,
+                                                      int s0, const int32_t* __restrict__ voff, int64_t G, F&& f) {
+  uint64_t bits = q.own;
+  while (bits) {
+    const int j = __ffsll((long long)bits) - 1;
+    bits &= bits - 1;
+    const int sl = j / 3, a = j - 3 * sl, s = s0 + sl;
+    const float t = mc_weight(q.d0, q.d1[a], __ldg(level_sets + s));
+    f(vertex_of(voff, G, q.e, s, q.own, s0, a), t, true);
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    uint64_t nbits = q.nb[a] & (0x1249249249249249ull << a);  // axis-a bits only
+    while (nbits) {
+      const int j = __ffsll((long long)nbits) - 1;
+      nbits &= nbits - 1;
+      const int s = s0 + j / 3;
+      const float t = mc_weight(q.nd0[a], q.nd1[a], __ldg(level_sets + s));
+      f(vertex_of(voff, G, q.h[a], s, q.nb[a], s0, a), t, false);
+    }
+  }
+}
+
+// (1 - t) g, written g - t g as the reference's adjoint forms it, or t g.
+__device__ __forceinline__ float weighted(float g, float t, bool origin) { return origin ? g - t * g : t * g; }
+
+constexpr int kRowsPerPass = 16;  // SH coefficient rows accumulated in registers at once
+
 __global__ void create_vertices_backward_kernel(const float* __restrict__ gsdf, int C,
                                                 const int32_t* __restrict__ lower, int64_t G,
                                                 const float* __restrict__ level_sets, int S,
                                                 const int32_t* __restrict__ voff,
+                                                const int32_t* __restrict__ inverse,
                                                 const float* __restrict__ dv, const float* __restrict__ dsdf,
                                                 const float* __restrict__ dsh, int64_t V, float* __restrict__ gdv,
                                                 float* __restrict__ gdsdf, float* __restrict__ gdsh) {
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < G; g += (int64_t)gridDim.x * blockDim.x) {
-    const Corners4 c = load_corners(gsdf, lower, G, g);
-    const int32_t i0 = __ldg(lower + g);
-    uint32_t any = 0;
-    for (int s = 0; s < S; ++s) any |= crossing_mask(c, __ldg(level_sets + s));
-    if (any == 0) continue;
-
-    // Scalar (sdf) and position gradients first.
-    float o_d = 0.f, o_vx = 0.f, o_vy = 0.f, o_vz = 0.f;
-    for (int a = 0; a < 3; ++a) {
-      if (!((any >> a) & 1u)) continue;
-      const int32_t i1 = c.idx[a];
-      float a_d = 0.f, a_vx = 0.f, a_vy = 0.f, a_vz = 0.f;
-      const uint32_t below_a = (1u << a) - 1u;
-      for (int s = 0; s < S; ++s) {
-        const float iso = __ldg(level_sets + s);
-        const uint32_t m = crossing_mask(c, iso);
-        if (!((m >> a) & 1u)) continue;
-        const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
-        const float t = mc_weight(c.d0, c.d[a], iso);
-        const float gd = dsdf ? __ldg(dsdf + vi) : 0.f;
-        o_d += gd - t * gd;
-        a_d += t * gd;
-        if (dv) {
-          const float gx = __ldg(dv + 3 * vi), gy = __ldg(dv + 3 * vi + 1), gz = __ldg(dv + 3 * vi + 2);
-          o_vx += gx - t * gx;
-          o_vy += gy - t * gy;
-          o_vz += gz - t * gz;
-          a_vx += t * gx;
-          a_vy += t * gy;
-          a_vz += t * gz;
-        }
-      }
-      atomicAdd(gdsdf + i1, a_d);
-      if (dv) {
-        atomicAdd(gdv + 3 * (int64_t)i1, a_vx);
-        atomicAdd(gdv + 3 * (int64_t)i1 + 1, a_vy);
-        atomicAdd(gdv + 3 * (int64_t)i1 + 2, a_vz);
-      }
-    }
-    atomicAdd(gdsdf + i0, o_d);
-    if (dv) {
-      atomicAdd(gdv + 3 * (int64_t)i0, o_vx);
-      atomicAdd(gdv + 3 * (int64_t)i0 + 1, o_vy);
-      atomicAdd(gdv + 3 * (int64_t)i0 + 2, o_vz);
-    }
-
-    // Spherical harmonics, one coefficient row at a time.
-    if (dsh == nullptr) continue;
-    for (int k = 0; k < C; ++k) {
-      float o[3] = {0.f, 0.f, 0.f};
-      for (int a = 0; a < 3; ++a) {
-        if (!((any >> a) & 1u)) continue;
-        const int32_t i1 = c.idx[a];
-        float acc[3] = {0.f, 0.f, 0.f};
-        const uint32_t below_a = (1u << a) - 1u;
-        for (int s = 0; s < S; ++s) {
-          const float iso = __ldg(level_sets + s);
-          const uint32_t m = crossing_mask(c, iso);
-          if (!((m >> a) & 1u)) continue;
-          const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
-          const float t = mc_weight(c.d0, c.d[a], iso);
-          const float* q = dsh + ((int64_t)k * V + vi) * 3;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < G; x += (int64_t)gridDim.x * blockDim.x) {
+    GatherChunk q;
+    q.e = __ldg(inverse + x);
+    Corners4 own{};
+    if (q.e >= 0) own = load_corners(gsdf, lower, G, q.e);
+    q.d0 = own.d0;
 #pragma unroll
-          for (int ch = 0; ch < 3; ++ch) {
-            const float gq = __ldg(q + ch);
-            o[ch] += gq - t * gq;
-            acc[ch] += t * gq;
+    for (int a = 0; a < 3; ++a) {
+      q.d1[a] = own.d[a];
+      q.h[a] = __ldg(inverse + (int64_t)(a + 1) * G + x);
+    }
+    Corners4 nb[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (q.h[a] >= 0) {
+        nb[a] = load_corners(gsdf, lower, G, q.h[a]);
+        q.nd0[a] = nb[a].d0;
+        q.nd1[a] = nb[a].d[a];
+      }
+    }
+    const int chunks = S > 0 ? (S + kShellsPerChunk - 1) / kShellsPerChunk : 1;
+    for (int chunk = 0; chunk < chunks; ++chunk) {
+      const int s0 = chunk * kShellsPerChunk, s1 = min(S, s0 + kShellsPerChunk);
+      q.own = q.e >= 0 ? crossing_bits(own, level_sets, s0, s1) : 0ull;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) q.nb[a] = q.h[a] >= 0 ? crossing_bits(nb[a], level_sets, s0, s1) : 0ull;
+      const bool first = chunk == 0;
+      auto put = [&](float* dst, float value) { *dst = first ? value : *dst + value; };
+
+      float d = 0.f, p[3] = {0.f, 0.f, 0.f};
+      for_each_contribution(q, level_sets, s0, voff, G, [&](int64_t vi, float t, bool origin) {
+        if (dsdf) d += weighted(__ldg(dsdf + vi), t, origin);
+        if (dv) {
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) p[ch] += weighted(__ldg(dv + 3 * vi + ch), t, origin);
+        }
+      });
+      put(gdsdf + x, d);
+      if (gdv) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) put(gdv + 3 * x + ch, p[ch]);
+      }
+      // SH rows in passes of 16: every contribution's 48 loads are independent.
+      for (int k0 = 0; k0 < C; k0 += kRowsPerPass) {
+        float r[kRowsPerPass][3];
+#pragma unroll
+        for (int kk = 0; kk < kRowsPerPass; ++kk) r[kk][0] = r[kk][1] = r[kk][2] = 0.f;
+        if (dsh) {
+          for_each_contribution(q, level_sets, s0, voff, G, [&](int64_t vi, float t, bool origin) {
+#pragma unroll
+            for (int kk = 0; kk < kRowsPerPass; ++kk) {
+              if (k0 + kk < C) {
+                const float* src = dsh + ((int64_t)(k0 + kk) * V + vi) * 3;
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) r[kk][ch] += weighted(__ldg(src + ch), t, origin);
+              }
+            }
+          });
+        }
+#pragma unroll
+        for (int kk = 0; kk < kRowsPerPass; ++kk) {
+          if (k0 + kk < C) {
+            float* dst = gdsh + ((int64_t)(k0 + kk) * G + x) * 3;
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) put(dst + ch, r[kk][ch]);
           }
         }
-        float* dst = gdsh + ((int64_t)k * G + i1) * 3;
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) atomicAdd(dst + ch, acc[ch]);
       }
-      float* dst = gdsh + ((int64_t)k * G + i0) * 3;
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) atomicAdd(dst + ch, o[ch]);
     }
   }
 }
@@ -630,14 +708,18 @@ int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_si
                                 const float* grid_spherical_harmonics, int32_t C, const int32_t* lower_corners,
                                 int64_t G, const float* level_sets, int32_t S, const int32_t* vertex_offsets,
                                 int64_t V, float* vertices, float* signed_distances, float* spherical_harmonics,
-                                uint8_t* vertex_types, mt_stream_t stream) {
+                                uint8_t* vertex_types, int32_t* vertex_sources, mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
   if (G == 0 || S == 0 || V == 0) return MT_OK;
   MT_REQUIRE(grid_vertices && grid_signed_distances && grid_spherical_harmonics && lower_corners && level_sets &&
-             vertex_offsets && vertices && signed_distances && spherical_harmonics && vertex_types);
+             vertex_offsets && vertices && signed_distances && spherical_harmonics && vertex_types &&
+             vertex_sources);
   create_vertices_kernel<<<grid_stride_blocks(G, 128), 128, 0, as_stream(stream)>>>(
-      grid_vertices, grid_signed_distances, grid_spherical_harmonics, C, lower_corners, G, level_sets, S,
-      vertex_offsets, V, vertices, signed_distances, spherical_harmonics, vertex_types);
+      grid_vertices, grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, V, vertices,
+      signed_distances, vertex_types, vertex_sources);
+  MT_CHECK_LAUNCH();
+  interpolate_vertex_sh_kernel<<<grid_stride_blocks((int64_t)C * V, 256), 256, 0, as_stream(stream)>>>(
+      grid_spherical_harmonics, C, G, vertex_sources, V, spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -646,17 +728,26 @@ int mt_create_triangle_vertices_backward(const float* grid_signed_distances, int
                                          int64_t G, const float* level_sets, int32_t S,
                                          const int32_t* vertex_offsets, const float* grad_vertices,
                                          const float* grad_signed_distances, const float* grad_spherical_harmonics,
-                                         int64_t V, float* grad_grid_vertices, float* grad_grid_signed_distances,
-                                         float* grad_grid_spherical_harmonics, mt_stream_t stream) {
+                                         int64_t V, int32_t* corner_inverse, float* grad_grid_vertices,
+                                         float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
+                                         mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
-  if (G == 0 || S == 0 || V == 0) return MT_OK;
-  MT_REQUIRE(grid_signed_distances && lower_corners && level_sets && vertex_offsets);
+  if (G == 0) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && lower_corners && corner_inverse);
   MT_REQUIRE(grad_grid_signed_distances && grad_grid_spherical_harmonics);
+  MT_REQUIRE(S == 0 || (level_sets && vertex_offsets));
   MT_REQUIRE(grad_vertices == nullptr || grad_grid_vertices != nullptr);
-  create_vertices_backward_kernel<<<grid_stride_blocks(G, 128), 128, 0, as_stream(stream)>>>(
-      grid_signed_distances, C, lower_corners, G, level_sets, S, vertex_offsets, grad_vertices,
-      grad_signed_distances, grad_spherical_harmonics, V, grad_grid_vertices, grad_grid_signed_distances,
-      grad_grid_spherical_harmonics);
+  cudaStream_t st = as_stream(stream);
+  if (cudaMemsetAsync(corner_inverse, 0xff, (size_t)G * 4 * sizeof(int32_t), st) != cudaSuccess) return MT_ERR_CUDA;
+  invert_corners_kernel<<<grid_stride_blocks(G, 256), 256, 0, st>>>(lower_corners, G, corner_inverse);
+  MT_CHECK_LAUNCH();
+  // With no level sets or no vertices, the gather writes zeros everywhere.
+  const float* gv = V > 0 ? grad_vertices : nullptr;
+  const float* gd = V > 0 ? grad_signed_distances : nullptr;
+  const float* gs = V > 0 ? grad_spherical_harmonics : nullptr;
+  create_vertices_backward_kernel<<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+      grid_signed_distances, C, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, gv, gd, gs, V,
+      grad_grid_vertices, grad_grid_signed_distances, grad_grid_spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

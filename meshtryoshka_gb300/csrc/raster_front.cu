@@ -145,9 +145,10 @@ __global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, co
   }
 }
 
-// d sh_k += sum_b basis_k(dir_b) * d rgb_b * [rgb_b + 0.5 > 0]; the mask is
+// d sh_k = sum_b basis_k(dir_b) * d rgb_b * [rgb_b + 0.5 > 0]; the mask is
 // read from the forward output (out > 0 exactly when the pre-clamp value is).
-__global__ void sh_backward_kernel(const float* __restrict__ verts, int64_t V, int n_coeff,
+// Every row of the output is written (rows k >= n_coeff get zeros).
+__global__ void sh_backward_kernel(const float* __restrict__ verts, int64_t V, int n_coeff, int C,
                                    const float* __restrict__ campos, int B, const float* __restrict__ colors,
                                    const float* __restrict__ dcolors, float* __restrict__ dsh) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
@@ -177,11 +178,15 @@ __global__ void sh_backward_kernel(const float* __restrict__ verts, int64_t V, i
     }
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      if (k < n_coeff) {
+      if (k < C) {
         float* d = dsh + ((int64_t)k * V + v) * 3;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) d[c] += acc[k][c];
+        for (int c = 0; c < 3; ++c) d[c] = acc[k][c];
       }
+    }
+    for (int k = 16; k < C; ++k) {
+      float* d = dsh + ((int64_t)k * V + v) * 3;
+      d[0] = d[1] = d[2] = 0.f;
     }
   }
 }
@@ -360,10 +365,15 @@ int mt_evaluate_spherical_harmonics_backward(const float* vertices, int64_t V, i
   MT_REQUIRE(V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
   const int n = (sh_degree + 1) * (sh_degree + 1);
   MT_REQUIRE(C >= n);
-  if (V == 0 || B == 0) return MT_OK;
-  MT_REQUIRE(vertices && camera_positions && out_colors && grad_colors && grad_spherical_harmonics);
+  if (V == 0) return MT_OK;
+  MT_REQUIRE(grad_spherical_harmonics);
+  if (B == 0) {
+    const size_t bytes = (size_t)C * (size_t)V * 3 * sizeof(float);
+    return cudaMemsetAsync(grad_spherical_harmonics, 0, bytes, as_stream(stream)) == cudaSuccess ? MT_OK : MT_ERR_CUDA;
+  }
+  MT_REQUIRE(vertices && camera_positions && out_colors && grad_colors);
   sh_backward_kernel<<<grid_stride_blocks(V, 128), 128, 0, as_stream(stream)>>>(
-      vertices, V, n, camera_positions, B, out_colors, grad_colors, grad_spherical_harmonics);
+      vertices, V, n, C, camera_positions, B, out_colors, grad_colors, grad_spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

@@ -277,11 +277,12 @@ class CreateTriangleVertices(torch.autograd.Function):
             sdf = torch.empty((v,), **kw)
             sh = torch.empty((c, v, 3), **kw)
             types = torch.empty((v,), dtype=torch.uint8, device=device)
+            sources = torch.empty((3, v), dtype=torch.int32, device=device)
             nt.call(
                 "mt_create_triangle_vertices",
                 nt.ptr(grid_vertices), nt.ptr(grid_signed_distances), nt.ptr(grid_spherical_harmonics), c,
                 nt.ptr(voxel_lower_corners), g, nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v,
-                nt.ptr(vertices), nt.ptr(sdf), nt.ptr(sh), nt.ptr(types), nt.stream(device),
+                nt.ptr(vertices), nt.ptr(sdf), nt.ptr(sh), nt.ptr(types), nt.ptr(sources), nt.stream(device),
             )
             ctx.save_for_backward(grid_signed_distances, voxel_lower_corners, level_sets, vertex_offsets)
             ctx.shapes = (grid_vertices.shape, grid_spherical_harmonics.shape, v)
@@ -298,16 +299,21 @@ class CreateTriangleVertices(torch.autograd.Function):
             g = lower_corners.shape[1]
             (s,) = level_sets.shape
             c = gsh_shape[0]
-            grad_grid_vertices = torch.zeros(gv_shape, dtype=torch.float32, device=device)
-            grad_grid_sdf = torch.zeros_like(grid_signed_distances)
-            grad_grid_sh = torch.zeros(gsh_shape, dtype=torch.float32, device=device)
+            # The kernel writes every entry of the grid gradients: one per grid
+            # vertex, and every grid vertex is the origin of exactly one entry.
+            if grid_signed_distances.shape[0] != g:
+                raise ValueError("grid_signed_distances must have one value per voxel-lower-corner entry")
+            grad_grid_vertices = torch.empty(gv_shape, dtype=torch.float32, device=device)
+            grad_grid_sdf = torch.empty_like(grid_signed_distances)
+            grad_grid_sh = torch.empty(gsh_shape, dtype=torch.float32, device=device)
+            inverse = torch.empty((4, g), dtype=torch.int32, device=device)
             gv = grad_vertices.contiguous() if grad_vertices is not None else None
             gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
             gs = grad_spherical_harmonics.contiguous() if grad_spherical_harmonics is not None else None
             nt.call(
                 "mt_create_triangle_vertices_backward",
                 nt.ptr(grid_signed_distances), c, nt.ptr(lower_corners), g, nt.ptr(level_sets), s,
-                nt.ptr(vertex_offsets), nt.ptr(gv), nt.ptr(gd), nt.ptr(gs), v,
+                nt.ptr(vertex_offsets), nt.ptr(gv), nt.ptr(gd), nt.ptr(gs), v, nt.ptr(inverse),
                 nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), nt.stream(device),
             )
             return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None

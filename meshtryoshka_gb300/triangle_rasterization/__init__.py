@@ -317,7 +317,7 @@ class EvaluateSphericalHarmonics(torch.autograd.Function):
             vertices, campos, colors = ctx.saved_tensors
             grad_colors = grad_colors.contiguous()
             device = vertices.device
-            grad_sh = torch.zeros(ctx.sh_shape, dtype=torch.float32, device=device)
+            grad_sh = torch.empty(ctx.sh_shape, dtype=torch.float32, device=device)  # fully written
             nt.call("mt_evaluate_spherical_harmonics_backward", nt.ptr(vertices), vertices.shape[0],
                     ctx.sh_shape[0], ctx.sh_degree, nt.ptr(campos), campos.shape[0], nt.ptr(colors),
                     nt.ptr(grad_colors), nt.ptr(grad_sh), nt.stream(device))
