@@ -232,7 +232,7 @@ def run_reference(args, rank, world):
 def run_ours(args, rank, world, local):
     import torch
 
-    from meshtryoshka_gb300 import _native, pipeline
+    from meshtryoshka_gb300 import _native, graph, pipeline
 
     device = torch.device("cuda", local)
     torch.manual_seed(0)
@@ -240,7 +240,7 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.current_stream(device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)  # > L2 (129 MB)
 
-    def step():
+    def eager_step():
         w.grid_sdf.grad = None
         w.grid_sh.grad = None
         loss, stats = pipeline.forward(w)
@@ -248,53 +248,75 @@ def run_ours(args, rank, world, local):
         return loss, stats
 
     for _ in range(max(args.warmup, 3)):
-        step()
+        eager_step()
     torch.cuda.synchronize(device)
 
-    # Timed device region: per-step events, L2 flushed between steps (outside
-    # the step's events), library launches counted and timed per entry point.
+    # Eager steps with every library entry point timed by CUDA events on the
+    # launching stream: the per-kernel breakdown and the roofline's launch time.
+    eager_steps = min(args.steps, 50)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(eager_steps)]
+    with _native.record_launches(timed=True) as rec:
+        for i in range(eager_steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            loss, stats = eager_step()
+            ev[i][1].record(stream)
+    torch.cuda.synchronize(device)
+    eager_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    per_call = rec.times_ms()
+
+    # The training step as one CUDA graph (capacity-sized buffers, no host
+    # reads); the timed region. L2 flushed between steps, outside the events.
+    step = graph.CapturedTrainingStep(w)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(device)
+    if not step.check():
+        for _ in range(max(args.warmup, 3)):
+            step()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier(world)
     torch.cuda.synchronize(device)
     clocks = ClockSampler(local) if rank == 0 else None
     wall0 = time.perf_counter()
-    with _native.record_launches(timed=True) as rec:
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            torch.cuda.nvtx.range_push("step")
-            ev[i][0].record(stream)
-            loss, stats = step()
-            ev[i][1].record(stream)
-            torch.cuda.nvtx.range_pop()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        torch.cuda.nvtx.range_push("step")
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+        torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize(device)
     wall = time.perf_counter() - wall0
     barrier(world)
     clock_info = clocks.stop() if clocks else None
+    fits = step.check()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = max_over_ranks(statistics.mean(step_ms), world)
-    per_call = rec.times_ms()
-    launches_per_step = rec.launches / args.steps
+    launches_per_step = step.launches_per_replay
 
-    # End to end through the public API: inputs from pinned host memory,
-    # loss read back, every step.
+    # End to end through the public API: every step copies the parameters,
+    # target and cameras from pinned host memory into the step's inputs,
+    # replays the step and reads the loss back.
     host = {k: v.detach().cpu().pin_memory() for k, v in
             (("sdf", w.grid_sdf), ("sh", w.grid_sh), ("target", w.target), ("ext", w.extrinsics),
              ("intr", w.intrinsics))}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
+    loss_host = torch.empty((), dtype=torch.float32).pin_memory()
 
     def e2e_step():
-        sdf = host["sdf"].to(device, non_blocking=True).requires_grad_(True)
-        sh = host["sh"].to(device, non_blocking=True).requires_grad_(True)
-        target = host["target"].to(device, non_blocking=True)
-        w.extrinsics.copy_(host["ext"], non_blocking=True)
-        w.intrinsics.copy_(host["intr"], non_blocking=True)
-        loss, _ = pipeline.forward(w, grid_sdf=sdf, grid_sh=sh, target=target)
-        loss.backward()
-        return float(loss.detach().cpu())
+        with torch.no_grad():
+            w.grid_sdf.copy_(host["sdf"], non_blocking=True)
+            w.grid_sh.copy_(host["sh"], non_blocking=True)
+            w.target.copy_(host["target"], non_blocking=True)
+            w.extrinsics.copy_(host["ext"], non_blocking=True)
+            w.intrinsics.copy_(host["intr"], non_blocking=True)
+        loss_host.copy_(step(), non_blocking=True)
+        torch.cuda.synchronize(device)
+        return float(loss_host)
 
     for _ in range(2):
         e2e_step()
-    torch.cuda.synchronize(device)
     barrier(world)
     e_ms = []
     for i in range(args.steps):
@@ -302,7 +324,6 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize(device)
         t0 = time.perf_counter()
         e2e_step()
-        torch.cuda.synchronize(device)
         e_ms.append(1000.0 * (time.perf_counter() - t0))
     e2e_value = max_over_ranks(statistics.mean(e_ms), world)
 
@@ -358,6 +379,9 @@ def run_ours(args, rank, world, local):
         "step_ms_median": statistics.median(step_ms),
         "step_ms_p90": sorted(step_ms)[int(0.9 * (len(step_ms) - 1))],
         "wall_s_timed_region": wall,
+        "step_form": "CUDA graph replay of the whole fused forward+backward (capacity-sized buffers)",
+        "capacities_fit": fits,
+        "eager_ms_per_step": eager_ms,
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "gpu_launches_per_step": launches_per_step,
         "kernel_ms": {k: statistics.mean(v) for k, v in sorted(per_call.items(), key=lambda kv: -sum(kv[1]))},

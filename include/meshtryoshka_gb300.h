@@ -152,13 +152,16 @@ MT_API int mt_count_triangle_vertices(const float* signed_distances,
  * grid_sh [C,G,3]; outputs vertices [V,3], signed_distances [V],
  * spherical_harmonics [C,V,3], vertex_types [V] (uint8 axis 0/1/2), and
  * vertex_sources [3,V] int32: origin corner, axis corner and the float bits
- * of the (detached) weight t of every vertex. */
+ * of the (detached) weight t of every vertex. num_vertices: NULL, or a
+ * device int32 (the last vertex offset); V is then the buffers' capacity
+ * (the row stride of spherical_harmonics) and vertices past it are dropped. */
 MT_API int mt_create_triangle_vertices(const float* grid_vertices,
                                 const float* grid_signed_distances,
                                 const float* grid_spherical_harmonics,
                                 int32_t C, const int32_t* lower_corners,
                                 int64_t G, const float* level_sets, int32_t S,
                                 const int32_t* vertex_offsets, int64_t V,
+                                const int32_t* num_vertices,
                                 float* vertices, float* signed_distances,
                                 float* spherical_harmonics,
                                 uint8_t* vertex_types, int32_t* vertex_sources,
@@ -191,9 +194,11 @@ MT_API int mt_count_triangle_faces(const float* signed_distances,
 
 /* triangle_extraction/create_triangle_faces.slang:5-78. face_offsets is the
  * exclusive scan of face_counts. Outputs faces [F,3] int32 (reversed slot
- * order as in the reference) and voxel_indices [F]. */
+ * order as in the reference) and voxel_indices [F]. V is the length of
+ * vertex_types. F and V may be capacities: faces past F are not written and
+ * no vertex past V is looked up. */
 MT_API int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices,
-                             int64_t Nv, int64_t G,
+                             int64_t Nv, int64_t G, int64_t V,
                              const int32_t* vertex_offsets,
                              const uint8_t* vertex_types,
                              const uint8_t* cell_codes, int32_t S,
@@ -211,9 +216,14 @@ MT_API int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* ind
 
 MT_API size_t mt_sort_pairs_workspace_bytes(int64_t n);
 
+/* n is the capacity of the buffers (and sizes the workspace). count: NULL,
+ * or a device int64 holding how many leading pairs to sort (clamped to n);
+ * with a device count the sort makes no host synchronisation and can be
+ * captured in a CUDA graph. Outputs past the count are left unchanged. */
 MT_API int mt_sort_pairs_i64_i32(const int64_t* keys_in, const int32_t* values_in,
                                  int64_t* keys_out, int32_t* values_out, int64_t n,
-                                 int32_t begin_bit, int32_t end_bit, void* workspace,
+                                 const int64_t* count, int32_t begin_bit,
+                                 int32_t end_bit, void* workspace,
                                  size_t workspace_bytes, mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
@@ -254,9 +264,12 @@ MT_API int mt_evaluate_spherical_harmonics_backward(
 
 /* triangle_rasterization/bound_triangles.slang:144-192.
  * out_min / out_max [B,F,2] (row, col) tile bounds [min, max); out_count
- * [B,F] = tiles touched (0 for back-facing or near-plane-culled faces). */
+ * [B,F] = tiles touched (0 for back-facing or near-plane-culled faces).
+ * num_faces: NULL, or a device int32; rows at or past it touch no tile (F is
+ * then the capacity). A face naming a vertex outside [0, V) touches no tile. */
 MT_API int mt_bound_triangles(const float* xy, const float* depth, int64_t V,
-                              const int32_t* faces, int64_t F, int32_t B,
+                              const int32_t* faces, int64_t F,
+                              const int32_t* num_faces, int32_t B,
                               int32_t tile_h, int32_t tile_w, int32_t rows,
                               int32_t cols, float near_plane, int32_t* out_min,
                               int32_t* out_max, int32_t* out_count,
@@ -275,8 +288,10 @@ MT_API int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces,
 
 /* triangle_rasterization/delineate_tiles.slang:14-58 (+ the zero fill of
  * delineate_tiles.py:40, done here). out_boundaries [B, shell_dim,
- * num_tiles, 2] int64; shell_dim = S when separate_shells, else 1. */
+ * num_tiles, 2] int64; shell_dim = S when separate_shells, else 1.
+ * num_keys: NULL (all K keys), or a device int64 count of live keys. */
 MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
+                              const int64_t* num_keys,
                               const int32_t* layout, int32_t separate_shells,
                               int32_t B, int32_t shell_dim, int64_t num_tiles,
                               int64_t* out_boundaries, mt_stream_t stream);
@@ -291,14 +306,16 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
  * threads per (camera, tile); its warps work independently.
  * warp_masks [K] uint32 is scratch written by the forward (per key, the warps
  * of its tile the triangle can cover) and read by the backward.
+ * num_keys: NULL (all K keys live), or a device int64 count of live keys
+ * (K is then the capacity of the key buffers).
  * ---------------------------------------------------------------------- */
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
     const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
-    const int32_t* sorted_triangles, int64_t K, const int64_t* tile_boundaries,
-    int32_t B, int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
-    int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
-    uint32_t* warp_masks, float* out, mt_stream_t stream);
+    const int32_t* sorted_triangles, int64_t K, const int64_t* num_keys,
+    const int64_t* tile_boundaries, int32_t B, int32_t num_shells, int32_t rows,
+    int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H, int32_t W,
+    const int32_t* layout, uint32_t* warp_masks, float* out, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the

@@ -44,7 +44,7 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_count_triangle_vertices": (I32, [P, P, I64, P, I32, P, P]),
     "mt_create_triangle_vertices": (
         I32,
-        [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P, P],
+        [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P, P, P],
     ),
     "mt_create_triangle_vertices_backward": (
         I32,
@@ -53,20 +53,20 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_count_triangle_faces": (I32, [P, P, I64, P, I64, P, I32, P, P, P]),
     "mt_create_triangle_faces": (
         I32,
-        [P, P, I64, I64, P, P, P, I32, P, I64, P, P, P],
+        [P, P, I64, I64, I64, P, P, P, I32, P, I64, P, P, P],
     ),
     "mt_sort_pairs_workspace_bytes": (c_size_t, [I64]),
-    "mt_sort_pairs_i64_i32": (I32, [P, P, P, P, I64, I32, I32, P, c_size_t, P]),
+    "mt_sort_pairs_i64_i32": (I32, [P, P, P, P, I64, P, I32, I32, P, c_size_t, P]),
     "mt_camera_positions": (I32, [P, I32, P, P]),
     "mt_project_vertices": (I32, [P, I64, P, P, I32, P, P, P]),
     "mt_evaluate_spherical_harmonics": (I32, [P, I64, P, I32, I32, P, I32, P, P]),
     "mt_evaluate_spherical_harmonics_backward": (I32, [P, I64, I32, I32, P, I32, P, P, P, P]),
-    "mt_bound_triangles": (I32, [P, P, I64, P, I64, I32, I32, I32, I32, I32, c_float, P, P, P, P]),
+    "mt_bound_triangles": (I32, [P, P, I64, P, I64, P, I32, I32, I32, I32, I32, c_float, P, P, P, P]),
     "mt_generate_keys": (I32, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, I64, P, P, P]),
-    "mt_delineate_tiles": (I32, [P, I64, P, I32, I32, I32, I64, P, P]),
+    "mt_delineate_tiles": (I32, [P, I64, P, P, I32, I32, I32, I64, P, P]),
     "mt_intersect_and_composite_forward": (
         I32,
-        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P],
+        [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P],
     ),
     "mt_intersect_and_composite_backward": (
         I32,

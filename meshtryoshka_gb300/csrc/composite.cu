@@ -122,8 +122,12 @@ __device__ __forceinline__ void warp_block_rect(int w, int tile_w, int tile_h, i
 }
 
 // One mask per sorted key: bit w = warp w of the key's tile may be covered.
-__global__ void warp_mask_kernel(CompositeArgs a, int64_t K, uint32_t* __restrict__ masks) {
+// Keys past num_keys (a device value; all K when NULL) get no mask: no tile
+// range reaches them.
+__global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int64_t* __restrict__ num_keys,
+                                 uint32_t* __restrict__ masks) {
   const int warps = (a.tile_h * a.tile_w + 31) / 32;
+  const int64_t K = num_keys ? min(max(*num_keys, (int64_t)0), K_capacity) : K_capacity;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K; k += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
     const int cam = (int)field(key, a.cam_off, a.cam_len);
@@ -501,14 +505,6 @@ int check_args(const CompositeArgs& a) {
 
 inline int block_threads(const CompositeArgs& a) { return (a.tile_h * a.tile_w + 31) / 32 * 32; }
 
-template <typename K>
-int set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) {
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
-      return MT_ERR_CUDA;
-  }
-  return MT_OK;
-}
 
 CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, int64_t V, const int32_t* faces,
                         const float* sharpness, const int64_t* keys, const int32_t* tri, const int64_t* bounds,
@@ -552,10 +548,10 @@ extern "C" {
 int mt_intersect_and_composite_forward(const float* xy, const float* colors, const float* signed_distances,
                                        int64_t V, const int32_t* faces, const float* sharpness,
                                        const int64_t* sorted_keys, const int32_t* sorted_triangles, int64_t K,
-                                       const int64_t* tile_boundaries, int32_t B, int32_t num_shells,
-                                       int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
-                                       int32_t W, const int32_t* layout, uint32_t* warp_masks, float* out,
-                                       mt_stream_t stream) {
+                                       const int64_t* num_keys, const int64_t* tile_boundaries, int32_t B,
+                                       int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
+                                       int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
+                                       uint32_t* warp_masks, float* out, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr);
@@ -568,17 +564,17 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   MT_REQUIRE(blocks < ((int64_t)1 << 31));
   cudaStream_t s = as_stream(stream);
   if (K > 0) {
-    warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, warp_masks);
+    warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
     MT_CHECK_LAUNCH();
   }
   const int bs = block_threads(a);
   const size_t smem = sizeof(WarpForward) * (bs / 32);
   if (bs <= 256) {
-    rc = set_smem(composite_forward_kernel<256>, smem);
+    rc = set_smem<composite_forward_kernel<256>>(smem);
     if (rc != MT_OK) return rc;
     composite_forward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
   } else {
-    rc = set_smem(composite_forward_kernel<1024>, smem);
+    rc = set_smem<composite_forward_kernel<1024>>(smem);
     if (rc != MT_OK) return rc;
     composite_forward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
   }
@@ -611,11 +607,11 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   const size_t smem = sizeof(WarpBackward) * (bs / 32);
   cudaStream_t s = as_stream(stream);
   if (bs <= 256) {
-    rc = set_smem(composite_backward_kernel<256>, smem);
+    rc = set_smem<composite_backward_kernel<256>>(smem);
     if (rc != MT_OK) return rc;
     composite_backward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
   } else {
-    rc = set_smem(composite_backward_kernel<1024>, smem);
+    rc = set_smem<composite_backward_kernel<1024>>(smem);
     if (rc != MT_OK) return rc;
     composite_backward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
   }

@@ -267,9 +267,7 @@ int mt_intersect(const float* xy, int64_t V, const int32_t* faces, const int32_t
   MT_REQUIRE(blocks < ((int64_t)1 << 31));
   const int bs = tile_h * tile_w;
   const size_t smem = (size_t)bs * sizeof(ExplicitFace);
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(intersect_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return MT_ERR_CUDA;
+  if (set_smem<intersect_kernel>(smem) != MT_OK) return MT_ERR_CUDA;
   intersect_kernel<<<(unsigned)blocks, bs, smem, as_stream(stream)>>>(xy, V, faces, sorted_triangles,
                                                                       tile_boundaries, B, S, rows, cols, tile_h,
                                                                       tile_w, H, W, out_uv, out_index);

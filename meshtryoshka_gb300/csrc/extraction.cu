@@ -362,6 +362,7 @@ __global__ void create_vertices_kernel(const float* __restrict__ gv, const float
         const uint32_t m = crossing_mask(c, iso);
         if (!((m >> a) & 1u)) continue;
         const int64_t vi = (int64_t)__ldg(voff + (int64_t)s * G + g) + __popc(m & below_a);
+        if (vi >= V) continue;  // beyond the caller's capacity (reported by the caller's count check)
         const float t = mc_weight(c.d0, d1, iso);
         out_v[3 * vi + 0] = lerp_ref(v0x, v1x, t);
         out_v[3 * vi + 1] = lerp_ref(v0y, v1y, t);
@@ -376,17 +377,20 @@ __global__ void create_vertices_kernel(const float* __restrict__ gv, const float
   }
 }
 
+// Rows have stride V (the buffer's capacity); only the first `count`
+// vertices (device value, clamped to V; all V when count is NULL) are real.
 __global__ void interpolate_vertex_sh_kernel(const float* __restrict__ gsh, int C, int64_t G,
                                              const int32_t* __restrict__ sources, int64_t V,
-                                             float* __restrict__ out_sh) {
-  const int64_t total = (int64_t)C * V;
+                                             const int32_t* __restrict__ count, float* __restrict__ out_sh) {
+  const int64_t n = count ? min((int64_t)max(*count, 0), V) : V;
+  const int64_t total = (int64_t)C * n;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = o / V, vi = o - k * V;
+    const int64_t k = o / n, vi = o - k * n;
     const int32_t i0 = __ldg(sources + vi), i1 = __ldg(sources + V + vi);
     const float t = __int_as_float(__ldg(sources + 2 * V + vi));
     const float* p0 = gsh + (k * G + i0) * 3;
     const float* p1 = gsh + (k * G + i1) * 3;
-    float* q = out_sh + o * 3;
+    float* q = out_sh + (k * V + vi) * 3;
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) q[ch] = lerp_ref(__ldg(p0 + ch), __ldg(p1 + ch), t);
   }
@@ -442,16 +446,20 @@ __device__ __forceinline__ int64_t vertex_of(const int32_t* __restrict__ voff, i
 // Calls f(vertex, weight) for each of x's contributions in this shell chunk:
 // weight (1 - t) for the vertices of x's own entry, t for the axis-a vertices
 // of the entries whose axis-a corner x is.
+// Vertices at or past V (the buffers' capacity; only reached when the live
+// count overflowed it) were never written and are skipped.
 template <typename F>
 __device__ __forceinline__ void for_each_contribution(const GatherChunk& q, const float* __restrict__ level_sets,
-                                                      int s0, const int32_t* __restrict__ voff, int64_t G, F&& f) {
+                                                      int s0, const int32_t* __restrict__ voff, int64_t G,
+                                                      int64_t V, F&& f) {
   uint64_t bits = q.own;
   while (bits) {
     const int j = __ffsll((long long)bits) - 1;
     bits &= bits - 1;
     const int sl = j / 3, a = j - 3 * sl, s = s0 + sl;
-    const float t = mc_weight(q.d0, q.d1[a], __ldg(level_sets + s));
-    f(vertex_of(voff, G, q.e, s, q.own, s0, a), t, true);
+    const int64_t vi = vertex_of(voff, G, q.e, s, q.own, s0, a);
+    if (vi >= V) continue;
+    f(vi, mc_weight(q.d0, q.d1[a], __ldg(level_sets + s)), true);
   }
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -460,8 +468,9 @@ __device__ __forceinline__ void for_each_contribution(const GatherChunk& q, cons
       const int j = __ffsll((long long)nbits) - 1;
       nbits &= nbits - 1;
       const int s = s0 + j / 3;
-      const float t = mc_weight(q.nd0[a], q.nd1[a], __ldg(level_sets + s));
-      f(vertex_of(voff, G, q.h[a], s, q.nb[a], s0, a), t, false);
+      const int64_t vi = vertex_of(voff, G, q.h[a], s, q.nb[a], s0, a);
+      if (vi >= V) continue;
+      f(vi, mc_weight(q.nd0[a], q.nd1[a], __ldg(level_sets + s)), false);
     }
   }
 }
@@ -509,7 +518,7 @@ __global__ void create_vertices_backward_kernel(const float* __restrict__ gsdf, 
       auto put = [&](float* dst, float value) { *dst = first ? value : *dst + value; };
 
       float d = 0.f, p[3] = {0.f, 0.f, 0.f};
-      for_each_contribution(q, level_sets, s0, voff, G, [&](int64_t vi, float t, bool origin) {
+      for_each_contribution(q, level_sets, s0, voff, G, V, [&](int64_t vi, float t, bool origin) {
         if (dsdf) d += weighted(__ldg(dsdf + vi), t, origin);
         if (dv) {
 #pragma unroll
@@ -527,7 +536,7 @@ __global__ void create_vertices_backward_kernel(const float* __restrict__ gsdf, 
 #pragma unroll
         for (int kk = 0; kk < kRowsPerPass; ++kk) r[kk][0] = r[kk][1] = r[kk][2] = 0.f;
         if (dsh) {
-          for_each_contribution(q, level_sets, s0, voff, G, [&](int64_t vi, float t, bool origin) {
+          for_each_contribution(q, level_sets, s0, voff, G, V, [&](int64_t vi, float t, bool origin) {
 #pragma unroll
             for (int kk = 0; kk < kRowsPerPass; ++kk) {
               if (k0 + kk < C) {
@@ -591,10 +600,12 @@ __global__ void count_faces_kernel(const float* __restrict__ sdf, const int32_t*
 // neighbour) -> that entry's vertices at this level set -> the one whose
 // type is the edge's axis. Triangles are written in reversed slot order.
 // ---------------------------------------------------------------------------
+// Writes only faces below F and searches only vertices below V (the
+// buffers' capacities); with consistent offsets neither bound is reached.
 __global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const int32_t* __restrict__ indices,
-                                    int64_t Nv, int64_t G, const int32_t* __restrict__ voff,
+                                    int64_t Nv, int64_t G, int64_t V, const int32_t* __restrict__ voff,
                                     const uint8_t* __restrict__ types, const uint8_t* __restrict__ codes, int S,
-                                    const int32_t* __restrict__ foff, int32_t* __restrict__ faces,
+                                    const int32_t* __restrict__ foff, int64_t F, int32_t* __restrict__ faces,
                                     int32_t* __restrict__ voxel_indices) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
     const int32_t linear = __ldg(indices + v);
@@ -614,6 +625,7 @@ __global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const
         const int32_t count = __ldg(voff + vo + 1) - start;
         int32_t target = -1;
         for (int q = 0; q < count; ++q) {
+          if ((int64_t)start + q >= V) break;
           if (types[start + q] == axis) {
             target = start + q;
             break;
@@ -621,6 +633,7 @@ __global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const
         }
         const int64_t slot = ctr + e;
         const int64_t tri = slot / 3;
+        if (tri >= F) break;
         const int corner = 2 - (int)(slot % 3);
         faces[tri * 3 + corner] = target;
         if (corner == 0) voxel_indices[tri] = linear;
@@ -707,8 +720,9 @@ int mt_count_triangle_vertices(const float* signed_distances, const int32_t* low
 int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_signed_distances,
                                 const float* grid_spherical_harmonics, int32_t C, const int32_t* lower_corners,
                                 int64_t G, const float* level_sets, int32_t S, const int32_t* vertex_offsets,
-                                int64_t V, float* vertices, float* signed_distances, float* spherical_harmonics,
-                                uint8_t* vertex_types, int32_t* vertex_sources, mt_stream_t stream) {
+                                int64_t V, const int32_t* num_vertices, float* vertices, float* signed_distances,
+                                float* spherical_harmonics, uint8_t* vertex_types, int32_t* vertex_sources,
+                                mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
   if (G == 0 || S == 0 || V == 0) return MT_OK;
   MT_REQUIRE(grid_vertices && grid_signed_distances && grid_spherical_harmonics && lower_corners && level_sets &&
@@ -719,7 +733,7 @@ int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_si
       signed_distances, vertex_types, vertex_sources);
   MT_CHECK_LAUNCH();
   interpolate_vertex_sh_kernel<<<grid_stride_blocks((int64_t)C * V, 256), 256, 0, as_stream(stream)>>>(
-      grid_spherical_harmonics, C, G, vertex_sources, V, spherical_harmonics);
+      grid_spherical_harmonics, C, G, vertex_sources, V, num_vertices, spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -764,16 +778,17 @@ int mt_count_triangle_faces(const float* signed_distances, const int32_t* lower_
   return MT_OK;
 }
 
-int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, int64_t Nv, int64_t G,
+int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, int64_t Nv, int64_t G, int64_t V,
                              const int32_t* vertex_offsets, const uint8_t* vertex_types, const uint8_t* cell_codes,
                              int32_t S, const int32_t* face_offsets, int64_t F, int32_t* faces,
                              int32_t* voxel_indices, mt_stream_t stream) {
-  MT_REQUIRE(Nv >= 0 && G >= 0 && S >= 0 && F >= 0);
+  MT_REQUIRE(Nv >= 0 && G >= 0 && V >= 0 && S >= 0 && F >= 0);
   if (Nv == 0 || S == 0 || F == 0) return MT_OK;
   MT_REQUIRE(neighbors && indices && vertex_offsets && vertex_types && cell_codes && face_offsets && faces &&
              voxel_indices);
   create_faces_kernel<<<grid_stride_blocks(Nv, 128), 128, 0, as_stream(stream)>>>(
-      neighbors, indices, Nv, G, vertex_offsets, vertex_types, cell_codes, S, face_offsets, faces, voxel_indices);
+      neighbors, indices, Nv, G, V, vertex_offsets, vertex_types, cell_codes, S, face_offsets, F, faces,
+      voxel_indices);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

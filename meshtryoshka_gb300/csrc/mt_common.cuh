@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/meshtryoshka_gb300.h"
 
 #define MT_CHECK_LAUNCH()                                   \
@@ -51,6 +53,25 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // Record the first device-side error code in a status word (0 = ok).
 __device__ __forceinline__ void set_device_error(int* status, int code) {
   if (status != nullptr) atomicCAS(status, 0, code);
+}
+
+// Raises a kernel's dynamic shared-memory limit once per device and size, so
+// repeated launches (and launches under stream capture) make no attribute
+// calls. The template argument is the kernel itself, so each kernel keeps its
+// own record of the largest size set per device.
+template <auto Kernel>
+inline int set_smem(size_t bytes) {
+  if (bytes <= 48 * 1024) return MT_OK;
+  static std::atomic<size_t> granted[64];
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return MT_ERR_CUDA;
+  if (granted[device].load(std::memory_order_acquire) >= bytes) return MT_OK;
+  if (cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return MT_ERR_CUDA;
+  size_t prev = granted[device].load(std::memory_order_relaxed);
+  while (prev < bytes && !granted[device].compare_exchange_weak(prev, bytes)) {
+  }
+  return MT_OK;
 }
 
 }  // namespace mt

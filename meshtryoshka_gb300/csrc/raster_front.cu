@@ -205,10 +205,13 @@ __device__ __forceinline__ TileBounds triangle_tile_bounds(const float* __restri
                                                            int tile_h, int tile_w, int rows, int cols, float near) {
   const int64_t base = (int64_t)b * V;
   const int32_t ia = faces[3 * f], ib = faces[3 * f + 1], ic = faces[3 * f + 2];
+  TileBounds t{0, 0, 0, 0};
+  // A face that names a vertex outside [0, V) (only possible when an upstream
+  // capacity overflowed) covers no tile.
+  if ((uint64_t)ia >= (uint64_t)V || (uint64_t)ib >= (uint64_t)V || (uint64_t)ic >= (uint64_t)V) return t;
   const float ax = xy[2 * (base + ia)], ay = xy[2 * (base + ia) + 1], ad = depth[base + ia];
   const float bx = xy[2 * (base + ib)], by = xy[2 * (base + ib) + 1], bd = depth[base + ib];
   const float cx = xy[2 * (base + ic)], cy = xy[2 * (base + ic) + 1], cd = depth[base + ic];
-  TileBounds t{0, 0, 0, 0};
   const float check = __fsub_rn(__fmul_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay)),
                                 __fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
   if (check < 0.0f) return t;
@@ -222,15 +225,19 @@ __device__ __forceinline__ TileBounds triangle_tile_bounds(const float* __restri
   return t;
 }
 
+// Rows f >= num_faces (a device value; all F when NULL) cover no tile.
 __global__ void bound_kernel(const float* __restrict__ xy, const float* __restrict__ depth, int64_t V,
-                             const int32_t* __restrict__ faces, int64_t F, int B, int tile_h, int tile_w, int rows,
-                             int cols, float near, int32_t* __restrict__ out_min, int32_t* __restrict__ out_max,
+                             const int32_t* __restrict__ faces, int64_t F, const int32_t* __restrict__ num_faces,
+                             int B, int tile_h, int tile_w, int rows, int cols, float near,
+                             int32_t* __restrict__ out_min, int32_t* __restrict__ out_max,
                              int32_t* __restrict__ out_count) {
   const int64_t total = (int64_t)B * F;
+  const int64_t live = num_faces ? min((int64_t)max(*num_faces, 0), F) : F;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(i / F);
     const int64_t f = i - (int64_t)b * F;
-    const TileBounds t = triangle_tile_bounds(xy, depth, V, faces, f, b, tile_h, tile_w, rows, cols, near);
+    const TileBounds t = f < live ? triangle_tile_bounds(xy, depth, V, faces, f, b, tile_h, tile_w, rows, cols, near)
+                                  : TileBounds{0, 0, 0, 0};
     out_min[2 * i] = t.r0;
     out_min[2 * i + 1] = t.c0;
     out_max[2 * i] = t.r1;
@@ -289,8 +296,10 @@ __global__ void keys_kernel(const float* __restrict__ depth, int64_t V, const in
 // delineate_tiles.slang:14-58: [start, end) per (camera, shell|0, tile) where
 // the (camera, shell|0, tile) index changes between consecutive sorted keys.
 // ---------------------------------------------------------------------------
-__global__ void delineate_kernel(const uint64_t* __restrict__ keys, int64_t K, KeyLayout L, int separate_shells,
-                                 int B, int Sd, int64_t T, int64_t* __restrict__ out) {
+__global__ void delineate_kernel(const uint64_t* __restrict__ keys, int64_t K_capacity,
+                                 const int64_t* __restrict__ num_keys, KeyLayout L, int separate_shells, int B,
+                                 int Sd, int64_t T, int64_t* __restrict__ out) {
+  const int64_t K = num_keys ? min(max(*num_keys, (int64_t)0), K_capacity) : K_capacity;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < K; i += (int64_t)gridDim.x * blockDim.x) {
     auto index_of = [&](uint64_t key) -> int64_t {
       const int64_t cam = (int64_t)((key >> L.cam_off) & field_mask(L.cam_len));
@@ -378,14 +387,15 @@ int mt_evaluate_spherical_harmonics_backward(const float* vertices, int64_t V, i
   return MT_OK;
 }
 
-int mt_bound_triangles(const float* xy, const float* depth, int64_t V, const int32_t* faces, int64_t F, int32_t B,
-                       int32_t tile_h, int32_t tile_w, int32_t rows, int32_t cols, float near_plane,
-                       int32_t* out_min, int32_t* out_max, int32_t* out_count, mt_stream_t stream) {
+int mt_bound_triangles(const float* xy, const float* depth, int64_t V, const int32_t* faces, int64_t F,
+                       const int32_t* num_faces, int32_t B, int32_t tile_h, int32_t tile_w, int32_t rows,
+                       int32_t cols, float near_plane, int32_t* out_min, int32_t* out_max, int32_t* out_count,
+                       mt_stream_t stream) {
   MT_REQUIRE(V >= 0 && F >= 0 && B >= 0 && tile_h > 0 && tile_w > 0 && rows >= 0 && cols >= 0);
   if (F == 0 || B == 0) return MT_OK;
   MT_REQUIRE(xy && depth && faces && out_min && out_max && out_count);
   bound_kernel<<<grid_stride_blocks((int64_t)B * F, 256), 256, 0, as_stream(stream)>>>(
-      xy, depth, V, faces, F, B, tile_h, tile_w, rows, cols, near_plane, out_min, out_max, out_count);
+      xy, depth, V, faces, F, num_faces, B, tile_h, tile_w, rows, cols, near_plane, out_min, out_max, out_count);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -408,9 +418,9 @@ int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces, int64_
   return MT_OK;
 }
 
-int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K, const int32_t* layout, int32_t separate_shells,
-                       int32_t B, int32_t shell_dim, int64_t num_tiles, int64_t* out_boundaries,
-                       mt_stream_t stream) {
+int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K, const int64_t* num_keys, const int32_t* layout,
+                       int32_t separate_shells, int32_t B, int32_t shell_dim, int64_t num_tiles,
+                       int64_t* out_boundaries, mt_stream_t stream) {
   MT_REQUIRE(K >= 0 && B >= 0 && shell_dim >= 1 && num_tiles >= 0 && layout);
   KeyLayout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
   MT_REQUIRE(layout_ok(L));
@@ -421,7 +431,7 @@ int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K, const int32_t* lay
   if (K == 0) return MT_OK;
   MT_REQUIRE(sorted_keys);
   delineate_kernel<<<grid_stride_blocks(K, 256), 256, 0, as_stream(stream)>>>(
-      reinterpret_cast<const uint64_t*>(sorted_keys), K, L, separate_shells, B, shell_dim, num_tiles,
+      reinterpret_cast<const uint64_t*>(sorted_keys), K, num_keys, L, separate_shells, B, shell_dim, num_tiles,
       out_boundaries);
   MT_CHECK_LAUNCH();
   return MT_OK;

@@ -17,6 +17,12 @@
 //      per-digit counts, looks back over predecessor tiles (bounded spin),
 //      and scatters through shared memory so global writes are digit runs;
 //   4. copy: in->out when every pass was skipped.
+//
+// The pair count may live on the device (the output of a preceding scan):
+// every kernel then reads it and sorts min(count, capacity) pairs, so the
+// sort needs no host synchronisation and can be captured in a graph. Tiles
+// past the count return right after claiming their index; no live tile ever
+// looks back at them.
 
 #include "mt_common.cuh"
 
@@ -65,6 +71,10 @@ inline size_t lookback_bytes(int64_t n) {
 
 inline size_t alt_offset(int64_t n) { return (kOffLookback + lookback_bytes(n) + 255) / 256 * 256; }
 
+__device__ __forceinline__ int64_t live_count(int64_t capacity, const int64_t* count) {
+  return count ? min(max(*count, (int64_t)0), capacity) : capacity;
+}
+
 __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
   uint64_t v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -80,9 +90,11 @@ __device__ __forceinline__ uint64_t lb_pack(int pass, uint64_t flag, uint64_t va
   return ((uint64_t)(pass + 1) << 60) | (flag << 58) | (value & ((1ull << 58) - 1));
 }
 
-__global__ void __launch_bounds__(256) sort_histogram_kernel(const uint64_t* __restrict__ keys, int64_t n,
-                                                             int num_passes, int begin_bit, int end_bit,
+__global__ void __launch_bounds__(256) sort_histogram_kernel(const uint64_t* __restrict__ keys, int64_t capacity,
+                                                             const int64_t* __restrict__ count, int num_passes,
+                                                             int begin_bit, int end_bit,
                                                              uint32_t* __restrict__ hist) {
+  const int64_t n = live_count(capacity, count);
   __shared__ uint32_t s_hist[kMaxPasses][kRadix];
   for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
   __syncthreads();
@@ -104,9 +116,10 @@ __global__ void __launch_bounds__(256) sort_histogram_kernel(const uint64_t* __r
 
 __global__ void __launch_bounds__(kRadix) sort_plan_kernel(const uint64_t* keys_in, const int32_t* vals_in,
                                                            uint64_t* keys_out, int32_t* vals_out, uint64_t* keys_alt,
-                                                           int32_t* vals_alt, int64_t n, int num_passes,
-                                                           int begin_bit, int end_bit, uint32_t* hist,
-                                                           SortPlan* plan) {
+                                                           int32_t* vals_alt, int64_t capacity,
+                                                           const int64_t* count, int num_passes, int begin_bit,
+                                                           int end_bit, uint32_t* hist, SortPlan* plan) {
+  const int64_t n = live_count(capacity, count);
   __shared__ int s_active[kMaxPasses];
   __shared__ uint32_t s_warp[kRadix / 32];
   const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
@@ -159,10 +172,12 @@ __global__ void __launch_bounds__(kRadix) sort_plan_kernel(const uint64_t* keys_
 __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const SortPlan* __restrict__ plan, int p,
                                                                  const uint32_t* __restrict__ hist,
                                                                  uint32_t* __restrict__ counter,
-                                                                 uint64_t* __restrict__ lookback, int64_t n,
+                                                                 uint64_t* __restrict__ lookback,
+                                                                 int64_t capacity, const int64_t* __restrict__ live,
                                                                  int* __restrict__ status) {
   const SortPass ps = plan->pass[p];
   if (!ps.active) return;
+  const int64_t n = live_count(capacity, live);
 
   __shared__ uint32_t s_warp_hist[kSortWarps][kRadix];
   __shared__ uint32_t s_digit_start[kRadix];
@@ -178,6 +193,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const SortPlan*
   __syncthreads();
   const int64_t tile = s_tile;
   const int64_t tile_base = tile * kSortTile;
+  if (tile_base >= n) return;  // past the live pairs: nothing to publish
 
   // Warp-striped load: warp w owns [w * 32 * items, (w + 1) * 32 * items) of
   // the tile; item i of lane l sits at i * 32 + l, so (item, lane) order is
@@ -290,8 +306,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(const SortPlan*
 
 __global__ void sort_copy_kernel(const SortPlan* __restrict__ plan, const uint64_t* __restrict__ kin,
                                  const int32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-                                 int32_t* __restrict__ vout, int64_t n) {
+                                 int32_t* __restrict__ vout, int64_t capacity, const int64_t* __restrict__ count) {
   if (!plan->copy_needed) return;
+  const int64_t n = live_count(capacity, count);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     kout[i] = kin[i];
     vout[i] = vin[i];
@@ -311,8 +328,8 @@ size_t mt_sort_pairs_workspace_bytes(int64_t n) {
 }
 
 int mt_sort_pairs_i64_i32(const int64_t* keys_in, const int32_t* values_in, int64_t* keys_out, int32_t* values_out,
-                          int64_t n, int32_t begin_bit, int32_t end_bit, void* workspace, size_t workspace_bytes,
-                          mt_stream_t stream) {
+                          int64_t n, const int64_t* count, int32_t begin_bit, int32_t end_bit, void* workspace,
+                          size_t workspace_bytes, mt_stream_t stream) {
   MT_REQUIRE(n >= 0);
   MT_REQUIRE(begin_bit >= 0 && end_bit <= 64 && begin_bit < end_bit);
   if (n == 0) return MT_OK;
@@ -337,16 +354,17 @@ int mt_sort_pairs_i64_i32(const int64_t* keys_in, const int32_t* values_in, int6
   const uint64_t* kin = reinterpret_cast<const uint64_t*>(keys_in);
   uint64_t* kout = reinterpret_cast<uint64_t*>(keys_out);
 
-  sort_histogram_kernel<<<grid_stride_blocks(n, 256, 4), 256, 0, s>>>(kin, n, num_passes, begin_bit, end_bit, hist);
+  sort_histogram_kernel<<<grid_stride_blocks(n, 256, 4), 256, 0, s>>>(kin, n, count, num_passes, begin_bit, end_bit,
+                                                                      hist);
   MT_CHECK_LAUNCH();
-  sort_plan_kernel<<<1, kRadix, 0, s>>>(kin, values_in, kout, values_out, kalt, valt, n, num_passes, begin_bit,
-                                        end_bit, hist, plan);
+  sort_plan_kernel<<<1, kRadix, 0, s>>>(kin, values_in, kout, values_out, kalt, valt, n, count, num_passes,
+                                        begin_bit, end_bit, hist, plan);
   MT_CHECK_LAUNCH();
   for (int p = 0; p < num_passes; ++p) {
-    sort_pass_kernel<<<(unsigned)tiles, kSortThreads, 0, s>>>(plan, p, hist, counters, lookback, n, status);
+    sort_pass_kernel<<<(unsigned)tiles, kSortThreads, 0, s>>>(plan, p, hist, counters, lookback, n, count, status);
     MT_CHECK_LAUNCH();
   }
-  sort_copy_kernel<<<grid_stride_blocks(n, 256, 2), 256, 0, s>>>(plan, kin, values_in, kout, values_out, n);
+  sort_copy_kernel<<<grid_stride_blocks(n, 256, 2), 256, 0, s>>>(plan, kin, values_in, kout, values_out, n, count);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

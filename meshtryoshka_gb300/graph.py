@@ -1,0 +1,107 @@
+"""The fused training step captured as one CUDA graph.
+
+The eager step reads sizes back to the host twice (the vertex / face totals
+after the marching-cubes counts and the key total after the tile counts),
+and each of its ~30 library kernels and ~40 tensor ops is launched from
+Python. The captured step instead allocates its vertex, face and key buffers
+once, at capacities (the sizes of a first eager step times a margin), keeps
+the live sizes on the device, and replays tessellation, render, loss and the
+whole backward as a single graph: no host synchronisation and no per-launch
+host cost.
+
+A live size above its capacity drops the excess (every kernel stays inside
+its buffers: writers are capacity-guarded and faces naming a dropped vertex
+cover no tile) and sets an overflow flag on the device. ``check()`` reads the
+flag; on overflow it re-captures with larger capacities and the step has to
+be run again.
+
+The graph reads the workload's parameters (``grid_sdf``, ``grid_sh``) and
+target in place; after each replay ``grid_sdf.grad`` / ``grid_sh.grad`` are
+the step's gradients (tensors owned by the graph, overwritten by every
+replay, never accumulated), so a trainer updates the parameters in place
+between replays.
+"""
+
+from __future__ import annotations
+
+import torch
+from torch import Tensor
+
+from . import _native as nt
+from . import pipeline
+
+
+class CapturedTrainingStep:
+    """Fused forward + backward of ``pipeline.Workload`` as one CUDA graph."""
+
+    def __init__(self, workload: pipeline.Workload, gradient_mode: str | None = None, margin: float = 1.25,
+                 capacities: pipeline.Capacities | None = None, warmup: int = 2):
+        self.w = workload
+        self.gradient_mode = gradient_mode
+        self.margin = margin
+        self.warmup = warmup
+        if capacities is None:
+            capacities = pipeline.Capacities.around(self._measure(), margin)
+        self.capacities = capacities
+        self.recaptures = 0
+        self._capture()
+
+    def _measure(self) -> dict:
+        """Live sizes of one eager forward (no autograd graph is kept)."""
+        with torch.no_grad():
+            _, stats = pipeline.forward(self.w, "fused", self.gradient_mode)
+        return stats
+
+    def _step(self) -> tuple[Tensor, Tensor, Tensor, Tensor]:
+        # The graph differentiates with respect to aliases of the parameters
+        # (same storage, fresh autograd leaves made on the capture stream) and
+        # returns the gradients instead of accumulating them: autograd state
+        # left on the parameters by eager steps on another stream would
+        # otherwise make the capture wait on that stream.
+        loss, overflow = pipeline.forward_counted(self.w, self.capacities, self.gradient_mode,
+                                                  self._sdf, self._sh)
+        grad_sdf, grad_sh = torch.autograd.grad(loss, (self._sdf, self._sh))
+        return loss.detach(), overflow, grad_sdf, grad_sh
+
+    def _capture(self) -> None:
+        w = self.w
+        device = w.grid_sdf.device
+        self.stream = torch.cuda.Stream(device)
+        self.stream.wait_stream(torch.cuda.current_stream(device))
+        with torch.cuda.stream(self.stream):
+            self._sdf = w.grid_sdf.detach().requires_grad_(True)
+            self._sh = w.grid_sh.detach().requires_grad_(True)
+            # Warm-up on the capture stream: allocates this stream's library
+            # workspace and raises kernel shared-memory limits outside capture.
+            for _ in range(self.warmup):
+                self._step()
+            self._workspace = nt.workspace(device).buffer  # kept alive for the graph
+        torch.cuda.current_stream(device).wait_stream(self.stream)
+        self.graph = torch.cuda.CUDAGraph()
+        with nt.record_launches() as rec:
+            with torch.cuda.graph(self.graph, stream=self.stream):
+                # Gradient tensors written by every replay (graph-owned memory).
+                self.loss, self.overflow, self.grad_sdf, self.grad_sh = self._step()
+        self.launches_per_replay = rec.launches
+
+    def __call__(self) -> Tensor:
+        """Replay one step on the current stream; returns the (device) loss.
+        The parameters' ``.grad`` point at the graph's gradient tensors."""
+        self.graph.replay()
+        self.w.grid_sdf.grad = self.grad_sdf
+        self.w.grid_sh.grad = self.grad_sh
+        return self.loss
+
+    def check(self) -> bool:
+        """True when the last replay fit its capacities. Otherwise re-captures
+        with capacities grown to the measured sizes (times the margin) and
+        returns False: the step must be replayed again. Synchronizes."""
+        if not bool(self.overflow.item()):
+            return True
+        grown = pipeline.Capacities.around(self._measure(), self.margin)
+        c = self.capacities
+        self.capacities = pipeline.Capacities(max(c.vertices, grown.vertices), max(c.faces, grown.faces),
+                                              max(c.keys, grown.keys))
+        self.recaptures += 1
+        self._capture()
+        return False

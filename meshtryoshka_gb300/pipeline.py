@@ -65,6 +65,44 @@ def build_workload(name: str, device: torch.device) -> Workload:
     )
 
 
+@dataclass(frozen=True)
+class Capacities:
+    """Row capacities of the per-step vertex, face and key buffers."""
+
+    vertices: int
+    faces: int
+    keys: int
+
+    @staticmethod
+    def around(stats: dict, margin: float = 1.25, minimum: int = 4096) -> "Capacities":
+        grow = lambda n: max(int(n * margin) + minimum, minimum)  # noqa: E731
+        return Capacities(grow(stats["V"]), grow(stats["F"]), grow(stats["K"]))
+
+
+def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = None,
+                    grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None) -> tuple[Tensor, Tensor]:
+    """The fused step's forward with capacity-sized buffers and no
+    device->host reads (capturable in a CUDA graph). Returns the loss and a
+    device flag that is true when a live vertex, face or key count exceeded
+    its capacity (the step's result is then incomplete)."""
+    grid_sdf = w.grid_sdf if grid_sdf is None else grid_sdf
+    grid_sh = w.grid_sh if grid_sh is None else grid_sh
+    tri, counts = te.tessellate_voxels_counted(
+        grid_sdf, w.voxels.vertices, grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
+        w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces)
+    with torch.no_grad():
+        vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
+    image = tr.render_fused(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
+                            tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
+                            gradient_mode=gradient_mode, num_faces=counts.num_faces, key_capacity=caps.keys)
+    key_count = tr.LAST_RENDER_STATS["key_count"]
+    loss = ((image - w.target) ** 2).mean()
+    with torch.no_grad():
+        overflow = ((counts.num_vertices > caps.vertices) | (counts.num_faces > caps.faces)
+                    | (key_count > caps.keys))
+    return loss, overflow
+
+
 def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
             grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None,
             target: Tensor | None = None) -> tuple[Tensor, dict]:

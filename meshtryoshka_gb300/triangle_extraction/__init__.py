@@ -258,7 +258,7 @@ class CreateTriangleVertices(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners,
-                level_sets, vertex_offsets, num_vertices=None):
+                level_sets, vertex_offsets, num_vertices=None, capacity=None):
         with record_function("create_triangle_vertices_forward"):
             grid_vertices = _f32(grid_vertices, "grid_vertices")
             grid_signed_distances = _f32(grid_signed_distances, "grid_signed_distances")
@@ -271,7 +271,14 @@ class CreateTriangleVertices(torch.autograd.Function):
             (s,) = level_sets.shape
             _, g = voxel_lower_corners.shape
             c = grid_spherical_harmonics.shape[0]
-            v = int(vertex_offsets[-1].item()) if num_vertices is None else int(num_vertices)
+            if capacity is not None:
+                # Buffers of `capacity` rows; the live count stays on the device
+                # (the last vertex offset), so nothing is read back.
+                v = int(capacity)
+                count_ptr = vertex_offsets.data_ptr() + 4 * (vertex_offsets.numel() - 1)
+            else:
+                v = int(vertex_offsets[-1].item()) if num_vertices is None else int(num_vertices)
+                count_ptr = None
             kw = dict(dtype=torch.float32, device=device)
             vertices = torch.empty((v, 3), **kw)
             sdf = torch.empty((v,), **kw)
@@ -281,7 +288,7 @@ class CreateTriangleVertices(torch.autograd.Function):
             nt.call(
                 "mt_create_triangle_vertices",
                 nt.ptr(grid_vertices), nt.ptr(grid_signed_distances), nt.ptr(grid_spherical_harmonics), c,
-                nt.ptr(voxel_lower_corners), g, nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v,
+                nt.ptr(voxel_lower_corners), g, nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v, count_ptr,
                 nt.ptr(vertices), nt.ptr(sdf), nt.ptr(sh), nt.ptr(types), nt.ptr(sources), nt.stream(device),
             )
             ctx.save_for_backward(grid_signed_distances, voxel_lower_corners, level_sets, vertex_offsets)
@@ -316,7 +323,7 @@ class CreateTriangleVertices(torch.autograd.Function):
                 nt.ptr(vertex_offsets), nt.ptr(gv), nt.ptr(gd), nt.ptr(gs), v, nt.ptr(inverse),
                 nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), nt.stream(device),
             )
-            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None
+            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None
 
 
 def create_triangle_vertices(
@@ -327,12 +334,15 @@ def create_triangle_vertices(
     level_sets: Tensor,
     vertex_offsets: Tensor,
     num_vertices: int | None = None,
+    capacity: int | None = None,
 ) -> CreateTriangleVerticesResult:
     """``num_vertices`` (optional, not in the reference signature) skips the
-    device->host read of ``vertex_offsets[-1]`` when the caller knows it."""
+    device->host read of ``vertex_offsets[-1]`` when the caller knows it.
+    ``capacity`` (optional) sizes the outputs to a fixed row count instead and
+    keeps the live count on the device; rows past it are unused."""
     result = CreateTriangleVertices.apply(
         grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners, level_sets,
-        vertex_offsets, num_vertices,
+        vertex_offsets, num_vertices, capacity,
     )
     return CreateTriangleVerticesResult(*result)
 
@@ -383,12 +393,18 @@ def create_triangle_faces(
     level_sets: Tensor,
     face_offsets: Tensor,
     num_faces: int | None = None,
+    capacity: int | None = None,
 ) -> CreateTriangleFacesResult:
+    """``capacity`` (optional) sizes the outputs to a fixed row count; faces
+    past it are not written and nothing is read back."""
     device = nt.require_cuda(signed_distances, neighbors, indices, vertex_offsets, face_offsets)
     _, nv = neighbors.shape
     (s,) = level_sets.shape
     g = (vertex_offsets.shape[0] - 1) // s if s > 0 else 0
-    f = int(face_offsets[-1].item()) // 3 if num_faces is None else int(num_faces)
+    if capacity is not None:
+        f = int(capacity)
+    else:
+        f = int(face_offsets[-1].item()) // 3 if num_faces is None else int(num_faces)
     faces = torch.empty((f, 3), dtype=torch.int32, device=device)
     voxel_indices = torch.empty((f,), dtype=torch.int32, device=device)
     neighbors, indices = _i32(neighbors, "neighbors"), _i32(indices, "indices")
@@ -396,7 +412,8 @@ def create_triangle_faces(
     types, codes = triangle_vertex_types.contiguous(), voxel_cell_codes.contiguous()
     nt.call(
         "mt_create_triangle_faces",
-        nt.ptr(neighbors), nt.ptr(indices), nv, g, nt.ptr(vertex_offsets), nt.ptr(types), nt.ptr(codes), s,
+        nt.ptr(neighbors), nt.ptr(indices), nv, g, types.shape[0], nt.ptr(vertex_offsets), nt.ptr(types),
+        nt.ptr(codes), s,
         nt.ptr(face_offsets), f, nt.ptr(faces), nt.ptr(voxel_indices), nt.stream(device),
     )
     return CreateTriangleFacesResult(faces, voxel_indices)
@@ -410,6 +427,13 @@ class Triangles(NamedTuple):
     voxel_indices: Tensor  # [face] int32
     vertex_boundaries: Tensor  # [level_set] int32 (cumulative ends)
     face_boundaries: Tensor  # [level_set] int32 (cumulative ends)
+
+
+class TessellationCounts(NamedTuple):
+    """Live sizes of a capacity-sized tessellation, as device scalars."""
+
+    num_vertices: Tensor  # [] int32
+    num_faces: Tensor  # [] int32
 
 
 @record_function("tessellate_voxels")
@@ -429,6 +453,37 @@ def tessellate_voxels(
     ``spherical_harmonics`` (and ``vertices``) through the triangle vertices'
     signed distances / colours, exactly as the reference.
     """
+    triangles, _ = _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners,
+                               upper_corners, indices, level_sets, None)
+    return triangles
+
+
+def tessellate_voxels_counted(
+    signed_distances: Tensor,
+    vertices: Tensor,
+    spherical_harmonics: Tensor,
+    neighbors: Tensor,
+    lower_corners: Tensor,
+    upper_corners: Tensor,
+    indices: Tensor,
+    level_sets: Tensor,
+    vertex_capacity: int,
+    face_capacity: int,
+) -> tuple[Triangles, TessellationCounts]:
+    """tessellate_voxels without any device->host read, for CUDA-graph capture.
+
+    Not in the reference. The outputs have ``vertex_capacity`` / ``face_capacity``
+    rows; the live counts are returned as device scalars. Rows past the live
+    counts are unused (faces never name them). When a live count exceeds its
+    capacity the extra vertices / faces are dropped; callers compare the counts
+    with the capacities (see ``meshtryoshka_gb300.graph``).
+    """
+    return _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners, upper_corners,
+                       indices, level_sets, (int(vertex_capacity), int(face_capacity)))
+
+
+def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners, upper_corners, indices,
+                level_sets, capacity):
     (num_level_sets,) = level_sets.shape
     device = nt.require_cuda(signed_distances, lower_corners, level_sets)
     logging.debug(f"Tessellating {neighbors.shape[1]} voxels with {num_level_sets} level sets.")
@@ -441,20 +496,25 @@ def tessellate_voxels(
         face_offsets, voxel_cell_codes = count_triangle_faces(signed_distances, lower_corners, upper_corners,
                                                               level_sets)
         compute_exclusive_cumsum(face_offsets)
-        # One device->host read for both totals (and the scan status word).
-        totals = torch.stack((vertex_offsets[-1], face_offsets[-1])).cpu()
-        nt.workspace(device).check()
-    num_vertices = int(totals[0])
-    num_faces = int(totals[1]) // 3
+        if capacity is None:
+            # One device->host read for both totals (and the scan status word).
+            totals = torch.stack((vertex_offsets[-1], face_offsets[-1])).cpu()
+            nt.workspace(device).check()
+            num_vertices, num_faces = int(totals[0]), int(totals[1]) // 3
+            counts = None
+        else:
+            num_vertices, num_faces = capacity
+            counts = TessellationCounts(vertex_offsets[-1], torch.div(face_offsets[-1], 3, rounding_mode="floor"))
 
     triangle_vertices, triangle_sdf, triangle_sh, triangle_types = create_triangle_vertices(
-        vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets, num_vertices,
+        vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets,
+        num_vertices if capacity is None else None, None if capacity is None else num_vertices,
     )
 
     with torch.no_grad():
         faces, voxel_indices = create_triangle_faces(
             signed_distances, neighbors, indices, vertex_offsets, triangle_types, voxel_cell_codes, level_sets,
-            face_offsets, num_faces,
+            face_offsets, num_faces if capacity is None else None, None if capacity is None else num_faces,
         )
         if g > 0 and num_level_sets > 0:
             vertex_boundaries = vertex_offsets[1:].view(num_level_sets, -1)[:, -1].clone()
@@ -467,4 +527,4 @@ def tessellate_voxels(
 
     logging.debug(f"Created {num_vertices} vertices and {num_faces} faces.")
     return Triangles(triangle_vertices, triangle_sdf, triangle_sh, faces, voxel_indices, vertex_boundaries,
-                     face_boundaries)
+                     face_boundaries), counts

@@ -194,7 +194,9 @@ class TriangleBounds:
 
 @record_function("bound_triangles")
 def bound_triangles(vertices: Tensor, depths: Tensor, faces: Tensor, grid: TileGrid,
-                    near_plane: float) -> TriangleBounds:
+                    near_plane: float, num_faces: Tensor | None = None) -> TriangleBounds:
+    """``num_faces`` (optional, not in the reference signature): a device
+    int32 scalar; face rows at or past it touch no tile."""
     assert near_plane >= 0
     vertices, depths, faces = _f32(vertices), _f32(depths), _i32(faces)
     device = nt.require_cuda(vertices, depths, faces)
@@ -205,9 +207,10 @@ def bound_triangles(vertices: Tensor, depths: Tensor, faces: Tensor, grid: TileG
     tmax = torch.empty((c, f, 2), **kw)
     count = torch.empty((c, f), **kw)
     rows, cols = grid.grid_shape
-    nt.call("mt_bound_triangles", nt.ptr(vertices), nt.ptr(depths), v, nt.ptr(faces), f, c, grid.tile_shape[0],
-            grid.tile_shape[1], rows, cols, float(near_plane), nt.ptr(tmin), nt.ptr(tmax), nt.ptr(count),
-            nt.stream(device))
+    nf = _i32(num_faces) if num_faces is not None else None
+    nt.call("mt_bound_triangles", nt.ptr(vertices), nt.ptr(depths), v, nt.ptr(faces), f, nt.ptr(nf), c,
+            grid.tile_shape[0], grid.tile_shape[1], rows, cols, float(near_plane), nt.ptr(tmin), nt.ptr(tmax),
+            nt.ptr(count), nt.stream(device))
     return TriangleBounds(tmin, tmax, count)
 
 
@@ -215,6 +218,9 @@ def bound_triangles(vertices: Tensor, depths: Tensor, faces: Tensor, grid: TileG
 class PairedKeys:
     keys: Tensor  # [K] int64
     triangle_indices: Tensor  # [K] int32
+    # Capacity mode only: device int64 scalar with the live key count (the
+    # buffers then have capacity rows and the rows past the count are unused).
+    count: Tensor | None = None
 
     @property
     def num_keys(self) -> int:
@@ -224,7 +230,10 @@ class PairedKeys:
 @record_function("generate_keys")
 def generate_keys(depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor, tile_minima: Tensor,
                   tile_maxima: Tensor, num_tiles_overlapped: Tensor, grid: TileGrid,
-                  key_defines) -> PairedKeys:
+                  key_defines, capacity: int | None = None) -> PairedKeys:
+    """``capacity`` (optional, not in the reference signature): allocate that
+    many key slots and keep the live count on the device instead of reading
+    it back; keys past the capacity are dropped (the caller checks the count)."""
     depths, faces, sfb = _f32(depths), _i32(faces), _i32(shell_face_boundaries)
     device = nt.require_cuda(depths, faces)
     _check_key_budget(grid, key_defines)
@@ -235,17 +244,20 @@ def generate_keys(depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor, 
         ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_scan_workspace_bytes(n))
         nt.call("mt_inclusive_scan_i32_to_i64", counts.data_ptr(), offsets.data_ptr(), n, ws_ptr, ws_bytes,
                 nt.stream(device))
-        num_keys = int(offsets[-1].item())
+    live = None
+    if capacity is not None:
+        num_keys = int(capacity)
+        live = offsets[-1] if n > 0 else torch.zeros((), dtype=torch.int64, device=device)
     else:
-        num_keys = 0
-    keys = torch.zeros(num_keys, dtype=torch.int64, device=device)
-    tri = torch.zeros(num_keys, dtype=torch.int32, device=device)
+        num_keys = int(offsets[-1].item()) if n > 0 else 0
+    keys = torch.empty(num_keys, dtype=torch.int64, device=device)
+    tri = torch.empty(num_keys, dtype=torch.int32, device=device)
     b, v = depths.shape
     tile_minima, tile_maxima = _i32(tile_minima), _i32(tile_maxima)
     nt.call("mt_generate_keys", nt.ptr(depths), v, nt.ptr(faces), faces.shape[0], nt.ptr(sfb), sfb.shape[0],
             nt.ptr(tile_minima), nt.ptr(tile_maxima), nt.ptr(offsets), b, grid.grid_shape[1],
             _layout(key_defines), num_keys, nt.ptr(keys), nt.ptr(tri), nt.stream(device))
-    return PairedKeys(keys, tri)
+    return PairedKeys(keys, tri, live)
 
 
 @record_function("sort_keys")
@@ -257,13 +269,14 @@ def sort_keys(paired_keys: PairedKeys, grid: TileGrid | None = None) -> PairedKe
     n = keys.numel()
     out_keys = torch.empty_like(keys)
     out_tri = torch.empty_like(tri)
+    live = paired_keys.count
     if n == 0:
-        return PairedKeys(out_keys, out_tri)
+        return PairedKeys(out_keys, out_tri, live)
     device = nt.require_cuda(keys, tri)
     ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_sort_pairs_workspace_bytes(n))
     nt.call("mt_sort_pairs_i64_i32", keys.data_ptr(), tri.data_ptr(), out_keys.data_ptr(), out_tri.data_ptr(), n,
-            0, 64, ws_ptr, ws_bytes, nt.stream(device))
-    return PairedKeys(out_keys, out_tri)
+            nt.ptr(live), 0, 64, ws_ptr, ws_bytes, nt.stream(device))
+    return PairedKeys(out_keys, out_tri, live)
 
 
 @record_function("delineate_tiles")
@@ -276,8 +289,9 @@ def delineate_tiles(sorted_paired_keys: PairedKeys, grid: TileGrid, key_defines,
     if out.numel() == 0:
         return out
     nt.require_cuda(keys, out)
-    nt.call("mt_delineate_tiles", nt.ptr(keys), keys.numel(), _layout(key_defines), int(separate_shells),
-            shape[0], shape[1], shape[2], out.data_ptr(), nt.stream(device))
+    nt.call("mt_delineate_tiles", nt.ptr(keys), keys.numel(), nt.ptr(sorted_paired_keys.count),
+            _layout(key_defines), int(separate_shells), shape[0], shape[1], shape[2], out.data_ptr(),
+            nt.stream(device))
     return out
 
 
@@ -335,7 +349,7 @@ def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, 
 class IntersectAndComposite(torch.autograd.Function):
     @staticmethod
     def forward(ctx, vertices, colors, signed_distances, faces, sharpness, sorted_keys, sorted_triangle_indices,
-                tile_boundaries, num_shells, grid, key_defines, gradient_mode=None):
+                tile_boundaries, num_shells, grid, key_defines, gradient_mode=None, num_keys=None):
         with record_function("intersect_and_composite_forward"):
             xy, colors, sdf, faces = _f32(vertices), _f32(colors), _f32(signed_distances), _i32(faces)
             device = nt.require_cuda(xy, colors, sdf, faces)
@@ -349,7 +363,8 @@ class IntersectAndComposite(torch.autograd.Function):
             masks = torch.empty((k,), dtype=torch.int32, device=device)
             out = torch.empty((b, 4, h, w), dtype=torch.float32, device=device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
-                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(bounds), b, int(num_shells),
+                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
+                    int(num_shells),
                     rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines), nt.ptr(masks),
                     nt.ptr(out), nt.stream(device))
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
@@ -376,15 +391,17 @@ class IntersectAndComposite(torch.autograd.Function):
                     nt.ptr(masks), nt.ptr(out), nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf),
                     nt.ptr(grad_sharp), int(mode == "exact"), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
-                    None, None, None, None)
+                    None, None, None, None, None)
 
 
 def intersect_and_composite(vertices, colors, signed_distances, faces, sharpness, sorted_keys,
                             sorted_triangle_indices, tile_boundaries, num_shells, grid, key_defines,
-                            gradient_mode: str | None = None) -> Tensor:
+                            gradient_mode: str | None = None, num_keys: Tensor | None = None) -> Tensor:
+    """``num_keys`` (optional): device int64 count of live keys when the key
+    buffers are capacity-sized."""
     return IntersectAndComposite.apply(vertices, colors, signed_distances, faces, sharpness, sorted_keys,
                                        sorted_triangle_indices, tile_boundaries, num_shells, grid, key_defines,
-                                       gradient_mode)
+                                       gradient_mode, num_keys)
 
 
 # ---------------------------------------------------------------------------
@@ -557,7 +574,15 @@ def render_explicit(extrinsics, intrinsics, image_shape, vertices, faces, shell_
 @record_function("render_fused")
 def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, signed_distances,
                  spherical_harmonics, sh_degree, sharpness, background, tile_shape=(16, 16), near_plane=0.2, ssaa=1,
-                 num_camera_bits=6, num_shell_bits=6, num_tile_bits=20, gradient_mode=None) -> Tensor:
+                 num_camera_bits=6, num_shell_bits=6, num_tile_bits=20, gradient_mode=None,
+                 num_faces: Tensor | None = None, key_capacity: int | None = None) -> Tensor:
+    """Fused render (triangle_rasterization/__init__.py:167-287).
+
+    Capacity mode (not in the reference): with ``num_faces`` (device int32
+    count of live face rows) and ``key_capacity`` the call reads nothing back
+    from the device, so it can be captured in a CUDA graph; keys past the
+    capacity are dropped and ``LAST_RENDER_STATS["key_count"]`` holds the live
+    key count as a device scalar for the caller to check."""
     b = extrinsics.shape[0]
     h, w = image_shape
     if vertices.numel() == 0 or faces.numel() == 0:
@@ -569,18 +594,18 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
     key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
                                      ("shell", num_shell_bits))
     positions, depths = project_vertices(vertices, extrinsics, intrinsics)
-    bounds = bound_triangles(positions, depths, faces, grid, near_plane)
+    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
     paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
-                           bounds.num_tiles_overlapped, grid, key_defines)
+                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
     del bounds, depths
-    LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.num_tiles_per_image)
+    LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.num_tiles_per_image, key_count=paired.count)
     paired = sort_keys(paired, grid)
     tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
     t = tile_boundaries.shape[2]
     images = intersect_and_composite(positions, colors, signed_distances, faces, sharpness, paired.keys,
                                      paired.triangle_indices, tile_boundaries.view(b, t, 2), s, grid, key_defines,
-                                     gradient_mode)
+                                     gradient_mode, paired.count)
     images = images[:, :3] + images[:, 3:4] * background[:, None, None]
     if ssaa > 1:
         images = _mean_pool(images, ssaa)

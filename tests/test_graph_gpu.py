@@ -1,0 +1,104 @@
+"""The CUDA-graph training step against the eager step.
+
+* capacity-sized tessellation holds the eager tessellation as its live prefix
+  (bit for bit);
+* a captured fused step gives the eager step's loss and gradients (within
+  1e-5 of the largest gradient: both accumulate with atomics), and repeated
+  replays agree;
+* capacities below the live sizes are detected by ``check()``, which
+  re-captures; the replay after that matches the eager step. Undersized
+  buffers are safe by construction: every writer is capacity-guarded and the
+  readers clamp the device counts.
+"""
+
+from __future__ import annotations
+
+import pytest
+import torch
+
+from meshtryoshka_gb300 import graph, pipeline
+from meshtryoshka_gb300 import triangle_extraction as te
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-5
+
+
+def _close(got, want, rtol=GRAD_RTOL):
+    scale = max(float(want.abs().max()), 1e-30)
+    err = float((got - want).abs().max())
+    assert err <= rtol * scale, f"max abs err {err:.3e} > {rtol:g} x {scale:.3e}"
+
+
+def _eager(w):
+    w.grid_sdf.grad = None
+    w.grid_sh.grad = None
+    loss, stats = pipeline.forward(w, "fused")
+    loss.backward()
+    out = float(loss), w.grid_sdf.grad.clone(), w.grid_sh.grad.clone(), stats
+    w.grid_sdf.grad = None
+    w.grid_sh.grad = None
+    return out
+
+
+def test_counted_tessellation_prefix_is_eager(cuda_device):
+    w = pipeline.build_workload("small", cuda_device)
+    args = (w.grid_sdf.detach(), w.voxels.vertices, w.grid_sh.detach(), w.voxels.neighbors, w.voxels.lower_corners,
+            w.voxels.upper_corners, w.voxels.indices, w.level_sets)
+    eager = te.tessellate_voxels(*args)
+    v, f = eager.vertices.shape[0], eager.faces.shape[0]
+    tri, counts = te.tessellate_voxels_counted(*args, v + 1000, f + 777)
+    assert int(counts.num_vertices) == v and int(counts.num_faces) == f
+    assert tri.vertices.shape[0] == v + 1000 and tri.faces.shape[0] == f + 777
+    torch.testing.assert_close(tri.vertices[:v], eager.vertices, rtol=0, atol=0)
+    torch.testing.assert_close(tri.signed_distances[:v], eager.signed_distances, rtol=0, atol=0)
+    torch.testing.assert_close(tri.spherical_harmonics[:, :v], eager.spherical_harmonics, rtol=0, atol=0)
+    torch.testing.assert_close(tri.faces[:f], eager.faces, rtol=0, atol=0)
+    torch.testing.assert_close(tri.face_boundaries, eager.face_boundaries, rtol=0, atol=0)
+
+
+def test_captured_step_matches_eager(cuda_device):
+    w = pipeline.build_workload("small", cuda_device)
+    loss_e, gsdf_e, gsh_e, _ = _eager(w)
+    step = graph.CapturedTrainingStep(w)
+    assert step.launches_per_replay > 20
+    for _ in range(3):
+        loss = step()
+        torch.cuda.synchronize()
+        assert step.check()
+        assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
+        _close(w.grid_sdf.grad, gsdf_e)
+        _close(w.grid_sh.grad, gsh_e)
+
+
+def test_captured_step_recaptures_when_capacity_overflows(cuda_device):
+    w = pipeline.build_workload("small", cuda_device)
+    loss_e, gsdf_e, gsh_e, stats = _eager(w)
+    small = pipeline.Capacities(stats["V"] // 2, stats["F"] // 2, stats["K"] // 2)
+    step = graph.CapturedTrainingStep(w, capacities=small)
+    step()
+    torch.cuda.synchronize()
+    assert not step.check()
+    assert step.recaptures == 1
+    c = step.capacities
+    assert c.vertices >= stats["V"] and c.faces >= stats["F"] and c.keys >= stats["K"]
+    loss = step()
+    torch.cuda.synchronize()
+    assert step.check()
+    assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
+    _close(w.grid_sdf.grad, gsdf_e)
+    _close(w.grid_sh.grad, gsh_e)
+
+
+def test_captured_step_follows_parameter_updates(cuda_device):
+    """Parameters are read in place: an update between replays is seen."""
+    w = pipeline.build_workload("small", cuda_device)
+    step = graph.CapturedTrainingStep(w)
+    step()
+    with torch.no_grad():
+        w.grid_sh.mul_(0.5)
+    loss = step()
+    torch.cuda.synchronize()
+    assert step.check()
+    loss_e, gsdf_e, gsh_e, _ = _eager(w)
+    assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
