@@ -152,7 +152,8 @@ __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int6
   }
 }
 
-// Gathers triangle `k` of the sorted list into batch slot `slot`.
+// Gathers triangle `k` of the sorted list into batch slot `slot`; returns its
+// vertex ids.
 __device__ __forceinline__ int3 gather(const CompositeArgs& a, int cam, int64_t k, TriGeom* geo, TriAttr* attr,
                                        int slot) {
   const int32_t f = __ldg(a.tri + k);
@@ -207,36 +208,71 @@ __device__ __forceinline__ void pop(int* queue, int queued, int nb, int lane) {
   __syncwarp();
 }
 
+// Test phase of a batch: bit i = triangle i of the batch passes the exact
+// hit test at this pixel. Triangles of shells the pixel has already passed
+// are skipped (last_shell only grows, so they would be skipped later too).
+// The costly per-hit work then runs in a separate loop over each pixel's own
+// bits, so the warp executes it as often as its busiest pixel has hits, not
+// once for every triangle that any of its pixels hits.
+__device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float fx, float fy, int last_shell) {
+  uint32_t hits = 0;
+  for (int i = 0; i < nb; ++i) {
+    const TriGeom& g = geo[i];
+    if (g.shell <= last_shell) continue;
+    float u, v, w;
+    if (hit_test(g, fx, fy, u, v, w)) hits |= 1u << i;
+  }
+  return hits;
+}
+
 struct Pixel {
   int cam;
   int64_t tile;
   int px, py;
   bool in_image;
   float fx, fy;
+  bool live;        // the warp has a (camera, tile) to work on
+  int wt;           // warp index inside its tile
 };
+
+// Warps are independent, so CTAs are only containers of kWarpsPerCta warps:
+// global warp g covers warp (g mod tile_warps) of (camera, tile) =
+// g / tile_warps. Every tile size runs with the same 256-thread CTAs (small
+// tiles share a CTA, large ones span several), and the per-warp shared
+// memory never exceeds 8 warps' worth.
+constexpr int kWarpsPerCta = 8;
+constexpr int kCtaThreads = 32 * kWarpsPerCta;
+
+__device__ __forceinline__ int tile_warps(const CompositeArgs& a) { return (a.tile_h * a.tile_w + 31) / 32; }
 
 __device__ __forceinline__ Pixel pixel_of(const CompositeArgs& a) {
   Pixel p;
   const int64_t T = (int64_t)a.rows * a.cols;
-  p.tile = blockIdx.x % T;
-  p.cam = (int)(blockIdx.x / T);
+  const int tw = tile_warps(a);
+  const int64_t gw = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  p.live = gw < (int64_t)a.B * T * tw;
+  const int64_t ct = gw / tw;
+  p.wt = (int)(gw - ct * tw);
+  p.tile = ct % T;
+  p.cam = (int)(ct / T);
+  const int tid = p.wt * 32 + (threadIdx.x & 31);  // thread index inside the tile
   int lx = 0, ly = 0;
-  tile_pixel(threadIdx.x, a.tile_w, a.tile_h, lx, ly);
+  tile_pixel(tid, a.tile_w, a.tile_h, lx, ly);
   p.px = (int)(p.tile % a.cols) * a.tile_w + lx;
   p.py = (int)(p.tile / a.cols) * a.tile_h + ly;
-  p.in_image = (int)threadIdx.x < a.tile_h * a.tile_w && p.px < a.W && p.py < a.H;
+  p.in_image = p.live && tid < a.tile_h * a.tile_w && p.px < a.W && p.py < a.H;
   p.fx = (float)p.px + 0.5f;
   p.fy = (float)p.py + 0.5f;
   return p;
 }
 
-template <int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(kCtaThreads)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out) {
   extern __shared__ float4 smem_f4[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[warp];
+  const int lane = threadIdx.x & 31;
+  WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const Pixel px = pixel_of(a);
+  if (!px.live) return;  // whole warp
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -252,18 +288,21 @@ __global__ void __launch_bounds__(kMaxThreads)
   int64_t next = start;
   int queued = 0;
   while (__any_sync(0xffffffffu, active)) {
-    queued = refill(masks, start, end, next, queued, ws.queue, warp, lane);
+    queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
     const int nb = min(queued, kBatch);
     if (nb == 0) break;
     if (lane < nb) gather(a, px.cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
     if (active) {
-      for (int i = 0; i < nb; ++i) {
+      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell);
+      while (hits) {
+        const int i = __ffs(hits) - 1;
+        hits &= hits - 1;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
-        if (!hit_test(g, px.fx, px.fy, u, v, w)) continue;
+        hit_test(g, px.fx, px.fy, u, v, w);  // a hit: recomputes its (u, v, w)
         const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
@@ -343,13 +382,13 @@ __device__ __forceinline__ void flush_half(const CompositeArgs& a, const Composi
   __syncwarp();
 }
 
-template <int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(kCtaThreads)
     composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr) {
   extern __shared__ float4 smem_f4[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[warp];
+  const int lane = threadIdx.x & 31;
+  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
   const Pixel px = pixel_of(a);
+  if (!px.live) return;  // whole warp
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -392,7 +431,7 @@ __global__ void __launch_bounds__(kMaxThreads)
   int queued = 0;
   int batch = 0;
   while (__any_sync(0xffffffffu, active)) {
-    queued = refill(masks, start, end, next, queued, ws.queue, warp, lane);
+    queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
     const int nb = min(queued, kBatch);
     if (nb == 0) break;
     const int half = batch & 1;
@@ -402,11 +441,14 @@ __global__ void __launch_bounds__(kMaxThreads)
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
     if (active) {
-      for (int i = 0; i < nb; ++i) {
+      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell);
+      while (hits) {
+        const int i = __ffs(hits) - 1;
+        hits &= hits - 1;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
-        if (!hit_test(g, px.fx, px.fy, u, v, w)) continue;
+        hit_test(g, px.fx, px.fy, u, v, w);  // a hit: recomputes its (u, v, w)
         const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
@@ -503,7 +545,11 @@ int check_args(const CompositeArgs& a) {
   return MT_OK;
 }
 
-inline int block_threads(const CompositeArgs& a) { return (a.tile_h * a.tile_w + 31) / 32 * 32; }
+// CTAs for every (camera, tile) warp.
+inline int64_t composite_ctas(const CompositeArgs& a) {
+  const int64_t warps = (int64_t)a.B * a.rows * a.cols * ((a.tile_h * a.tile_w + 31) / 32);
+  return (warps + kWarpsPerCta - 1) / kWarpsPerCta;
+}
 
 
 CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, int64_t V, const int32_t* faces,
@@ -557,7 +603,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
-  const int64_t blocks = (int64_t)B * rows * cols;
+  const int64_t blocks = composite_ctas(a);
   if (blocks == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
@@ -567,17 +613,10 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
     warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
     MT_CHECK_LAUNCH();
   }
-  const int bs = block_threads(a);
-  const size_t smem = sizeof(WarpForward) * (bs / 32);
-  if (bs <= 256) {
-    rc = set_smem<composite_forward_kernel<256>>(smem);
-    if (rc != MT_OK) return rc;
-    composite_forward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
-  } else {
-    rc = set_smem<composite_forward_kernel<1024>>(smem);
-    if (rc != MT_OK) return rc;
-    composite_forward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, out);
-  }
+  const size_t smem = sizeof(WarpForward) * kWarpsPerCta;
+  rc = set_smem<composite_forward_kernel>(smem);
+  if (rc != MT_OK) return rc;
+  composite_forward_kernel<<<(unsigned)blocks, kCtaThreads, smem, s>>>(a, warp_masks, out);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -596,25 +635,18 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
-  const int64_t blocks = (int64_t)B * rows * cols;
+  const int64_t blocks = composite_ctas(a);
   if (blocks == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && grad_out);
   MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
   MT_REQUIRE(blocks < ((int64_t)1 << 31));
   CompositeGrads gr{grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
-  const int bs = block_threads(a);
-  const size_t smem = sizeof(WarpBackward) * (bs / 32);
+  const size_t smem = sizeof(WarpBackward) * kWarpsPerCta;
   cudaStream_t s = as_stream(stream);
-  if (bs <= 256) {
-    rc = set_smem<composite_backward_kernel<256>>(smem);
-    if (rc != MT_OK) return rc;
-    composite_backward_kernel<256><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
-  } else {
-    rc = set_smem<composite_backward_kernel<1024>>(smem);
-    if (rc != MT_OK) return rc;
-    composite_backward_kernel<1024><<<(unsigned)blocks, bs, smem, s>>>(a, warp_masks, gr);
-  }
+  rc = set_smem<composite_backward_kernel>(smem);
+  if (rc != MT_OK) return rc;
+  composite_backward_kernel<<<(unsigned)blocks, kCtaThreads, smem, s>>>(a, warp_masks, gr);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

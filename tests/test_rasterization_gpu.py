@@ -170,9 +170,17 @@ def test_fused_forward(cuda_device, name):
 @pytest.mark.parametrize("name", list(SCENES))
 @pytest.mark.parametrize("mode", ["reference", "exact"])
 def test_fused_backward(cuda_device, name, mode):
-    scene = make_scene(**SCENES[name])
-    d = cuda_device
-    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
+    _check_fused_backward(make_scene(**SCENES[name]), cuda_device, mode, (16, 16))
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (32, 32), (16, 8), (12, 20)])
+def test_fused_backward_tile_shapes(cuda_device, tile):
+    """8x4-block tiles use per-triangle coverage; other shapes per-pixel tests."""
+    _check_fused_backward(make_scene(**SCENES["three_cams_odd"]), cuda_device, "reference", tile)
+
+
+def _check_fused_backward(scene, d, mode, tile):
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d, tile)
     colors_np = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
     colors = _t(colors_np, d).requires_grad_(True)
     sdf = _t(scene.sdf, d).requires_grad_(True)
@@ -208,7 +216,7 @@ def test_reference_and_exact_routing_differ_only_with_multiple_hits(cuda_device)
     _close_grad(grads["reference"], grads["exact"], rtol=1e-6)
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 32), (16, 8)])
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 32), (16, 8), (12, 20)])
 def test_fused_tile_shapes(cuda_device, tile):
     scene = make_scene(**SCENES["three_cams_odd"])
     inputs = _fused_inputs(scene, cuda_device)
