@@ -266,25 +266,30 @@ MT_API int mt_evaluate_spherical_harmonics_backward(
  * out_min / out_max [B,F,2] (row, col) tile bounds [min, max); out_count
  * [B,F] = tiles touched (0 for back-facing or near-plane-culled faces).
  * num_faces: NULL, or a device int32; rows at or past it touch no tile (F is
- * then the capacity). A face naming a vertex outside [0, V) touches no tile. */
+ * then the capacity). A face naming a vertex outside [0, V) touches no tile.
+ * cameras: NULL, or the ragged camera table of the compositing entry points
+ * (each camera clamps to its own rows x cols grid). */
 MT_API int mt_bound_triangles(const float* xy, const float* depth, int64_t V,
                               const int32_t* faces, int64_t F,
                               const int32_t* num_faces, int32_t B,
                               int32_t tile_h, int32_t tile_w, int32_t rows,
-                              int32_t cols, float near_plane, int32_t* out_min,
+                              int32_t cols, const int64_t* cameras,
+                              float near_plane, int32_t* out_min,
                               int32_t* out_max, int32_t* out_count,
                               mt_stream_t stream);
 
 /* triangle_rasterization/generate_keys.slang:4-68. offsets [B*F] is the
  * inclusive int64 prefix sum of out_count; K = offsets[B*F-1]. Writes one
- * key per (camera, face, tile) in (camera, face, row, col) order. */
+ * key per (camera, face, tile) in (camera, face, row, col) order. cameras:
+ * NULL (tile = row * grid_width + col), or the ragged camera table (each
+ * camera's own grid width). */
 MT_API int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces,
                             int64_t F, const int32_t* shell_face_boundaries,
                             int32_t S, const int32_t* tile_min,
                             const int32_t* tile_max, const int64_t* offsets,
-                            int32_t B, int32_t grid_width, const int32_t* layout,
-                            int64_t K, int64_t* out_keys, int32_t* out_triangles,
-                            mt_stream_t stream);
+                            int32_t B, int32_t grid_width, const int64_t* cameras,
+                            const int32_t* layout, int64_t K, int64_t* out_keys,
+                            int32_t* out_triangles, mt_stream_t stream);
 
 /* triangle_rasterization/delineate_tiles.slang:14-58 (+ the zero fill of
  * delineate_tiles.py:40, done here). out_boundaries [B, shell_dim,
@@ -308,6 +313,15 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
  * of its tile the triangle can cover) and read by the backward.
  * num_keys: NULL (all K keys live), or a device int64 count of live keys
  * (K is then the capacity of the key buffers).
+ * Cameras of different sizes (not in the reference): cameras = NULL (every
+ * camera rows x cols tiles of H x W pixels, out [B,4,H,W]), or a device table
+ * int64 [B, 6] = (rows, cols, height, width, first tile, first output
+ * element) per camera, with camera_tiles = the total of rows x cols over
+ * cameras; each camera's output is then [4, height, width] at its first
+ * output element, tile_boundaries stay [B, rows*cols, 2] with rows / cols /
+ * H / W the maxima, and keys carry the camera-local tile index.
+ * work_counter: one uint64 of device scratch (reset here): the kernel's
+ * persistent warps pull (camera, tile, warp) work items from it.
  * ---------------------------------------------------------------------- */
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
@@ -315,7 +329,8 @@ MT_API int mt_intersect_and_composite_forward(
     const int32_t* sorted_triangles, int64_t K, const int64_t* num_keys,
     const int64_t* tile_boundaries, int32_t B, int32_t num_shells, int32_t rows,
     int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H, int32_t W,
-    const int32_t* layout, uint32_t* warp_masks, float* out, mt_stream_t stream);
+    const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
+    uint32_t* warp_masks, uint64_t* work_counter, float* out, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
@@ -328,7 +343,8 @@ MT_API int mt_intersect_and_composite_backward(
     const int32_t* sorted_triangles, int64_t K, const int64_t* tile_boundaries,
     int32_t B, int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
     int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
-    const uint32_t* warp_masks, const float* out, const float* grad_out,
+    const int64_t* cameras, int64_t camera_tiles, const uint32_t* warp_masks,
+    uint64_t* work_counter, const float* out, const float* grad_out,
     float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
     int32_t exact_adjoint, mt_stream_t stream);
 

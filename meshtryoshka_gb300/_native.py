@@ -61,16 +61,17 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_project_vertices": (I32, [P, I64, P, P, I32, P, P, P]),
     "mt_evaluate_spherical_harmonics": (I32, [P, I64, P, I32, I32, P, I32, P, P]),
     "mt_evaluate_spherical_harmonics_backward": (I32, [P, I64, I32, I32, P, I32, P, P, P, P]),
-    "mt_bound_triangles": (I32, [P, P, I64, P, I64, P, I32, I32, I32, I32, I32, c_float, P, P, P, P]),
-    "mt_generate_keys": (I32, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, I64, P, P, P]),
+    "mt_bound_triangles": (I32, [P, P, I64, P, I64, P, I32, I32, I32, I32, I32, P, c_float, P, P, P, P]),
+    "mt_generate_keys": (I32, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, P, I64, P, P, P]),
     "mt_delineate_tiles": (I32, [P, I64, P, P, I32, I32, I32, I64, P, P]),
     "mt_intersect_and_composite_forward": (
         I32,
-        [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P],
+        [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P],
     ),
     "mt_intersect_and_composite_backward": (
         I32,
-        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P, P, P, P, P, I32, P],
+        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P, P, I32,
+         P],
     ),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),

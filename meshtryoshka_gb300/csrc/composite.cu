@@ -34,6 +34,8 @@
 //   exact (exact_adjoint = 1): with the previous hit's own weights.
 // The sharpness gradient is warp-reduced before one global atomic per warp.
 
+#include <atomic>
+
 #include "bary.cuh"
 #include "mt_common.cuh"
 
@@ -58,10 +60,17 @@ struct CompositeArgs {
   const float* sharpness;
   const uint64_t* keys;   // sorted keys
   const int32_t* tri;     // sorted triangle indices
-  const int64_t* bounds;  // [B, T, 2]
+  const int64_t* bounds;  // [B, rows * cols, 2]
   int B, S, rows, cols, tile_h, tile_w, H, W;
   int shell_off, shell_len, cam_off, cam_len, tile_off, tile_len;
-  const float* out;  // forward output [B, 4, H, W] (input to backward)
+  const float* out;  // forward output (input to backward)
+  // Ragged cameras: NULL (every camera rows x cols tiles, H x W pixels, output
+  // [B, 4, H, W]) or a device table [B, 6] = (rows, cols, height, width,
+  // first tile, first output element): each camera's output is [4, h, w] at
+  // its first output element and its tiles follow its first tile in the work
+  // order. rows / cols / H / W are then the maxima over cameras.
+  const int64_t* cameras;
+  int64_t total_tiles;  // tiles over all cameras
 };
 
 struct CompositeGrads {
@@ -133,7 +142,9 @@ __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int6
     const int cam = (int)field(key, a.cam_off, a.cam_len);
     const int tile = (int)field(key, a.tile_off, a.tile_len);
     uint32_t m = 0;
-    if (cam < a.B && tile < a.rows * a.cols) {
+    const int cols_b = (a.cameras && cam < a.B) ? (int)__ldg(a.cameras + 6 * cam + 1) : a.cols;
+    const int rows_b = (a.cameras && cam < a.B) ? (int)__ldg(a.cameras + 6 * cam) : a.rows;
+    if (cam < a.B && tile < rows_b * cols_b) {
       const int32_t f = __ldg(a.tri + k);
       const float2* xy = reinterpret_cast<const float2*>(a.xy) + (int64_t)cam * a.V;
       const float2 pa = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f)), pb = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f + 1)),
@@ -141,7 +152,7 @@ __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int6
       TriGeom g;
       setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
       const CullBox box = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
-      const int tx = tile % a.cols, ty = tile / a.cols;
+      const int tx = tile % cols_b, ty = tile / cols_b;
       for (int w = 0; w < warps; ++w) {
         float x0, x1, y0, y1;
         warp_block_rect(w, a.tile_w, a.tile_h, tx, ty, x0, x1, y0, y1);
@@ -227,52 +238,78 @@ __device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float
 
 struct Pixel {
   int cam;
-  int64_t tile;
-  int px, py;
+  int64_t tile;     // tile inside its camera's grid
+  int px, py;       // pixel inside its camera's image
   bool in_image;
   float fx, fy;
-  bool live;        // the warp has a (camera, tile) to work on
   int wt;           // warp index inside its tile
+  int64_t out_base;  // first output element of the camera
+  int64_t plane;     // pixels per output channel of the camera
+  int width;         // image width of the camera
 };
 
-// Warps are independent, so CTAs are only containers of kWarpsPerCta warps:
-// global warp g covers warp (g mod tile_warps) of (camera, tile) =
-// g / tile_warps. Every tile size runs with the same 256-thread CTAs (small
-// tiles share a CTA, large ones span several), and the per-warp shared
-// memory never exceeds 8 warps' worth.
+// Work is a list of (camera, tile, warp-in-tile) items, warp-in-tile
+// fastest, cameras in order; warps are independent, so CTAs are containers of
+// kWarpsPerCta warps that each pull items from a device counter until the
+// list is exhausted (persistent warps: any camera sizes and tile loads in one
+// launch). Every tile size runs with the same 256-thread CTAs.
 constexpr int kWarpsPerCta = 8;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
 __device__ __forceinline__ int tile_warps(const CompositeArgs& a) { return (a.tile_h * a.tile_w + 31) / 32; }
 
-__device__ __forceinline__ Pixel pixel_of(const CompositeArgs& a) {
+__device__ __forceinline__ int64_t total_items(const CompositeArgs& a) { return a.total_tiles * tile_warps(a); }
+
+__device__ __forceinline__ Pixel pixel_of(const CompositeArgs& a, int64_t item) {
   Pixel p;
-  const int64_t T = (int64_t)a.rows * a.cols;
   const int tw = tile_warps(a);
-  const int64_t gw = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-  p.live = gw < (int64_t)a.B * T * tw;
-  const int64_t ct = gw / tw;
-  p.wt = (int)(gw - ct * tw);
-  p.tile = ct % T;
-  p.cam = (int)(ct / T);
+  const int64_t gt = item / tw;  // global tile
+  p.wt = (int)(item - gt * tw);
+  int rows_b = a.rows, cols_b = a.cols, h = a.H, w = a.W;
+  if (a.cameras == nullptr) {
+    const int64_t T = (int64_t)a.rows * a.cols;
+    p.cam = (int)(gt / T);
+    p.tile = gt - (int64_t)p.cam * T;
+    p.plane = (int64_t)a.H * a.W;
+    p.out_base = (int64_t)p.cam * 4 * p.plane;
+  } else {
+    int lo = 0, hi = a.B - 1;  // last camera whose first tile <= gt
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(a.cameras + 6 * mid + 4) <= gt) lo = mid; else hi = mid - 1;
+    }
+    const int64_t* c = a.cameras + 6 * lo;
+    p.cam = lo;
+    rows_b = (int)__ldg(c);
+    cols_b = (int)__ldg(c + 1);
+    h = (int)__ldg(c + 2);
+    w = (int)__ldg(c + 3);
+    p.tile = gt - __ldg(c + 4);
+    p.plane = (int64_t)h * w;
+    p.out_base = __ldg(c + 5);
+  }
+  (void)rows_b;
+  p.width = w;
   const int tid = p.wt * 32 + (threadIdx.x & 31);  // thread index inside the tile
   int lx = 0, ly = 0;
   tile_pixel(tid, a.tile_w, a.tile_h, lx, ly);
-  p.px = (int)(p.tile % a.cols) * a.tile_w + lx;
-  p.py = (int)(p.tile / a.cols) * a.tile_h + ly;
-  p.in_image = p.live && tid < a.tile_h * a.tile_w && p.px < a.W && p.py < a.H;
+  p.px = (int)(p.tile % cols_b) * a.tile_w + lx;
+  p.py = (int)(p.tile / cols_b) * a.tile_h + ly;
+  p.in_image = tid < a.tile_h * a.tile_w && p.px < w && p.py < h;
   p.fx = (float)p.px + 0.5f;
   p.fy = (float)p.py + 0.5f;
   return p;
 }
 
-__global__ void __launch_bounds__(kCtaThreads)
-    composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out) {
-  extern __shared__ float4 smem_f4[];
-  const int lane = threadIdx.x & 31;
-  WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
-  const Pixel px = pixel_of(a);
-  if (!px.live) return;  // whole warp
+// Next work item for the calling warp (lane 0 claims, the warp shares it).
+__device__ __forceinline__ int64_t next_item(unsigned long long* counter, int lane) {
+  unsigned long long item = 0;
+  if (lane == 0) item = atomicAdd(counter, 1ull);
+  return (int64_t)__shfl_sync(0xffffffffu, item, 0);
+}
+
+__device__ __forceinline__ void forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
+                                             float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -325,13 +362,24 @@ __global__ void __launch_bounds__(kCtaThreads)
     __syncwarp();
   }
   if (px.in_image) {
-    const int64_t plane = (int64_t)a.H * a.W;
-    float* o = out + (int64_t)px.cam * 4 * plane + (int64_t)px.py * a.W + px.px;
+    float* o = out + px.out_base + (int64_t)px.py * px.width + px.px;
     o[0] = acc[0];
-    o[plane] = acc[1];
-    o[2 * plane] = acc[2];
-    o[3 * plane] = T_;
+    o[px.plane] = acc[1];
+    o[2 * px.plane] = acc[2];
+    o[3 * px.plane] = T_;
   }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kCtaThreads)
+    composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
+                             unsigned long long* __restrict__ counter) {
+  extern __shared__ float4 smem_f4[];
+  const int lane = threadIdx.x & 31;
+  WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
+  const int64_t items = total_items(a);
+  for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
+    forward_item(a, masks, out, ws, pixel_of(a, item), lane);
 }
 
 __device__ __forceinline__ void scatter_global(const CompositeArgs& a, const CompositeGrads& gr, int cam, int3 vid,
@@ -382,13 +430,8 @@ __device__ __forceinline__ void flush_half(const CompositeArgs& a, const Composi
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(kCtaThreads)
-    composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr) {
-  extern __shared__ float4 smem_f4[];
-  const int lane = threadIdx.x & 31;
-  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
-  const Pixel px = pixel_of(a);
-  if (!px.live) return;  // whole warp
+__device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
+                                              const CompositeGrads& gr, WarpBackward& ws, const Pixel& px, int lane) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -396,15 +439,14 @@ __global__ void __launch_bounds__(kCtaThreads)
   float final_rgb[3] = {0.f, 0.f, 0.f}, dL_rgb[3] = {0.f, 0.f, 0.f};
   float final_T = 0.f, dL_T = 0.f;
   if (px.in_image) {
-    const int64_t plane = (int64_t)a.H * a.W;
-    const int64_t o = (int64_t)cam * 4 * plane + (int64_t)px.py * a.W + px.px;
+    const int64_t o = px.out_base + (int64_t)px.py * px.width + px.px;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      final_rgb[c] = a.out[o + c * plane];
-      dL_rgb[c] = gr.grad_out[o + c * plane];
+      final_rgb[c] = a.out[o + c * px.plane];
+      dL_rgb[c] = gr.grad_out[o + c * px.plane];
     }
-    final_T = a.out[o + 3 * plane];
-    dL_T = gr.grad_out[o + 3 * plane];
+    final_T = a.out[o + 3 * px.plane];
+    dL_T = gr.grad_out[o + 3 * px.plane];
   }
   for (int i = lane; i < kRing * 13; i += 32) (&ws.gslot[0][0])[i] = 0.f;
   ws.vids[lane] = make_int3(0, 0, 0);
@@ -532,6 +574,18 @@ __global__ void __launch_bounds__(kCtaThreads)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   if (lane == 0 && x != 0.f) atomicAdd(gr.grad_sharpness, x);
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kCtaThreads)
+    composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr,
+                              unsigned long long* __restrict__ counter) {
+  extern __shared__ float4 smem_f4[];
+  const int lane = threadIdx.x & 31;
+  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
+  const int64_t items = total_items(a);
+  for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
+    backward_item(a, masks, gr, ws, pixel_of(a, item), lane);
 }
 
 int check_args(const CompositeArgs& a) {
@@ -545,18 +599,37 @@ int check_args(const CompositeArgs& a) {
   return MT_OK;
 }
 
-// CTAs for every (camera, tile) warp.
-inline int64_t composite_ctas(const CompositeArgs& a) {
-  const int64_t warps = (int64_t)a.B * a.rows * a.cols * ((a.tile_h * a.tile_w + 31) / 32);
-  return (warps + kWarpsPerCta - 1) / kWarpsPerCta;
+// Persistent grid: as many CTAs as fit on the device at once (queried once
+// per kernel and device), but no more than there are work items for.
+template <auto Kernel>
+int persistent_ctas(const CompositeArgs& a, size_t smem, int64_t& ctas) {
+  static std::atomic<int> resident[64];
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return MT_ERR_CUDA;
+  int r = resident[device].load(std::memory_order_acquire);
+  if (r == 0) {
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MT_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, kCtaThreads, smem) != cudaSuccess)
+      return MT_ERR_CUDA;
+    r = max(1, sms * max(per_sm, 1));
+    resident[device].store(r, std::memory_order_release);
+  }
+  const int64_t warps = a.total_tiles * ((a.tile_h * a.tile_w + 31) / 32);
+  const int64_t needed = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
+  ctas = needed < (int64_t)r ? needed : (int64_t)r;
+  return MT_OK;
 }
 
 
 CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, int64_t V, const int32_t* faces,
                         const float* sharpness, const int64_t* keys, const int32_t* tri, const int64_t* bounds,
                         int32_t B, int32_t S, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
-                        int32_t W, const int32_t* layout, const float* out) {
+                        int32_t W, const int32_t* layout, const float* out, const int64_t* cameras,
+                        int64_t camera_tiles) {
   CompositeArgs a{};
+  a.cameras = cameras;
+  a.total_tiles = cameras ? camera_tiles : (int64_t)B * rows * cols;
   a.xy = xy;
   a.colors = colors;
   a.sdf = sdf;
@@ -597,17 +670,17 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        const int64_t* num_keys, const int64_t* tile_boundaries, int32_t B,
                                        int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
                                        int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
-                                       uint32_t* warp_masks, float* out, mt_stream_t stream) {
-  MT_REQUIRE(layout != nullptr && K >= 0);
+                                       const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
+                                       uint64_t* work_counter, float* out, mt_stream_t stream) {
+  MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
-                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr);
+                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
+                              cameras, camera_tiles);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
-  const int64_t blocks = composite_ctas(a);
-  if (blocks == 0 || H == 0 || W == 0) return MT_OK;
-  MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out);
+  if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
+  MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
-  MT_REQUIRE(blocks < ((int64_t)1 << 31));
   cudaStream_t s = as_stream(stream);
   if (K > 0) {
     warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
@@ -616,7 +689,12 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   const size_t smem = sizeof(WarpForward) * kWarpsPerCta;
   rc = set_smem<composite_forward_kernel>(smem);
   if (rc != MT_OK) return rc;
-  composite_forward_kernel<<<(unsigned)blocks, kCtaThreads, smem, s>>>(a, warp_masks, out);
+  int64_t ctas = 0;
+  rc = persistent_ctas<composite_forward_kernel>(a, smem, ctas);
+  if (rc != MT_OK) return rc;
+  if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
+  composite_forward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
+      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter));
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -626,27 +704,32 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         const int64_t* sorted_keys, const int32_t* sorted_triangles, int64_t K,
                                         const int64_t* tile_boundaries, int32_t B, int32_t num_shells,
                                         int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
-                                        int32_t W, const int32_t* layout, const uint32_t* warp_masks,
+                                        int32_t W, const int32_t* layout, const int64_t* cameras,
+                                        int64_t camera_tiles, const uint32_t* warp_masks, uint64_t* work_counter,
                                         const float* out, const float* grad_out, float* grad_colors,
                                         float* grad_signed_distances, float* grad_sharpness, int32_t exact_adjoint,
                                         mt_stream_t stream) {
-  MT_REQUIRE(layout != nullptr && K >= 0);
+  MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
-                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out);
+                              tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out,
+                              cameras, camera_tiles);
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
-  const int64_t blocks = composite_ctas(a);
-  if (blocks == 0 || H == 0 || W == 0) return MT_OK;
+  if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && grad_out);
-  MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness);
+  MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
-  MT_REQUIRE(blocks < ((int64_t)1 << 31));
   CompositeGrads gr{grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
   const size_t smem = sizeof(WarpBackward) * kWarpsPerCta;
   cudaStream_t s = as_stream(stream);
   rc = set_smem<composite_backward_kernel>(smem);
   if (rc != MT_OK) return rc;
-  composite_backward_kernel<<<(unsigned)blocks, kCtaThreads, smem, s>>>(a, warp_masks, gr);
+  int64_t ctas = 0;
+  rc = persistent_ctas<composite_backward_kernel>(a, smem, ctas);
+  if (rc != MT_OK) return rc;
+  if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
+  composite_backward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
+      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter));
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

@@ -226,17 +226,20 @@ __device__ __forceinline__ TileBounds triangle_tile_bounds(const float* __restri
 }
 
 // Rows f >= num_faces (a device value; all F when NULL) cover no tile.
+// cameras: NULL (every camera has rows x cols tiles) or the ragged camera
+// table [B, 6] whose first two columns give each camera's own grid.
 __global__ void bound_kernel(const float* __restrict__ xy, const float* __restrict__ depth, int64_t V,
                              const int32_t* __restrict__ faces, int64_t F, const int32_t* __restrict__ num_faces,
-                             int B, int tile_h, int tile_w, int rows, int cols, float near,
-                             int32_t* __restrict__ out_min, int32_t* __restrict__ out_max,
+                             int B, int tile_h, int tile_w, int rows, int cols, const int64_t* __restrict__ cameras,
+                             float near, int32_t* __restrict__ out_min, int32_t* __restrict__ out_max,
                              int32_t* __restrict__ out_count) {
   const int64_t total = (int64_t)B * F;
   const int64_t live = num_faces ? min((int64_t)max(*num_faces, 0), F) : F;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(i / F);
     const int64_t f = i - (int64_t)b * F;
-    const TileBounds t = f < live ? triangle_tile_bounds(xy, depth, V, faces, f, b, tile_h, tile_w, rows, cols, near)
+    const int rb = cameras ? (int)cameras[6 * b] : rows, cb = cameras ? (int)cameras[6 * b + 1] : cols;
+    const TileBounds t = f < live ? triangle_tile_bounds(xy, depth, V, faces, f, b, tile_h, tile_w, rb, cb, near)
                                   : TileBounds{0, 0, 0, 0};
     out_min[2 * i] = t.r0;
     out_min[2 * i + 1] = t.c0;
@@ -261,8 +264,8 @@ __device__ __forceinline__ uint64_t field_mask(int len) { return (uint64_t)((1u 
 __global__ void keys_kernel(const float* __restrict__ depth, int64_t V, const int32_t* __restrict__ faces,
                             int64_t F, const int32_t* __restrict__ sfb, int S, const int32_t* __restrict__ tmin,
                             const int32_t* __restrict__ tmax, const int64_t* __restrict__ offsets, int B,
-                            int grid_width, KeyLayout L, int64_t K, uint64_t* __restrict__ out_keys,
-                            int32_t* __restrict__ out_tri) {
+                            int grid_width, const int64_t* __restrict__ cameras, KeyLayout L, int64_t K,
+                            uint64_t* __restrict__ out_keys, int32_t* __restrict__ out_tri) {
   const int64_t total = (int64_t)B * F;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(i / F);
@@ -280,10 +283,11 @@ __global__ void keys_kernel(const float* __restrict__ depth, int64_t V, const in
                            (((uint64_t)shell & field_mask(L.shell_len)) << L.shell_off) |
                            ((uint64_t)__float_as_uint(mean) << L.depth_off);
     int64_t k = (i == 0) ? 0 : offsets[i - 1];
+    const int width = cameras ? (int)cameras[6 * b + 1] : grid_width;  // tiles per row of this camera
     for (int r = r0; r < r1; ++r) {
       for (int c = c0; c < c1; ++c) {
         if (k >= K) return;  // guarded: offsets and K always agree for valid inputs
-        const uint32_t tile = (uint32_t)(r * grid_width + c);
+        const uint32_t tile = (uint32_t)(r * width + c);
         out_keys[k] = fixed | (((uint64_t)tile & field_mask(L.tile_len)) << L.tile_off);
         out_tri[k] = (int32_t)f;
         ++k;
@@ -389,13 +393,14 @@ int mt_evaluate_spherical_harmonics_backward(const float* vertices, int64_t V, i
 
 int mt_bound_triangles(const float* xy, const float* depth, int64_t V, const int32_t* faces, int64_t F,
                        const int32_t* num_faces, int32_t B, int32_t tile_h, int32_t tile_w, int32_t rows,
-                       int32_t cols, float near_plane, int32_t* out_min, int32_t* out_max, int32_t* out_count,
-                       mt_stream_t stream) {
+                       int32_t cols, const int64_t* cameras, float near_plane, int32_t* out_min, int32_t* out_max,
+                       int32_t* out_count, mt_stream_t stream) {
   MT_REQUIRE(V >= 0 && F >= 0 && B >= 0 && tile_h > 0 && tile_w > 0 && rows >= 0 && cols >= 0);
   if (F == 0 || B == 0) return MT_OK;
   MT_REQUIRE(xy && depth && faces && out_min && out_max && out_count);
   bound_kernel<<<grid_stride_blocks((int64_t)B * F, 256), 256, 0, as_stream(stream)>>>(
-      xy, depth, V, faces, F, num_faces, B, tile_h, tile_w, rows, cols, near_plane, out_min, out_max, out_count);
+      xy, depth, V, faces, F, num_faces, B, tile_h, tile_w, rows, cols, cameras, near_plane, out_min, out_max,
+      out_count);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -403,8 +408,8 @@ int mt_bound_triangles(const float* xy, const float* depth, int64_t V, const int
 int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces, int64_t F,
                      const int32_t* shell_face_boundaries, int32_t S, const int32_t* tile_min,
                      const int32_t* tile_max, const int64_t* offsets, int32_t B, int32_t grid_width,
-                     const int32_t* layout, int64_t K, int64_t* out_keys, int32_t* out_triangles,
-                     mt_stream_t stream) {
+                     const int64_t* cameras, const int32_t* layout, int64_t K, int64_t* out_keys,
+                     int32_t* out_triangles, mt_stream_t stream) {
   MT_REQUIRE(V >= 0 && F >= 0 && B >= 0 && S >= 0 && K >= 0 && layout);
   KeyLayout L{layout[0], layout[1], layout[2], layout[3], layout[4], layout[5], layout[6]};
   MT_REQUIRE(layout_ok(L));
@@ -412,7 +417,7 @@ int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces, int64_
   MT_REQUIRE(depth && faces && tile_min && tile_max && offsets && out_keys && out_triangles);
   MT_REQUIRE(S == 0 || shell_face_boundaries);
   keys_kernel<<<grid_stride_blocks((int64_t)B * F, 256), 256, 0, as_stream(stream)>>>(
-      depth, V, faces, F, shell_face_boundaries, S, tile_min, tile_max, offsets, B, grid_width, L, K,
+      depth, V, faces, F, shell_face_boundaries, S, tile_min, tile_max, offsets, B, grid_width, cameras, L, K,
       reinterpret_cast<uint64_t*>(out_keys), out_triangles);
   MT_CHECK_LAUNCH();
   return MT_OK;

@@ -33,6 +33,8 @@ from .. import _native as nt
 __all__ = [
     "render",
     "render_fused",
+    "render_cameras",
+    "split_cameras",
     "render_explicit",
     "rasterize",
     "TileGrid",
@@ -94,9 +96,20 @@ def ceildiv(numerator, denominator):
 @dataclass(frozen=True)
 class TileGrid:
     tile_shape: tuple[int, int]  # (height, width) of one tile in pixels
-    image_shape: tuple[int, int]  # (height, width) of the image
+    image_shape: tuple[int, int]  # (height, width) of the image (the largest, with camera_shapes)
     num_cameras: int
     num_shells: int
+    # Not in the reference: per-camera image shapes for a batch of cameras of
+    # different sizes. Each camera gets its own grid of tiles; keys carry the
+    # camera-local tile index and tile ranges keep the [B, rows*cols, 2] shape
+    # of the largest grid.
+    camera_shapes: tuple[tuple[int, int], ...] | None = None
+
+    @staticmethod
+    def for_cameras(tile_shape, camera_shapes, num_shells) -> "TileGrid":
+        shapes = tuple((int(h), int(w)) for h, w in camera_shapes)
+        image = (max(h for h, _ in shapes), max(w for _, w in shapes))
+        return TileGrid(tuple(tile_shape), image, len(shapes), num_shells, shapes)
 
     @property
     def grid_shape(self) -> tuple[int, int]:
@@ -110,6 +123,46 @@ class TileGrid:
     def tile_numel(self) -> int:
         h, w = self.tile_shape
         return h * w
+
+    @property
+    def ragged(self) -> bool:
+        return self.camera_shapes is not None
+
+    def camera_grids(self) -> list[tuple[int, int]]:
+        shapes = self.camera_shapes or ((self.image_shape,) * self.num_cameras)
+        return [(ceildiv(h, self.tile_shape[0]), ceildiv(w, self.tile_shape[1])) for h, w in shapes]
+
+    @property
+    def camera_tiles(self) -> int:
+        return sum(r * c for r, c in self.camera_grids())
+
+    @property
+    def output_numel(self) -> int:
+        shapes = self.camera_shapes or ((self.image_shape,) * self.num_cameras)
+        return sum(4 * h * w for h, w in shapes)
+
+
+_CAMERA_TABLES: dict = {}
+
+
+def _camera_table(grid: TileGrid, device) -> Tensor | None:
+    """Device table [B, 6] int64 (rows, cols, height, width, first tile, first
+    output element) of a ragged grid; None for a uniform one. Built once per
+    grid and device, so later calls (and CUDA-graph capture) copy nothing."""
+    if not grid.ragged:
+        return None
+    key = (grid, str(device))
+    table = _CAMERA_TABLES.get(key)
+    if table is None:
+        rows = []
+        tile = out = 0
+        for (h, w), (r, c) in zip(grid.camera_shapes, grid.camera_grids()):
+            rows.append((r, c, h, w, tile, out))
+            tile += r * c
+            out += 4 * h * w
+        table = torch.tensor(rows, dtype=torch.int64).to(device)
+        _CAMERA_TABLES[key] = table
+    return table
 
 
 def create_key_defines(*sequence: tuple[str, int]) -> tuple[tuple[str, int], ...]:
@@ -160,7 +213,8 @@ def _i32(t: Tensor) -> Tensor:
 
 def _sharpness(sharpness, device) -> Tensor:
     if not torch.is_tensor(sharpness):
-        sharpness = torch.tensor(float(sharpness), dtype=torch.float32)
+        # A device fill, not a host->device copy, so it can be graph-captured.
+        return torch.full((), float(sharpness), dtype=torch.float32, device=device)
     return sharpness.to(device=device, dtype=torch.float32).reshape(())
 
 
@@ -208,9 +262,10 @@ def bound_triangles(vertices: Tensor, depths: Tensor, faces: Tensor, grid: TileG
     count = torch.empty((c, f), **kw)
     rows, cols = grid.grid_shape
     nf = _i32(num_faces) if num_faces is not None else None
+    table = _camera_table(grid, device)
     nt.call("mt_bound_triangles", nt.ptr(vertices), nt.ptr(depths), v, nt.ptr(faces), f, nt.ptr(nf), c,
-            grid.tile_shape[0], grid.tile_shape[1], rows, cols, float(near_plane), nt.ptr(tmin), nt.ptr(tmax),
-            nt.ptr(count), nt.stream(device))
+            grid.tile_shape[0], grid.tile_shape[1], rows, cols, nt.ptr(table), float(near_plane), nt.ptr(tmin),
+            nt.ptr(tmax), nt.ptr(count), nt.stream(device))
     return TriangleBounds(tmin, tmax, count)
 
 
@@ -256,7 +311,8 @@ def generate_keys(depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor, 
     tile_minima, tile_maxima = _i32(tile_minima), _i32(tile_maxima)
     nt.call("mt_generate_keys", nt.ptr(depths), v, nt.ptr(faces), faces.shape[0], nt.ptr(sfb), sfb.shape[0],
             nt.ptr(tile_minima), nt.ptr(tile_maxima), nt.ptr(offsets), b, grid.grid_shape[1],
-            _layout(key_defines), num_keys, nt.ptr(keys), nt.ptr(tri), nt.stream(device))
+            nt.ptr(_camera_table(grid, device)), _layout(key_defines), num_keys, nt.ptr(keys), nt.ptr(tri),
+            nt.stream(device))
     return PairedKeys(keys, tri, live)
 
 
@@ -361,12 +417,16 @@ class IntersectAndComposite(torch.autograd.Function):
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
             masks = torch.empty((k,), dtype=torch.int32, device=device)
-            out = torch.empty((b, 4, h, w), dtype=torch.float32, device=device)
+            counter = torch.empty((1,), dtype=torch.int64, device=device)
+            table = _camera_table(grid, device)
+            # Uniform cameras: [B, 4, H, W]; ragged: every camera's [4, h, w] back to back.
+            out = torch.empty((grid.output_numel,) if grid.ragged else (b, 4, h, w), dtype=torch.float32,
+                              device=device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
-                    int(num_shells),
-                    rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines), nt.ptr(masks),
-                    nt.ptr(out), nt.stream(device))
+                    int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
+                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out),
+                    nt.stream(device))
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness))
@@ -385,11 +445,13 @@ class IntersectAndComposite(torch.autograd.Function):
             b, v, _ = xy.shape
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
+            counter = torch.empty((1,), dtype=torch.int64, device=device)
             nt.call("mt_intersect_and_composite_backward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
-                    nt.ptr(masks), nt.ptr(out), nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf),
-                    nt.ptr(grad_sharp), int(mode == "exact"), nt.stream(device))
+                    nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
+                    nt.ptr(out), nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp),
+                    int(mode == "exact"), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
 
@@ -610,6 +672,55 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
     if ssaa > 1:
         images = _mean_pool(images, ssaa)
     return images.clip(min=0, max=1)
+
+
+def split_cameras(raw: Tensor, grid: TileGrid) -> list[Tensor]:
+    """Per-camera [4, h, w] views of a ragged compositing output."""
+    views, start = [], 0
+    for h, w in grid.camera_shapes:
+        views.append(raw[start:start + 4 * h * w].view(4, h, w))
+        start += 4 * h * w
+    return views
+
+
+@record_function("render_cameras")
+def render_cameras(extrinsics, intrinsics, image_shapes, vertices, faces, shell_face_boundaries, signed_distances,
+                   spherical_harmonics, sh_degree, sharpness, background, tile_shape=(16, 16), near_plane=0.2,
+                   num_camera_bits=6, num_shell_bits=6, num_tile_bits=20, gradient_mode=None,
+                   num_faces: Tensor | None = None, key_capacity: int | None = None) -> list[Tensor]:
+    """Fused render of cameras with different image sizes in one pass (not in
+    the reference, which renders one image size per call).
+
+    ``image_shapes``: one (height, width) per camera. Every stage runs once
+    for all cameras; the compositing kernel's persistent warps take (camera,
+    tile) work items of every camera from one queue. Returns one [3, h, w]
+    image per camera, equal to rendering each camera on its own with
+    ``render_fused``. ``num_faces`` / ``key_capacity`` as in ``render_fused``.
+    """
+    b = extrinsics.shape[0]
+    (s,) = shell_face_boundaries.shape
+    grid = TileGrid.for_cameras(tile_shape, image_shapes, s)
+    if len(grid.camera_shapes) != b:
+        raise ValueError("one image shape per camera is required")
+    if vertices.numel() == 0 or faces.numel() == 0:
+        return [background.reshape(3, 1, 1).expand(3, h, w) for h, w in grid.camera_shapes]
+    key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
+                                     ("shell", num_shell_bits))
+    positions, depths = project_vertices(vertices, extrinsics, intrinsics)
+    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
+    paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
+                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
+    del bounds, depths
+    LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
+    paired = sort_keys(paired, grid)
+    tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
+    colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
+    t = tile_boundaries.shape[2]
+    raw = intersect_and_composite(positions, colors, signed_distances, faces, sharpness, paired.keys,
+                                  paired.triangle_indices, tile_boundaries.view(b, t, 2), s, grid, key_defines,
+                                  gradient_mode, paired.count)
+    bg = background[:, None, None]
+    return [(r[:3] + r[3:4] * bg).clip(min=0, max=1) for r in split_cameras(raw, grid)]
 
 
 def render(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, signed_distances,

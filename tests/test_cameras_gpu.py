@@ -1,0 +1,98 @@
+"""Cameras of different image sizes rendered in one pass (``render_cameras``).
+
+Each camera's image must equal rendering that camera alone with
+``render_fused`` (bit for bit: a camera's keys keep their relative order in
+the batch, so every pixel sees the same hits in the same order), and the
+gradients of a loss over all cameras must equal the sum of the single-camera
+gradients (within 1e-5 of the largest: atomic accumulation order).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from meshtryoshka_gb300 import synthetic
+from meshtryoshka_gb300 import triangle_rasterization as tr
+from tests.scenes import make_scene
+
+pytestmark = pytest.mark.gpu
+
+CAMERAS = (  # eye, (height, width), fov
+    ((0.0, 0.0, 2.0), (75, 101), 55.0),
+    ((1.2, 0.8, 1.3), (128, 64), 60.0),
+    ((-1.5, -0.3, 1.1), (40, 200), 45.0),
+    ((0.3, 1.6, 0.9), (33, 47), 70.0),
+    ((0.0, -1.8, -1.0), (96, 96), 50.0),
+)
+
+
+def _t(a, device):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+def _scene(device):
+    sc = make_scene(sh_degree=2, levels=(0.03, 0.01, -0.01, -0.03))
+    ext = np.stack([synthetic.look_at(np.array(eye)) for eye, _, _ in CAMERAS]).astype(np.float32)
+    intr = np.stack([synthetic.pinhole(h, w, fov) for _, (h, w), fov in CAMERAS]).astype(np.float32)
+    shapes = [shape for _, shape, _ in CAMERAS]
+    d = device
+    args = dict(vertices=_t(sc.vertices, d), faces=_t(sc.faces, d), shell_face_boundaries=_t(sc.face_boundaries, d),
+                signed_distances=_t(sc.sdf, d).requires_grad_(True),
+                spherical_harmonics=_t(sc.sh, d).requires_grad_(True), sh_degree=sc.sh_degree,
+                sharpness=float(sc.sharpness), background=_t(sc.background, d))
+    return _t(ext, d), _t(intr, d), shapes, args
+
+
+def _close(got, want, rtol=1e-5):
+    scale = max(float(want.abs().max()), 1e-30)
+    err = float((got - want).abs().max())
+    assert err <= rtol * scale, f"max abs err {err:.3e} > {rtol:g} x {scale:.3e}"
+
+
+@pytest.mark.parametrize("tile", [(16, 16), (8, 8), (12, 20)])
+def test_cameras_match_single_camera_renders(cuda_device, tile):
+    ext, intr, shapes, args = _scene(cuda_device)
+    rng = np.random.default_rng(0)
+    targets = [_t(rng.normal(0, 1, (3, h, w)).astype(np.float32), cuda_device) for h, w in shapes]
+
+    images = tr.render_cameras(ext, intr, shapes, tile_shape=tile, **args)
+    assert [tuple(i.shape) for i in images] == [(3, h, w) for h, w in shapes]
+    sum(((img * t).sum() for img, t in zip(images, targets))).backward()
+    g_sdf, g_sh = args["signed_distances"].grad.clone(), args["spherical_harmonics"].grad.clone()
+    args["signed_distances"].grad = None
+    args["spherical_harmonics"].grad = None
+
+    loss = 0.0
+    for b, (h, w) in enumerate(shapes):
+        single = tr.render_fused(ext[b:b + 1], intr[b:b + 1], (h, w), tile_shape=tile, **args)[0]
+        torch.testing.assert_close(images[b], single, rtol=0, atol=0)
+        loss = loss + (single * targets[b]).sum()
+    loss.backward()
+    _close(g_sdf, args["signed_distances"].grad)
+    _close(g_sh, args["spherical_harmonics"].grad)
+    assert float(g_sdf.abs().max()) > 0
+
+
+def test_cameras_in_a_captured_graph(cuda_device):
+    """The ragged batch is capturable: no host reads with device counts."""
+    ext, intr, shapes, args = _scene(cuda_device)
+    want = [i.detach().clone() for i in tr.render_cameras(ext, intr, shapes, **args)]
+    faces = args["faces"]
+    nf = torch.tensor(faces.shape[0], dtype=torch.int32, device=cuda_device)
+    kw = dict(args, signed_distances=args["signed_distances"].detach(),
+              spherical_harmonics=args["spherical_harmonics"].detach())
+    key_capacity = int(tr.LAST_RENDER_STATS["num_keys"]) + 1000
+    stream = torch.cuda.Stream(cuda_device)
+    stream.wait_stream(torch.cuda.current_stream(cuda_device))
+    with torch.cuda.stream(stream):
+        tr.render_cameras(ext, intr, shapes, num_faces=nf, key_capacity=key_capacity, **kw)
+    torch.cuda.current_stream(cuda_device).wait_stream(stream)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        out = tr.render_cameras(ext, intr, shapes, num_faces=nf, key_capacity=key_capacity, **kw)
+    graph.replay()
+    torch.cuda.synchronize()
+    for got, ref in zip(out, want):
+        torch.testing.assert_close(got, ref, rtol=0, atol=0)

@@ -60,3 +60,19 @@ def test_cpu_tensors_are_rejected():
 
     with pytest.raises(ValueError, match="CUDA"):
         te.count_occupancy(torch.zeros((2, 2, 1), dtype=torch.int32))
+
+
+def test_ragged_camera_table():
+    """Per-camera grids, first tiles and first output elements of a batch of
+    cameras with different image sizes."""
+    from meshtryoshka_gb300 import triangle_rasterization as tr
+
+    grid = tr.TileGrid.for_cameras((16, 16), [(75, 101), (128, 64), (40, 200)], 4)
+    assert grid.image_shape == (128, 200) and grid.grid_shape == (8, 13)
+    assert grid.camera_grids() == [(5, 7), (8, 4), (3, 13)]
+    assert grid.camera_tiles == 35 + 32 + 39
+    assert grid.output_numel == 4 * (75 * 101 + 128 * 64 + 40 * 200)
+    table = tr._camera_table(grid, "cpu").tolist()
+    assert table == [[5, 7, 75, 101, 0, 0], [8, 4, 128, 64, 35, 4 * 75 * 101],
+                     [3, 13, 40, 200, 67, 4 * (75 * 101 + 128 * 64)]]
+    assert tr._camera_table(tr.TileGrid((16, 16), (64, 64), 2, 3), "cpu") is None
