@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
     p.add_argument("--config", default=CONFIG_NAME)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-cameras", action="store_true", help="skip the uneven-camera batching comparison")
     return p.parse_args()
 
 
@@ -400,6 +401,8 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
         "clocks": clock_info,
     }
+    if not args.no_cameras and world == 1:
+        line["cameras_batched"] = run_cameras(device, min(args.steps, 20))
     if not args.no_cpu_baseline and world == 1:
         tess_s, render_s = cpu_sample(w, 0)
         cpu_ms = 1000.0 * (tess_s + b * render_s)
@@ -408,6 +411,60 @@ def run_ours(args, rank, world, local):
             "sample": f"full tessellation fwd+bwd + fused render fwd+bwd of 1 of {b} cameras, render time x{b}",
         }
     print(json.dumps(line))
+
+
+def run_cameras(device, steps):
+    """Cameras of uneven size: the small scene seen by 32 cameras of 200-1600
+    px per side, 8 shells. One batched training step (render_cameras, tile
+    shape autotuned over 8/16/32, as a CUDA graph) against the plain form that
+    renders each camera with its own call (eager), plus the images' largest
+    difference between the two."""
+    import torch
+
+    from meshtryoshka_gb300 import autotune, graph, pipeline
+    from meshtryoshka_gb300 import triangle_extraction as te
+    from meshtryoshka_gb300 import triangle_rasterization as tr
+
+    w = pipeline.build_workload("uneven", device)
+    tile, tile_ms = autotune.tune_tile_shape(w, repeats=max(3, min(steps, 10)))
+    captured = graph.CapturedTrainingStep(w)
+    batched_graph = autotune.time_ms(captured, repeats=steps)
+
+    def batched_eager():
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+        pipeline.training_step(w)
+
+    def per_camera():
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+        pipeline.per_camera_training_step(w)
+
+    eager_ms = autotune.time_ms(batched_eager, repeats=steps)
+    plain_ms = autotune.time_ms(per_camera, repeats=steps)
+    with torch.no_grad():
+        tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors,
+                                   w.voxels.lower_corners, w.voxels.upper_corners, w.voxels.indices, w.level_sets)
+        vertices = 2.0 * tri.vertices - 1.0
+        args = (vertices, tri.faces, tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics, w.sh_degree,
+                w.sharpness, w.background)
+        images = tr.render_cameras(w.extrinsics, w.intrinsics, w.image_shapes, *args, tile_shape=tile)
+        diff = 0.0
+        for b, (h, wd) in enumerate(w.image_shapes):
+            single = tr.render_fused(w.extrinsics[b:b + 1], w.intrinsics[b:b + 1], (h, wd), *args, tile_shape=tile)
+            diff = max(diff, float((single[0] - images[b]).abs().max()))
+    return {
+        "workload": f"uneven: {w.config.resolution}^3 sphere band, {w.level_sets.numel()} shells, "
+                    f"{len(w.image_shapes)} cameras of 200-1600 px per side ({w.num_pixels} pixels), "
+                    "fused fwd+bwd training step",
+        "tile": list(tile),
+        "tile_ms": {f"{a}x{b}": v for (a, b), v in tile_ms.items()},
+        "batched_graph_ms": batched_graph,
+        "batched_eager_ms": eager_ms,
+        "per_camera_eager_ms": plain_ms,
+        "speedup_vs_per_camera": plain_ms / batched_graph,
+        "max_image_diff_vs_per_camera": diff,
+    }
 
 
 def main():

@@ -30,13 +30,30 @@ class Workload:
     extrinsics: Tensor  # [B, 4, 4]
     intrinsics: Tensor  # [B, 3, 3]
     image_shape: tuple[int, int]
-    target: Tensor  # [B, 3, H, W]
+    target: Tensor  # [B, 3, H, W]; cameras of different sizes: every camera's [3, h, w] back to back
     sharpness: Tensor  # [] constant, as the trainer rebuilds it every call
     background: Tensor  # [3]
+    image_shapes: tuple[tuple[int, int], ...] | None = None  # cameras of different sizes
+    tile_shape: tuple[int, int] = (16, 16)
 
     @property
     def sh_degree(self) -> int:
         return self.config.sh_degree
+
+    def targets(self) -> list[Tensor]:
+        """Per-camera [3, h, w] targets."""
+        if self.image_shapes is None:
+            return list(self.target)
+        views, start = [], 0
+        for h, w in self.image_shapes:
+            views.append(self.target[start:start + 3 * h * w].view(3, h, w))
+            start += 3 * h * w
+        return views
+
+    @property
+    def num_pixels(self) -> int:
+        shapes = self.image_shapes or ((self.image_shape,) * self.extrinsics.shape[0])
+        return sum(h * w for h, w in shapes)
 
 
 def build_workload(name: str, device: torch.device) -> Workload:
@@ -47,9 +64,16 @@ def build_workload(name: str, device: torch.device) -> Workload:
     sdf = synthetic.corner_sdf(cfg, voxels.vertices)
     sh = synthetic.corner_sh(cfg, voxels.vertices.shape[0], device)
     cams = synthetic.make_cameras(cfg)
-    if len(set(cams.image_shapes)) != 1:
-        raise ValueError("build_workload needs one image size per camera set")
-    h, w = cams.image_shapes[0]
+    shapes = tuple(tuple(x) for x in cams.image_shapes)
+    ragged = len(set(shapes)) != 1
+    if ragged:
+        h, w = max(x[0] for x in shapes), max(x[1] for x in shapes)
+        rng = np.random.default_rng(3)
+        target = torch.from_numpy(rng.uniform(0.0, 1.0, 3 * sum(a * b for a, b in shapes)).astype(np.float32))
+        target = target.to(device)
+    else:
+        h, w = shapes[0]
+        target = synthetic.make_target(cfg.num_cameras, h, w, device)
     return Workload(
         config=cfg,
         voxels=voxels,
@@ -59,10 +83,33 @@ def build_workload(name: str, device: torch.device) -> Workload:
         extrinsics=torch.from_numpy(cams.extrinsics).to(device),
         intrinsics=torch.from_numpy(cams.intrinsics).to(device),
         image_shape=(h, w),
-        target=synthetic.make_target(cfg.num_cameras, h, w, device),
+        target=target,
         sharpness=torch.tensor(cfg.sharpness, dtype=torch.float32, device=device),
         background=torch.tensor([0.0, 0.0, 0.0], dtype=torch.float32, device=device),
+        image_shapes=shapes if ragged else None,
     )
+
+
+def _loss(w: Workload, images) -> Tensor:
+    """Mean squared error over every pixel and channel of every camera."""
+    if w.image_shapes is None:
+        return ((images - w.target) ** 2).mean()
+    total = sum(((img - tgt) ** 2).sum() for img, tgt in zip(images, w.targets()))
+    return total / (3 * w.num_pixels)
+
+
+def _render(w: Workload, tri, vertices, gradient_mode, mode="fused", **counted):
+    if w.image_shapes is not None:
+        return tr.render_cameras(w.extrinsics, w.intrinsics, w.image_shapes, vertices, tri.faces, tri.face_boundaries,
+                                 tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
+                                 tile_shape=w.tile_shape, gradient_mode=gradient_mode, **counted)
+    if counted:
+        return tr.render_fused(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
+                               tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
+                               tile_shape=w.tile_shape, gradient_mode=gradient_mode, **counted)
+    return tr.render(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
+                     tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
+                     tile_shape=w.tile_shape, mode=mode, gradient_mode=gradient_mode)
 
 
 @dataclass(frozen=True)
@@ -92,11 +139,9 @@ def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = N
         w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces)
     with torch.no_grad():
         vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
-    image = tr.render_fused(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
-                            tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
-                            gradient_mode=gradient_mode, num_faces=counts.num_faces, key_capacity=caps.keys)
+    image = _render(w, tri, vertices, gradient_mode, num_faces=counts.num_faces, key_capacity=caps.keys)
     key_count = tr.LAST_RENDER_STATS["key_count"]
-    loss = ((image - w.target) ** 2).mean()
+    loss = _loss(w, image)
     with torch.no_grad():
         overflow = ((counts.num_vertices > caps.vertices) | (counts.num_faces > caps.faces)
                     | (key_count > caps.keys))
@@ -113,10 +158,8 @@ def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
                                w.voxels.upper_corners, w.voxels.indices, w.level_sets)
     with torch.no_grad():
         vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
-    image = tr.render(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
-                      tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
-                      mode=mode, gradient_mode=gradient_mode)
-    loss = ((image - target) ** 2).mean()
+    image = _render(w, tri, vertices, gradient_mode, mode)
+    loss = _loss(w, image) if target is w.target else ((image - target) ** 2).mean()
     stats = {
         "G": int(w.voxels.lower_corners.shape[1]),
         "Nv": int(w.voxels.upper_corners.shape[1]),
@@ -125,7 +168,7 @@ def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
         "C": int(grid_sh.shape[0]),
         "S": int(w.level_sets.shape[0]),
         "B": int(w.extrinsics.shape[0]),
-        "P": int(w.extrinsics.shape[0] * w.image_shape[0] * w.image_shape[1]),
+        "P": int(w.num_pixels),
         "K": int(tr.LAST_RENDER_STATS.get("num_keys", 0)),
         "T": int(tr.LAST_RENDER_STATS.get("num_tiles", 0)),
     }
@@ -135,6 +178,27 @@ def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
 def training_step(w: Workload, mode: str = "fused", **kw) -> Tensor:
     """One forward + backward; gradients accumulate into w.grid_sdf / w.grid_sh."""
     loss, _ = forward(w, mode, **kw)
+    loss.backward()
+    return loss
+
+
+def per_camera_training_step(w: Workload, gradient_mode: str | None = None) -> Tensor:
+    """The plain form of a multi-camera step: one tessellation, then every
+    camera rendered by its own ``render_fused`` call (the reference renders
+    one image size per call), one backward. Gives the batched step's loss and
+    gradients; used as its comparison baseline."""
+    tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
+                               w.voxels.upper_corners, w.voxels.indices, w.level_sets)
+    with torch.no_grad():
+        vertices = 2.0 * tri.vertices - 1.0
+    shapes = w.image_shapes or ((w.image_shape,) * w.extrinsics.shape[0])
+    total = 0.0
+    for b, ((h, wd), target) in enumerate(zip(shapes, w.targets())):
+        image = tr.render_fused(w.extrinsics[b:b + 1], w.intrinsics[b:b + 1], (h, wd), vertices, tri.faces,
+                                tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics, w.sh_degree,
+                                w.sharpness, w.background, tile_shape=w.tile_shape, gradient_mode=gradient_mode)[0]
+        total = total + ((image - target) ** 2).sum()
+    loss = total / (3 * w.num_pixels)
     loss.backward()
     return loss
 
