@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--config", default=CONFIG_NAME)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-cameras", action="store_true", help="skip the uneven-camera batching comparison")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    p.add_argument("--serve-seconds", type=float, default=0.5, help="arrival window per request rate")
     return p.parse_args()
 
 
@@ -403,6 +405,8 @@ def run_ours(args, rank, world, local):
     }
     if not args.no_cameras and world == 1:
         line["cameras_batched"] = run_cameras(device, min(args.steps, 20))
+    if not args.no_serving and world == 1:
+        line["serving"] = run_serving(device, args.serve_seconds)
     if not args.no_cpu_baseline and world == 1:
         tess_s, render_s = cpu_sample(w, 0)
         cpu_ms = 1000.0 * (tess_s + b * render_s)
@@ -464,6 +468,44 @@ def run_cameras(device, steps):
         "per_camera_eager_ms": plain_ms,
         "speedup_vs_per_camera": plain_ms / batched_graph,
         "max_image_diff_vs_per_camera": diff,
+    }
+
+
+SERVE_RATES = (50, 200, 500, 1000, 2000)
+
+
+def run_serving(device, seconds):
+    """Serving sweep: four resident scenes (256^3 sphere x2, 128^3, 512^3; 8
+    shells), Poisson arrivals at each rate for `seconds`, 80 % render-only and
+    20 % render + gradient, images of 256-1920 x 256-1080 px. Continuous
+    batching (serving.Server) against the plain per-request form at the same
+    arrival times; p50 / p99 latency and throughput for both."""
+    import torch
+
+    from meshtryoshka_gb300 import serving
+
+    scenes = serving.default_scenes(device)
+    server = serving.Server(scenes)
+    warm = serving.poisson_requests(scenes, 500.0, 0.05, seed=99)
+    server.run(warm)
+    serving.run_plain(scenes, warm[:10])
+    torch.cuda.synchronize(device)
+    rows = []
+    for rate in SERVE_RATES:
+        window = max(seconds, 200.0 / rate)  # at least ~200 requests per rate for the p99
+        requests = serving.poisson_requests(scenes, float(rate), window, seed=4 + rate)
+        batched = serving.latency_summary(serving.Server(scenes).run(requests))
+        torch.cuda.synchronize(device)
+        plain = serving.latency_summary(serving.run_plain(scenes, requests))
+        rows.append({"rate_rps": rate, "batched": batched, "plain": plain,
+                     "p99_ratio_plain_over_batched": plain["p99_ms"] / batched["p99_ms"]})
+        del requests
+        torch.cuda.empty_cache()
+    return {
+        "workload": "4 resident scenes (sphere band 256^3 x2, 128^3, 512^3; 8 shells, SH deg 0); Poisson arrivals, "
+                    f"max({seconds} s, 200 requests) per rate; 80 % render, 20 % render+gradient (MSE vs U[0,1] "
+                    "target); images 256-1920 x 256-1080, fov 40-70",
+        "rates": rows,
     }
 
 

@@ -29,6 +29,7 @@ from torch import Tensor
 
 from . import _native as nt
 from . import pipeline
+from . import triangle_rasterization as tr
 
 
 class CapturedTrainingStep:
@@ -83,6 +84,8 @@ class CapturedTrainingStep:
                 # Gradient tensors written by every replay (graph-owned memory).
                 self.loss, self.overflow, self.grad_sdf, self.grad_sh = self._step()
         self.launches_per_replay = rec.launches
+        # Device tables the graph reads (ragged camera grids) stay alive with it.
+        self._tables = list(tr._CAMERA_TABLES.values())
 
     def __call__(self) -> Tensor:
         """Replay one step on the current stream; returns the (device) loss.

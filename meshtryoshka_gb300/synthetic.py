@@ -66,6 +66,14 @@ CONFIGS: dict[str, SceneConfig] = {
     # 512^3, 32 spheres + background sphere, SH degree 3, 16 shells, 4 x 1297x840.
     "large": SceneConfig("large", 512, 32, 0.7, (0.05, 0.25), 0.95, 2.0, 0.001, 3, _even(-0.02, 0.02, 16), 50.0,
                          "ring", 4, (840, 1297), 55.0),
+    # Resident scenes of the serving workload: the sphere scene at 256^3 (two),
+    # 128^3 and 512^3, 8 shells each; cameras come with the requests.
+    "serve_256": SceneConfig("serve_256", 256, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
+                             50.0, "front", 1, (256, 256), 60.0),
+    "serve_128": SceneConfig("serve_128", 128, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
+                             50.0, "front", 1, (256, 256), 60.0),
+    "serve_512": SceneConfig("serve_512", 512, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
+                             50.0, "front", 1, (256, 256), 60.0),
 }
 
 

@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import contextlib
 import ctypes
+from collections import OrderedDict
 from dataclasses import dataclass
 from math import prod
 from typing import Literal, NamedTuple
@@ -142,18 +143,23 @@ class TileGrid:
         return sum(4 * h * w for h, w in shapes)
 
 
-_CAMERA_TABLES: dict = {}
+_CAMERA_TABLES: "OrderedDict" = OrderedDict()
+_CAMERA_TABLES_MAX = 256
 
 
 def _camera_table(grid: TileGrid, device) -> Tensor | None:
     """Device table [B, 6] int64 (rows, cols, height, width, first tile, first
     output element) of a ragged grid; None for a uniform one. Built once per
-    grid and device, so later calls (and CUDA-graph capture) copy nothing."""
+    grid and device and kept in a bounded most-recently-used cache, so repeated
+    calls (and CUDA-graph capture) copy nothing; whoever captures a graph keeps
+    its own reference to the tables the graph reads (see graph.py)."""
     if not grid.ragged:
         return None
     key = (grid, str(device))
     table = _CAMERA_TABLES.get(key)
-    if table is None:
+    if table is not None:
+        _CAMERA_TABLES.move_to_end(key)
+    else:
         rows = []
         tile = out = 0
         for (h, w), (r, c) in zip(grid.camera_shapes, grid.camera_grids()):
@@ -162,6 +168,8 @@ def _camera_table(grid: TileGrid, device) -> Tensor | None:
             out += 4 * h * w
         table = torch.tensor(rows, dtype=torch.int64).to(device)
         _CAMERA_TABLES[key] = table
+        while len(_CAMERA_TABLES) > _CAMERA_TABLES_MAX:
+            _CAMERA_TABLES.popitem(last=False)
     return table
 
 
