@@ -182,6 +182,28 @@ MT_API int mt_create_triangle_vertices_backward(
     float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
     mt_stream_t stream);
 
+/* triangle_extraction/compute_sdf_regularizers.slang:18-128 (forward) and its
+ * automatic derivative (backward). Per voxel: eikonal_loss_pos / _neg [Nv]
+ * (squared excess / deficit of the trilinear SDF's gradient norm at the
+ * voxel centre, scaled by the grid size voxel_x/y/z, over 1) and
+ * curvature_loss [Nv] (squared Laplacian at the +xyz corner). The backward
+ * writes (=) every entry of grad_grid_signed_distances [G]; any of the three
+ * input gradients may be NULL (zero). */
+MT_API int mt_compute_sdf_regularizers(
+    const float* grid_signed_distances, const int32_t* voxel_neighbors,
+    const int32_t* voxel_lower_corners, int64_t G, const int32_t* voxel_upper_corners,
+    int64_t Nv, int32_t voxel_x, int32_t voxel_y, int32_t voxel_z,
+    float* eikonal_loss_pos, float* eikonal_loss_neg, float* curvature_loss,
+    mt_stream_t stream);
+
+MT_API int mt_compute_sdf_regularizers_backward(
+    const float* grid_signed_distances, const int32_t* voxel_neighbors,
+    const int32_t* voxel_lower_corners, int64_t G, const int32_t* voxel_upper_corners,
+    int64_t Nv, int32_t voxel_x, int32_t voxel_y, int32_t voxel_z,
+    const float* grad_eikonal_loss_pos, const float* grad_eikonal_loss_neg,
+    const float* grad_curvature_loss, float* grad_grid_signed_distances,
+    mt_stream_t stream);
+
 /* triangle_extraction/count_triangle_faces.slang:15-50.
  * face_counts: S*Nv+1 int32 (3 x triangles; last entry 0);
  * cell_codes: [S, Nv] uint8 cube codes. */
@@ -322,6 +344,13 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
  * H / W the maxima, and keys carry the camera-local tile index.
  * work_counter: one uint64 of device scratch (reset here): the kernel's
  * persistent warps pull (camera, tile, warp) work items from it.
+ * Optional MSE epilogue (not in the reference, where the trainer blends,
+ * clips and takes the loss with separate tensor ops): with target != NULL
+ * ([B,3,H,W], or each camera's [3,h,w] back to back for ragged cameras) and
+ * background [3], the forward also sets the device scalar *loss_sum =
+ * loss_scale x sum over pixels and channels of
+ * (clip(rgb + T * background, 0, 1) - target)^2, and the backward takes
+ * d L / d loss from the device scalar grad_loss instead of grad_out.
  * ---------------------------------------------------------------------- */
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
@@ -330,7 +359,8 @@ MT_API int mt_intersect_and_composite_forward(
     const int64_t* tile_boundaries, int32_t B, int32_t num_shells, int32_t rows,
     int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H, int32_t W,
     const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
-    uint32_t* warp_masks, uint64_t* work_counter, float* out, mt_stream_t stream);
+    uint32_t* warp_masks, uint64_t* work_counter, float* out, const float* target,
+    const float* background, float loss_scale, float* loss_sum, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
@@ -345,8 +375,9 @@ MT_API int mt_intersect_and_composite_backward(
     int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
     const int64_t* cameras, int64_t camera_tiles, const uint32_t* warp_masks,
     uint64_t* work_counter, const float* out, const float* grad_out,
-    float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
-    int32_t exact_adjoint, mt_stream_t stream);
+    const float* target, const float* background, float loss_scale,
+    const float* grad_loss, float* grad_colors, float* grad_signed_distances,
+    float* grad_sharpness, int32_t exact_adjoint, mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Explicit mode (triangle_rasterization/__init__.py:22-164).

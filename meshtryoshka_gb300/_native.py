@@ -51,6 +51,8 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P, P],
     ),
     "mt_count_triangle_faces": (I32, [P, P, I64, P, I64, P, I32, P, P, P]),
+    "mt_compute_sdf_regularizers": (I32, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P, P]),
+    "mt_compute_sdf_regularizers_backward": (I32, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P, P, P]),
     "mt_create_triangle_faces": (
         I32,
         [P, P, I64, I64, I64, P, P, P, I32, P, I64, P, P, P],
@@ -66,12 +68,13 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_delineate_tiles": (I32, [P, I64, P, P, I32, I32, I32, I64, P, P]),
     "mt_intersect_and_composite_forward": (
         I32,
-        [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P],
+        [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
+         c_float, P, P],
     ),
     "mt_intersect_and_composite_backward": (
         I32,
-        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P, P, I32,
-         P],
+        [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P,
+         c_float, P, P, P, P, I32, P],
     ),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),

@@ -71,9 +71,17 @@ struct CompositeArgs {
   // order. rows / cols / H / W are then the maxima over cameras.
   const int64_t* cameras;
   int64_t total_tiles;  // tiles over all cameras
+  // Optional MSE epilogue (target NULL: none). The image is
+  // clip(rgb + T * background, 0, 1) as the render entry points form it; the
+  // target holds each camera's [3, h, w] at 3/4 of its first output element;
+  // the loss is loss_scale x the sum of squared errors.
+  const float* target;
+  const float* background;
+  float loss_scale;
 };
 
 struct CompositeGrads {
+  const float* grad_loss;  // with the epilogue: d L / d loss (device scalar)
   const float* grad_out;  // [B, 4, H, W]
   float* grad_colors;     // [B, V, 3]
   float* grad_sdf;        // [V]
@@ -308,8 +316,22 @@ __device__ __forceinline__ int64_t next_item(unsigned long long* counter, int la
   return (int64_t)__shfl_sync(0xffffffffu, item, 0);
 }
 
-__device__ __forceinline__ void forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
-                                             float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane) {
+// Background blend and clip of the render entry points (images[:, :3] +
+// images[:, 3:4] * background, then clip to [0, 1]); `inside` is clip's
+// pass-through test (inclusive, as torch's clamp backward).
+__device__ __forceinline__ float blend_clip(float rgb, float T, float bg, bool& inside) {
+  const float x = __fadd_rn(rgb, __fmul_rn(T, bg));
+  inside = x >= 0.0f && x <= 1.0f;
+  return fminf(fmaxf(x, 0.0f), 1.0f);
+}
+
+__device__ __forceinline__ const float* target_of(const CompositeArgs& a, const Pixel& px) {
+  return a.target + px.out_base / 4 * 3 + (int64_t)px.py * px.width + px.px;
+}
+
+// Returns the pixel's sum of squared errors when the epilogue is on.
+__device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
+                                              float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -361,25 +383,42 @@ __device__ __forceinline__ void forward_item(const CompositeArgs& a, const uint3
     }
     __syncwarp();
   }
+  float sq = 0.0f;
   if (px.in_image) {
     float* o = out + px.out_base + (int64_t)px.py * px.width + px.px;
     o[0] = acc[0];
     o[px.plane] = acc[1];
     o[2 * px.plane] = acc[2];
     o[3 * px.plane] = T_;
+    if (a.target) {
+      const float* tg = target_of(a, px);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        bool inside;
+        const float d = blend_clip(acc[c], T_, a.background[c], inside) - tg[c * px.plane];
+        sq += d * d;
+      }
+    }
   }
   __syncwarp();
+  return sq;
 }
 
 __global__ void __launch_bounds__(kCtaThreads)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
-                             unsigned long long* __restrict__ counter) {
+                             unsigned long long* __restrict__ counter, float* __restrict__ loss_sum) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
+  float sq = 0.0f;
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    forward_item(a, masks, out, ws, pixel_of(a, item), lane);
+    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane);
+  if (a.target) {  // one atomic per warp for the whole launch
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (lane == 0 && sq != 0.0f) atomicAdd(loss_sum, sq * a.loss_scale);
+  }
 }
 
 __device__ __forceinline__ void scatter_global(const CompositeArgs& a, const CompositeGrads& gr, int cam, int3 vid,
@@ -441,12 +480,26 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
   if (px.in_image) {
     const int64_t o = px.out_base + (int64_t)px.py * px.width + px.px;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      final_rgb[c] = a.out[o + c * px.plane];
-      dL_rgb[c] = gr.grad_out[o + c * px.plane];
-    }
+    for (int c = 0; c < 3; ++c) final_rgb[c] = a.out[o + c * px.plane];
     final_T = a.out[o + 3 * px.plane];
-    dL_T = gr.grad_out[o + 3 * px.plane];
+    if (a.target) {
+      // d loss / d image = 2 (image - target) loss_scale, through the clip
+      // and the background blend.
+      const float gscale = 2.0f * a.loss_scale * *gr.grad_loss;
+      const float* tg = target_of(a, px);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        bool inside;
+        const float img = blend_clip(final_rgb[c], final_T, a.background[c], inside);
+        const float g = inside ? gscale * (img - tg[c * px.plane]) : 0.0f;
+        dL_rgb[c] = g;
+        dL_T += g * a.background[c];
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dL_rgb[c] = gr.grad_out[o + c * px.plane];
+      dL_T = gr.grad_out[o + 3 * px.plane];
+    }
   }
   for (int i = lane; i < kRing * 13; i += 32) (&ws.gslot[0][0])[i] = 0.f;
   ws.vids[lane] = make_int3(0, 0, 0);
@@ -628,6 +681,9 @@ CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, 
                         int32_t W, const int32_t* layout, const float* out, const int64_t* cameras,
                         int64_t camera_tiles) {
   CompositeArgs a{};
+  a.target = nullptr;
+  a.background = nullptr;
+  a.loss_scale = 0.0f;
   a.cameras = cameras;
   a.total_tiles = cameras ? camera_tiles : (int64_t)B * rows * cols;
   a.xy = xy;
@@ -671,17 +727,24 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        int32_t num_shells, int32_t rows, int32_t cols, int32_t tile_h,
                                        int32_t tile_w, int32_t H, int32_t W, const int32_t* layout,
                                        const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
-                                       uint64_t* work_counter, float* out, mt_stream_t stream) {
+                                       uint64_t* work_counter, float* out, const float* target,
+                                       const float* background, float loss_scale, float* loss_sum,
+                                       mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
                               cameras, camera_tiles);
+  a.target = target;
+  a.background = background;
+  a.loss_scale = loss_scale;
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
+  MT_REQUIRE(target == nullptr || (background && loss_sum));
+  cudaStream_t s = as_stream(stream);
+  if (target && cudaMemsetAsync(loss_sum, 0, sizeof(float), s) != cudaSuccess) return MT_ERR_CUDA;
   if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
-  cudaStream_t s = as_stream(stream);
   if (K > 0) {
     warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
     MT_CHECK_LAUNCH();
@@ -694,7 +757,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   composite_forward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter));
+      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -706,20 +769,25 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
                                         int32_t W, const int32_t* layout, const int64_t* cameras,
                                         int64_t camera_tiles, const uint32_t* warp_masks, uint64_t* work_counter,
-                                        const float* out, const float* grad_out, float* grad_colors,
-                                        float* grad_signed_distances, float* grad_sharpness, int32_t exact_adjoint,
-                                        mt_stream_t stream) {
+                                        const float* out, const float* grad_out, const float* target,
+                                        const float* background, float loss_scale, const float* grad_loss,
+                                        float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
+                                        int32_t exact_adjoint, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out,
                               cameras, camera_tiles);
+  a.target = target;
+  a.background = background;
+  a.loss_scale = loss_scale;
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
   if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
-  MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && grad_out);
+  MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out);
+  MT_REQUIRE(target ? (background && grad_loss) : grad_out != nullptr);
   MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
-  CompositeGrads gr{grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
+  CompositeGrads gr{grad_loss, grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
   const size_t smem = sizeof(WarpBackward) * kWarpsPerCta;
   cudaStream_t s = as_stream(stream);
   rc = set_smem<composite_backward_kernel>(smem);

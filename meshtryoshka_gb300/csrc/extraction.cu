@@ -642,6 +642,155 @@ __global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const
   }
 }
 
+// ---------------------------------------------------------------------------
+// triangle_extraction/compute_sdf_regularizers.slang:18-128. Per voxel: the
+// Eikonal terms of the trilinear SDF's gradient at the voxel centre (grid
+// units) and a Laplacian curvature term at its +xyz corner. The operation
+// order is the reference's (this unit is compiled without contraction).
+// ---------------------------------------------------------------------------
+struct VoxelCorners {
+  int32_t i000, i001, i010, i100, i111, i110, i101, i011;  // grid vertex ids
+  float d000, d001, d010, d100, d111, d110, d101, d011;
+};
+
+__device__ __forceinline__ VoxelCorners load_voxel_corners(const float* __restrict__ sdf,
+                                                           const int32_t* __restrict__ lower, int64_t G,
+                                                           const int32_t* __restrict__ upper, int64_t Nv, int64_t v) {
+  VoxelCorners c;
+  c.i000 = __ldg(lower + v);
+  c.i001 = __ldg(lower + G + v);
+  c.i010 = __ldg(lower + 2 * G + v);
+  c.i100 = __ldg(lower + 3 * G + v);
+  c.i111 = __ldg(upper + v);
+  c.i110 = __ldg(upper + Nv + v);
+  c.i101 = __ldg(upper + 2 * Nv + v);
+  c.i011 = __ldg(upper + 3 * Nv + v);
+  c.d000 = __ldg(sdf + c.i000);
+  c.d001 = __ldg(sdf + c.i001);
+  c.d010 = __ldg(sdf + c.i010);
+  c.d100 = __ldg(sdf + c.i100);
+  c.d111 = __ldg(sdf + c.i111);
+  c.d110 = __ldg(sdf + c.i110);
+  c.d101 = __ldg(sdf + c.i101);
+  c.d011 = __ldg(sdf + c.i011);
+  return c;
+}
+
+// Trilinear gradient at (0.5, 0.5, 0.5): weights (1 - t)(1 - t), t(1 - t), ...
+// are all 0.25; the sums keep the reference's association.
+__device__ __forceinline__ void centre_gradient(const VoxelCorners& c, float& dx, float& dy, float& dz) {
+  const float t = 0.5f, t1 = 1.0f - t;
+  const float w11 = t1 * t1, w01 = t * t1, w10 = t1 * t, w00 = t * t;
+  dx = w11 * (c.d001 - c.d000) + w01 * (c.d011 - c.d010) + w10 * (c.d101 - c.d100) + w00 * (c.d111 - c.d110);
+  dy = w11 * (c.d010 - c.d000) + w01 * (c.d011 - c.d001) + w10 * (c.d110 - c.d100) + w00 * (c.d111 - c.d101);
+  dz = w11 * (c.d100 - c.d000) + w01 * (c.d101 - c.d001) + w10 * (c.d110 - c.d010) + w00 * (c.d111 - c.d011);
+}
+
+// stable_norm of compute_sdf_regularizers.slang:3-16.
+__device__ __forceinline__ float stable_norm(float a, float b, float c) {
+  const float scale = fmaxf(fmaxf(fabsf(a), fabsf(b)), fabsf(c));
+  if (scale < 1e-10f) return 0.0f;
+  const float inv = 1.0f / scale;
+  const float sa = inv * a, sb = inv * b, sc = inv * c;
+  return scale * sqrtf(sa * sa + sb * sb + sc * sc);
+}
+
+// Curvature sum: +yz, +xz, +xy corners, the present lower corners (+x, +y,
+// +z) of the +xyz neighbour entry, minus (count) x the +xyz corner.
+__device__ __forceinline__ float curvature_sum(const float* __restrict__ sdf, const VoxelCorners& c,
+                                               const int32_t* __restrict__ lower, int64_t G, int32_t sub,
+                                               int32_t (&extra)[3], int& counted) {
+  float sum = c.d110 + c.d101 + c.d011;
+  counted = 3;
+#pragma unroll
+  for (int i = 1; i < 4; ++i) {
+    const int32_t corner = __ldg(lower + (int64_t)i * G + sub);
+    extra[i - 1] = corner;
+    if (corner >= 0) {
+      sum += __ldg(sdf + corner);
+      ++counted;
+    }
+  }
+  return sum - (float)counted * c.d111;
+}
+
+__global__ void sdf_regularizers_kernel(const float* __restrict__ sdf, const int32_t* __restrict__ neighbors,
+                                        const int32_t* __restrict__ lower, int64_t G,
+                                        const int32_t* __restrict__ upper, int64_t Nv, int vx, int vy, int vz,
+                                        float* __restrict__ eik_pos, float* __restrict__ eik_neg,
+                                        float* __restrict__ curv) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const VoxelCorners c = load_voxel_corners(sdf, lower, G, upper, Nv, v);
+    float dx, dy, dz;
+    centre_gradient(c, dx, dy, dz);
+    const float delta = stable_norm((float)vx * dx, (float)vy * dy, (float)vz * dz) - 1.0f;
+    float pos = 0.0f, neg = 0.0f;
+    if (delta < 0.0f) neg += delta * delta;
+    if (delta > 0.0f) pos += delta * delta;
+    eik_pos[v] = pos / 1.0f;
+    eik_neg[v] = neg / 1.0f;
+    int32_t extra[3];
+    int counted;
+    const float cs = curvature_sum(sdf, c, lower, G, __ldg(neighbors + 6 * Nv + v), extra, counted);
+    curv[v] = cs * cs;
+  }
+}
+
+// Adjoint (the reference differentiates the kernel automatically): with
+// n = |(a, b, c)| and delta = n - 1, d delta / d a = a / n (0 when n is 0);
+// each loss's gradient is scattered to the corners it reads.
+__global__ void sdf_regularizers_backward_kernel(const float* __restrict__ sdf,
+                                                 const int32_t* __restrict__ neighbors,
+                                                 const int32_t* __restrict__ lower, int64_t G,
+                                                 const int32_t* __restrict__ upper, int64_t Nv, int vx, int vy,
+                                                 int vz, const float* __restrict__ g_pos,
+                                                 const float* __restrict__ g_neg, const float* __restrict__ g_curv,
+                                                 float* __restrict__ grad_sdf) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const VoxelCorners c = load_voxel_corners(sdf, lower, G, upper, Nv, v);
+    float dx, dy, dz;
+    centre_gradient(c, dx, dy, dz);
+    const float a = (float)vx * dx, b = (float)vy * dy, cc = (float)vz * dz;
+    const float n = stable_norm(a, b, cc);
+    const float delta = n - 1.0f;
+    float g_delta = 0.0f;
+    if (g_pos && delta > 0.0f) g_delta += 2.0f * delta * g_pos[v];
+    if (g_neg && delta < 0.0f) g_delta += 2.0f * delta * g_neg[v];
+    float gd[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // 000 001 010 100 111 110 101 011
+    if (g_delta != 0.0f && n > 0.0f) {
+      const float gx = g_delta * a / n * (float)vx, gy = g_delta * b / n * (float)vy,
+                  gz = g_delta * cc / n * (float)vz;
+      const float w = 0.25f;
+      // dx: +(001, 011, 101, 111), -(000, 010, 100, 110)
+      gd[1] += w * gx; gd[7] += w * gx; gd[6] += w * gx; gd[4] += w * gx;
+      gd[0] -= w * gx; gd[2] -= w * gx; gd[3] -= w * gx; gd[5] -= w * gx;
+      // dy: +(010, 011, 110, 111), -(000, 001, 100, 101)
+      gd[2] += w * gy; gd[7] += w * gy; gd[5] += w * gy; gd[4] += w * gy;
+      gd[0] -= w * gy; gd[1] -= w * gy; gd[3] -= w * gy; gd[6] -= w * gy;
+      // dz: +(100, 101, 110, 111), -(000, 001, 010, 011)
+      gd[3] += w * gz; gd[6] += w * gz; gd[5] += w * gz; gd[4] += w * gz;
+      gd[0] -= w * gz; gd[1] -= w * gz; gd[2] -= w * gz; gd[7] -= w * gz;
+    }
+    int32_t extra[3];
+    int counted;
+    const float cs = curvature_sum(sdf, c, lower, G, __ldg(neighbors + 6 * Nv + v), extra, counted);
+    const float g_cs = g_curv ? 2.0f * cs * g_curv[v] : 0.0f;
+    if (g_cs != 0.0f) {
+      gd[5] += g_cs;
+      gd[6] += g_cs;
+      gd[7] += g_cs;
+      gd[4] -= (float)counted * g_cs;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        if (extra[i] >= 0) atomicAdd(grad_sdf + extra[i], g_cs);
+    }
+    const int32_t ids[8] = {c.i000, c.i001, c.i010, c.i100, c.i111, c.i110, c.i101, c.i011};
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (gd[q] != 0.0f) atomicAdd(grad_sdf + ids[q], gd[q]);
+  }
+}
+
 }  // namespace
 }  // namespace mt
 
@@ -789,6 +938,41 @@ int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, i
   create_faces_kernel<<<grid_stride_blocks(Nv, 128), 128, 0, as_stream(stream)>>>(
       neighbors, indices, Nv, G, V, vertex_offsets, vertex_types, cell_codes, S, face_offsets, F, faces,
       voxel_indices);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_compute_sdf_regularizers(const float* grid_signed_distances, const int32_t* voxel_neighbors,
+                                const int32_t* voxel_lower_corners, int64_t G, const int32_t* voxel_upper_corners,
+                                int64_t Nv, int32_t voxel_x, int32_t voxel_y, int32_t voxel_z,
+                                float* eikonal_loss_pos, float* eikonal_loss_neg, float* curvature_loss,
+                                mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && Nv >= 0);
+  if (Nv == 0) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && voxel_neighbors && voxel_lower_corners && voxel_upper_corners &&
+             eikonal_loss_pos && eikonal_loss_neg && curvature_loss);
+  sdf_regularizers_kernel<<<grid_stride_blocks(Nv, 256), 256, 0, as_stream(stream)>>>(
+      grid_signed_distances, voxel_neighbors, voxel_lower_corners, G, voxel_upper_corners, Nv, voxel_x, voxel_y,
+      voxel_z, eikonal_loss_pos, eikonal_loss_neg, curvature_loss);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_compute_sdf_regularizers_backward(const float* grid_signed_distances, const int32_t* voxel_neighbors,
+                                         const int32_t* voxel_lower_corners, int64_t G,
+                                         const int32_t* voxel_upper_corners, int64_t Nv, int32_t voxel_x,
+                                         int32_t voxel_y, int32_t voxel_z, const float* grad_eikonal_loss_pos,
+                                         const float* grad_eikonal_loss_neg, const float* grad_curvature_loss,
+                                         float* grad_grid_signed_distances, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && Nv >= 0 && grad_grid_signed_distances);
+  cudaStream_t st = as_stream(stream);
+  if (G > 0 && cudaMemsetAsync(grad_grid_signed_distances, 0, (size_t)G * sizeof(float), st) != cudaSuccess)
+    return MT_ERR_CUDA;
+  if (Nv == 0) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && voxel_neighbors && voxel_lower_corners && voxel_upper_corners);
+  sdf_regularizers_backward_kernel<<<grid_stride_blocks(Nv, 256), 256, 0, st>>>(
+      grid_signed_distances, voxel_neighbors, voxel_lower_corners, G, voxel_upper_corners, Nv, voxel_x, voxel_y,
+      voxel_z, grad_eikonal_loss_pos, grad_eikonal_loss_neg, grad_curvature_loss, grad_grid_signed_distances);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

@@ -35,6 +35,7 @@ class Workload:
     background: Tensor  # [3]
     image_shapes: tuple[tuple[int, int], ...] | None = None  # cameras of different sizes
     tile_shape: tuple[int, int] = (16, 16)
+    fused_loss: bool = True  # fused render: blend, clip and MSE inside the compositing kernels
 
     @property
     def sh_degree(self) -> int:
@@ -98,6 +99,13 @@ def _loss(w: Workload, images) -> Tensor:
     return total / (3 * w.num_pixels)
 
 
+def _fused_loss(w: Workload, tri, vertices, gradient_mode, **counted) -> Tensor:
+    return tr.render_fused_loss(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
+                                tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness,
+                                w.background, w.target, tile_shape=w.tile_shape, gradient_mode=gradient_mode,
+                                camera_shapes=w.image_shapes, **counted)
+
+
 def _render(w: Workload, tri, vertices, gradient_mode, mode="fused", **counted):
     if w.image_shapes is not None:
         return tr.render_cameras(w.extrinsics, w.intrinsics, w.image_shapes, vertices, tri.faces, tri.face_boundaries,
@@ -139,9 +147,12 @@ def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = N
         w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces)
     with torch.no_grad():
         vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
-    image = _render(w, tri, vertices, gradient_mode, num_faces=counts.num_faces, key_capacity=caps.keys)
+    counted = dict(num_faces=counts.num_faces, key_capacity=caps.keys)
+    if w.fused_loss:
+        loss = _fused_loss(w, tri, vertices, gradient_mode, **counted)
+    else:
+        loss = _loss(w, _render(w, tri, vertices, gradient_mode, **counted))
     key_count = tr.LAST_RENDER_STATS["key_count"]
-    loss = _loss(w, image)
     with torch.no_grad():
         overflow = ((counts.num_vertices > caps.vertices) | (counts.num_faces > caps.faces)
                     | (key_count > caps.keys))
@@ -158,8 +169,11 @@ def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
                                w.voxels.upper_corners, w.voxels.indices, w.level_sets)
     with torch.no_grad():
         vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
-    image = _render(w, tri, vertices, gradient_mode, mode)
-    loss = _loss(w, image) if target is w.target else ((image - target) ** 2).mean()
+    if mode == "fused" and w.fused_loss and target is w.target:
+        loss = _fused_loss(w, tri, vertices, gradient_mode)
+    else:
+        image = _render(w, tri, vertices, gradient_mode, mode)
+        loss = _loss(w, image) if target is w.target else ((image - target) ** 2).mean()
     stats = {
         "G": int(w.voxels.lower_corners.shape[1]),
         "Nv": int(w.voxels.upper_corners.shape[1]),

@@ -28,6 +28,8 @@ __all__ = [
     "Triangles",
     "extract_voxels",
     "tessellate_voxels",
+    "compute_sdf_regularizers",
+    "SDFRegularizerLosses",
     "pack_occupancy",
     "unpack_occupancy",
     "dilate_occupancy",
@@ -427,6 +429,62 @@ class Triangles(NamedTuple):
     voxel_indices: Tensor  # [face] int32
     vertex_boundaries: Tensor  # [level_set] int32 (cumulative ends)
     face_boundaries: Tensor  # [level_set] int32 (cumulative ends)
+
+
+# ---------------------------------------------------------------------------
+# SDF regularizers (triangle_extraction/compute_sdf_regularizers.py:21-150)
+# ---------------------------------------------------------------------------
+class SDFRegularizerLosses(NamedTuple):
+    eikonal_loss_pos: Tensor  # [voxel]
+    eikonal_loss_neg: Tensor  # [voxel]
+    curvature_loss: Tensor  # [voxel]
+
+
+class ComputeSDFRegularizers(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, grid_signed_distances, voxel_neighbors, voxel_lower_corners, voxel_upper_corners, grid_size):
+        with record_function("compute_sdf_regularizers_forward"):
+            sdf = _f32(grid_signed_distances, "grid_signed_distances")
+            neighbors = _i32(voxel_neighbors, "voxel_neighbors")
+            lower, upper = _i32(voxel_lower_corners, "voxel_lower_corners"), _i32(voxel_upper_corners,
+                                                                                 "voxel_upper_corners")
+            device = nt.require_cuda(sdf, neighbors, lower, upper)
+            _, g = lower.shape
+            _, nv = upper.shape
+            i, j, k = (int(x) for x in grid_size)
+            kw = dict(dtype=torch.float32, device=device)
+            pos, neg, curv = torch.empty((nv,), **kw), torch.empty((nv,), **kw), torch.empty((nv,), **kw)
+            nt.call("mt_compute_sdf_regularizers", nt.ptr(sdf), nt.ptr(neighbors), nt.ptr(lower), g, nt.ptr(upper),
+                    nv, k, j, i, nt.ptr(pos), nt.ptr(neg), nt.ptr(curv), nt.stream(device))
+            ctx.save_for_backward(sdf, neighbors, lower, upper)
+            ctx.grid_size = (i, j, k)
+            ctx.set_materialize_grads(False)
+            return pos, neg, curv
+
+    @staticmethod
+    def backward(ctx, grad_pos, grad_neg, grad_curv):
+        with record_function("compute_sdf_regularizers_backward"):
+            sdf, neighbors, lower, upper = ctx.saved_tensors
+            i, j, k = ctx.grid_size
+            _, g = lower.shape
+            _, nv = upper.shape
+            grad = torch.empty_like(sdf)  # fully written
+            gp = grad_pos.contiguous() if grad_pos is not None else None
+            gn = grad_neg.contiguous() if grad_neg is not None else None
+            gc = grad_curv.contiguous() if grad_curv is not None else None
+            nt.call("mt_compute_sdf_regularizers_backward", nt.ptr(sdf), nt.ptr(neighbors), nt.ptr(lower), g,
+                    nt.ptr(upper), nv, k, j, i, nt.ptr(gp), nt.ptr(gn), nt.ptr(gc), nt.ptr(grad),
+                    nt.stream(sdf.device))
+            return grad, None, None, None, None
+
+
+def compute_sdf_regularizers(grid_signed_distances: Tensor, voxel_neighbors: Tensor, voxel_lower_corners: Tensor,
+                             voxel_upper_corners: Tensor, grid_size: tuple[int, int, int]) -> SDFRegularizerLosses:
+    """Eikonal (split by sign) and curvature regularizers per voxel; grid_size
+    is the voxel grid's (i, j, k) extent (the Eikonal gradient is scaled by
+    (k, j, i) along (x, y, z))."""
+    return SDFRegularizerLosses(*ComputeSDFRegularizers.apply(
+        grid_signed_distances, voxel_neighbors, voxel_lower_corners, voxel_upper_corners, grid_size))
 
 
 class TessellationCounts(NamedTuple):

@@ -36,6 +36,8 @@ __all__ = [
     "render_fused",
     "render_cameras",
     "split_cameras",
+    "render_fused_loss",
+    "IntersectCompositeLoss",
     "render_explicit",
     "rasterize",
     "TileGrid",
@@ -433,8 +435,8 @@ class IntersectAndComposite(torch.autograd.Function):
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
-                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out),
-                    nt.stream(device))
+                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
+                    0.0, None, nt.stream(device))
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness))
@@ -458,10 +460,75 @@ class IntersectAndComposite(torch.autograd.Function):
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
-                    nt.ptr(out), nt.ptr(grad_out), nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp),
-                    int(mode == "exact"), nt.stream(device))
+                    nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, nt.ptr(grad_colors), nt.ptr(grad_sdf),
+                    nt.ptr(grad_sharp), int(mode == "exact"), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
+
+
+class IntersectCompositeLoss(torch.autograd.Function):
+    """Fused compositing with the MSE epilogue in the same kernels (not in the
+    reference): returns mean((clip(rgb + T * background, 0, 1) - target)^2)
+    over every pixel and channel; the image is never materialised and the
+    backward forms d loss / d (rgb, T) inside the compositing adjoint."""
+
+    @staticmethod
+    def forward(ctx, vertices, colors, signed_distances, faces, sharpness, sorted_keys, sorted_triangle_indices,
+                tile_boundaries, num_shells, grid, key_defines, target, background, gradient_mode=None,
+                num_keys=None):
+        with record_function("intersect_composite_loss_forward"):
+            xy, colors, sdf, faces = _f32(vertices), _f32(colors), _f32(signed_distances), _i32(faces)
+            target, background = _f32(target), _f32(background)
+            device = nt.require_cuda(xy, colors, sdf, faces, target, background)
+            sharp = _sharpness(sharpness, device)
+            keys, tri = sorted_keys.contiguous(), _i32(sorted_triangle_indices)
+            bounds = tile_boundaries.contiguous()
+            b, v, _ = xy.shape
+            k = keys.numel()
+            h, w = grid.image_shape
+            rows, cols = grid.grid_shape
+            if target.numel() * 4 != grid.output_numel * 3:
+                raise ValueError("target must hold 3 channels of every camera's image")
+            masks = torch.empty((k,), dtype=torch.int32, device=device)
+            counter = torch.empty((1,), dtype=torch.int64, device=device)
+            table = _camera_table(grid, device)
+            out = torch.empty((grid.output_numel,) if grid.ragged else (b, 4, h, w), dtype=torch.float32,
+                              device=device)
+            loss = torch.empty((), dtype=torch.float32, device=device)
+            scale = 1.0 / target.numel()
+            nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
+                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
+                    int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
+                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), nt.ptr(target),
+                    nt.ptr(background), scale, loss.data_ptr(), nt.stream(device))
+            ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background)
+            ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
+                        torch.is_tensor(sharpness), scale)
+            return loss
+
+    @staticmethod
+    def backward(ctx, grad_loss):
+        with record_function("intersect_composite_loss_backward"):
+            xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background = ctx.saved_tensors
+            num_shells, grid, key_defines, mode, sharp_is_tensor, scale = ctx.meta
+            device = xy.device
+            grad_loss = grad_loss.to(torch.float32).contiguous()
+            grad_colors = torch.zeros_like(colors)
+            grad_sdf = torch.zeros_like(sdf)
+            grad_sharp = torch.zeros_like(sharp)
+            b, v, _ = xy.shape
+            h, w = grid.image_shape
+            rows, cols = grid.grid_shape
+            counter = torch.empty((1,), dtype=torch.int64, device=device)
+            nt.call("mt_intersect_and_composite_backward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
+                    nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
+                    num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
+                    nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
+                    nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(),
+                    nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp), int(mode == "exact"),
+                    nt.stream(device))
+            return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
+                    None, None, None, None, None, None, None)
 
 
 def intersect_and_composite(vertices, colors, signed_distances, faces, sharpness, sorted_keys,
@@ -729,6 +796,45 @@ def render_cameras(extrinsics, intrinsics, image_shapes, vertices, faces, shell_
                                   gradient_mode, paired.count)
     bg = background[:, None, None]
     return [(r[:3] + r[3:4] * bg).clip(min=0, max=1) for r in split_cameras(raw, grid)]
+
+
+@record_function("render_fused_loss")
+def render_fused_loss(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, signed_distances,
+                      spherical_harmonics, sh_degree, sharpness, background, target, tile_shape=(16, 16),
+                      near_plane=0.2, num_camera_bits=6, num_shell_bits=6, num_tile_bits=20, gradient_mode=None,
+                      num_faces: Tensor | None = None, key_capacity: int | None = None,
+                      camera_shapes=None) -> Tensor:
+    """mean((render_fused(...) - target)^2) with the background blend, clip and
+    MSE inside the compositing kernels (not in the reference, where the
+    trainer applies them as separate tensor ops). Same loss and gradients as
+    the unfused composition. target: [B, 3, H, W]; with ``camera_shapes``
+    (one (h, w) per camera, as ``render_cameras``) every camera's [3, h, w]
+    back to back. SSAA is not part of this form."""
+    b = extrinsics.shape[0]
+    (s,) = shell_face_boundaries.shape
+    grid = (TileGrid.for_cameras(tile_shape, camera_shapes, s) if camera_shapes is not None
+            else TileGrid(tuple(tile_shape), tuple(image_shape), b, s))
+    if vertices.numel() == 0 or faces.numel() == 0:
+        if camera_shapes is None:
+            image = background.reshape(1, 3, 1, 1).expand(b, 3, *image_shape)
+            return ((image - target) ** 2).mean()
+        images = torch.cat([background.reshape(3, 1).expand(3, h * w).reshape(-1) for h, w in grid.camera_shapes])
+        return ((images - target) ** 2).mean()
+    key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
+                                     ("shell", num_shell_bits))
+    positions, depths = project_vertices(vertices, extrinsics, intrinsics)
+    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
+    paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
+                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
+    del bounds, depths
+    LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
+    paired = sort_keys(paired, grid)
+    tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
+    colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
+    t = tile_boundaries.shape[2]
+    return IntersectCompositeLoss.apply(positions, colors, signed_distances, faces, sharpness, paired.keys,
+                                        paired.triangle_indices, tile_boundaries.view(b, t, 2), s, grid, key_defines,
+                                        target, background, gradient_mode, paired.count)
 
 
 def render(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, signed_distances,

@@ -50,6 +50,7 @@ SOURCES = {
     ("triangle_extraction", "create_triangle_vertices.slang"): ["create_triangle_vertices_backward"],
     ("triangle_extraction", "count_triangle_faces.slang"): [],
     ("triangle_extraction", "create_triangle_faces.slang"): [],
+    ("triangle_extraction", "compute_sdf_regularizers.slang"): [],
     ("triangle_rasterization", "keys.slang"): [],
     ("triangle_rasterization", "project_vertices.slang"): [],
     ("triangle_rasterization", "bound_triangles.slang"): [],

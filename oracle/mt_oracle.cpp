@@ -309,6 +309,120 @@ void or_create_voxels(const int32_t* occ, const int32_t* xoff, const int32_t* vo
 }
 
 // ---------------------------------------------------------------------------
+// triangle_extraction/compute_sdf_regularizers.slang:18-128 (forward) and its
+// automatic derivative (backward, derived here by hand).
+// ---------------------------------------------------------------------------
+namespace {
+struct RegCorners {
+  int32_t id[8];  // 000 001 010 100 111 110 101 011
+  float d[8];
+};
+
+inline RegCorners reg_corners(const float* sdf, const int32_t* lower, int64_t G, const int32_t* upper, int64_t Nv,
+                              int64_t v) {
+  RegCorners c;
+  const int32_t ids[8] = {lower[v], lower[G + v], lower[2 * G + v], lower[3 * G + v],
+                          upper[v], upper[Nv + v], upper[2 * Nv + v], upper[3 * Nv + v]};
+  for (int q = 0; q < 8; ++q) {
+    c.id[q] = ids[q];
+    c.d[q] = sdf[ids[q]];
+  }
+  return c;
+}
+
+inline void reg_gradient(const RegCorners& c, float& dx, float& dy, float& dz) {
+  const float d000 = c.d[0], d001 = c.d[1], d010 = c.d[2], d100 = c.d[3], d111 = c.d[4], d110 = c.d[5],
+              d101 = c.d[6], d011 = c.d[7];
+  const float t = 0.5f, t1 = 1.0f - t;
+  dx = t1 * t1 * (d001 - d000) + t * t1 * (d011 - d010) + t1 * t * (d101 - d100) + t * t * (d111 - d110);
+  dy = t1 * t1 * (d010 - d000) + t * t1 * (d011 - d001) + t1 * t * (d110 - d100) + t * t * (d111 - d101);
+  dz = t1 * t1 * (d100 - d000) + t * t1 * (d101 - d001) + t1 * t * (d110 - d010) + t * t * (d111 - d011);
+}
+
+inline float reg_norm(float a, float b, float c) {
+  const float scale = std::fmax(std::fmax(std::fabs(a), std::fabs(b)), std::fabs(c));
+  if (scale < 1e-10f) return 0.0f;
+  const float inv = 1.0f / scale;
+  const float sa = inv * a, sb = inv * b, sc = inv * c;
+  return scale * std::sqrt(sa * sa + sb * sb + sc * sc);
+}
+
+inline float reg_curvature(const float* sdf, const RegCorners& c, const int32_t* lower, int64_t G, int32_t sub,
+                           int32_t* extra, int& counted) {
+  float sum = c.d[5] + c.d[6] + c.d[7];
+  counted = 3;
+  for (int i = 1; i < 4; ++i) {
+    extra[i - 1] = lower[(int64_t)i * G + sub];
+    if (extra[i - 1] >= 0) {
+      sum += sdf[extra[i - 1]];
+      ++counted;
+    }
+  }
+  return sum - (float)counted * c.d[4];
+}
+}  // namespace
+
+void or_compute_sdf_regularizers(const float* sdf, const int32_t* neighbors, const int32_t* lower, int64_t G,
+                                 const int32_t* upper, int64_t Nv, int vx, int vy, int vz, float* pos, float* neg,
+                                 float* curv) {
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < Nv; ++v) {
+    const RegCorners c = reg_corners(sdf, lower, G, upper, Nv, v);
+    float dx, dy, dz;
+    reg_gradient(c, dx, dy, dz);
+    const float delta = reg_norm((float)vx * dx, (float)vy * dy, (float)vz * dz) - 1.0f;
+    float p = 0.f, n = 0.f;
+    if (delta < 0) n += delta * delta;
+    if (delta > 0) p += delta * delta;
+    pos[v] = p / 1.0f;
+    neg[v] = n / 1.0f;
+    int32_t extra[3];
+    int counted;
+    const float cs = reg_curvature(sdf, c, lower, G, neighbors[6 * Nv + v], extra, counted);
+    curv[v] = cs * cs;
+  }
+}
+
+// d delta / d a = a / n (n = |(a, b, c)| > 0), gradients scattered to the
+// corners each term reads; grad_sdf is accumulated (+=).
+void or_compute_sdf_regularizers_backward(const float* sdf, const int32_t* neighbors, const int32_t* lower, int64_t G,
+                                          const int32_t* upper, int64_t Nv, int vx, int vy, int vz,
+                                          const float* g_pos, const float* g_neg, const float* g_curv,
+                                          float* grad_sdf) {
+  for (int64_t v = 0; v < Nv; ++v) {
+    const RegCorners c = reg_corners(sdf, lower, G, upper, Nv, v);
+    float dx, dy, dz;
+    reg_gradient(c, dx, dy, dz);
+    const float a = (float)vx * dx, b = (float)vy * dy, cc = (float)vz * dz;
+    const float n = reg_norm(a, b, cc);
+    const float delta = n - 1.0f;
+    float g_delta = 0.f;
+    if (g_pos && delta > 0) g_delta += 2.0f * delta * g_pos[v];
+    if (g_neg && delta < 0) g_delta += 2.0f * delta * g_neg[v];
+    if (g_delta != 0.f && n > 0.f) {
+      const float gx = g_delta * a / n * (float)vx, gy = g_delta * b / n * (float)vy, gz = g_delta * cc / n * (float)vz;
+      const float w = 0.25f;
+      // sign of each corner in dx, dy, dz (000 001 010 100 111 110 101 011)
+      const int sx[8] = {-1, 1, -1, -1, 1, -1, 1, 1}, sy[8] = {-1, -1, 1, -1, 1, 1, -1, 1},
+                sz[8] = {-1, -1, -1, 1, 1, 1, 1, -1};
+      for (int q = 0; q < 8; ++q) grad_sdf[c.id[q]] += w * (sx[q] * gx + sy[q] * gy + sz[q] * gz);
+    }
+    int32_t extra[3];
+    int counted;
+    const float cs = reg_curvature(sdf, c, lower, G, neighbors[6 * Nv + v], extra, counted);
+    const float g_cs = g_curv ? 2.0f * cs * g_curv[v] : 0.f;
+    if (g_cs != 0.f) {
+      grad_sdf[c.id[5]] += g_cs;
+      grad_sdf[c.id[6]] += g_cs;
+      grad_sdf[c.id[7]] += g_cs;
+      grad_sdf[c.id[4]] -= (float)counted * g_cs;
+      for (int i = 0; i < 3; ++i)
+        if (extra[i] >= 0) grad_sdf[extra[i]] += g_cs;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // triangle_extraction/dilate_occupancy.slang:9-94
 // ---------------------------------------------------------------------------
 void or_dilate_occupancy(const int32_t* occ, int I, int J, int KP, int d, int32_t* out) {

@@ -37,6 +37,8 @@ _SIGNATURES = {
     "or_create_triangle_vertices": (None, [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P]),
     "or_create_triangle_vertices_backward": (None, [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P]),
     "or_triangle_vertex_sources": (None, [P, P, I64, P, I32, P, P, P, P]),
+    "or_compute_sdf_regularizers": (None, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P]),
+    "or_compute_sdf_regularizers_backward": (None, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P, P]),
     "or_count_triangle_faces": (None, [P, P, I64, P, I64, P, I32, P, P]),
     "or_create_triangle_faces": (None, [P, P, I64, I64, P, P, P, I32, P, P, P]),
 }
@@ -212,6 +214,30 @@ def tessellate_voxels(sdf, vertices, sh, neighbors, lower, upper, indices, level
     vb = voff[1:].reshape(s, -1)[:, -1].copy() if g > 0 else np.zeros((s,), np.int32)
     fb = foff[1:].reshape(s, -1)[:, -1].copy() // 3 if nv > 0 else np.zeros((s,), np.int32)
     return Triangles(out_v, out_sdf, out_sh, faces, vidx, vb, fb, voff, foff, codes, types)
+
+
+def compute_sdf_regularizers(sdf, neighbors, lower, upper, grid_size):
+    """(eikonal_pos, eikonal_neg, curvature) per voxel; grid_size = (i, j, k)."""
+    sdf, neighbors = _c(sdf, np.float32), _c(neighbors, np.int32)
+    lower, upper = _c(lower, np.int32), _c(upper, np.int32)
+    g, nv = lower.shape[1], upper.shape[1]
+    i, j, k = (int(x) for x in grid_size)
+    out = [np.zeros((nv,), np.float32) for _ in range(3)]
+    lib().or_compute_sdf_regularizers(_p(sdf), _p(neighbors), _p(lower), g, _p(upper), nv, k, j, i,
+                                      *(_p(o) for o in out))
+    return tuple(out)
+
+
+def compute_sdf_regularizers_backward(sdf, neighbors, lower, upper, grid_size, g_pos, g_neg, g_curv):
+    sdf, neighbors = _c(sdf, np.float32), _c(neighbors, np.int32)
+    lower, upper = _c(lower, np.int32), _c(upper, np.int32)
+    g_pos, g_neg, g_curv = _c(g_pos, np.float32), _c(g_neg, np.float32), _c(g_curv, np.float32)
+    g, nv = lower.shape[1], upper.shape[1]
+    i, j, k = (int(x) for x in grid_size)
+    grad = np.zeros_like(sdf)
+    lib().or_compute_sdf_regularizers_backward(_p(sdf), _p(neighbors), _p(lower), g, _p(upper), nv, k, j, i,
+                                               _p(g_pos), _p(g_neg), _p(g_curv), _p(grad))
+    return grad
 
 
 def triangle_vertex_sources(sdf, lower, level_sets, vertex_offsets, num_vertices):

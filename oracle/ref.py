@@ -25,6 +25,7 @@ _SIGNATURES = {
     "ref_count_triangle_vertices": [P, P, I64, P, I, P],
     "ref_create_triangle_vertices": [P, P, P, I, P, I64, P, I, P, I64, P, P, P, P],
     "ref_count_triangle_faces": [P, P, I64, P, I64, P, I, P, P],
+    "ref_compute_sdf_regularizers": [P, I64, P, P, P, I64, I, I, I, P, P, P],
     "ref_create_triangle_faces": [P, I64, P, P, I64, P, P, I64, P, P, I, P, P, P, I64],
     "ref_project_vertices": [P, P, I, P, I64, P, P],
     "ref_bound_triangles": [P, P, I, I64, P, I64, I, I, I, I, F32, P, P, P],
@@ -239,3 +240,14 @@ def composite_backward(sdf, colors, mask, sharpness, out_colors, out_t, grad_col
     lib().ref_composite_backward(_p(sdf), _p(colors), _p(mask), p, s, float(sharpness), _p(out_colors), _p(out_t),
                                  _p(grad_colors), _p(grad_t), _p(gsdf), _p(gcol), _p(gsh))
     return gsdf, gcol, float(gsh[0])
+
+
+def compute_sdf_regularizers(sdf, neighbors, lower, upper, grid_size):
+    sdf, neighbors = _c(sdf, np.float32), _c(neighbors, np.int32)
+    lower, upper = _c(lower, np.int32), _c(upper, np.int32)
+    g, nv = lower.shape[1], upper.shape[1]
+    i, j, k = (int(x) for x in grid_size)
+    out = [np.zeros((nv,), np.float32) for _ in range(3)]
+    lib().ref_compute_sdf_regularizers(_p(sdf), g, _p(neighbors), _p(lower), _p(upper), nv, k, j, i,
+                                       *(_p(o) for o in out))
+    return tuple(out)

@@ -105,6 +105,9 @@ namespace k_count_faces {
 namespace k_create_faces {
 #include "triangle_extraction__create_triangle_faces.inc"
 }
+namespace k_regularizers {
+#include "triangle_extraction__compute_sdf_regularizers.inc"
+}
 namespace k_project {
 #include "triangle_rasterization__project_vertices.inc"
 }
@@ -267,6 +270,17 @@ void ref_create_triangle_vertices(float* gv, float* gsdf, float* gsh, int C, int
     run_grid(grid, block, [&] { k_create_vertices_16::create_triangle_vertices_forward(v, d, sh, lc, vo, ls, ov, od, osh, ot); });
   else
     std::abort();
+}
+
+// compute_sdf_regularizers.py:47-71 (forward).
+void ref_compute_sdf_regularizers(float* sdf, int64_t G, int32_t* neighbors, int32_t* lower, int32_t* upper,
+                                  int64_t Nv, int vx, int vy, int vz, float* pos, float* neg, float* curv) {
+  DiffTensorView d(TensorView<float>(sdf, {(uint64_t)G}));
+  TensorView<int> nb(neighbors, {7, (uint64_t)Nv}), lc(lower, {4, (uint64_t)G}), uc(upper, {4, (uint64_t)Nv});
+  DiffTensorView p(TensorView<float>(pos, {(uint64_t)Nv})), n(TensorView<float>(neg, {(uint64_t)Nv}));
+  DiffTensorView c(TensorView<float>(curv, {(uint64_t)Nv}));
+  run_grid(uint3((uint)((Nv + 255) / 256), 1, 1), uint3(256, 1, 1),
+           [&] { k_regularizers::compute_sdf_regularizers(d, nb, lc, uc, vx, vy, vz, p, n, c); });
 }
 
 // count_triangle_faces.py:48-61

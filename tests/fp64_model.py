@@ -111,3 +111,30 @@ def central_difference(f, x: np.ndarray, index: tuple, h: float) -> float:
     fm = f()
     x[index] = old
     return (fp - fm) / (2 * h)
+
+
+def sdf_regularizers(sdf: np.ndarray, neighbors: np.ndarray, lower: np.ndarray, upper: np.ndarray,
+                     grid_size) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """compute_sdf_regularizers.slang:18-128 in float64 (same case split)."""
+    i, j, k = (float(x) for x in grid_size)
+    nv = upper.shape[1]
+    d000, d001, d010, d100 = (sdf[lower[r][:nv]] for r in range(4))  # voxel entries come first
+    d111, d110, d101, d011 = (sdf[upper[r]] for r in range(4))
+    dx = 0.25 * ((d001 - d000) + (d011 - d010) + (d101 - d100) + (d111 - d110))
+    dy = 0.25 * ((d010 - d000) + (d011 - d001) + (d110 - d100) + (d111 - d101))
+    dz = 0.25 * ((d100 - d000) + (d101 - d001) + (d110 - d010) + (d111 - d011))
+    norm = np.sqrt((k * dx) ** 2 + (j * dy) ** 2 + (i * dz) ** 2)
+    scale = np.maximum(np.maximum(np.abs(k * dx), np.abs(j * dy)), np.abs(i * dz))
+    delta = np.where(scale < 1e-10, 0.0, norm) - 1.0
+    pos = np.where(delta > 0, delta * delta, 0.0)
+    neg = np.where(delta < 0, delta * delta, 0.0)
+    sub = neighbors[6]
+    cs = d110 + d101 + d011
+    counted = np.full(sdf[upper[0]].shape, 3.0)
+    for r in range(1, 4):
+        corner = lower[r][sub]
+        present = corner >= 0
+        cs = cs + np.where(present, sdf[np.where(present, corner, 0)], 0.0)
+        counted = counted + present
+    cs = cs - counted * d111
+    return pos, neg, cs * cs

@@ -102,6 +102,26 @@ def extraction_fixture(ref) -> dict[str, np.ndarray]:
     out["tess/level_sets"] = level_sets
     for field, value in tri.items():
         out[f"tess/out_{field}"] = value
+
+    # SDF regularizers: the sphere grid with the SDF in the grid vertices'
+    # [0, 1] units (Eikonal terms of both signs), and the random grid with a
+    # random SDF and an anisotropic grid size.
+    cases = {
+        "sphere": (grids["sphere"], (0.5 * (np.linalg.norm(p, axis=1) - 0.5)
+                                     + rng.normal(0, 0.003, len(p))).astype(np.float32)),
+        "random": (grids["random"], None),
+    }
+    for name, (occ, reg_sdf) in cases.items():
+        v = ref.extract_voxels(occ)
+        if reg_sdf is None:
+            reg_sdf = rng.normal(0, 0.05, v["vertices"].shape[0]).astype(np.float32)
+        i, j, kp = occ.shape
+        grid_size = np.array([i, j, 32 * kp], np.int32)
+        pos, neg, curv = ref.compute_sdf_regularizers(reg_sdf, v["neighbors"], v["lower_corners"],
+                                                      v["upper_corners"], grid_size)
+        out.update({f"reg_{name}/signed_distances": reg_sdf, f"reg_{name}/grid_size": grid_size,
+                    f"reg_{name}/eikonal_loss_pos": pos, f"reg_{name}/eikonal_loss_neg": neg,
+                    f"reg_{name}/curvature_loss": curv})
     return out
 
 

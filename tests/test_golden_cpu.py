@@ -164,3 +164,14 @@ def test_fixtures_regenerate_from_reference():
                 close_grad(value, committed[key], rtol=1e-5, what=f"{name}:{key}")
             else:
                 np.testing.assert_array_equal(np.asarray(value), committed[key], err_msg=f"{name}:{key}")
+
+
+@pytest.mark.parametrize("case", ["sphere", "random"])
+def test_oracle_sdf_regularizers_match_reference(extraction, case):
+    e = extraction
+    grid = "sphere" if case == "sphere" else "random"
+    got = oracle.compute_sdf_regularizers(e[f"reg_{case}/signed_distances"], e[f"{grid}/neighbors"],
+                                          e[f"{grid}/lower_corners"], e[f"{grid}/upper_corners"],
+                                          e[f"reg_{case}/grid_size"])
+    for value, name in zip(got, ("eikonal_loss_pos", "eikonal_loss_neg", "curvature_loss")):
+        np.testing.assert_array_equal(value, e[f"reg_{case}/{name}"], err_msg=name)

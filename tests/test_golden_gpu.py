@@ -191,3 +191,22 @@ def test_explicit_composite_backward_matches_reference(cuda_device, scene):
     _close_grad(_n(sdf.grad), g["explicit/grad_shell_signed_distances"], "signed distances")
     _close_grad(_n(col.grad), g["explicit/grad_shell_colors"], "colours")
     _close_grad([float(sharp.grad)], [g["explicit/grad_sharpness"]], "sharpness")
+
+
+@pytest.mark.parametrize("case", ["sphere", "random"])
+def test_sdf_regularizers_match_reference(cuda_device, extraction, case):
+    from oracle import oracle
+
+    e, d = extraction, cuda_device
+    grid = "sphere" if case == "sphere" else "random"
+    args = [e[f"{grid}/neighbors"], e[f"{grid}/lower_corners"], e[f"{grid}/upper_corners"]]
+    size = tuple(int(x) for x in e[f"reg_{case}/grid_size"])
+    sdf = _t(e[f"reg_{case}/signed_distances"], d).requires_grad_(True)
+    losses = te.compute_sdf_regularizers(sdf, *(_t(a, d) for a in args), size)
+    for value, name in zip(losses, ("eikonal_loss_pos", "eikonal_loss_neg", "curvature_loss")):
+        _eq(value, e[f"reg_{case}/{name}"], name)
+    rng = np.random.default_rng(3)
+    g = [rng.normal(0, 1, e[f"reg_{case}/curvature_loss"].shape).astype(np.float32) for _ in range(3)]
+    torch.autograd.backward(list(losses), [_t(x, d) for x in g])
+    want = oracle.compute_sdf_regularizers_backward(e[f"reg_{case}/signed_distances"], *args, size, *g)
+    _close_grad(_n(sdf.grad), want, "signed distances")

@@ -252,3 +252,35 @@ def test_gpu_grid_chain_matches_fd(cuda_device):
     assert np.linalg.norm(fd_sdf) > 0 and np.linalg.norm(fd_sh) > 0
     assert _rel([g_sdf[i] for i in sdf_idx], fd_sdf) <= FD_RTOL
     assert _rel([g_sh[i] for i in sh_idx], fd_sh) <= FD_RTOL
+
+
+def test_oracle_sdf_regularizers_adjoint_matches_fd():
+    """The hand-derived adjoint of the SDF regularizers (the reference
+    differentiates them automatically) against FP64 central differences."""
+    rng = np.random.default_rng(21)
+    n = 32
+    coords = -1 + (np.arange(n) + 0.5) * 2 / n
+    z, y, x = np.meshgrid(coords, coords, coords, indexing="ij")
+    occ = semantics.pack(np.abs(np.sqrt(x * x + y * y + z * z) - 0.5) < 2.5 * 2 / n)
+    vox = oracle.extract_voxels(occ)
+    p = 2 * vox.vertices.astype(np.float64) - 1
+    sdf = (0.5 * (np.linalg.norm(p, axis=1) - 0.5) + rng.normal(0, 0.003, len(p))).astype(np.float32)
+    grid_size = (n, n, n)
+    nv = vox.upper_corners.shape[1]
+    gp, gn, gc = (rng.normal(0, 1, nv).astype(np.float32) for _ in range(3))
+    grad = oracle.compute_sdf_regularizers_backward(sdf, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                                    grid_size, gp, gn, gc)
+    sdf64 = sdf.astype(np.float64)
+
+    def loss64():
+        pos, neg, curv = m.sdf_regularizers(sdf64, vox.neighbors, vox.lower_corners, vox.upper_corners, grid_size)
+        return float((pos * gp).sum() + (neg * gn).sum() + (curv * gc).sum())
+
+    pos, neg, curv = oracle.compute_sdf_regularizers(sdf, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                                     grid_size)
+    p64, n64, c64 = m.sdf_regularizers(sdf64, vox.neighbors, vox.lower_corners, vox.upper_corners, grid_size)
+    assert np.abs(pos - p64).max() < 1e-4 and np.abs(neg - n64).max() < 1e-4 and np.abs(curv - c64).max() < 1e-6
+    idx = [(int(i),) for i in rng.choice(np.unique(vox.lower_corners[0]), N_ENTRIES, replace=False)]
+    fd = [m.central_difference(loss64, sdf64, i, STEP) for i in idx]
+    assert np.linalg.norm(fd) > 0
+    assert _rel([grad[i] for i in idx], fd) <= FD_RTOL
