@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--no-cameras", action="store_true", help="skip the uneven-camera batching comparison")
     p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     p.add_argument("--serve-seconds", type=float, default=0.5, help="arrival window per request rate")
+    p.add_argument("--no-subdivision", action="store_true", help="skip the subdivision step measurement")
+    p.add_argument("--no-large", action="store_true", help="skip the large-configuration step in both modes")
     return p.parse_args()
 
 
@@ -407,6 +409,10 @@ def run_ours(args, rank, world, local):
         line["cameras_batched"] = run_cameras(device, min(args.steps, 20))
     if not args.no_serving and world == 1:
         line["serving"] = run_serving(device, args.serve_seconds)
+    if not args.no_large and world == 1:
+        line["large"] = run_large(device, min(args.steps, 10))
+    if not args.no_subdivision and world == 1:
+        line["subdivision"] = run_subdivision(device, min(args.steps, 20), cpu=not args.no_cpu_baseline)
     if not args.no_cpu_baseline and world == 1:
         tess_s, render_s = cpu_sample(w, 0)
         cpu_ms = 1000.0 * (tess_s + b * render_s)
@@ -418,8 +424,8 @@ def run_ours(args, rank, world, local):
 
 
 def run_cameras(device, steps):
-    """Cameras of uneven size: the small scene seen by 32 cameras of 200-1600
-    px per side, 8 shells. One batched training step (render_cameras, tile
+    """Cameras of uneven size: the mid scene (256^3, 8 spheres, SH degree 3,
+    8 shells) seen by 32 cameras of 200-1600 px per side on its orbit. One batched training step (render_cameras, tile
     shape autotuned over 8/16/32, as a CUDA graph) against the plain form that
     renders each camera with its own call (eager), plus the images' largest
     difference between the two."""
@@ -458,7 +464,7 @@ def run_cameras(device, steps):
             single = tr.render_fused(w.extrinsics[b:b + 1], w.intrinsics[b:b + 1], (h, wd), *args, tile_shape=tile)
             diff = max(diff, float((single[0] - images[b]).abs().max()))
     return {
-        "workload": f"uneven: {w.config.resolution}^3 sphere band, {w.level_sets.numel()} shells, "
+        "workload": f"uneven: {w.config.resolution}^3 band around 8 spheres, SH deg 3, {w.level_sets.numel()} shells, "
                     f"{len(w.image_shapes)} cameras of 200-1600 px per side ({w.num_pixels} pixels), "
                     "fused fwd+bwd training step",
         "tile": list(tile),
@@ -471,13 +477,133 @@ def run_cameras(device, steps):
     }
 
 
+def run_large(device, steps):
+    """The large training step: 512^3 band around 32 spheres plus an
+    inward-facing background sphere, SH degree 3, 16 shells, 4 cameras at
+    1297x840 inside the background. Forward + backward in both render modes
+    (eager; the fused mode also as a CUDA graph), each with its peak HBM
+    above the resident scene, and the largest difference between the two
+    modes' images."""
+    import torch
+
+    from meshtryoshka_gb300 import autotune, graph, pipeline
+    from meshtryoshka_gb300 import triangle_extraction as te
+
+    w = pipeline.build_workload("large", device)
+    out = {}
+    for mode in ("fused", "explicit"):
+        def step(mode=mode):
+            w.grid_sdf.grad = None
+            w.grid_sh.grad = None
+            pipeline.training_step(w, mode)
+
+        step()
+        torch.cuda.synchronize(device)
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+        torch.cuda.empty_cache()
+        resident = torch.cuda.memory_allocated(device)
+        torch.cuda.reset_peak_memory_stats(device)
+        step()
+        torch.cuda.synchronize(device)
+        peak = torch.cuda.max_memory_allocated(device) - resident
+        out[mode] = {"eager_ms": autotune.time_ms(step, repeats=steps), "peak_hbm_gb": peak / 1e9,
+                     "resident_gb": resident / 1e9}
+    w.grid_sdf.grad = None
+    w.grid_sh.grad = None
+    captured = graph.CapturedTrainingStep(w)
+    out["fused"]["graph_ms"] = autotune.time_ms(captured, repeats=steps)
+    _, stats = pipeline.forward(w, "fused")
+    del captured
+    with torch.no_grad():
+        tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors,
+                                   w.voxels.lower_corners, w.voxels.upper_corners, w.voxels.indices, w.level_sets)
+        vertices = 2.0 * tri.vertices - 1.0
+        fused = pipeline._render(w, tri, vertices, None, "fused")
+        explicit = pipeline._render(w, tri, vertices, None, "explicit")
+        diff = float((fused - explicit).abs().max())
+    h, wd = w.image_shape
+    out.update({
+        "workload": f"large: {w.config.resolution}^3 band around 32 spheres + background sphere, SH deg 3, "
+                    f"{w.level_sets.numel()} shells, {w.extrinsics.shape[0]}x{h}x{wd}, fwd+bwd training step",
+        "sizes": {k: stats[k] for k in ("G", "Nv", "V", "F", "K", "P")},
+        "max_image_diff_fused_vs_explicit": diff,
+    })
+    return out
+
+
+def run_subdivision(device, steps, cpu=True, config="mid"):
+    """Coarse-to-fine subdivision step (subdivision.subdivide: canonical
+    vertex copy, triangle-voxel mask, dilation by 4, occupancy and parameter
+    upscaling) of a scene to twice its resolution (the mid scene: 256^3 ->
+    512^3 with SH degree 3), against the oracle on the host cores; the two
+    results are compared bit for bit."""
+    import time
+
+    import numpy as np
+    import torch
+
+    from meshtryoshka_gb300 import _native as nt
+    from meshtryoshka_gb300 import subdivision, synthetic
+    from meshtryoshka_gb300 import triangle_extraction as te
+
+    cfg = synthetic.CONFIGS[config]
+    occ = synthetic.make_occupancy(cfg, device)
+    vox = te.extract_voxels(occ)
+    sdf = synthetic.corner_sdf(cfg, vox.vertices)
+    sh = synthetic.corner_sh(cfg, vox.num_vertices, device)
+    with torch.no_grad():
+        tri = te.tessellate_voxels(sdf, vox.vertices, sh, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                   vox.indices, synthetic.level_sets(cfg, device))
+    target = (2 * cfg.resolution,) * 3
+
+    def step():
+        return subdivision.subdivide(vox, sdf, sh, occ, tri.voxel_indices, target)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize(device)
+    times = []
+    for _ in range(max(steps, 5)):
+        t0 = time.perf_counter()
+        out = step()
+        torch.cuda.synchronize(device)
+        times.append(1000.0 * (time.perf_counter() - t0))
+    with nt.record_launches(timed=True) as rec:
+        step()
+        torch.cuda.synchronize(device)
+    kernels = {name: round(sum(v), 4) for name, v in rec.times_ms().items()}
+    result = {
+        "workload": f"{config} scene {cfg.resolution}^3 ({vox.num_voxels} voxels, {vox.num_vertices} vertices, SH "
+                    f"C={sh.shape[0]}, {tri.voxel_indices.numel()} triangles) -> {target[0]}^3, dilation 4",
+        "new_vertices": int(out.signed_distances.numel()),
+        "gpu_ms_median": float(np.median(times)),
+        "gpu_ms_min": float(np.min(times)),
+        "kernel_ms": kernels,
+    }
+    if cpu:
+        from oracle import oracle
+
+        args = (vox.vertices.cpu().numpy(), sdf.cpu().numpy(), sh.cpu().numpy(), occ.cpu().numpy(),
+                tri.voxel_indices.cpu().numpy(), target)
+        t0 = time.perf_counter()
+        want = oracle.subdivide(*args)
+        cpu_ms = 1000.0 * (time.perf_counter() - t0)
+        identical = all(np.array_equal(a, b.cpu().numpy()) for a, b in
+                        zip(want, (out.signed_distances, out.spherical_harmonics, out.occupancy)))
+        result.update({"cpu_ms": cpu_ms, "cpu_cores": cpu_threads(), "cpu_kind": "port",
+                       "identical_to_oracle": bool(identical)})
+    return result
+
+
 SERVE_RATES = (50, 200, 500, 1000, 2000)
 
 
 def run_serving(device, seconds):
-    """Serving sweep: four resident scenes (256^3 sphere x2, 128^3, 512^3; 8
-    shells), Poisson arrivals at each rate for `seconds`, 80 % render-only and
-    20 % render + gradient, images of 256-1920 x 256-1080 px. Continuous
+    """Serving sweep: four resident scenes (mid layout at 256^3 x2 and 128^3,
+    large layout at 512^3; SH degree 3, 8 shells), Poisson arrivals at each
+    rate for `seconds`, 80 % render-only and 20 % render + gradient, images of
+    256-1920 x 256-1080 px. Continuous
     batching (serving.Server) against the plain per-request form at the same
     arrival times; p50 / p99 latency and throughput for both."""
     import torch
@@ -502,7 +628,8 @@ def run_serving(device, seconds):
         del requests
         torch.cuda.empty_cache()
     return {
-        "workload": "4 resident scenes (sphere band 256^3 x2, 128^3, 512^3; 8 shells, SH deg 0); Poisson arrivals, "
+        "workload": "4 resident scenes (mid layout at 256^3 x2 and 128^3, large layout at 512^3; 8 shells, SH deg "
+                    "3); Poisson arrivals, "
                     f"max({seconds} s, 200 requests) per rate; 80 % render, 20 % render+gradient (MSE vs U[0,1] "
                     "target); images 256-1920 x 256-1080, fov 40-70",
         "rates": rows,

@@ -135,6 +135,75 @@ MT_API int mt_dilate_occupancy(const int32_t* occupancy, int32_t I, int32_t J,
                         mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Coarse-to-fine subdivision (meshtryoshka/model/tesseract.py:396-486).
+ * ---------------------------------------------------------------------- */
+
+/* write_occupancy.py:22-46 / write_occupancy.slang:1-20: sets bit v & 31 of
+ * word v >> 5 for each of the n voxel indices (atomic OR into a caller-zeroed
+ * grid of `words` int32). Indices outside [0, 32 words) are skipped. */
+MT_API int mt_write_occupancy(const int32_t* voxel_indices, int64_t n,
+                       int32_t* occupancy, int64_t words, mt_stream_t stream);
+
+/* upscale_occupancy.py:24-54 / upscale_occupancy.slang:1-74: [I, J, KP] ->
+ * [I2, J2, KP2] (every new extent >= the old one). `mask` (nullable, same
+ * shape as `occupancy`) is AND-ed into every old word read, which is the
+ * `old_occupancy & occupancy_to_upscale` of upscale_parameters.py:49. */
+MT_API int mt_upscale_occupancy(const int32_t* occupancy, const int32_t* mask,
+                         int32_t I, int32_t J, int32_t KP, int32_t I2,
+                         int32_t J2, int32_t KP2, int32_t* out,
+                         mt_stream_t stream);
+
+/* upscale_parameters.slang:129-198 (launch at upscale_parameters.py:77-93):
+ * trilinear resampling of [Vold] signed distances and [C, Vold, 3] SH from
+ * the old vertex grid ([I1, J1, KP1] vertex occupancy + exclusive per-word
+ * vertex offsets, as compute_vertex_occupancy + scan give) onto the new one
+ * ([I1n, J1n, KP1n]); writes Vnew entries. */
+MT_API int mt_upscale_parameters(
+    const int32_t* old_vertex_occupancy, const int32_t* old_vertex_offsets,
+    const float* old_signed_distances, const float* old_spherical_harmonics,
+    int32_t C, int64_t Vold, int32_t I1, int32_t J1, int32_t KP1,
+    const int32_t* new_vertex_occupancy, const int32_t* new_vertex_offsets,
+    int32_t I1n, int32_t J1n, int32_t KP1n, int64_t Vnew,
+    float* new_signed_distances, float* new_spherical_harmonics,
+    mt_stream_t stream);
+
+/* get_occupancy_mesh.slang:1-54 count_triangles: counts[(I+1)(J+1)(KP+1)+1]
+ * int32, 2 x boundary faces owned per entry (last entry set to 0, ready for
+ * an exclusive scan). */
+MT_API int mt_count_occupancy_mesh_triangles(const int32_t* occupancy, int32_t I,
+                                      int32_t J, int32_t KP, int32_t* counts,
+                                      mt_stream_t stream);
+
+/* get_occupancy_mesh.slang:122-220 create_triangles: writes T triangles,
+ * vertices [T, 3, 3] and triangle_colors [T, 3] from colors [3, 2, 3]
+ * (axis, side, rgb), at the scanned offsets. */
+MT_API int mt_create_occupancy_mesh_triangles(const int32_t* occupancy, int32_t I,
+                                       int32_t J, int32_t KP,
+                                       const int32_t* offsets, int64_t T,
+                                       const float* colors, float* vertices,
+                                       float* triangle_colors,
+                                       mt_stream_t stream);
+
+/* index_vertices.py:17-21: quantized[3V] = int64(round(points * inv_tol))
+ * (round half to even) and *max_abs = max |quantized| (device uint64). */
+MT_API int mt_quantize_points(const float* points, int64_t V, float inv_tol,
+                       int64_t* quantized, uint64_t* max_abs,
+                       mt_stream_t stream);
+
+/* index_vertices.py:23-25: keys[v] = (x << 2 shift) | (y << shift) | z,
+ * values[v] = v. */
+MT_API int mt_pack_point_keys(const int64_t* quantized, int64_t V, int32_t shift,
+                       int64_t* keys, int32_t* values, mt_stream_t stream);
+
+/* values[v] = v for v < n. */
+MT_API int mt_iota_i32(int64_t n, int32_t* values, mt_stream_t stream);
+
+/* index_vertices.py:30-51 index_keys, after a stable sort of (key, v):
+ * out[order[p]] = order[first position of p's run of equal keys]. */
+MT_API int mt_index_sorted_runs(const int64_t* sorted_keys, const int32_t* order,
+                         int64_t n, int32_t* out, mt_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Per-step marching cubes (triangle_extraction/__init__.py:75-157
  * tessellate_voxels). G = voxels + subvoxels, Nv = voxels, S = level sets,
  * C = spherical-harmonic coefficients per colour channel.

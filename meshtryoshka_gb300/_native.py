@@ -41,6 +41,15 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_count_occupancy": (I32, [P, I32, I32, I32, P, P]),
     "mt_create_voxels": (I32, [P, P, P, P, I32, I32, I32, I64, I64, P, P, P, P, P, P]),
     "mt_dilate_occupancy": (I32, [P, I32, I32, I32, I32, P, P]),
+    "mt_write_occupancy": (I32, [P, I64, P, I64, P]),
+    "mt_upscale_occupancy": (I32, [P, P, I32, I32, I32, I32, I32, I32, P, P]),
+    "mt_upscale_parameters": (I32, [P, P, P, P, I32, I64, I32, I32, I32, P, P, I32, I32, I32, I64, P, P, P]),
+    "mt_count_occupancy_mesh_triangles": (I32, [P, I32, I32, I32, P, P]),
+    "mt_create_occupancy_mesh_triangles": (I32, [P, I32, I32, I32, P, I64, P, P, P, P]),
+    "mt_quantize_points": (I32, [P, I64, c_float, P, P, P]),
+    "mt_pack_point_keys": (I32, [P, I64, I32, P, P, P]),
+    "mt_iota_i32": (I32, [I64, P, P]),
+    "mt_index_sorted_runs": (I32, [P, P, I64, P, P]),
     "mt_count_triangle_vertices": (I32, [P, P, I64, P, I32, P, P]),
     "mt_create_triangle_vertices": (
         I32,

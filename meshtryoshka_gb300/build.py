@@ -43,7 +43,7 @@ NVCC_FLAGS = [
 # contraction anywhere in them. The compositing kernels keep contraction for
 # speed and spell every result-defining operation with explicit
 # __fmul_rn / __fadd_rn intrinsics instead.
-UNCONTRACTED = {"extraction", "raster_front", "explicit"}
+UNCONTRACTED = {"extraction", "raster_front", "explicit", "subdivision"}
 
 
 def find_nvcc() -> str:

@@ -248,10 +248,11 @@ def run_plain(scenes: list[Scene], requests: list[Request], tile_shape=(16, 16))
 def poisson_requests(scenes: list[Scene], rate: float, duration: float, seed: int = 4,
                      gradient_fraction: float = 0.2, first_id: int = 0) -> list[Request]:
     """Poisson arrivals at ``rate`` requests/s for ``duration`` s: uniform
-    scene, camera at 2-2.5 units looking at the origin from a random
-    direction, image width U{256..1920} x height U{256..1080}, fov U[40, 70]
-    degrees; a ``gradient_fraction`` of the requests also asks for the
-    gradient of the MSE against a U[0, 1] target."""
+    scene, camera looking at the origin from a random direction (2-2.5 units
+    away; 0.5-0.7 units, near the horizontal plane, inside a scene's
+    background sphere), image width U{256..1920} x height U{256..1080}, fov
+    U[40, 70] degrees; a ``gradient_fraction`` of the requests also asks for
+    the gradient of the MSE against a U[0, 1] target."""
     rng = np.random.default_rng(seed)
     device = scenes[0].grid_sdf.device
     gen = torch.Generator(device=device)
@@ -261,16 +262,24 @@ def poisson_requests(scenes: list[Scene], rate: float, duration: float, seed: in
         t += rng.exponential(1.0 / rate)
         if t > duration:
             break
+        scene = int(rng.integers(len(scenes)))
         direction = rng.normal(size=3)
-        direction /= np.linalg.norm(direction)
-        eye = direction * rng.uniform(2.0, 2.5)
+        if synthetic.CONFIGS[scenes[scene].name].background_radius is not None:
+            # Inside the background sphere: a ring of radius 0.5-0.7 around
+            # the origin, near the horizontal plane.
+            direction[1] *= 0.2
+            direction /= np.linalg.norm(direction)
+            eye = direction * rng.uniform(0.5, 0.7)
+        else:
+            direction /= np.linalg.norm(direction)
+            eye = direction * rng.uniform(2.0, 2.5)
         w, h = int(rng.integers(256, 1921)), int(rng.integers(256, 1081))
         fov = float(rng.uniform(40.0, 70.0))
         grad = bool(rng.random() < gradient_fraction)
         target = None
         if grad:
             target = torch.rand((3, h, w), generator=gen, device=device)
-        out.append(Request(first_id + len(out), int(rng.integers(len(scenes))),
+        out.append(Request(first_id + len(out), scene,
                            torch.from_numpy(synthetic.look_at(eye)).to(device),
                            torch.from_numpy(synthetic.pinhole(h, w, fov)).to(device), (h, w), grad, target, t))
     return out
@@ -287,6 +296,8 @@ def latency_summary(done: list[Completed]) -> dict:
 
 
 def default_scenes(device) -> list[Scene]:
-    """Two 256^3 sphere scenes (different noise), one 128^3, one 512^3."""
+    """Two 256^3 scenes of the mid layout (8 spheres, different noise), one at
+    128^3, and one 512^3 scene of the large layout (32 spheres inside a
+    background sphere); SH degree 3 and 8 shells each."""
     return [Scene.build("serve_256", device, seed=0), Scene.build("serve_256", device, seed=7),
             Scene.build("serve_128", device), Scene.build("serve_512", device)]

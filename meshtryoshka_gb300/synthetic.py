@@ -60,20 +60,23 @@ CONFIGS: dict[str, SceneConfig] = {
     # 256^3, union of 8 spheres, SH degree 3, 8 shells, 4 x 800^2 cameras.
     "mid": SceneConfig("mid", 256, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8), 50.0,
                        "orbit", 4, (800, 800), 50.0),
-    # The small scene seen by 32 cameras of uneven resolution, 8 shells.
-    "uneven": SceneConfig("uneven", 64, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8), 50.0,
+    # The mid scene seen by 32 cameras of uneven resolution (200-1600 px per
+    # side, fov 40-70 degrees) placed on the mid scene's orbit.
+    "uneven": SceneConfig("uneven", 256, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8), 50.0,
                           "uneven", 32, (0, 0), (40.0, 70.0)),
     # 512^3, 32 spheres + background sphere, SH degree 3, 16 shells, 4 x 1297x840.
     "large": SceneConfig("large", 512, 32, 0.7, (0.05, 0.25), 0.95, 2.0, 0.001, 3, _even(-0.02, 0.02, 16), 50.0,
                          "ring", 4, (840, 1297), 55.0),
-    # Resident scenes of the serving workload: the sphere scene at 256^3 (two),
-    # 128^3 and 512^3, 8 shells each; cameras come with the requests.
-    "serve_256": SceneConfig("serve_256", 256, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
-                             50.0, "front", 1, (256, 256), 60.0),
-    "serve_128": SceneConfig("serve_128", 128, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
-                             50.0, "front", 1, (256, 256), 60.0),
-    "serve_512": SceneConfig("serve_512", 512, 0, 0.0, (0.5, 0.5), None, 2.0, 0.002, 0, _even(-0.02, 0.02, 8),
-                             50.0, "front", 1, (256, 256), 60.0),
+    # Resident scenes of the serving workload, 8 shells each; cameras come with
+    # the requests: the mid scene's layout at 256^3 (two, different noise) and
+    # at 128^3, and the large scene's layout (inside a background sphere) at
+    # 512^3.
+    "serve_256": SceneConfig("serve_256", 256, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8),
+                             50.0, "orbit", 1, (256, 256), 50.0),
+    "serve_128": SceneConfig("serve_128", 128, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8),
+                             50.0, "orbit", 1, (256, 256), 50.0),
+    "serve_512": SceneConfig("serve_512", 512, 32, 0.7, (0.05, 0.25), 0.95, 2.0, 0.001, 3, _even(-0.02, 0.02, 8),
+                             50.0, "ring", 1, (256, 256), 55.0),
 }
 
 
@@ -189,7 +192,9 @@ def make_cameras(cfg: SceneConfig) -> CameraSet:
             h, w = cfg.image_shape
             fov = cfg.fov_degrees
         elif cfg.cameras == "uneven":
-            eye = np.array([0.0, 0.0, 2.0])
+            az = math.radians(rng.uniform(0.0, 360.0))
+            el = math.radians(rng.uniform(10.0, 60.0))
+            eye = 2.5 * np.array([math.cos(el) * math.cos(az), math.sin(el), math.cos(el) * math.sin(az)])
             w = int(rng.integers(200, 1601))
             h = int(rng.integers(200, 1601))
             fov = float(rng.uniform(*cfg.fov_degrees))

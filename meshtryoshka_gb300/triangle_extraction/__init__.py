@@ -17,6 +17,7 @@ from __future__ import annotations
 import logging
 from typing import NamedTuple
 
+import numpy as np
 import torch
 from torch import Tensor
 from torch.profiler import record_function
@@ -46,6 +47,14 @@ __all__ = [
     "CountTriangleFacesResult",
     "CreateTriangleFacesResult",
     "VertexOccupancyFnResult",
+    "write_occupancy",
+    "upscale_occupancy",
+    "upscale_parameters",
+    "UpscaledParameters",
+    "get_occupancy_mesh",
+    "Mesh",
+    "index_vertices",
+    "index_keys",
 ]
 
 
@@ -225,6 +234,185 @@ def dilate_occupancy(occupancy: Tensor, dilation: int) -> Tensor:
     if out.numel() > 0:
         nt.call("mt_dilate_occupancy", occupancy.data_ptr(), i, j, kp, dilation, out.data_ptr(), nt.stream(device))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Coarse-to-fine subdivision (tesseract.py:396-486), occupancy mesh and
+# vertex de-duplication. These run at subdivision steps and in the viewer.
+# ---------------------------------------------------------------------------
+@record_function("write_occupancy")
+def write_occupancy(voxel_indices: Tensor, packed_occupancy_shape: tuple[int, ...], min_shell: int,
+                    max_shell: int) -> Tensor:
+    """Packed occupancy with the bit of every triangle's voxel set
+    (write_occupancy.py:22-46). ``min_shell`` / ``max_shell`` are accepted
+    and unused, as in the reference kernel."""
+    voxel_indices = _i32(voxel_indices, "voxel_indices")
+    device = nt.require_cuda(voxel_indices)
+    occupancy = torch.zeros(packed_occupancy_shape, dtype=torch.int32, device=device)
+    n = voxel_indices.numel()
+    if n > 0 and occupancy.numel() > 0:
+        nt.call("mt_write_occupancy", voxel_indices.data_ptr(), n, occupancy.data_ptr(), occupancy.numel(),
+                nt.stream(device))
+    return occupancy
+
+
+def _upscale_occupancy(occupancy: Tensor, mask: Tensor | None, target_shape: tuple[int, int, int]) -> Tensor:
+    occupancy = _i32(occupancy, "occupancy")
+    device = nt.require_cuda(occupancy)
+    i, j, k_packed = occupancy.shape
+    i_target, j_target, k_target = target_shape
+    assert k_target % 32 == 0
+    k_packed_target = k_target // 32
+    assert i_target >= i and j_target >= j and k_packed_target >= k_packed
+    out = torch.empty((i_target, j_target, k_packed_target), dtype=torch.int32, device=device)
+    if out.numel() > 0:
+        if mask is not None:
+            mask = _i32(mask, "occupancy_to_upscale")
+            if mask.shape != occupancy.shape:
+                raise ValueError(f"occupancy_to_upscale shape {tuple(mask.shape)} != {tuple(occupancy.shape)}")
+        nt.call("mt_upscale_occupancy", occupancy.data_ptr(), nt.ptr(mask), i, j, k_packed, i_target, j_target,
+                k_packed_target, out.data_ptr(), nt.stream(device))
+    return out
+
+
+@record_function("upscale_occupancy")
+def upscale_occupancy(occupancy: Tensor, target_shape: tuple[int, int, int]) -> Tensor:
+    """[i, j, kp] -> [i', j', k'/32] with every extent at least the old one
+    (upscale_occupancy.py:24-54)."""
+    return _upscale_occupancy(occupancy, None, target_shape)
+
+
+class UpscaledParameters(NamedTuple):
+    signed_distances: Tensor  # [vertex] float32
+    spherical_harmonics: Tensor  # [sh, vertex, 3] float32
+    occupancy: Tensor  # [i, j, k_packed] int32
+
+
+@record_function("upscale_parameters")
+@torch.no_grad()
+def upscale_parameters(old_signed_distances: Tensor, old_spherical_harmonics: Tensor, old_occupancy: Tensor,
+                       occupancy_to_upscale: Tensor, new_resolution: tuple[int, int, int]) -> UpscaledParameters:
+    """Upscaled occupancy of ``old_occupancy & occupancy_to_upscale`` and the
+    old vertices' parameters resampled trilinearly onto its vertices
+    (upscale_parameters.py:35-99). One host read (the new vertex count)."""
+    old_signed_distances = _f32(old_signed_distances, "old_signed_distances")
+    old_spherical_harmonics = _f32(old_spherical_harmonics, "old_spherical_harmonics")
+    old_occupancy = _i32(old_occupancy, "old_occupancy")
+    device = nt.require_cuda(old_signed_distances, old_spherical_harmonics, old_occupancy)
+    num_sh, num_old, _ = old_spherical_harmonics.shape
+    if old_signed_distances.shape[0] != num_old:
+        raise ValueError("old_signed_distances and old_spherical_harmonics disagree on the vertex count")
+
+    # The AND of upscale_parameters.py:49 is applied to every word the
+    # upscaling kernel reads.
+    new_occupancy = _upscale_occupancy(old_occupancy, occupancy_to_upscale, new_resolution)
+
+    old_vertex_occupancy, old_vertex_offsets = compute_vertex_occupancy(old_occupancy)
+    compute_exclusive_cumsum(old_vertex_offsets)
+    new_vertex_occupancy, new_vertex_offsets = compute_vertex_occupancy(new_occupancy)
+    compute_exclusive_cumsum(new_vertex_offsets)
+    num_vertices = int(new_vertex_offsets[-1].item())
+
+    new_signed_distances = torch.empty((num_vertices,), dtype=torch.float32, device=device)
+    new_spherical_harmonics = torch.empty((num_sh, num_vertices, 3), dtype=torch.float32, device=device)
+    if num_vertices > 0:
+        i1, j1, k1 = old_vertex_occupancy.shape
+        i1n, j1n, k1n = new_vertex_occupancy.shape
+        nt.call("mt_upscale_parameters", old_vertex_occupancy.data_ptr(), old_vertex_offsets.data_ptr(),
+                nt.ptr(old_signed_distances), nt.ptr(old_spherical_harmonics), num_sh, num_old, i1, j1, k1,
+                new_vertex_occupancy.data_ptr(), new_vertex_offsets.data_ptr(), i1n, j1n, k1n, num_vertices,
+                new_signed_distances.data_ptr(), new_spherical_harmonics.data_ptr(), nt.stream(device))
+    return UpscaledParameters(new_signed_distances, new_spherical_harmonics, new_occupancy)
+
+
+class Mesh(NamedTuple):
+    vertices: Tensor  # [triangle, 3, 3] float32 (xyz)
+    colors: Tensor  # [triangle, 3] float32
+
+
+@record_function("get_occupancy_mesh")
+def get_occupancy_mesh(occupancy: Tensor, colors: Tensor) -> Mesh:
+    """Two triangles per face between occupied and free voxels, coloured by
+    ``colors[axis, side]`` (get_occupancy_mesh.py:32-80). One host read."""
+    occupancy = _i32(occupancy, "occupancy")
+    colors = _f32(colors, "colors")
+    device = nt.require_cuda(occupancy, colors)
+    if tuple(colors.shape) != (3, 2, 3):
+        raise ValueError(f"colors must be [3, 2, 3], got {tuple(colors.shape)}")
+    i, j, k_packed = occupancy.shape
+    counts = torch.empty(((i + 1) * (j + 1) * (k_packed + 1) + 1,), dtype=torch.int32, device=device)
+    nt.call("mt_count_occupancy_mesh_triangles", nt.ptr(occupancy), i, j, k_packed, counts.data_ptr(),
+            nt.stream(device))
+    compute_exclusive_cumsum(counts)
+    num_triangles = int(counts[-1].item())
+    vertices = torch.empty((num_triangles, 3, 3), dtype=torch.float32, device=device)
+    triangle_colors = torch.empty((num_triangles, 3), dtype=torch.float32, device=device)
+    if num_triangles > 0:
+        nt.call("mt_create_occupancy_mesh_triangles", occupancy.data_ptr(), i, j, k_packed, counts.data_ptr(),
+                num_triangles, colors.data_ptr(), vertices.data_ptr(), triangle_colors.data_ptr(),
+                nt.stream(device))
+    return Mesh(vertices, triangle_colors)
+
+
+def _index_pairs(keys: Tensor, values: Tensor) -> Tensor:
+    """Stable sort of (key, original index), then every index mapped to the
+    first original index of its run of equal keys."""
+    device = keys.device
+    n = keys.numel()
+    sorted_keys = torch.empty_like(keys)
+    order = torch.empty_like(values)
+    out = torch.empty((n,), dtype=torch.int32, device=device)
+    ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_sort_pairs_workspace_bytes(n))
+    nt.call("mt_sort_pairs_i64_i32", keys.data_ptr(), values.data_ptr(), sorted_keys.data_ptr(), order.data_ptr(), n,
+            None, 0, 64, ws_ptr, ws_bytes, nt.stream(device))
+    nt.call("mt_index_sorted_runs", sorted_keys.data_ptr(), order.data_ptr(), n, out.data_ptr(), nt.stream(device))
+    return out
+
+
+def index_keys(keys: Tensor) -> Tensor:
+    """int32 [n]: for every key, the index of the first equal key
+    (index_vertices.py:30-51)."""
+    if keys.dtype != torch.int64:
+        raise TypeError(f"keys must be int64, got {keys.dtype}")
+    keys = keys.contiguous()
+    device = nt.require_cuda(keys)
+    (n,) = keys.shape
+    if n == 0:
+        return torch.empty((0,), dtype=torch.int32, device=device)
+    if n > 2**31 - 1:
+        raise ValueError("index_keys handles at most 2^31 - 1 keys")
+    values = torch.empty((n,), dtype=torch.int32, device=device)
+    nt.call("mt_iota_i32", n, values.data_ptr(), nt.stream(device))
+    return _index_pairs(keys, values)
+
+
+def index_vertices(points: Tensor, tol: float = 1e-5) -> Tensor:
+    """int32 [vertex]: for every point, the index of the first point with the
+    same quantized position round(points / tol) (index_vertices.py:6-27).
+
+    Quantization is that of the reference on its CUDA device: the division
+    by the Python scalar ``tol`` is a multiplication by the float32
+    reciprocal of float32(tol), rounded half to even."""
+    points = _f32(points, "points")
+    device = nt.require_cuda(points)
+    v, _ = points.shape
+    if v == 0:
+        raise RuntimeError("index_vertices: max() of an empty tensor (no points)")
+    if v > 2**31 - 1:
+        raise ValueError("index_vertices handles at most 2^31 - 1 points")
+    inv_tol = float(np.float32(1.0) / np.float32(tol))
+    quantized = torch.empty((v, 3), dtype=torch.int64, device=device)
+    max_abs = torch.empty((1,), dtype=torch.int64, device=device)
+    nt.call("mt_quantize_points", points.data_ptr(), v, inv_tol, quantized.data_ptr(), max_abs.data_ptr(),
+            nt.stream(device))
+    bits = (int(max_abs.item()) & 0xFFFFFFFFFFFFFFFF).bit_length() + 1
+    if bits * 3 > 63:
+        raise RuntimeError(f"need {bits*3} bits, exceed 63 bits total")
+    keys = torch.empty((v,), dtype=torch.int64, device=device)
+    values = torch.empty((v,), dtype=torch.int32, device=device)
+    nt.call("mt_pack_point_keys", quantized.data_ptr(), v, bits, keys.data_ptr(), values.data_ptr(),
+            nt.stream(device))
+    return _index_pairs(keys, values)
 
 
 # ---------------------------------------------------------------------------

@@ -51,6 +51,10 @@ SOURCES = {
     ("triangle_extraction", "count_triangle_faces.slang"): [],
     ("triangle_extraction", "create_triangle_faces.slang"): [],
     ("triangle_extraction", "compute_sdf_regularizers.slang"): [],
+    ("triangle_extraction", "write_occupancy.slang"): [],
+    ("triangle_extraction", "upscale_occupancy.slang"): [],
+    ("triangle_extraction", "upscale_parameters.slang"): [],
+    ("triangle_extraction", "get_occupancy_mesh.slang"): [],
     ("triangle_rasterization", "keys.slang"): [],
     ("triangle_rasterization", "project_vertices.slang"): [],
     ("triangle_rasterization", "bound_triangles.slang"): [],
@@ -73,7 +77,12 @@ AUTODIFF = {
 
 # Files whose local/struct arrays are copied as values (aggregate returns):
 # their array declarations become std::array.
-ARRAY_VALUE_FILES = {"create_triangle_vertices.slang", "evaluate_spherical_harmonics.slang"}
+ARRAY_VALUE_FILES = {"create_triangle_vertices.slang", "evaluate_spherical_harmonics.slang",
+                     "upscale_parameters.slang"}
+
+# Files that apply Slang's floating-point `%` (fmod) as `x % 1`.
+FLOAT_MOD = re.compile(r"\b(\w+)\s*%\s*1\s*;")
+FLOAT_MOD_FILES = {"upscale_parameters.slang"}
 
 ATTRIBUTE = re.compile(r"^\s*\[(AutoPyBindCUDA|CUDAKernel|Differentiable|NoDiffThis|require\(cuda\)|"
                        r"BackwardDerivative\([^)]*\))\]\s*$", re.M)
@@ -149,6 +158,10 @@ def translate(src: str, fname: str, drops: list[str]) -> tuple[str, list[str]]:
     src = re.sub(r"\bvar\b", "auto", src)
     src = re.sub(r"\bno_diff\s+", "", src)
     src = re.sub(r"\bgroupshared\b", "static", src)
+    src = re.sub(r"\bMemoryOrder\.(\w+)", r"MemoryOrder::\1", src)
+    src = re.sub(r"\b__atomic_or\(", "slang_atomic_or(", src)
+    if fname in FLOAT_MOD_FILES:
+        src = FLOAT_MOD.sub(r"std::fmod(\1, 1.0f);", src)
     src = re.sub(r"typealias\s+(\w+)\s*=\s*(\w+)\[(\w+)\]\s*;", r"using \1 = std::array<\2, \3>;", src)
     src = FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", src)
     if fname in ARRAY_VALUE_FILES:
@@ -181,8 +194,12 @@ def generate(root: Path) -> list[Path]:
     return written
 
 
+def reference_root() -> Path:
+    return Path(os.environ.get("MESHTRYOSHKA_REFERENCE", DEFAULT_ROOT))
+
+
 def build(root: Path | str | None = None, force: bool = False) -> Path | None:
-    root = Path(root) if root else Path(os.environ.get("MESHTRYOSHKA_REFERENCE", DEFAULT_ROOT))
+    root = Path(root) if root else reference_root()
     if not (root / "triangle_extraction").is_dir():
         return None
     driver = SHIM_DIR / "driver.cpp"

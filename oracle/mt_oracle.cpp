@@ -483,6 +483,202 @@ void or_dilate_occupancy(const int32_t* occ, int I, int J, int KP, int d, int32_
 }
 
 // ---------------------------------------------------------------------------
+// Coarse-to-fine subdivision and the occupancy mesh.
+// ---------------------------------------------------------------------------
+
+// write_occupancy.slang:1-20 (one atomic OR per index; indices outside the
+// grid are skipped).
+void or_write_occupancy(const int32_t* voxel_indices, int64_t n, int32_t* occ, int64_t words) {
+  for (int64_t t = 0; t < n; ++t) {
+    const int32_t v = voxel_indices[t];
+    if (v < 0 || (int64_t)(v >> 5) >= words) continue;
+    occ[v >> 5] = (int32_t)((uint32_t)occ[v >> 5] | (1u << (v % 32)));
+  }
+}
+
+// upscale_occupancy.slang:1-74: per new voxel, the 8 corners sampled with
+// unsigned 32-bit arithmetic (sample_corner, :1-24); `mask` (nullable) is
+// AND-ed into every old word (upscale_parameters.py:49).
+void or_upscale_occupancy(const int32_t* occ, const int32_t* mask, int I, int J, int KP, int I2, int J2, int KP2,
+                          int32_t* out) {
+  const uint32_t i_max_sampled = (uint32_t)I, j_max_sampled = (uint32_t)J, k_max_sampled = (uint32_t)KP << 5;
+  const uint32_t i_max = (uint32_t)I2, j_max = (uint32_t)J2, k_max = (uint32_t)KP2 << 5;
+  auto word = [&](uint32_t i, uint32_t j, uint32_t kp) {
+    const int64_t w = ((int64_t)i * J + j) * KP + kp;
+    uint32_t x = (uint32_t)occ[w];
+    if (mask) x &= (uint32_t)mask[w];
+    return x;
+  };
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < I2; ++i)
+    for (int j = 0; j < J2; ++j)
+      for (int kp = 0; kp < KP2; ++kp) {
+        int32_t result = 0;
+        for (int bit = 0; bit < 32; ++bit) {
+          const uint32_t k = ((uint32_t)kp << 5) + (uint32_t)bit;
+          bool value = false;
+          for (uint32_t di = 0; di < 2; ++di)
+            for (uint32_t dj = 0; dj < 2; ++dj)
+              for (uint32_t dk = 0; dk < 2; ++dk) {
+                const uint32_t is = (((uint32_t)i + di) * i_max_sampled - di) / i_max;
+                const uint32_t js = (((uint32_t)j + dj) * j_max_sampled - dj) / j_max;
+                const uint32_t ks = ((k + dk) * k_max_sampled - dk) / k_max;
+                value |= ((word(is, js, ks >> 5) >> (ks % 32)) & 1u) != 0;
+              }
+          result |= (int32_t)((uint32_t)value << bit);
+        }
+        out[((int64_t)i * J2 + j) * KP2 + kp] = result;
+      }
+}
+
+// upscale_parameters.slang:1-198: every new vertex (in vertex-occupancy
+// order) samples the old vertices trilinearly (sample_trilinear, :55-127),
+// skipping absent corners and renormalising by the summed weight.
+void or_upscale_parameters(const int32_t* ovocc, const int32_t* ovoff, const float* osdf, const float* osh, int C,
+                           int64_t Vold, int I1, int J1, int KP1, const int32_t* nvocc, const int32_t* nvoff, int I1n,
+                           int J1n, int KP1n, int64_t Vnew, float* nsdf, float* nsh) {
+  const int i_max = I1n - 1, j_max = J1n - 1, k_packed_max = KP1n - 1;
+  const float inv_i_max = 1 / (float)i_max;
+  const float inv_j_max = 1 / (float)j_max;
+  const float inv_k_max = 1 / (float)(32 * k_packed_max);
+  // read_vertex (:9-53): the old vertex index, or -1.
+  auto read_vertex = [&](int i, int j, int k) -> int64_t {
+    if (i < 0 || j < 0 || k < 0) return -1;
+    const int k_packed = k / 32;
+    if (i >= I1 || j >= J1 || k_packed >= KP1) return -1;
+    const int bit = k % 32;
+    const int64_t w = ((int64_t)i * J1 + j) * KP1 + k_packed;
+    uint32_t chunk = (uint32_t)ovocc[w];
+    if ((chunk & (1u << bit)) == 0) return -1;
+    int64_t index = ovoff[w];
+    for (int d = 0; d < bit; ++d) {
+      if (chunk & 1u) ++index;
+      chunk >>= 1;
+    }
+    return index < Vold ? index : -1;
+  };
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i <= i_max; ++i) {
+    std::vector<float> sh((size_t)C * 3);
+    for (int j = 0; j <= j_max; ++j)
+      for (int kp = 0; kp <= k_packed_max; ++kp) {
+        const int64_t w = ((int64_t)i * J1n + j) * KP1n + kp;
+        int64_t vertex_index = nvoff[w];
+        uint32_t chunk = (uint32_t)nvocc[w];
+        int k = 32 * kp;
+        for (int bit = 0; bit < 32; ++bit, chunk >>= 1, ++k) {
+          if ((chunk & 1u) == 0) continue;
+          const float x = (float)k * inv_k_max, y = (float)j * inv_j_max, z = (float)i * inv_i_max;
+          const float xu = x * (float)((KP1 - 1) * 32), yu = y * (float)(J1 - 1), zu = z * (float)(I1 - 1);
+          const int oi = (int)zu, oj = (int)yu, ok = (int)xu;
+          const float ti = std::fmod(zu, 1.0f), tj = std::fmod(yu, 1.0f), tk = std::fmod(xu, 1.0f);
+          std::fill(sh.begin(), sh.end(), 0.0f);
+          float sd = 0.0f, denominator = 0.0f;
+          for (int di = 0; di < 2; ++di)
+            for (int dj = 0; dj < 2; ++dj)
+              for (int dk = 0; dk < 2; ++dk) {
+                const int64_t v = read_vertex(oi + di, oj + dj, ok + dk);
+                if (v < 0) continue;
+                const float weight = (di == 0 ? 1 - ti : ti) * (dj == 0 ? 1 - tj : tj) * (dk == 0 ? 1 - tk : tk);
+                for (int s = 0; s < C; ++s)
+                  for (int c = 0; c < 3; ++c) sh[s * 3 + c] += weight * osh[((int64_t)s * Vold + v) * 3 + c];
+                sd += weight * osdf[v];
+                denominator += weight;
+              }
+          const float multiplier = 1 / denominator;
+          if (vertex_index >= 0 && vertex_index < Vnew) {
+            for (int s = 0; s < C; ++s)
+              for (int c = 0; c < 3; ++c) nsh[((int64_t)s * Vnew + vertex_index) * 3 + c] = sh[s * 3 + c] * multiplier;
+            nsdf[vertex_index] = sd * multiplier;
+          }
+          ++vertex_index;
+        }
+      }
+  }
+}
+
+// get_occupancy_mesh.slang:1-54 count_triangles, over (I+1)(J+1)(KP+1)
+// entries; counts has one more entry, set to 0.
+void or_count_occupancy_mesh_triangles(const int32_t* occ, int I, int J, int KP, int32_t* counts) {
+  auto OCC = [&](int i, int j, int kp) { return (uint32_t)occ[((int64_t)i * J + j) * KP + kp]; };
+  const int64_t total = (int64_t)(I + 1) * (J + 1) * (KP + 1);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i <= I; ++i)
+    for (int j = 0; j <= J; ++j)
+      for (int kp = 0; kp <= KP; ++kp) {
+        const bool il = i == I, jl = j == J, kl = kp == KP;
+        uint32_t here = (il || jl || kl) ? 0u : OCC(i, j, kp);
+        uint32_t minus_i = (jl || kl || i == 0) ? 0u : OCC(i - 1, j, kp);
+        uint32_t minus_j = (il || kl || j == 0) ? 0u : OCC(i, j - 1, kp);
+        bool minus_k = (il || jl || kp == 0) ? false : (OCC(i, j, kp - 1) & 0x80000000u) != 0;
+        int faces = 0;
+        for (int bit = 0; bit < 32; ++bit) {
+          const bool h = here & 1u, mi = minus_i & 1u, mj = minus_j & 1u;
+          faces += (int)(h != mi) + (int)(h != mj) + (int)(h != minus_k);
+          minus_k = h;
+          here >>= 1;
+          minus_i >>= 1;
+          minus_j >>= 1;
+        }
+        counts[((int64_t)i * (J + 1) + j) * (KP + 1) + kp] = 2 * faces;
+      }
+  counts[total] = 0;
+}
+
+// get_occupancy_mesh.slang:56-220 create_face / create_triangles.
+void or_create_occupancy_mesh_triangles(const int32_t* occ, int I, int J, int KP, const int32_t* offsets,
+                                        const float* colors, float* verts, float* tri_colors) {
+  auto OCC = [&](int i, int j, int kp) { return (uint32_t)occ[((int64_t)i * J + j) * KP + kp]; };
+  const int ijk_max[3] = {I, J, KP * 32};
+  auto create_face = [&](int64_t index, const int ijk[3], int axis, bool upper_bit) {
+    const int axis0 = (axis + 1) % 3, axis1 = (axis + 2) % 3;
+    float v00[3], v01[3], v10[3], v11[3];
+    const float plane = (float)ijk[axis] / (float)ijk_max[axis];
+    v00[axis] = v01[axis] = v10[axis] = v11[axis] = plane;
+    const float v0x = (float)ijk[axis0] / (float)ijk_max[axis0];
+    const float v1x = (float)(ijk[axis0] + 1) / (float)ijk_max[axis0];
+    const float vx0 = (float)ijk[axis1] / (float)ijk_max[axis1];
+    const float vx1 = (float)(ijk[axis1] + 1) / (float)ijk_max[axis1];
+    v00[axis0] = v0x, v00[axis1] = vx0;
+    v01[axis0] = v0x, v01[axis1] = vx1;
+    v10[axis0] = v1x, v10[axis1] = vx0;
+    v11[axis0] = v1x, v11[axis1] = vx1;
+    const int side = upper_bit ? 1 : 0;
+    const float* face_color = colors + (axis * 2 + side) * 3;
+    const float* triangles[2][3] = {{v00, upper_bit ? v01 : v10, upper_bit ? v10 : v01},
+                                    {v11, upper_bit ? v10 : v01, upper_bit ? v01 : v10}};
+    for (int t = 0; t < 2; ++t) {
+      for (int c = 0; c < 3; ++c)
+        for (int a = 0; a < 3; ++a) verts[((index + t) * 3 + c) * 3 + a] = triangles[t][c][2 - a];
+      for (int a = 0; a < 3; ++a) tri_colors[(index + t) * 3 + a] = face_color[a];
+    }
+  };
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i <= I; ++i)
+    for (int j = 0; j <= J; ++j)
+      for (int kp = 0; kp <= KP; ++kp) {
+        const bool il = i == I, jl = j == J, kl = kp == KP;
+        uint32_t here = (il || jl || kl) ? 0u : OCC(i, j, kp);
+        uint32_t minus_i = (jl || kl || i == 0) ? 0u : OCC(i - 1, j, kp);
+        uint32_t minus_j = (il || kl || j == 0) ? 0u : OCC(i, j - 1, kp);
+        bool minus_k = (il || jl || kp == 0) ? false : (OCC(i, j, kp - 1) & 0x80000000u) != 0;
+        int64_t index = offsets[((int64_t)i * (J + 1) + j) * (KP + 1) + kp];
+        int k = kp * 32;
+        for (int bit = 0; bit < 32; ++bit, ++k) {
+          const bool h = here & 1u, mi = minus_i & 1u, mj = minus_j & 1u;
+          const int ijk[3] = {i, j, k};
+          if (h != mi) create_face(index, ijk, 0, h), index += 2;
+          if (h != mj) create_face(index, ijk, 1, h), index += 2;
+          if (h != minus_k) create_face(index, ijk, 2, h), index += 2;
+          minus_k = h;
+          here >>= 1;
+          minus_i >>= 1;
+          minus_j >>= 1;
+        }
+      }
+}
+
+// ---------------------------------------------------------------------------
 // triangle_extraction/count_triangle_vertices.slang:3-37
 // ---------------------------------------------------------------------------
 void or_count_triangle_vertices(const float* sdf, const int32_t* lower, int64_t G, const float* level_sets, int S,

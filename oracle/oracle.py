@@ -33,6 +33,11 @@ _SIGNATURES = {
     "or_count_occupancy": (None, [P, I32, I32, I32, P]),
     "or_create_voxels": (None, [P, P, P, P, I32, I32, I32, I64, I64, P, P, P, P, P]),
     "or_dilate_occupancy": (None, [P, I32, I32, I32, I32, P]),
+    "or_write_occupancy": (None, [P, I64, P, I64]),
+    "or_upscale_occupancy": (None, [P, P, I32, I32, I32, I32, I32, I32, P]),
+    "or_upscale_parameters": (None, [P, P, P, P, I32, I64, I32, I32, I32, P, P, I32, I32, I32, I64, P, P]),
+    "or_count_occupancy_mesh_triangles": (None, [P, I32, I32, I32, P]),
+    "or_create_occupancy_mesh_triangles": (None, [P, I32, I32, I32, P, P, P, P]),
     "or_count_triangle_vertices": (None, [P, P, I64, P, I32, P]),
     "or_create_triangle_vertices": (None, [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P]),
     "or_create_triangle_vertices_backward": (None, [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P]),
@@ -147,6 +152,103 @@ def dilate_occupancy(occ: np.ndarray, dilation: int) -> np.ndarray:
     out = np.empty_like(occ)
     lib().or_dilate_occupancy(_p(occ), i, j, kp, dilation, _p(out))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Coarse-to-fine subdivision, occupancy mesh, vertex de-duplication
+# ---------------------------------------------------------------------------
+def write_occupancy(voxel_indices, packed_shape) -> np.ndarray:
+    idx = _c(voxel_indices, np.int32)
+    occ = np.zeros(packed_shape, np.int32)
+    lib().or_write_occupancy(_p(idx), idx.size, _p(occ), occ.size)
+    return occ
+
+
+def upscale_occupancy(occ, target_shape, mask=None) -> np.ndarray:
+    """upscale_occupancy.py:24-54; ``mask`` is AND-ed into the old words."""
+    occ = _c(occ, np.int32)
+    i, j, kp = occ.shape
+    it, jt, kt = target_shape
+    assert kt % 32 == 0 and it >= i and jt >= j and kt // 32 >= kp
+    out = np.empty((it, jt, kt // 32), np.int32)
+    mask = None if mask is None else _c(mask, np.int32)
+    lib().or_upscale_occupancy(_p(occ), _p(mask), i, j, kp, it, jt, kt // 32, _p(out))
+    return out
+
+
+def upscale_parameters(old_sdf, old_sh, old_occ, occ_to_upscale, new_resolution):
+    """upscale_parameters.py:35-99 on the host -> (sdf, sh, occupancy)."""
+    old_sdf = _c(old_sdf, np.float32)
+    old_sh = _c(old_sh, np.float32)
+    old_occ = _c(old_occ, np.int32)
+    new_occ = upscale_occupancy(old_occ, new_resolution, mask=occ_to_upscale)
+    ovocc, ovcounts = compute_vertex_occupancy(old_occ)
+    ovoff = exclusive_cumsum(ovcounts)
+    nvocc, nvcounts = compute_vertex_occupancy(new_occ)
+    nvoff = exclusive_cumsum(nvcounts)
+    n = int(nvoff[-1])
+    c = old_sh.shape[0]
+    sdf = np.zeros((n,), np.float32)
+    sh = np.zeros((c, n, 3), np.float32)
+    if n > 0:
+        lib().or_upscale_parameters(_p(ovocc), _p(ovoff), _p(old_sdf), _p(old_sh), c, old_sdf.shape[0],
+                                    *ovocc.shape, _p(nvocc), _p(nvoff), *nvocc.shape, n, _p(sdf), _p(sh))
+    return sdf, sh, new_occ
+
+
+def get_occupancy_mesh(occ, colors):
+    """get_occupancy_mesh.py:32-80 on the host -> (vertices [T,3,3], colors [T,3])."""
+    occ = _c(occ, np.int32)
+    colors = _c(colors, np.float32)
+    i, j, kp = occ.shape
+    counts = np.empty(((i + 1) * (j + 1) * (kp + 1) + 1,), np.int32)
+    lib().or_count_occupancy_mesh_triangles(_p(occ), i, j, kp, _p(counts))
+    offsets = exclusive_cumsum(counts)
+    t = int(offsets[-1])
+    verts = np.zeros((t, 3, 3), np.float32)
+    tcol = np.zeros((t, 3), np.float32)
+    if t > 0:
+        lib().or_create_occupancy_mesh_triangles(_p(occ), i, j, kp, _p(offsets), _p(colors), _p(verts), _p(tcol))
+    return verts, tcol
+
+
+def subdivide(vertices, sdf, sh, occ, triangle_voxel_indices, new_resolution, dilation=4, tol=1e-6):
+    """tesseract.py:432-475 for one component on the host -> (sdf, sh, occupancy)."""
+    canonical = index_vertices(vertices, tol).astype(np.int64)
+    sdf = np.asarray(sdf, np.float32)[canonical]
+    sh = np.asarray(sh, np.float32)[:, canonical, :]
+    mask = write_occupancy(triangle_voxel_indices, np.asarray(occ).shape)
+    mask = dilate_occupancy(mask, dilation)
+    return upscale_parameters(sdf, sh, occ, mask, new_resolution)
+
+
+def index_keys(keys) -> np.ndarray:
+    """index_vertices.py:30-51: every key mapped to the index of the first
+    equal key (a stable sort puts it at the start of its run)."""
+    keys = np.asarray(keys, np.int64)
+    n = keys.size
+    order = np.argsort(keys, kind="stable")
+    sk = keys[order]
+    head = np.ones(n, bool)
+    head[1:] = sk[1:] != sk[:-1]
+    start = np.maximum.accumulate(np.where(head, np.arange(n), 0))
+    out = np.empty(n, np.int32)
+    out[order] = order[start]
+    return out
+
+
+def index_vertices(points, tol=1e-5) -> np.ndarray:
+    """index_vertices.py:6-27 with the reference device's quantization:
+    round-half-even of points * float32(1 / float32(tol))."""
+    points = np.asarray(points, np.float32)
+    inv = np.float32(1.0) / np.float32(tol)
+    q = np.rint(points * inv).astype(np.int64)
+    bits = int(np.abs(q).max()).bit_length() + 1
+    if bits * 3 > 63:
+        raise RuntimeError(f"need {bits*3} bits, exceed 63 bits total")
+    x, y, z = q[:, 0], q[:, 1], q[:, 2]
+    keys = (x << (2 * bits)) | (y << bits) | z
+    return index_keys(keys)
 
 
 # ---------------------------------------------------------------------------
@@ -484,6 +586,33 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
     bg = np.asarray(background, np.float32)
     image = np.clip(raw[:, :3] + raw[:, 3:4] * bg[None, :, None, None], 0.0, 1.0)
     return FusedRender(xy, depth, tmin, tmax, count, keys, tri, sk, st, tb, colors, raw, image)
+
+
+def render_explicit(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, sdf, sh, sh_degree,
+                    sharpness, background, tile_shape=(16, 16), near_plane=0.2, num_camera_bits=6, num_shell_bits=6,
+                    num_tile_bits=20) -> np.ndarray:
+    """triangle_rasterization/__init__.py:97-164 on the host (ssaa = 1):
+    per-shell rasterization, interpolation, then compositing with the
+    background blended in (composite.py:117). Returns [B, 3, H, W]."""
+    h, w = image_shape
+    b = extrinsics.shape[0]
+    s = shell_face_boundaries.shape[0]
+    rows, cols = -(-h // tile_shape[0]), -(-w // tile_shape[1])
+    kd = explicit_key_defines(num_camera_bits, num_shell_bits, num_tile_bits)
+    xy, depth = project_vertices(vertices, extrinsics, intrinsics)
+    tmin, tmax, count = bound_triangles(xy, depth, faces, tile_shape, (rows, cols), near_plane)
+    keys, tri = generate_keys(depth, faces, shell_face_boundaries, tmin, tmax, count, cols, kd)
+    sk, st = sort_pairs(keys, tri)
+    tb = delineate_tiles(sk, kd, True, b, s, rows * cols)
+    uv, index = intersect(xy, faces, st, tb, s, tile_shape, image_shape)
+    colors = evaluate_spherical_harmonics(vertices, sh, extrinsics, sh_degree)
+    isdf, icol = interpolate(uv, index, faces, sdf, colors)
+    per_pixel_sdf = isdf.transpose(0, 2, 3, 1).reshape(-1, s)
+    per_pixel_col = icol.transpose(0, 2, 3, 1, 4).reshape(-1, s, 3)
+    mask = (index != -1).transpose(0, 2, 3, 1).reshape(-1, s)
+    out_c, out_t = composite(per_pixel_sdf, per_pixel_col, mask, sharpness)
+    image = out_c + np.asarray(background, np.float32)[None, :] * out_t[:, None]
+    return image.reshape(b, h, w, 3).transpose(0, 3, 1, 2)
 
 
 def intersect(xy, faces, sorted_tri, tile_boundaries, num_shells, tile_shape, image_shape):

@@ -22,6 +22,11 @@ _SIGNATURES = {
     "ref_count_occupancy": [P, I, I, I, P],
     "ref_create_voxels": [P, P, P, P, I, I, I, I64, I64, P, P, P, P, P],
     "ref_dilate_occupancy": [P, I, I, I, I, P],
+    "ref_write_occupancy": [P, I64, P, I64],
+    "ref_upscale_occupancy": [P, I, I, I, I, I, I, P],
+    "ref_upscale_parameters": [I, P, P, P, P, I64, I, I, I, P, P, I, I, I, I64, P, P],
+    "ref_count_occupancy_mesh_triangles": [P, I, I, I, P],
+    "ref_create_occupancy_mesh_triangles": [P, I, I, I, P, I64, P, P, P],
     "ref_count_triangle_vertices": [P, P, I64, P, I, P],
     "ref_create_triangle_vertices": [P, P, P, I, P, I64, P, I, P, I64, P, P, P, P],
     "ref_count_triangle_faces": [P, P, I64, P, I64, P, I, P, P],
@@ -96,6 +101,89 @@ def dilate_occupancy(occ, d):
     out = np.zeros_like(occ)
     lib().ref_dilate_occupancy(_p(occ), *occ.shape, d, _p(out))
     return out
+
+
+def python_module(relative_path: str):
+    """Imports one of the reference's pure-Python modules (e.g.
+    ``triangle_extraction/index_vertices.py``) from the mounted tree. Its
+    ``jaxtyping`` annotations are satisfied by a stand-in module when the
+    package is not installed (annotations only; no behaviour)."""
+    import importlib.util
+    import sys
+    import types
+
+    if "jaxtyping" not in sys.modules:
+        try:
+            import jaxtyping  # noqa: F401
+        except ImportError:
+            stub = types.ModuleType("jaxtyping")
+
+            class _Annotation:
+                def __class_getitem__(cls, item):
+                    return object
+
+            for name in ("Float", "Float32", "Int", "Int32", "Int64", "Bool", "Shaped"):
+                setattr(stub, name, _Annotation)
+            sys.modules["jaxtyping"] = stub
+    path = build_ref.reference_root() / relative_path
+    spec = importlib.util.spec_from_file_location("reference_" + path.stem, path)
+    module = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(module)
+    return module
+
+
+def write_occupancy(voxel_indices, packed_shape):
+    idx = _c(voxel_indices, np.int32)
+    occ = np.zeros(packed_shape, np.int32)
+    lib().ref_write_occupancy(_p(idx), idx.size, _p(occ), occ.size)
+    return occ
+
+
+def upscale_occupancy(occ, target_shape):
+    occ = _c(occ, np.int32)
+    it, jt, kt = target_shape
+    out = np.zeros((it, jt, kt // 32), np.int32)
+    lib().ref_upscale_occupancy(_p(occ), *occ.shape, it, jt, kt // 32, _p(out))
+    return out
+
+
+def _vertex_offsets(occ):
+    i, j, kp = occ.shape
+    vocc = np.zeros((i + 1, j + 1, kp + 1), np.int32)
+    vcounts = np.zeros(((i + 1) * (j + 1) * (kp + 1) + 1,), np.int32)
+    lib().ref_compute_vertex_occupancy(_p(occ), i, j, kp, _p(vocc), _p(vcounts))
+    voff = np.concatenate(([0], np.cumsum(vcounts)[:-1])).astype(np.int32)
+    return vocc, voff
+
+
+def upscale_parameters(old_sdf, old_sh, old_occ, occ_to_upscale, new_resolution):
+    """upscale_parameters.py:35-99 with the reference's kernels (numpy scans)."""
+    old_sdf, old_sh = _c(old_sdf, np.float32), _c(old_sh, np.float32)
+    old_occ = _c(old_occ, np.int32)
+    new_occ = upscale_occupancy(old_occ & _c(occ_to_upscale, np.int32), new_resolution)
+    ovocc, ovoff = _vertex_offsets(old_occ)
+    nvocc, nvoff = _vertex_offsets(new_occ)
+    n, c = int(nvoff[-1]), old_sh.shape[0]
+    sdf, sh = np.zeros((n,), np.float32), np.zeros((c, n, 3), np.float32)
+    if n > 0:
+        lib().ref_upscale_parameters(c, _p(ovocc), _p(ovoff), _p(old_sdf), _p(old_sh), old_sdf.shape[0],
+                                     *ovocc.shape, _p(nvocc), _p(nvoff), *nvocc.shape, n, _p(sdf), _p(sh))
+    return sdf, sh, new_occ
+
+
+def get_occupancy_mesh(occ, colors):
+    """get_occupancy_mesh.py:32-80 with the reference's kernels (numpy scan)."""
+    occ, colors = _c(occ, np.int32), _c(colors, np.float32)
+    i, j, kp = occ.shape
+    counts = np.zeros(((i + 1) * (j + 1) * (kp + 1) + 1,), np.int32)
+    lib().ref_count_occupancy_mesh_triangles(_p(occ), i, j, kp, _p(counts))
+    offsets = np.concatenate(([0], np.cumsum(counts)[:-1])).astype(np.int32)
+    t = int(offsets[-1])
+    verts, tcol = np.zeros((t, 3, 3), np.float32), np.zeros((t, 3), np.float32)
+    if t > 0:
+        lib().ref_create_occupancy_mesh_triangles(_p(occ), i, j, kp, _p(offsets), t, _p(verts), _p(tcol),
+                                                  _p(colors))
+    return verts, tcol
 
 
 def tessellate(sdf, vertices, sh, neighbors, lower, upper, indices, level_sets):

@@ -108,6 +108,35 @@ namespace k_create_faces {
 namespace k_regularizers {
 #include "triangle_extraction__compute_sdf_regularizers.inc"
 }
+namespace k_write_occupancy {
+#include "triangle_extraction__write_occupancy.inc"
+}
+namespace k_upscale_occupancy {
+#include "triangle_extraction__upscale_occupancy.inc"
+}
+#define NUM_SPHERICAL_HARMONICS 1
+namespace k_upscale_parameters_1 {
+#include "triangle_extraction__upscale_parameters.inc"
+}
+#undef NUM_SPHERICAL_HARMONICS
+#define NUM_SPHERICAL_HARMONICS 4
+namespace k_upscale_parameters_4 {
+#include "triangle_extraction__upscale_parameters.inc"
+}
+#undef NUM_SPHERICAL_HARMONICS
+#define NUM_SPHERICAL_HARMONICS 9
+namespace k_upscale_parameters_9 {
+#include "triangle_extraction__upscale_parameters.inc"
+}
+#undef NUM_SPHERICAL_HARMONICS
+#define NUM_SPHERICAL_HARMONICS 16
+namespace k_upscale_parameters_16 {
+#include "triangle_extraction__upscale_parameters.inc"
+}
+#undef NUM_SPHERICAL_HARMONICS
+namespace k_occupancy_mesh {
+#include "triangle_extraction__get_occupancy_mesh.inc"
+}
 namespace k_project {
 #include "triangle_rasterization__project_vertices.inc"
 }
@@ -239,6 +268,59 @@ void ref_dilate_occupancy(int32_t* occ, int I, int J, int KP, int d, int32_t* ou
   TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP}), n(out, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
   run_grid(ceil_grid(uint3(I, J, KP), uint3(32, 32, 1)), uint3(32, 32, 1),
            [&] { k_dilate::dilate_occupancy(o, n, d); });
+}
+
+// write_occupancy.py:30-44 (grid zero-filled by the caller)
+void ref_write_occupancy(int32_t* voxel_indices, int64_t n, int32_t* occ, int64_t words) {
+  TensorView<int> o(occ, {(uint64_t)words}), v(voxel_indices, {(uint64_t)n});
+  run_grid(uint3((uint)((n + 255) / 256), 1, 1), uint3(256, 1, 1),
+           [&] { k_write_occupancy::write_occupancy(o, v, 0, 1); });
+}
+
+// upscale_occupancy.py:42-52
+void ref_upscale_occupancy(int32_t* occ, int I, int J, int KP, int I2, int J2, int KP2, int32_t* out) {
+  TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
+  TensorView<int> n(out, {(uint64_t)I2, (uint64_t)J2, (uint64_t)KP2});
+  run_grid(ceil_grid(uint3(I2, J2, KP2), uint3(32, 32, 1)), uint3(32, 32, 1),
+           [&] { k_upscale_occupancy::upscale_occupancy(o, n); });
+}
+
+// upscale_parameters.py:77-93
+void ref_upscale_parameters(int C, int32_t* ovocc, int32_t* ovoff, float* osdf, float* osh, int64_t Vold, int I1,
+                            int J1, int KP1, int32_t* nvocc, int32_t* nvoff, int I1n, int J1n, int KP1n,
+                            int64_t Vnew, float* nsdf, float* nsh) {
+  TensorView<int> ov(ovocc, {(uint64_t)I1, (uint64_t)J1, (uint64_t)KP1});
+  TensorView<int> oo(ovoff, {(uint64_t)I1, (uint64_t)J1, (uint64_t)KP1});
+  TensorView<float> od(osdf, {(uint64_t)Vold}), osv(osh, {(uint64_t)C, (uint64_t)Vold, 3});
+  TensorView<int> nv(nvocc, {(uint64_t)I1n, (uint64_t)J1n, (uint64_t)KP1n});
+  TensorView<int> no(nvoff, {(uint64_t)I1n, (uint64_t)J1n, (uint64_t)KP1n});
+  TensorView<float> nd(nsdf, {(uint64_t)Vnew}), nsv(nsh, {(uint64_t)C, (uint64_t)Vnew, 3});
+  const uint3 grid = ceil_grid(uint3(I1n, J1n, KP1n), uint3(32, 32, 1)), block(32, 32, 1);
+  switch (C) {
+    case 1: run_grid(grid, block, [&] { k_upscale_parameters_1::upscale_parameters(ov, oo, od, osv, nv, no, nd, nsv); }); break;
+    case 4: run_grid(grid, block, [&] { k_upscale_parameters_4::upscale_parameters(ov, oo, od, osv, nv, no, nd, nsv); }); break;
+    case 9: run_grid(grid, block, [&] { k_upscale_parameters_9::upscale_parameters(ov, oo, od, osv, nv, no, nd, nsv); }); break;
+    case 16: run_grid(grid, block, [&] { k_upscale_parameters_16::upscale_parameters(ov, oo, od, osv, nv, no, nd, nsv); }); break;
+    default: std::abort();
+  }
+}
+
+// get_occupancy_mesh.py:43-56 (counts zero-filled by the caller)
+void ref_count_occupancy_mesh_triangles(int32_t* occ, int I, int J, int KP, int32_t* counts) {
+  TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
+  TensorView<int> c(counts, {(uint64_t)I + 1, (uint64_t)J + 1, (uint64_t)KP + 1});
+  run_grid(ceil_grid(uint3(I + 1, J + 1, KP + 1), uint3(32, 32, 1)), uint3(32, 32, 1),
+           [&] { k_occupancy_mesh::count_triangles(o, c); });
+}
+
+// get_occupancy_mesh.py:66-78
+void ref_create_occupancy_mesh_triangles(int32_t* occ, int I, int J, int KP, int32_t* offsets, int64_t T,
+                                         float* verts, float* tri_colors, float* colors) {
+  TensorView<int> o(occ, {(uint64_t)I, (uint64_t)J, (uint64_t)KP});
+  TensorView<int> off(offsets, {(uint64_t)I + 1, (uint64_t)J + 1, (uint64_t)KP + 1});
+  TensorView<float> tv(verts, {(uint64_t)T, 3, 3}), tc(tri_colors, {(uint64_t)T, 3}), col(colors, {3, 2, 3});
+  run_grid(ceil_grid(uint3(I + 1, J + 1, KP + 1), uint3(32, 32, 1)), uint3(32, 32, 1),
+           [&] { k_occupancy_mesh::create_triangles(o, off, tv, tc, col); });
 }
 
 // count_triangle_vertices.py:31-50

@@ -240,6 +240,10 @@ struct TensorView {
   }
   uint size(int i) const { return (uint)sizes[i]; }
   T* data_ptr() const { return ptr; }
+  template <typename I, typename = std::enable_if_t<std::is_integral_v<I>>>
+  T* data_ptr_at(I i) const {
+    return ptr + (int64_t)i;
+  }
 
   template <typename... I>
   uint64_t offset(I... idx) const {
@@ -312,6 +316,12 @@ T store(const TensorView<T>& x, I idx, V value) {
 template <typename U, int N>
 void store_once(const DiffTensorView& x, const vec<U, N>& idx, float value) {
   x[idx] = value;
+}
+
+// Atomics (emulated blocks run in parallel threads).
+enum class MemoryOrder { Relaxed };
+inline int slang_atomic_or(int& target, int value, MemoryOrder) {
+  return std::atomic_ref<int>(target).fetch_or(value, std::memory_order_relaxed);
 }
 
 // ---------------------------------------------------------------------------

@@ -126,6 +126,77 @@ def extraction_fixture(ref) -> dict[str, np.ndarray]:
 
 
 # ---------------------------------------------------------------------------
+# Subdivision: write / upscale occupancy, parameter upscaling, occupancy mesh,
+# vertex de-duplication
+# ---------------------------------------------------------------------------
+SUBDIVISION_CASES = {
+    # name: (old grid bits shape, new resolution, SH coefficients)
+    "double": ((4, 4, 32), (8, 8, 64), 4),
+    "odd": ((5, 3, 32), (9, 7, 96), 1),
+    "same": ((3, 4, 32), (3, 4, 32), 9),
+}
+
+
+def _lattice_points(rng, n_unique: int, n: int, tol: float) -> np.ndarray:
+    """Points within 0.3 tol of a lattice of multiples of tol: duplicates
+    within the tolerance, and no coordinate near a rounding boundary, so that
+    round(p / tol) is the same whether the division is exact or a
+    multiplication by the reciprocal (as torch does on CUDA)."""
+    cells = rng.integers(-2000, 2000, size=(n_unique, 3))
+    pick = rng.integers(0, n_unique, size=n)
+    jitter = rng.uniform(-0.3, 0.3, size=(n, 3))
+    pts = ((cells[pick] + jitter) * tol).astype(np.float32)
+    by_div = np.rint(pts / np.float32(tol))
+    by_mul = np.rint(pts * (np.float32(1.0) / np.float32(tol)))
+    assert np.array_equal(by_div, by_mul) and np.array_equal(by_div, cells[pick])
+    return pts
+
+
+def subdivision_fixture(ref) -> dict[str, np.ndarray]:
+    import torch
+
+    rng = np.random.default_rng(11)
+    out: dict[str, np.ndarray] = {}
+    for name, (shape, resolution, c) in SUBDIVISION_CASES.items():
+        occ = _pack(rng.random(shape) < 0.35)
+        mask = _pack(rng.random(shape) < 0.6)
+        vox = ref.extract_voxels(occ)
+        v = vox["vertices"].shape[0]
+        sdf = rng.normal(0, 0.1, v).astype(np.float32)
+        sh = rng.normal(0, 1, (c, v, 3)).astype(np.float32)
+        new_sdf, new_sh, new_occ = ref.upscale_parameters(sdf, sh, occ, mask, resolution)
+        out.update({f"{name}/occupancy": occ, f"{name}/mask": mask, f"{name}/resolution": np.array(resolution),
+                    f"{name}/signed_distances": sdf, f"{name}/spherical_harmonics": sh,
+                    f"{name}/upscaled_occupancy": ref.upscale_occupancy(occ, resolution),
+                    f"{name}/new_signed_distances": new_sdf, f"{name}/new_spherical_harmonics": new_sh,
+                    f"{name}/new_occupancy": new_occ})
+        colors = rng.uniform(0, 1, (3, 2, 3)).astype(np.float32)
+        verts, tcol = ref.get_occupancy_mesh(occ, colors)
+        out.update({f"{name}/mesh_colors_in": colors, f"{name}/mesh_vertices": verts, f"{name}/mesh_colors": tcol})
+        indices = rng.integers(0, occ.size * 32, size=300).astype(np.int32)
+        out.update({f"{name}/voxel_indices": indices, f"{name}/written": ref.write_occupancy(indices, occ.shape)})
+
+    # index_vertices / index_keys: the reference's Python run with a stable
+    # sort, which is what torch's CUDA sort is above 4096 elements (a radix
+    # sort); the CPU default sort chooses an arbitrary member of each group.
+    module = ref.python_module("triangle_extraction/index_vertices.py")
+    sort = torch.Tensor.sort
+    torch.Tensor.sort = lambda self, *a, **k: sort(self, *a, **{**k, "stable": True})
+    try:
+        for tol in (1e-6, 1e-5):
+            pts = _lattice_points(rng, 1500, 4000, tol)
+            key = f"index_{tol:g}"
+            out[f"{key}/points"] = pts
+            out[f"{key}/index"] = module.index_vertices(torch.from_numpy(pts), tol).numpy()
+        keys = rng.integers(-40, 40, size=3000).astype(np.int64) * (1 << 40) + rng.integers(0, 3, size=3000)
+        out["index_keys/keys"] = keys
+        out["index_keys/index"] = module.index_keys(torch.from_numpy(keys)).numpy()
+    finally:
+        torch.Tensor.sort = sort
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Rasterization: a tessellated sphere seen by a few cameras
 # ---------------------------------------------------------------------------
 SCENES = {
@@ -214,7 +285,7 @@ def generate(reference: str | None = None) -> dict[str, dict[str, np.ndarray]]:
 
     if not ref.available():
         raise SystemExit("reference tree not found; cannot build its kernels")
-    fixtures = {"extraction": extraction_fixture(ref)}
+    fixtures = {"extraction": extraction_fixture(ref), "subdivision": subdivision_fixture(ref)}
     for name, kw in SCENES.items():
         fixtures[f"raster_{name}"] = raster_fixture(ref, **kw)
     return fixtures

@@ -10,6 +10,8 @@ import numpy as np
 GOLDEN_DIR = Path(__file__).resolve().parent / "golden"
 RASTER_SCENES = ("two_cams", "close_up")
 EXTRACTION_GRIDS = ("random", "sphere", "edges")
+SUBDIVISION_CASES = ("double", "odd", "same")
+INDEX_TOLERANCES = (1e-6, 1e-5)
 TESS_FIELDS = ("vertices", "signed_distances", "spherical_harmonics", "faces", "voxel_indices", "vertex_offsets",
                "face_offsets", "cell_codes", "vertex_types")
 

@@ -3,9 +3,11 @@ oracle consume identical input arrays."""
 
 from __future__ import annotations
 
+import dataclasses
 from dataclasses import dataclass
 
 import numpy as np
+import torch
 
 from meshtryoshka_gb300 import synthetic
 from oracle import oracle
@@ -47,9 +49,32 @@ def sphere_mesh(n=64, levels=(0.02, 0.0, -0.02), sh_degree=0, seed=0, radius=0.5
     return tri
 
 
+def multi_sphere_mesh(n=64, levels=(0.02, 0.0, -0.02), sh_degree=0, seed=0, spheres=6):
+    """The large configuration's layout at resolution n: a band around the
+    union of `spheres` spheres and an inward-facing background sphere."""
+    cfg = dataclasses.replace(synthetic.CONFIGS["large"], resolution=n, num_spheres=spheres, radius_range=(0.15, 0.3))
+    occ = synthetic.make_occupancy(cfg, "cpu").numpy()
+    vox = oracle.extract_voxels(occ)
+    centres, radii = synthetic.sphere_layout(cfg)
+    p = torch.from_numpy(2 * vox.vertices - 1)
+    d = synthetic.analytic_sdf(p, torch.from_numpy(centres), torch.from_numpy(radii), cfg.background_radius).numpy()
+    rng = np.random.default_rng(seed)
+    gsdf = (d + rng.normal(0, 0.002, len(d))).astype(np.float32)
+    c = (sh_degree + 1) ** 2
+    gsh = np.empty((c, len(d), 3), np.float32)
+    gsh[0] = rng.uniform(0, 1, (len(d), 3))
+    if c > 1:
+        gsh[1:] = rng.normal(0, 0.05, (c - 1, len(d), 3))
+    return oracle.tessellate_voxels(gsdf, vox.vertices, gsh, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                    vox.indices, np.array(levels, np.float32))
+
+
 def make_scene(n=64, levels=(0.02, 0.0, -0.02), sh_degree=0, cameras=((0.0, 0.0, 2.0),), image_shape=(128, 128),
-               fov=60.0, sharpness=50.0, seed=0) -> Scene:
-    tri = sphere_mesh(n, levels, sh_degree, seed)
+               fov=60.0, sharpness=50.0, seed=0, spheres=0) -> Scene:
+    if spheres:
+        tri = multi_sphere_mesh(n, levels, sh_degree, seed, spheres)
+    else:
+        tri = sphere_mesh(n, levels, sh_degree, seed)
     ext = np.stack([synthetic.look_at(np.array(c)) for c in cameras])
     intr = np.stack([synthetic.pinhole(image_shape[0], image_shape[1], fov) for _ in cameras])
     return Scene(
@@ -73,4 +98,9 @@ SCENES = {
                            fov=55.0, sh_degree=3, levels=(0.03, 0.01, -0.01, -0.03)),
     "close_up": dict(cameras=((0.3, 0.2, 0.9),), image_shape=(96, 64), fov=70.0, levels=(0.01, -0.01),
                      sh_degree=1),
+    # Several objects and a background seen from inside, 16 shells: shells of
+    # different objects interleave in depth, where the fused walk and the
+    # per-shell explicit mode give different images.
+    "multi_inside": dict(spheres=6, cameras=((0.6, 0.1, 0.0), (0.0, 0.2, 0.6)), image_shape=(48, 64), fov=55.0,
+                         levels=tuple(float(x) for x in np.linspace(0.02, -0.02, 16)), sh_degree=1),
 }

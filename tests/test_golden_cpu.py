@@ -175,3 +175,54 @@ def test_oracle_sdf_regularizers_match_reference(extraction, case):
                                           e[f"reg_{case}/grid_size"])
     for value, name in zip(got, ("eikonal_loss_pos", "eikonal_loss_neg", "curvature_loss")):
         np.testing.assert_array_equal(value, e[f"reg_{case}/{name}"], err_msg=name)
+
+
+# ---------------------------------------------------------------------------
+# Subdivision, occupancy mesh and vertex de-duplication
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def subdivision():
+    return goldens.load("subdivision")
+
+
+@pytest.mark.parametrize("case", goldens.SUBDIVISION_CASES)
+def test_oracle_subdivision_matches_reference(subdivision, case):
+    g = {k.split("/", 1)[1]: v for k, v in subdivision.items() if k.startswith(case + "/")}
+    resolution = tuple(int(x) for x in g["resolution"])
+    np.testing.assert_array_equal(oracle.upscale_occupancy(g["occupancy"], resolution), g["upscaled_occupancy"])
+    sdf, sh, occ = oracle.upscale_parameters(g["signed_distances"], g["spherical_harmonics"], g["occupancy"],
+                                             g["mask"], resolution)
+    np.testing.assert_array_equal(occ, g["new_occupancy"])
+    np.testing.assert_array_equal(sdf, g["new_signed_distances"])
+    np.testing.assert_array_equal(sh, g["new_spherical_harmonics"])
+    verts, colors = oracle.get_occupancy_mesh(g["occupancy"], g["mesh_colors_in"])
+    np.testing.assert_array_equal(verts, g["mesh_vertices"])
+    np.testing.assert_array_equal(colors, g["mesh_colors"])
+    np.testing.assert_array_equal(oracle.write_occupancy(g["voxel_indices"], g["occupancy"].shape), g["written"])
+
+
+@pytest.mark.parametrize("tol", goldens.INDEX_TOLERANCES)
+def test_oracle_index_vertices_matches_reference(subdivision, tol):
+    key = f"index_{tol:g}"
+    np.testing.assert_array_equal(oracle.index_vertices(subdivision[f"{key}/points"], tol), subdivision[f"{key}/index"])
+
+
+def test_oracle_index_keys_matches_reference(subdivision):
+    np.testing.assert_array_equal(oracle.index_keys(subdivision["index_keys/keys"]), subdivision["index_keys/index"])
+
+
+def test_oracle_index_vertices_groups_like_unstable_reference():
+    """With the reference's default (unstable) CPU sort, each group's member
+    is arbitrary but the grouping is the same as the oracle's."""
+    from oracle import ref
+
+    if not ref.available():
+        pytest.skip("reference sources not mounted")
+    import torch
+
+    module = ref.python_module("triangle_extraction/index_vertices.py")
+    keys = np.random.default_rng(2).integers(-30, 30, size=5000).astype(np.int64)
+    got = module.index_keys(torch.from_numpy(keys)).numpy()
+    want = oracle.index_keys(keys)
+    assert np.array_equal(keys[got], keys)  # every index names an equal key
+    assert len(set(zip(got.tolist(), want.tolist()))) == len(np.unique(want)) == len(np.unique(got))

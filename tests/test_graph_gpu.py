@@ -22,6 +22,8 @@ from meshtryoshka_gb300 import triangle_extraction as te
 pytestmark = pytest.mark.gpu
 
 GRAD_RTOL = 1e-5
+# Losses are float32 sums accumulated by per-warp atomics in scheduling order.
+LOSS_RTOL = 1e-5
 
 
 def _close(got, want, rtol=GRAD_RTOL):
@@ -66,7 +68,7 @@ def test_captured_step_matches_eager(cuda_device):
         loss = step()
         torch.cuda.synchronize()
         assert step.check()
-        assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
+        assert abs(float(loss) - loss_e) <= LOSS_RTOL * abs(loss_e)
         _close(w.grid_sdf.grad, gsdf_e)
         _close(w.grid_sh.grad, gsh_e)
 
@@ -85,7 +87,7 @@ def test_captured_step_recaptures_when_capacity_overflows(cuda_device):
     loss = step()
     torch.cuda.synchronize()
     assert step.check()
-    assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
+    assert abs(float(loss) - loss_e) <= LOSS_RTOL * abs(loss_e)
     _close(w.grid_sdf.grad, gsdf_e)
     _close(w.grid_sh.grad, gsh_e)
 
@@ -101,4 +103,4 @@ def test_captured_step_follows_parameter_updates(cuda_device):
     torch.cuda.synchronize()
     assert step.check()
     loss_e, gsdf_e, gsh_e, _ = _eager(w)
-    assert abs(float(loss) - loss_e) <= 1e-6 * abs(loss_e)
+    assert abs(float(loss) - loss_e) <= LOSS_RTOL * abs(loss_e)

@@ -374,3 +374,19 @@ def test_fused_adversarial_triangles_exact_hits(cuda_device, seed):
                                           _n(paired.triangle_indices), _n(tb).reshape(1, t, 2), s, (16, 16), (h, w), kd)
     np.testing.assert_allclose(_n(out), want, atol=IMAGE_ATOL, rtol=0)
     assert (want[0, 3] < 1).mean() > 0.2
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_both_modes_match_oracle_renders(cuda_device, name):
+    """The full render in each mode equals the oracle's render of the same
+    mode (the two modes themselves differ where shells of several objects
+    interleave in depth, as the reference's do)."""
+    scene = make_scene(**SCENES[name])
+    inputs = _fused_inputs(scene, cuda_device)
+    args = (scene.extrinsics, scene.intrinsics, scene.image_shape, scene.vertices, scene.faces,
+            scene.face_boundaries, scene.sdf, scene.sh, scene.sh_degree, scene.sharpness, scene.background)
+    with torch.no_grad():
+        fused = _n(tr.render(**inputs, mode="fused"))
+        explicit = _n(tr.render(**inputs, mode="explicit"))
+    np.testing.assert_allclose(fused, oracle.render_fused(*args).image, atol=IMAGE_ATOL, rtol=0)
+    np.testing.assert_allclose(explicit, oracle.render_explicit(*args), atol=IMAGE_ATOL, rtol=0)
