@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -300,37 +301,62 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(statistics.mean(step_ms), world)
     launches_per_step = step.launches_per_replay
 
-    # End to end through the public API: every step copies the parameters,
-    # target and cameras from pinned host memory into the step's inputs,
-    # replays the step and reads the loss back.
+    # End to end through the public API: every step copies its parameters,
+    # target and cameras from pinned host memory, replays the step and reads
+    # its loss back, as a training loop with an input pipeline does: the
+    # copy of step i + 1's inputs (into one of two staging sets, on a copy
+    # stream) overlaps step i's compute; the compute stream waits for it,
+    # moves the staged inputs into place, flushes L2 and replays; each
+    # step's loss is read on the host one step later. The wall clock runs
+    # from the first copy to the last loss read.
     host = {k: v.detach().cpu().pin_memory() for k, v in
             (("sdf", w.grid_sdf), ("sh", w.grid_sh), ("target", w.target), ("ext", w.extrinsics),
              ("intr", w.intrinsics))}
+    inputs = {"sdf": w.grid_sdf, "sh": w.grid_sh, "target": w.target, "ext": w.extrinsics, "intr": w.intrinsics}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
-    loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+    copy_stream = torch.cuda.Stream(device)
+    staging = [{k: torch.empty_like(v) for k, v in inputs.items()} for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
+    consumed = [torch.cuda.Event() for _ in range(2)]
+    loss_host = [torch.empty((), dtype=torch.float32).pin_memory() for _ in range(2)]
+    loss_ready = [torch.cuda.Event() for _ in range(2)]
 
-    def e2e_step():
-        with torch.no_grad():
-            w.grid_sdf.copy_(host["sdf"], non_blocking=True)
-            w.grid_sh.copy_(host["sh"], non_blocking=True)
-            w.target.copy_(host["target"], non_blocking=True)
-            w.extrinsics.copy_(host["ext"], non_blocking=True)
-            w.intrinsics.copy_(host["intr"], non_blocking=True)
-        loss_host.copy_(step(), non_blocking=True)
-        torch.cuda.synchronize(device)
-        return float(loss_host)
+    def issue_copy(b):
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(consumed[b])
+            for k, t in host.items():
+                staging[b][k].copy_(t, non_blocking=True)
+            copied[b].record(copy_stream)
 
-    for _ in range(2):
-        e2e_step()
+    def run_e2e(n):
+        losses = []
+        issue_copy(0)
+        for i in range(n):
+            b = i & 1
+            if i + 1 < n:
+                issue_copy(1 - b)
+            stream.wait_event(copied[b])
+            with torch.no_grad():
+                for k, t in inputs.items():
+                    t.copy_(staging[b][k], non_blocking=True)
+            consumed[b].record(stream)
+            flush.fill_(float(i))
+            loss_host[b].copy_(step(), non_blocking=True)
+            loss_ready[b].record(stream)
+            if i > 0:
+                loss_ready[1 - b].synchronize()
+                losses.append(float(loss_host[1 - b]))
+        loss_ready[(n - 1) & 1].synchronize()
+        losses.append(float(loss_host[(n - 1) & 1]))
+        return losses
+
+    run_e2e(3)
     barrier(world)
-    e_ms = []
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        e2e_step()
-        e_ms.append(1000.0 * (time.perf_counter() - t0))
-    e2e_value = max_over_ranks(statistics.mean(e_ms), world)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    e2e_losses = run_e2e(args.steps)
+    e2e_value = max_over_ranks(1000.0 * (time.perf_counter() - t0) / args.steps, world)
+    assert len(e2e_losses) == args.steps and all(math.isfinite(x) for x in e2e_losses)
 
     if rank != 0:
         return
@@ -402,7 +428,10 @@ def run_ours(args, rank, world, local):
             "algorithmic_bytes_per_launch": dom_bytes,
             "launch_ms": dom_ms,
         },
-        "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4},
+        "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
+                "form": "per step: pinned-host copy of parameters, target and cameras on a copy stream (double "
+                        "buffered, overlapping the previous step), staged copy into place, L2 flush, graph "
+                        "replay, loss read on the host one step later; wall clock over all steps"},
         "clocks": clock_info,
     }
     if not args.no_cameras and world == 1:

@@ -45,6 +45,15 @@ namespace {
 constexpr int kBatch = 32;   // triangles gathered per warp batch
 constexpr int kQueue = 64;   // queued key offsets per warp
 constexpr int kRing = 64;    // gradient slots per warp (two batches)
+constexpr int kSavedFwd = 4;  // hits per lane per batch whose (u, v, w) the test phase keeps (forward)
+constexpr int kSavedBwd = 3;  // same, backward (its shared memory is tighter)
+
+// The (u, v, w) of the first K hits each lane finds in a batch, so that the
+// hit phase does not solve them again (later hits are re-solved).
+template <int K>
+struct SavedHits {
+  float u[K][32], v[K][32], w[K][32];
+};
 
 struct TriAttr {
   float ca[3], cb[3], cc[3];
@@ -93,12 +102,14 @@ struct CompositeGrads {
 struct WarpForward {
   TriGeom geo[kBatch];
   TriAttr attr[kBatch];
+  SavedHits<kSavedFwd> saved;
   int queue[kQueue];
 };
 
 struct WarpBackward {
   TriGeom geo[kBatch];
   TriAttr attr[kBatch];
+  SavedHits<kSavedBwd> saved;
   int3 vids[kRing];
   float gslot[kRing][13];  // 12 used; stride 13 keeps lanes on distinct banks
   int queue[kQueue];
@@ -232,16 +243,43 @@ __device__ __forceinline__ void pop(int* queue, int queued, int nb, int lane) {
 // are skipped (last_shell only grows, so they would be skipped later too).
 // The costly per-hit work then runs in a separate loop over each pixel's own
 // bits, so the warp executes it as often as its busiest pixel has hits, not
-// once for every triangle that any of its pixels hits.
-__device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float fx, float fy, int last_shell) {
+// once for every triangle that any of its pixels hits. The (u, v, w) of the
+// lane's first K hits are kept for that loop.
+template <int K>
+__device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float fx, float fy, int last_shell,
+                                               SavedHits<K>& saved, int lane) {
   uint32_t hits = 0;
+  int n = 0;
+#pragma unroll 2  // two independent tests in flight
   for (int i = 0; i < nb; ++i) {
     const TriGeom& g = geo[i];
     if (g.shell <= last_shell) continue;
     float u, v, w;
-    if (hit_test(g, fx, fy, u, v, w)) hits |= 1u << i;
+    if (hit_test(g, fx, fy, u, v, w)) {
+      hits |= 1u << i;
+      if (n < K) {
+        saved.u[n][lane] = u;
+        saved.v[n][lane] = v;
+        saved.w[n][lane] = w;
+      }
+      ++n;
+    }
   }
   return hits;
+}
+
+// (u, v, w) of the lane's n-th hit in the batch (triangle g): kept by the
+// test phase, or solved again.
+template <int K>
+__device__ __forceinline__ void hit_weights(const SavedHits<K>& saved, int n, int lane, const TriGeom& g, float fx,
+                                            float fy, float& u, float& v, float& w) {
+  if (n < K) {
+    u = saved.u[n][lane];
+    v = saved.v[n][lane];
+    w = saved.w[n][lane];
+  } else {
+    hit_test(g, fx, fy, u, v, w);
+  }
 }
 
 struct Pixel {
@@ -354,14 +392,16 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
     if (active) {
-      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell);
+      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
+      int n = 0;
       while (hits) {
         const int i = __ffs(hits) - 1;
         hits &= hits - 1;
+        const int k = n++;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
-        hit_test(g, px.fx, px.fy, u, v, w);  // a hit: recomputes its (u, v, w)
+        hit_weights(ws.saved, k, lane, g, px.fx, px.fy, u, v, w);
         const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
@@ -536,14 +576,16 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
     if (active) {
-      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell);
+      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
+      int n = 0;
       while (hits) {
         const int i = __ffs(hits) - 1;
         hits &= hits - 1;
+        const int k = n++;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
-        hit_test(g, px.fx, px.fy, u, v, w);  // a hit: recomputes its (u, v, w)
+        hit_weights(ws.saved, k, lane, g, px.fx, px.fy, u, v, w);
         const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;

@@ -153,12 +153,27 @@ __device__ __forceinline__ void upscale_planes(const OldGrid& g, int c0, const i
   }
 }
 
-// A warp reads 32 consecutive new vertex-occupancy words in one coalesced
-// load, then takes the non-empty ones in turn with one lane per bit: lane b
-// owns vertex offset + popc(bits below b), so the warp writes up to 32
-// consecutive vertices and every [C, V, 3] row it stores is contiguous. A
-// CTA's warps take consecutive spans, so neighbouring j rows (which sample
-// the same old rows in a doubling upscale) share the old vertices in L1.
+// Position of the n-th (0-based) set bit of x (n < popc(x)).
+__device__ __forceinline__ int select_bit(uint32_t x, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int width = 16; width > 0; width >>= 1) {
+    const int c = __popc(x & ((1u << width) - 1u));
+    if (n >= c) {
+      n -= c;
+      x >>= width;
+      pos += width;
+    }
+  }
+  return pos;
+}
+
+// A warp reads 32 consecutive new vertex-occupancy words (one coalesced
+// load) and deals their vertices out 32 at a time: lane r takes the r-th
+// vertex of the span, whose word is found by a shuffle search over the
+// warp's running bit counts and whose bit by a popcount select. Offsets are
+// an exclusive scan in word order, so that vertex is offset[first word] + r:
+// every lane is busy and every [C, V, 3] row the warp stores is contiguous.
 __global__ void __launch_bounds__(256)
     upscale_parameters_kernel(OldGrid g, int C, const int32_t* __restrict__ new_occ,
                               const int32_t* __restrict__ new_offsets, int I1n, int J1n, int KP1n, int64_t Vnew,
@@ -177,19 +192,34 @@ __global__ void __launch_bounds__(256)
   for (int64_t base = first_warp * 32; base < total; base += warps * 32) {
     const int64_t mine = base + lane;
     const uint32_t my_chunk = mine < total ? (uint32_t)__ldg(new_occ + mine) : 0u;
-    const int32_t my_offset = mine < total ? __ldg(new_offsets + mine) : 0;
-    uint32_t nonempty = __ballot_sync(0xffffffffu, my_chunk != 0);
-    while (nonempty) {
-      const int src = __ffs(nonempty) - 1;
-      nonempty &= nonempty - 1;
+    const int my_count = __popc(my_chunk);
+    int incl = my_count;  // inclusive scan of the bit counts over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int span = __shfl_sync(0xffffffffu, incl, 31);
+    if (span == 0) continue;
+    const int64_t first_vertex = __ldg(new_offsets + base);
+    for (int start = 0; start < span; start += 32) {
+      const int r = start + lane;
+      // Smallest word index src with incl[src] > r.
+      int src = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+        if (v <= r) src += step;
+      }
       const uint32_t chunk = __shfl_sync(0xffffffffu, my_chunk, src);
-      const int32_t offset = __shfl_sync(0xffffffffu, my_offset, src);
-      if (((chunk >> lane) & 1u) == 0) continue;
-      const int64_t vi = (int64_t)offset + __popc(chunk & ((1u << lane) - 1u));
+      const int before = __shfl_sync(0xffffffffu, incl - my_count, src);
+      if (r >= span) continue;
+      const int64_t vi = first_vertex + r;
       if (vi < 0 || vi >= Vnew) continue;
+      const int bit = select_bit(chunk, r - before);
       const int64_t w = base + src;
       const int kp = (int)(w % KP1n), j = (int)((w / KP1n) % J1n), i = (int)(w / ((int64_t)KP1n * J1n));
-      const int k = 32 * kp + lane;
+      const int k = 32 * kp + bit;
       const float x = (float)k * inv_k_max, y = (float)j * inv_j_max, z = (float)i * inv_i_max;
       const float xu = x * sx, yu = y * sy, zu = z * sz;
       const int oi = (int)zu, oj = (int)yu, ok = (int)xu;
