@@ -392,6 +392,24 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
                               int32_t B, int32_t shell_dim, int64_t num_tiles,
                               int64_t* out_boundaries, mt_stream_t stream);
 
+/* sort_keys.cu:241-267 (stable signed-key sort) followed by
+ * delineate_tiles.slang:14-58, for keys made by mt_generate_keys: keys are
+ * counted and scattered into their (camera, [shell,] tile) bins and each bin
+ * is sorted by its low key bits and original index, which gives the stable
+ * sort's order. Same outputs as mt_sort_pairs_i64_i32 + mt_delineate_tiles.
+ * Applicable when mt_sort_keys_by_tile_supported() returns 1 (the key
+ * layout is the fused or explicit one, no camera sets the key's sign bit,
+ * and the composite of low bits and index fits in 63 bits). */
+MT_API int mt_sort_keys_by_tile_supported(const int32_t* layout, int32_t separate_shells,
+                                   int32_t B, int64_t K);
+MT_API size_t mt_sort_keys_by_tile_workspace_bytes(int64_t K, int64_t num_bins);
+MT_API int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t K,
+                         const int64_t* num_keys, const int32_t* layout,
+                         int32_t separate_shells, int32_t B, int32_t shell_dim,
+                         int64_t num_tiles, int64_t* sorted_keys,
+                         int32_t* sorted_triangles, int64_t* out_boundaries,
+                         void* workspace, size_t workspace_bytes, mt_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Fused multi-shell compositing
  * (triangle_rasterization/intersect_and_composite.slang:224-564).

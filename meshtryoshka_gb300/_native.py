@@ -75,6 +75,9 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_bound_triangles": (I32, [P, P, I64, P, I64, P, I32, I32, I32, I32, I32, P, c_float, P, P, P, P]),
     "mt_generate_keys": (I32, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, P, I64, P, P, P]),
     "mt_delineate_tiles": (I32, [P, I64, P, P, I32, I32, I32, I64, P, P]),
+    "mt_sort_keys_by_tile_supported": (I32, [P, I32, I32, I64]),
+    "mt_sort_keys_by_tile_workspace_bytes": (c_size_t, [I64, I64]),
+    "mt_sort_keys_by_tile": (I32, [P, P, I64, P, P, I32, I32, I32, I64, P, P, P, P, c_size_t, P]),
     "mt_intersect_and_composite_forward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
@@ -130,6 +133,7 @@ KERNELS_PER_CALL = {
     "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows
     "mt_create_triangle_vertices_backward": 2,  # corner inverse, gather
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
+    "mt_sort_keys_by_tile": 6,  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
 }
 
 

@@ -361,6 +361,35 @@ def delineate_tiles(sorted_paired_keys: PairedKeys, grid: TileGrid, key_defines,
     return out
 
 
+def _sort_and_delineate(paired_keys: PairedKeys, grid: TileGrid, key_defines,
+                        separate_shells: bool) -> tuple[PairedKeys, Tensor]:
+    """``sort_keys`` followed by ``delineate_tiles`` (the render entry points'
+    sequence) with identical outputs. Keys made by ``generate_keys`` are
+    bucketed by tile and each tile is sorted on its own; layouts that do not
+    allow it (a camera setting the key's sign bit, too many keys for the
+    tie-breaking index) take the radix sort."""
+    keys = paired_keys.keys.contiguous()
+    tri = _i32(paired_keys.triangle_indices)
+    n = keys.numel()
+    layout = _layout(key_defines)
+    b = grid.num_cameras
+    sd = grid.num_shells if separate_shells else 1
+    t = grid.num_tiles_per_image
+    lib = nt.library()
+    if n == 0 or not lib.mt_sort_keys_by_tile_supported(layout, int(separate_shells), b, n):
+        paired = sort_keys(paired_keys, grid)
+        return paired, delineate_tiles(paired, grid, key_defines, separate_shells)
+    device = nt.require_cuda(keys, tri)
+    out_keys = torch.empty_like(keys)
+    out_tri = torch.empty_like(tri)
+    bounds = torch.empty((b, sd, t, 2), dtype=torch.int64, device=device)
+    ws_ptr, ws_bytes = nt.workspace(device).get(lib.mt_sort_keys_by_tile_workspace_bytes(n, b * sd * t))
+    nt.call("mt_sort_keys_by_tile", keys.data_ptr(), tri.data_ptr(), n, nt.ptr(paired_keys.count), layout,
+            int(separate_shells), b, sd, t, out_keys.data_ptr(), out_tri.data_ptr(), bounds.data_ptr(), ws_ptr,
+            ws_bytes, nt.stream(device))
+    return PairedKeys(out_keys, out_tri, paired_keys.count), bounds
+
+
 # ---------------------------------------------------------------------------
 # Spherical harmonics (evaluate_spherical_harmonics.py:23-111)
 # ---------------------------------------------------------------------------
@@ -669,8 +698,7 @@ def rasterize(vertices, faces, shell_face_boundaries, extrinsics, intrinsics, im
     paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
                            bounds.num_tiles_overlapped, grid, key_defines)
     del bounds, depths
-    paired = sort_keys(paired, grid)
-    tile_boundaries = delineate_tiles(paired, grid, key_defines, True)
+    paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, True)
     return intersect(positions, faces, paired.triangle_indices, tile_boundaries, grid, key_defines)
 
 
@@ -736,8 +764,7 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
                            bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
     del bounds, depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.num_tiles_per_image, key_count=paired.count)
-    paired = sort_keys(paired, grid)
-    tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
+    paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
     t = tile_boundaries.shape[2]
     images = intersect_and_composite(positions, colors, signed_distances, faces, sharpness, paired.keys,
@@ -787,8 +814,7 @@ def render_cameras(extrinsics, intrinsics, image_shapes, vertices, faces, shell_
                            bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
     del bounds, depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
-    paired = sort_keys(paired, grid)
-    tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
+    paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
     t = tile_boundaries.shape[2]
     raw = intersect_and_composite(positions, colors, signed_distances, faces, sharpness, paired.keys,
@@ -828,8 +854,7 @@ def render_fused_loss(extrinsics, intrinsics, image_shape, vertices, faces, shel
                            bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
     del bounds, depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
-    paired = sort_keys(paired, grid)
-    tile_boundaries = delineate_tiles(paired, grid, key_defines, False)
+    paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
     t = tile_boundaries.shape[2]
     return IntersectCompositeLoss.apply(positions, colors, signed_distances, faces, sharpness, paired.keys,

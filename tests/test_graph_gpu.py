@@ -63,7 +63,7 @@ def test_captured_step_matches_eager(cuda_device):
     w = pipeline.build_workload("small", cuda_device)
     loss_e, gsdf_e, gsh_e, _ = _eager(w)
     step = graph.CapturedTrainingStep(w)
-    assert step.launches_per_replay > 20
+    assert step.launches_per_replay >= 15  # the whole step: tessellation, render, loss, backward
     for _ in range(3):
         loss = step()
         torch.cuda.synchronize()

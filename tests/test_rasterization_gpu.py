@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 import torch
 
+from meshtryoshka_gb300 import _native as nt
 from meshtryoshka_gb300 import triangle_rasterization as tr
 from oracle import oracle
 from tests.scenes import SCENES, make_scene
@@ -390,3 +391,80 @@ def test_both_modes_match_oracle_renders(cuda_device, name):
         explicit = _n(tr.render(**inputs, mode="explicit"))
     np.testing.assert_allclose(fused, oracle.render_fused(*args).image, atol=IMAGE_ATOL, rtol=0)
     np.testing.assert_allclose(explicit, oracle.render_explicit(*args), atol=IMAGE_ATOL, rtol=0)
+
+
+# ---------------------------------------------------------------------------
+# Tile-bucketed sort: the same keys, triangles and tile ranges as the stable
+# radix sort followed by delineate_tiles.
+# ---------------------------------------------------------------------------
+def _random_keys(rng, n, b, s, rows, cols, explicit, hot_tile=None):
+    kd = tr.create_key_defines(*(EXPLICIT_KEYS if explicit else FUSED_KEYS))
+    d = dict(kd)
+    cam = rng.integers(0, b, n).astype(np.uint64)
+    tile = rng.integers(0, rows * cols, n).astype(np.uint64)
+    if hot_tile is not None:
+        tile[:] = hot_tile
+    shell = rng.integers(0, s, n).astype(np.uint64)
+    depth = rng.choice(rng.uniform(0.5, 4.0, max(n // 7, 1)).astype(np.float32), n).view(np.uint32).astype(np.uint64)
+    key = ((cam << np.uint64(d["CAMERA_BIT_OFFSET"])) | (tile << np.uint64(d["TILE_BIT_OFFSET"]))
+           | (depth << np.uint64(d["DEPTH_BIT_OFFSET"])) | (shell << np.uint64(d["SHELL_BIT_OFFSET"])))
+    tri = rng.integers(0, 1 << 30, n).astype(np.int32)
+    return key.view(np.int64), tri, kd
+
+
+FUSED_KEYS = (("camera", 6), ("tile", 20), ("depth", 32), ("shell", 6))
+EXPLICIT_KEYS = (("camera", 6), ("shell", 6), ("tile", 20), ("depth", 32))
+
+
+@pytest.mark.parametrize("explicit", [False, True])
+@pytest.mark.parametrize("n,b,s,rows,cols,hot", [
+    (1, 1, 1, 1, 1, None),
+    (5000, 4, 3, 7, 9, None),
+    (300_000, 32, 8, 40, 50, None),
+    (100_000, 2, 4, 3, 3, 4),  # one tile of 50k keys per camera: chunks and merge rounds
+    (20_000, 3, 2, 60, 70, 0),
+])
+def test_tile_sort_matches_radix_and_delineate(cuda_device, explicit, n, b, s, rows, cols, hot):
+    d = cuda_device
+    rng = np.random.default_rng(n + b + s)
+    keys, tri, kd = _random_keys(rng, n, b, s, rows, cols, explicit, hot)
+    grid = tr.TileGrid((16, 16), (16 * rows, 16 * cols), b, s)
+    paired = tr.PairedKeys(_t(keys, d), _t(tri, d), None)
+    got, got_bounds = tr._sort_and_delineate(paired, grid, kd, explicit)
+    want = tr.sort_keys(paired, grid)
+    want_bounds = tr.delineate_tiles(want, grid, kd, explicit)
+    np.testing.assert_array_equal(_n(got.keys), _n(want.keys))
+    np.testing.assert_array_equal(_n(got.triangle_indices), _n(want.triangle_indices))
+    np.testing.assert_array_equal(_n(got_bounds), _n(want_bounds))
+    assert nt.library().mt_sort_keys_by_tile_supported(tr._layout(kd), int(explicit), b, n) == 1
+
+
+def test_tile_sort_live_count(cuda_device):
+    """Keys past a device live count are neither sorted nor delineated."""
+    d = cuda_device
+    rng = np.random.default_rng(7)
+    keys, tri, kd = _random_keys(rng, 40_000, 4, 8, 20, 30, False)
+    grid = tr.TileGrid((16, 16), (320, 480), 4, 8)
+    live = torch.tensor(31_337, dtype=torch.int64, device=d)
+    paired = tr.PairedKeys(_t(keys, d), _t(tri, d), live)
+    got, got_bounds = tr._sort_and_delineate(paired, grid, kd, False)
+    want = tr.sort_keys(paired, grid)
+    want_bounds = tr.delineate_tiles(want, grid, kd, False)
+    np.testing.assert_array_equal(_n(got.keys)[:31_337], _n(want.keys)[:31_337])
+    np.testing.assert_array_equal(_n(got.triangle_indices)[:31_337], _n(want.triangle_indices)[:31_337])
+    np.testing.assert_array_equal(_n(got_bounds), _n(want_bounds))
+
+
+def test_tile_sort_falls_back_when_a_camera_sets_the_sign_bit(cuda_device):
+    """With more than 32 cameras in a 6-bit field, cameras 32.. sort first as
+    signed keys; the bucketed order would differ, so the radix sort runs."""
+    d = cuda_device
+    rng = np.random.default_rng(3)
+    keys, tri, kd = _random_keys(rng, 20_000, 40, 2, 4, 5, False)
+    assert nt.library().mt_sort_keys_by_tile_supported(tr._layout(kd), 0, 40, 20_000) == 0
+    grid = tr.TileGrid((16, 16), (64, 80), 40, 2)
+    paired = tr.PairedKeys(_t(keys, d), _t(tri, d), None)
+    got, got_bounds = tr._sort_and_delineate(paired, grid, kd, False)
+    want = tr.sort_keys(paired, grid)
+    np.testing.assert_array_equal(_n(got.keys), _n(want.keys))
+    np.testing.assert_array_equal(_n(got_bounds), _n(tr.delineate_tiles(want, grid, kd, False)))
