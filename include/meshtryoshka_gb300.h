@@ -241,7 +241,8 @@ MT_API int mt_create_triangle_vertices(const float* grid_vertices,
  * grad_vertices is NULL), grad_grid_signed_distances [G] and
  * grad_grid_spherical_harmonics [C,G,3]; no zero-filled outputs needed.
  * corner_inverse: scratch of 4*G int32. A NULL input gradient counts as
- * zero. The MC weight t is detached, as in the reference. */
+ * zero. The MC weight t is detached, as in the reference. workspace: see
+ * mt_create_triangle_vertices_backward_workspace_bytes (may be NULL). */
 MT_API int mt_create_triangle_vertices_backward(
     const float* grid_signed_distances, int32_t C,
     const int32_t* lower_corners, int64_t G, const float* level_sets,
@@ -249,7 +250,13 @@ MT_API int mt_create_triangle_vertices_backward(
     const float* grad_signed_distances, const float* grad_spherical_harmonics,
     int64_t V, int32_t* corner_inverse, float* grad_grid_vertices,
     float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
-    mt_stream_t stream);
+    void* workspace, size_t workspace_bytes, mt_stream_t stream);
+
+/* Workspace for mt_create_triangle_vertices_backward's list form (S <= 21:
+ * per-grid-vertex contribution lists, then a coalesced SH gather). With a
+ * NULL or smaller workspace the single-pass gather runs instead; both give
+ * the same results. */
+MT_API size_t mt_create_triangle_vertices_backward_workspace_bytes(int64_t G, int64_t V);
 
 /* triangle_extraction/compute_sdf_regularizers.slang:18-128 (forward) and its
  * automatic derivative (backward). Per voxel: eikonal_loss_pos / _neg [Nv]

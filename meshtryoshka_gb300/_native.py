@@ -57,8 +57,9 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     ),
     "mt_create_triangle_vertices_backward": (
         I32,
-        [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P, P],
+        [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P, P, c_size_t, P],
     ),
+    "mt_create_triangle_vertices_backward_workspace_bytes": (c_size_t, [I64, I64]),
     "mt_count_triangle_faces": (I32, [P, P, I64, P, I64, P, I32, P, P, P]),
     "mt_compute_sdf_regularizers": (I32, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P, P]),
     "mt_compute_sdf_regularizers_backward": (I32, [P, P, P, I64, P, I64, I32, I32, I32, P, P, P, P, P]),
@@ -131,7 +132,7 @@ KERNELS_PER_CALL = {
     "mt_sort_pairs_i64_i32": 11,  # histogram, plan, 8 digit passes, copy
     "mt_create_voxels": 1,
     "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows
-    "mt_create_triangle_vertices_backward": 2,  # corner inverse, gather
+    "mt_create_triangle_vertices_backward": 5,  # corner inverse, count, scan, list + grads, SH gather
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
     "mt_sort_keys_by_tile": 6,  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
 }

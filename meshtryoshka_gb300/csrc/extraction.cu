@@ -561,6 +561,126 @@ __global__ void create_vertices_backward_kernel(const float* __restrict__ gsdf, 
 }
 
 // ---------------------------------------------------------------------------
+// The same backward as a contribution list and a gather (S <= 21 shells).
+//
+// Pass 1 (count) and pass 2 (fill), one thread per grid vertex x, enumerate
+// x's contributions exactly as create_vertices_backward_kernel does; pass 2
+// writes the signed distance and position gradients and lists every
+// contribution (vertex | origin flag << 31, t) at x's offset in a CSR list of
+// at most 2V entries. Pass 3, one thread per (SH row k, grid vertex x), sums
+// the row-k gradient over x's list in list order (the same sums, so the same
+// bits) and writes it: consecutive threads write consecutive grid vertices
+// of one row, and low register use keeps the SMs full.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ GatherChunk gather_entries(const float* __restrict__ gsdf,
+                                                      const int32_t* __restrict__ lower, int64_t G,
+                                                      const float* __restrict__ level_sets, int S,
+                                                      const int32_t* __restrict__ inverse, int64_t x) {
+  GatherChunk q;
+  q.e = __ldg(inverse + x);
+  Corners4 own{};
+  if (q.e >= 0) own = load_corners(gsdf, lower, G, q.e);
+  q.d0 = own.d0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    q.d1[a] = own.d[a];
+    q.h[a] = __ldg(inverse + (int64_t)(a + 1) * G + x);
+  }
+  q.own = q.e >= 0 ? crossing_bits(own, level_sets, 0, S) : 0ull;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    q.nb[a] = 0ull;
+    if (q.h[a] >= 0) {
+      const Corners4 nb = load_corners(gsdf, lower, G, q.h[a]);
+      q.nd0[a] = nb.d0;
+      q.nd1[a] = nb.d[a];
+      q.nb[a] = crossing_bits(nb, level_sets, 0, S);
+    }
+  }
+  return q;
+}
+
+template <bool kFill>
+__global__ void vertex_grad_list_kernel(const float* __restrict__ gsdf, const int32_t* __restrict__ lower, int64_t G,
+                                        const float* __restrict__ level_sets, int S,
+                                        const int32_t* __restrict__ voff, const int32_t* __restrict__ inverse,
+                                        int64_t V, int32_t* __restrict__ counts, int2* __restrict__ list,
+                                        const float* __restrict__ dv, const float* __restrict__ dsdf,
+                                        float* __restrict__ gdv, float* __restrict__ gdsdf) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < G; x += (int64_t)gridDim.x * blockDim.x) {
+    const GatherChunk q = gather_entries(gsdf, lower, G, level_sets, S, inverse, x);
+    if (!kFill) {
+      int n = 0;
+      for_each_contribution(q, level_sets, 0, voff, G, V, [&](int64_t, float, bool) { ++n; });
+      counts[x] = n;
+    } else {
+      int64_t pos = counts[x];  // scanned: x's first list entry
+      float d = 0.f, p[3] = {0.f, 0.f, 0.f};
+      for_each_contribution(q, level_sets, 0, voff, G, V, [&](int64_t vi, float t, bool origin) {
+        list[pos++] = make_int2((int)vi | (origin ? (int)0x80000000 : 0), __float_as_int(t));
+        if (dsdf) d += weighted(__ldg(dsdf + vi), t, origin);
+        if (dv) {
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) p[ch] += weighted(__ldg(dv + 3 * vi + ch), t, origin);
+        }
+      });
+      gdsdf[x] = d;
+      if (gdv) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) gdv[3 * x + ch] = p[ch];
+      }
+    }
+  }
+  if (!kFill && blockIdx.x == 0 && threadIdx.x == 0) counts[G] = 0;
+}
+
+__global__ void vertex_sh_gather_kernel(const float* __restrict__ dsh, int C, int64_t V, int64_t G,
+                                        const int32_t* __restrict__ offsets, const int2* __restrict__ list,
+                                        float* __restrict__ gdsh) {
+  const int64_t total = (int64_t)C * G;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = o / G, x = o - k * G;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    if (dsh) {
+      const int32_t end = __ldg(offsets + x + 1);
+      for (int32_t p = __ldg(offsets + x); p < end; ++p) {
+        const int2 e = __ldg(list + p);
+        const int64_t vi = e.x & 0x7fffffff;
+        const bool origin = e.x < 0;
+        const float t = __int_as_float(e.y);
+        const float* src = dsh + (k * V + vi) * 3;
+        a0 += weighted(__ldg(src + 0), t, origin);
+        a1 += weighted(__ldg(src + 1), t, origin);
+        a2 += weighted(__ldg(src + 2), t, origin);
+      }
+    }
+    float* dst = gdsh + (k * G + x) * 3;
+    dst[0] = a0;
+    dst[1] = a1;
+    dst[2] = a2;
+  }
+}
+
+size_t vertex_grad_bytes(int64_t G, int64_t V, int32_t** counts, int2** list, void** scan_ws, size_t* scan_bytes,
+                         char* base) {
+  size_t off = 256;  // the workspace status word
+  auto take = [&](size_t bytes) {
+    char* q = base ? base + off : nullptr;
+    off += (bytes + 255) & ~(size_t)255;
+    return q;
+  };
+  char* c = take((size_t)(G + 1) * sizeof(int32_t));
+  char* l = take((size_t)2 * (V > 0 ? V : 0) * sizeof(int2));
+  const size_t sb = mt_scan_workspace_bytes(G + 1);
+  char* sw = take(sb);
+  if (counts) *counts = reinterpret_cast<int32_t*>(c);
+  if (list) *list = reinterpret_cast<int2*>(l);
+  if (scan_ws) *scan_ws = sw;
+  if (scan_bytes) *scan_bytes = sb;
+  return off;
+}
+
+// ---------------------------------------------------------------------------
 // count_triangle_faces.slang:15-50: cube code bit i <=> corner i >= iso with
 // corner order (origin, +x, +xy, +y, +z, +xz, +xyz, +yz).
 // ---------------------------------------------------------------------------
@@ -887,13 +1007,18 @@ int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_si
   return MT_OK;
 }
 
+size_t mt_create_triangle_vertices_backward_workspace_bytes(int64_t G, int64_t V) {
+  if (G < 0 || V < 0) return 0;
+  return vertex_grad_bytes(G, V, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
 int mt_create_triangle_vertices_backward(const float* grid_signed_distances, int32_t C, const int32_t* lower_corners,
                                          int64_t G, const float* level_sets, int32_t S,
                                          const int32_t* vertex_offsets, const float* grad_vertices,
                                          const float* grad_signed_distances, const float* grad_spherical_harmonics,
                                          int64_t V, int32_t* corner_inverse, float* grad_grid_vertices,
                                          float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
-                                         mt_stream_t stream) {
+                                         void* workspace, size_t workspace_bytes, mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
   if (G == 0) return MT_OK;
   MT_REQUIRE(grid_signed_distances && lower_corners && corner_inverse);
@@ -908,9 +1033,32 @@ int mt_create_triangle_vertices_backward(const float* grid_signed_distances, int
   const float* gv = V > 0 ? grad_vertices : nullptr;
   const float* gd = V > 0 ? grad_signed_distances : nullptr;
   const float* gs = V > 0 ? grad_spherical_harmonics : nullptr;
-  create_vertices_backward_kernel<<<grid_stride_blocks(G, 128), 128, 0, st>>>(
-      grid_signed_distances, C, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, gv, gd, gs, V,
-      grad_grid_vertices, grad_grid_signed_distances, grad_grid_spherical_harmonics);
+  const bool listed = S <= kShellsPerChunk && V < (int64_t)0x7fffffff && workspace &&
+                      workspace_bytes >= vertex_grad_bytes(G, V, nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (!listed) {
+    create_vertices_backward_kernel<<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+        grid_signed_distances, C, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, gv, gd, gs, V,
+        grad_grid_vertices, grad_grid_signed_distances, grad_grid_spherical_harmonics);
+    MT_CHECK_LAUNCH();
+    return MT_OK;
+  }
+  int32_t* counts = nullptr;
+  int2* list = nullptr;
+  void* scan_ws = nullptr;
+  size_t scan_bytes = 0;
+  vertex_grad_bytes(G, V, &counts, &list, &scan_ws, &scan_bytes, static_cast<char*>(workspace));
+  vertex_grad_list_kernel<false><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, counts, nullptr,
+      nullptr, nullptr, nullptr, nullptr);
+  MT_CHECK_LAUNCH();
+  const int rc = mt_exclusive_scan_i32(counts, G + 1, scan_ws, scan_bytes, stream);
+  if (rc != MT_OK) return rc;
+  vertex_grad_list_kernel<true><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, counts, list, gv,
+      gd, grad_grid_vertices, grad_grid_signed_distances);
+  MT_CHECK_LAUNCH();
+  vertex_sh_gather_kernel<<<grid_stride_blocks((int64_t)C * G, 256), 256, 0, st>>>(gs, C, V, G, counts, list,
+                                                                                 grad_grid_spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

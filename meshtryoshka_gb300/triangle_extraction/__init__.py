@@ -507,11 +507,14 @@ class CreateTriangleVertices(torch.autograd.Function):
             gv = grad_vertices.contiguous() if grad_vertices is not None else None
             gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
             gs = grad_spherical_harmonics.contiguous() if grad_spherical_harmonics is not None else None
+            ws_ptr, ws_bytes = nt.workspace(device).get(
+                nt.library().mt_create_triangle_vertices_backward_workspace_bytes(g, v))
             nt.call(
                 "mt_create_triangle_vertices_backward",
                 nt.ptr(grid_signed_distances), c, nt.ptr(lower_corners), g, nt.ptr(level_sets), s,
                 nt.ptr(vertex_offsets), nt.ptr(gv), nt.ptr(gd), nt.ptr(gs), v, nt.ptr(inverse),
-                nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), nt.stream(device),
+                nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), ws_ptr, ws_bytes,
+                nt.stream(device),
             )
             return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None
 
