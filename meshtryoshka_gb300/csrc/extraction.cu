@@ -722,42 +722,85 @@ __global__ void count_faces_kernel(const float* __restrict__ sdf, const int32_t*
 // ---------------------------------------------------------------------------
 // Writes only faces below F and searches only vertices below V (the
 // buffers' capacities); with consistent offsets neither bound is reached.
-__global__ void create_faces_kernel(const int32_t* __restrict__ neighbors, const int32_t* __restrict__ indices,
-                                    int64_t Nv, int64_t G, int64_t V, const int32_t* __restrict__ voff,
-                                    const uint8_t* __restrict__ types, const uint8_t* __restrict__ codes, int S,
-                                    const int32_t* __restrict__ foff, int64_t F, int32_t* __restrict__ faces,
-                                    int32_t* __restrict__ voxel_indices) {
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < Nv; v += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t linear = __ldg(indices + v);
-    for (int s = 0; s < S; ++s) {
-      const uint32_t code = codes[(int64_t)s * Nv + v];
-      const int n = c_mc_count[code];
-      if (n == 0) continue;
-      const uint64_t edges = c_mc_edges[code];
-      const int64_t ctr = __ldg(foff + (int64_t)s * Nv + v);
-      for (int e = 0; e < n; ++e) {
-        const int eid = (int)((edges >> (4 * e)) & 15u);
-        const int owner = c_mc_owner[eid];
-        const uint8_t axis = c_mc_axis[eid];
-        const int64_t nb = (owner < 0) ? v : (int64_t)__ldg(neighbors + (int64_t)owner * Nv + v);
-        const int64_t vo = (int64_t)s * G + nb;
-        const int32_t start = __ldg(voff + vo);
-        const int32_t count = __ldg(voff + vo + 1) - start;
-        int32_t target = -1;
-        for (int q = 0; q < count; ++q) {
-          if ((int64_t)start + q >= V) break;
-          if (types[start + q] == axis) {
-            target = start + q;
-            break;
-          }
-        }
-        const int64_t slot = ctr + e;
-        const int64_t tri = slot / 3;
-        if (tri >= F) break;
-        const int corner = 2 - (int)(slot % 3);
-        faces[tri * 3 + corner] = target;
-        if (corner == 0) voxel_indices[tri] = linear;
+//
+// Work is dealt by face slot: a warp reads 32 consecutive (shell, voxel)
+// items (shell-major, the order of the slot offsets) in one coalesced load;
+// their slots are contiguous, so lane r takes the r-th slot of the span (its
+// item by a shuffle search over the warp's running edge counts) and every
+// lane resolves one edge: full lanes, and consecutive lanes write
+// consecutive face corners. The case tables sit in shared memory, as lanes
+// read different cases.
+__global__ void __launch_bounds__(256)
+    create_faces_kernel(const int32_t* __restrict__ neighbors, const int32_t* __restrict__ indices, int64_t Nv,
+                        int64_t G, int64_t V, const int32_t* __restrict__ voff, const uint8_t* __restrict__ types,
+                        const uint8_t* __restrict__ codes, int S, const int32_t* __restrict__ foff, int64_t F,
+                        int32_t* __restrict__ faces, int32_t* __restrict__ voxel_indices) {
+  __shared__ uint64_t s_edges[256];
+  __shared__ uint8_t s_count[256];
+  __shared__ int8_t s_owner[12];
+  __shared__ uint8_t s_axis[12];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    s_edges[i] = c_mc_edges[i];
+    s_count[i] = c_mc_count[i];
+  }
+  if (threadIdx.x < 12) {
+    s_owner[threadIdx.x] = c_mc_owner[threadIdx.x];
+    s_axis[threadIdx.x] = c_mc_axis[threadIdx.x];
+  }
+  __syncthreads();
+  const int64_t total = (int64_t)S * Nv;
+  const int lane = threadIdx.x & 31;
+  const int64_t first_warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = first_warp * 32; base < total; base += warps * 32) {
+    const int64_t mine = base + lane;
+    const uint32_t code = mine < total ? (uint32_t)codes[mine] : 0u;
+    const int n = s_count[code];
+    int incl = n;  // inclusive scan of the edge counts over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    const int span = __shfl_sync(0xffffffffu, incl, 31);
+    if (span == 0) continue;
+    const int64_t first_slot = __ldg(foff + base);
+    for (int start = 0; start < span; start += 32) {
+      const int r = start + lane;
+      int src = 0;  // item holding slot r: smallest src with incl[src] > r
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int u = __shfl_sync(0xffffffffu, incl, src + step - 1);
+        if (u <= r) src += step;
       }
+      const uint32_t c = __shfl_sync(0xffffffffu, code, src);
+      const int before = __shfl_sync(0xffffffffu, incl - n, src);
+      if (r >= span) continue;
+      const int e = r - before;
+      const int64_t item = base + src;
+      const int s = (int)(item / Nv);
+      const int64_t v = item - (int64_t)s * Nv;
+      const int eid = (int)((s_edges[c] >> (4 * e)) & 15u);
+      const int owner = s_owner[eid];
+      const uint8_t axis = s_axis[eid];
+      const int64_t nb = (owner < 0) ? v : (int64_t)__ldg(neighbors + (int64_t)owner * Nv + v);
+      const int64_t vo = (int64_t)s * G + nb;
+      const int32_t vstart = __ldg(voff + vo);
+      const int32_t count = __ldg(voff + vo + 1) - vstart;
+      int32_t target = -1;
+      for (int q = 0; q < count; ++q) {
+        if ((int64_t)vstart + q >= V) break;
+        if (types[vstart + q] == axis) {
+          target = vstart + q;
+          break;
+        }
+      }
+      const int64_t slot = first_slot + r;
+      const int64_t tri = slot / 3;
+      if (tri >= F) continue;
+      const int corner = 2 - (int)(slot % 3);
+      faces[tri * 3 + corner] = target;
+      if (corner == 0) voxel_indices[tri] = __ldg(indices + v);
     }
   }
 }
@@ -1083,7 +1126,7 @@ int mt_create_triangle_faces(const int32_t* neighbors, const int32_t* indices, i
   if (Nv == 0 || S == 0 || F == 0) return MT_OK;
   MT_REQUIRE(neighbors && indices && vertex_offsets && vertex_types && cell_codes && face_offsets && faces &&
              voxel_indices);
-  create_faces_kernel<<<grid_stride_blocks(Nv, 128), 128, 0, as_stream(stream)>>>(
+  create_faces_kernel<<<grid_stride_blocks((int64_t)S * Nv, 256), 256, 0, as_stream(stream)>>>(
       neighbors, indices, Nv, G, V, vertex_offsets, vertex_types, cell_codes, S, face_offsets, F, faces,
       voxel_indices);
   MT_CHECK_LAUNCH();

@@ -12,8 +12,11 @@ against a target image.
 * admits the requests that have arrived into a FIFO queue;
 * retires finished batches (a CUDA event per batch, polled without blocking)
   and stamps their requests' completion times;
-* while a stream slot and the in-flight memory budget allow, forms the next
-  batch from the head of the queue: render-only requests of the head's scene
+* while a stream slot and the in-flight memory budget allow, and either
+  nothing is in flight or requests have queued up (``overlap_backlog``;
+  overlapping batches slow each other, which only pays when requests wait),
+  forms the next batch from the head of the queue: render-only requests of
+  the head's scene
   (in arrival order, up to ``max_batch`` and a pixel budget) go into one
   ``render_cameras`` call for cameras of any size; a gradient request runs
   on its own (its gradient is with respect to the scene's parameters, so it
@@ -157,6 +160,7 @@ class Server:
     streams: int = 4  # batches in flight at once
     max_batch: int = 16  # requests per render batch
     max_pixels: int = 16 * 1920 * 1080  # in-flight pixel budget (bounds the HBM in use)
+    overlap_backlog: int = 2  # queued requests needed to start a batch while another is in flight
     tile_shape: tuple[int, int] = (16, 16)
     batches: int = field(default=0, init=False)
 
@@ -210,6 +214,8 @@ class Server:
             inflight = still
             launched = False
             while queue and free:
+                if inflight and len(queue) < self.overlap_backlog:
+                    break
                 budget = self.max_pixels - sum(f.pixels for f in inflight)
                 batch = self._form_batch(queue, budget)
                 if not batch:
