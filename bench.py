@@ -195,19 +195,43 @@ def cpu_threads():
     return int(os.environ.get("OMP_NUM_THREADS") or os.cpu_count() or 1)
 
 
-def run_reference(args, rank, world):
-    """CPU restatement of the reference path on the host cores (rank 0 only)."""
-    if rank != 0:
-        return
+def host_workload(name: str):
+    """The benchmark scene built on the host with the oracle (same seeds and
+    arrays as pipeline.build_workload, whose voxels come from the GPU path),
+    so that the reference arm needs neither a GPU nor this library's kernels."""
+    import numpy as np
     import torch
 
-    from meshtryoshka_gb300 import pipeline
+    from meshtryoshka_gb300 import pipeline, synthetic
+    from meshtryoshka_gb300 import triangle_extraction as te
+    from oracle import oracle
 
-    device = torch.device("cuda", 0) if torch.cuda.is_available() else None
-    if device is None:
-        print(json.dumps({"impl": "reference", "unavailable": "needs the GPU-built scene inputs (no CUDA device)"}))
+    cfg = synthetic.CONFIGS[name]
+    occ = synthetic.make_occupancy(cfg, "cpu").numpy()
+    v = oracle.extract_voxels(occ)
+    voxels = te.Voxels(*(torch.from_numpy(np.ascontiguousarray(a)) for a in
+                         (v.vertices, v.neighbors, v.lower_corners, v.upper_corners, v.indices)), v.grid_shape)
+    sdf = synthetic.corner_sdf(cfg, voxels.vertices)
+    sh = synthetic.corner_sh(cfg, voxels.vertices.shape[0], "cpu")
+    cams = synthetic.make_cameras(cfg)
+    shapes = [tuple(x) for x in cams.image_shapes]
+    if len(set(shapes)) != 1:
+        raise ValueError("the reference arm takes one image size per step")
+    h, w = shapes[0]
+    return pipeline.Workload(
+        config=cfg, voxels=voxels, grid_sdf=sdf, grid_sh=sh, level_sets=synthetic.level_sets(cfg, "cpu"),
+        extrinsics=torch.from_numpy(cams.extrinsics), intrinsics=torch.from_numpy(cams.intrinsics),
+        image_shape=(h, w), target=synthetic.make_target(cfg.num_cameras, h, w, "cpu"),
+        sharpness=torch.tensor(cfg.sharpness, dtype=torch.float32),
+        background=torch.zeros(3, dtype=torch.float32))
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference path on the host cores (rank 0 only;
+    under torchrun the other ranks return without work)."""
+    if rank != 0:
         return
-    w = pipeline.build_workload(args.config, device)
+    w = host_workload(args.config)
     b = w.extrinsics.shape[0]
     times = []
     for i in range(args.warmup + args.steps):
