@@ -124,23 +124,47 @@ __device__ __forceinline__ void view_dir(const float* __restrict__ verts, int64_
   z = __fdiv_rn(dz, len);
 }
 
+// The vertex's coefficients are read once into registers and serve every
+// camera.
+template <int kCoeff>
+__device__ __forceinline__ void sh_forward_vertex(const float* __restrict__ verts, int64_t V,
+                                                  const float* __restrict__ sh, const float* __restrict__ campos,
+                                                  int B, int64_t v, float* __restrict__ out) {
+  float coef[kCoeff][3];
+#pragma unroll
+  for (int k = 0; k < kCoeff; ++k) {
+    const float* s = sh + ((int64_t)k * V + v) * 3;
+    coef[k][0] = __ldg(s);
+    coef[k][1] = __ldg(s + 1);
+    coef[k][2] = __ldg(s + 2);
+  }
+  for (int b = 0; b < B; ++b) {
+    float x, y, z;
+    view_dir(verts, v, campos + 3 * b, x, y, z);
+    float basis[16];
+    sh_basis(x, y, z, kCoeff, basis);
+    float rgb[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rgb[c] = __fmul_rn(basis[0], coef[0][c]);
+#pragma unroll
+    for (int k = 1; k < kCoeff; ++k) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rgb[c] = __fadd_rn(rgb[c], __fmul_rn(basis[k], coef[k][c]));
+    }
+    float* o = out + ((int64_t)b * V + v) * 3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o[c] = fmaxf(__fadd_rn(rgb[c], 0.5f), 0.0f);
+  }
+}
+
 __global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, const float* __restrict__ sh,
                                   int n_coeff, const float* __restrict__ campos, int B, float* __restrict__ out) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
-    for (int b = 0; b < B; ++b) {
-      float x, y, z;
-      view_dir(verts, v, campos + 3 * b, x, y, z);
-      float basis[16];
-      sh_basis(x, y, z, n_coeff, basis);
-      float rgb[3] = {0.f, 0.f, 0.f};
-      for (int k = 0; k < n_coeff; ++k) {
-        const float* s = sh + ((int64_t)k * V + v) * 3;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) rgb[c] = k == 0 ? __fmul_rn(basis[0], s[c]) : __fadd_rn(rgb[c], __fmul_rn(basis[k], s[c]));
-      }
-      float* o = out + ((int64_t)b * V + v) * 3;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) o[c] = fmaxf(__fadd_rn(rgb[c], 0.5f), 0.0f);
+    switch (n_coeff) {
+      case 1: sh_forward_vertex<1>(verts, V, sh, campos, B, v, out); break;
+      case 4: sh_forward_vertex<4>(verts, V, sh, campos, B, v, out); break;
+      case 9: sh_forward_vertex<9>(verts, V, sh, campos, B, v, out); break;
+      default: sh_forward_vertex<16>(verts, V, sh, campos, B, v, out); break;
     }
   }
 }
