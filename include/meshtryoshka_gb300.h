@@ -389,6 +389,28 @@ MT_API int mt_generate_keys(const float* depth, int64_t V, const int32_t* faces,
                             const int32_t* layout, int64_t K, int64_t* out_keys,
                             int32_t* out_triangles, mt_stream_t stream);
 
+/* mt_bound_triangles + the int64 inclusive scan of its counts +
+ * mt_generate_keys, for callers that give a key capacity K instead of reading
+ * the key count back (replaces the chain
+ * triangle_rasterization/__init__.py:218-236 when nothing may synchronise,
+ * e.g. inside a CUDA graph). Three kernels: tile rectangles and per-chunk key
+ * counts, a scan of the chunk counts, keys.
+ * The keys written, and their order, equal the three-stage chain's; keys past
+ * K are dropped. *out_num_keys (device int64) receives the live key count,
+ * which may exceed K. xy must be 8-byte aligned. workspace (16-byte
+ * aligned): at least mt_bound_and_generate_keys_workspace_bytes(B * F) bytes
+ * (about 20 bytes per item; it holds each item's tile rectangle and key depth
+ * between the kernels). */
+MT_API size_t mt_bound_and_generate_keys_workspace_bytes(int64_t items);
+MT_API int mt_bound_and_generate_keys(
+    const float* xy, const float* depth, int64_t V, const int32_t* faces,
+    int64_t F, const int32_t* num_faces, const int32_t* shell_face_boundaries,
+    int32_t S, int32_t B, int32_t tile_h, int32_t tile_w, int32_t rows,
+    int32_t cols, const int64_t* cameras, float near_plane,
+    const int32_t* layout, int64_t K, int64_t* out_keys, int32_t* out_triangles,
+    int64_t* out_num_keys, void* workspace, size_t workspace_bytes,
+    mt_stream_t stream);
+
 /* triangle_rasterization/delineate_tiles.slang:14-58 (+ the zero fill of
  * delineate_tiles.py:40, done here). out_boundaries [B, shell_dim,
  * num_tiles, 2] int64; shell_dim = S when separate_shells, else 1.

@@ -75,6 +75,11 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_evaluate_spherical_harmonics_backward": (I32, [P, I64, I32, I32, P, I32, P, P, P, P]),
     "mt_bound_triangles": (I32, [P, P, I64, P, I64, P, I32, I32, I32, I32, I32, P, c_float, P, P, P, P]),
     "mt_generate_keys": (I32, [P, I64, P, I64, P, I32, P, P, P, I32, I32, P, P, I64, P, P, P]),
+    "mt_bound_and_generate_keys_workspace_bytes": (c_size_t, [I64]),
+    "mt_bound_and_generate_keys": (
+        I32,
+        [P, P, I64, P, I64, P, P, I32, I32, I32, I32, I32, I32, P, c_float, P, I64, P, P, P, P, c_size_t, P],
+    ),
     "mt_delineate_tiles": (I32, [P, I64, P, P, I32, I32, I32, I64, P, P]),
     "mt_sort_keys_by_tile_supported": (I32, [P, I32, I32, I64]),
     "mt_sort_keys_by_tile_workspace_bytes": (c_size_t, [I64, I64]),
@@ -134,7 +139,8 @@ KERNELS_PER_CALL = {
     "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows
     "mt_create_triangle_vertices_backward": 5,  # corner inverse, count, scan, list + grads, SH gather
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
-    "mt_sort_keys_by_tile": 6,  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
+    "mt_sort_keys_by_tile": 6,
+    "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
 }
 
 

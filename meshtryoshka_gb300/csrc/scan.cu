@@ -16,7 +16,7 @@
 #include <atomic>
 #include <mutex>
 
-#include "mt_common.cuh"
+#include "lookback.cuh"
 
 namespace mt {
 namespace {
@@ -24,43 +24,7 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
-constexpr uint64_t kFlagAggregate = 1;
-constexpr uint64_t kFlagPrefix = 2;
-constexpr int kSpinLimit = 1 << 22;
 constexpr size_t kScanHeader = 256;
-
-__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
-  uint64_t v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-__device__ __forceinline__ uint64_t pack_desc(int64_t value, uint64_t flag) {
-  return ((uint64_t)value << 2) | flag;
-}
-
-__device__ __forceinline__ int64_t desc_value(uint64_t d) { return (int64_t)d >> 2; }
-
-template <typename T>
-__device__ __forceinline__ T warp_inclusive_sum(T x) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    T y = __shfl_up_sync(0xffffffffu, x, o);
-    if ((threadIdx.x & 31) >= o) x += y;
-  }
-  return x;
-}
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
 
 // Loads kScanItems consecutive elements owned by this thread.
 template <typename TI, typename TO, bool kVector>
@@ -132,40 +96,7 @@ __global__ void __launch_bounds__(kScanThreads)
     if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive per warp
     const TO block_total = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
 
-    // Decoupled look-back over predecessor tiles.
-    TO prefix = 0;
-    if (tile == 0) {
-      if (lane == 0) st_relaxed(&desc[0], pack_desc((int64_t)block_total, kFlagPrefix));
-    } else {
-      if (lane == 0) st_relaxed(&desc[tile], pack_desc((int64_t)block_total, kFlagAggregate));
-      int64_t window = tile - 1;
-      bool timed_out = false;
-      while (true) {
-        const int64_t pred = window - lane;
-        uint64_t d = pack_desc(0, kFlagPrefix);  // virtual prefix before tile 0
-        if (pred >= 0) {
-          int spins = 0;
-          d = ld_relaxed(&desc[pred]);
-          while ((d & 3) == 0) {
-            if (++spins > kSpinLimit) {
-              timed_out = true;
-              d = pack_desc(0, kFlagPrefix);
-              break;
-            }
-            __nanosleep(32);
-            d = ld_relaxed(&desc[pred]);
-          }
-        }
-        const unsigned prefix_lanes = __ballot_sync(0xffffffffu, (d & 3) == kFlagPrefix);
-        const int stop = prefix_lanes ? __ffs(prefix_lanes) - 1 : 31;
-        TO contrib = (lane <= stop) ? (TO)desc_value(d) : (TO)0;
-        prefix += warp_sum(contrib);
-        if (prefix_lanes) break;
-        window -= 32;
-      }
-      if (__any_sync(0xffffffffu, timed_out) && lane == 0) set_device_error(status, MT_ERR_DEVICE_TIMEOUT);
-      if (lane == 0) st_relaxed(&desc[tile], pack_desc((int64_t)(prefix + block_total), kFlagPrefix));
-    }
+    const TO prefix = lookback_prefix<TO>(desc, tile, block_total, status);
     if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();

@@ -95,6 +95,14 @@ class CapturedTrainingStep:
         self.w.grid_sh.grad = self.grad_sh
         return self.loss
 
+    def run_uncaptured(self) -> Tensor:
+        """The captured function run once outside the graph, on the capture
+        stream: the same library kernels with the same capacities, each
+        launched from the host (for per-kernel timing). Returns the loss."""
+        with torch.cuda.stream(self.stream):
+            loss = self._step()[0]
+        return loss
+
     def check(self) -> bool:
         """True when the last replay fit its capacities. Otherwise re-captures
         with capacities grown to the measured sizes (times the margin) and

@@ -48,6 +48,7 @@ __all__ = [
     "bound_triangles",
     "PairedKeys",
     "generate_keys",
+    "bound_and_generate_keys",
     "sort_keys",
     "delineate_tiles",
     "evaluate_spherical_harmonics",
@@ -324,6 +325,46 @@ def generate_keys(depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor, 
             nt.ptr(_camera_table(grid, device)), _layout(key_defines), num_keys, nt.ptr(keys), nt.ptr(tri),
             nt.stream(device))
     return PairedKeys(keys, tri, live)
+
+
+@record_function("bound_and_generate_keys")
+def bound_and_generate_keys(vertices: Tensor, depths: Tensor, faces: Tensor, shell_face_boundaries: Tensor,
+                            grid: TileGrid, near_plane: float, key_defines, capacity: int,
+                            num_faces: Tensor | None = None) -> PairedKeys:
+    """``bound_triangles`` followed by ``generate_keys(..., capacity)`` in one
+    three kernels (not in the reference): the same keys in the same order,
+    with no per-item offsets materialised. The live key count stays
+    on the device (``PairedKeys.count``); keys past the capacity are dropped."""
+    assert near_plane >= 0
+    vertices, depths, faces, sfb = _f32(vertices), _f32(depths), _i32(faces), _i32(shell_face_boundaries)
+    device = nt.require_cuda(vertices, depths, faces)
+    _check_key_budget(grid, key_defines)
+    c, v, _ = vertices.shape
+    f = faces.shape[0]
+    num_keys = int(capacity)
+    keys = torch.empty(num_keys, dtype=torch.int64, device=device)
+    tri = torch.empty(num_keys, dtype=torch.int32, device=device)
+    live = torch.empty((), dtype=torch.int64, device=device)
+    rows, cols = grid.grid_shape
+    nf = _i32(num_faces) if num_faces is not None else None
+    ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_bound_and_generate_keys_workspace_bytes(c * f))
+    nt.call("mt_bound_and_generate_keys", nt.ptr(vertices), nt.ptr(depths), v, nt.ptr(faces), f, nt.ptr(nf),
+            nt.ptr(sfb), sfb.shape[0], c, grid.tile_shape[0], grid.tile_shape[1], rows, cols,
+            nt.ptr(_camera_table(grid, device)), float(near_plane), _layout(key_defines), num_keys, nt.ptr(keys),
+            nt.ptr(tri), live.data_ptr(), ws_ptr, ws_bytes, nt.stream(device))
+    return PairedKeys(keys, tri, live)
+
+
+def _keys(positions, depths, faces, shell_face_boundaries, grid, near_plane, num_faces, key_defines,
+          key_capacity) -> PairedKeys:
+    """Keys of a render call: one fused kernel when the call has a key
+    capacity, else the reference's bound_triangles -> generate_keys chain."""
+    if key_capacity is not None:
+        return bound_and_generate_keys(positions, depths, faces, shell_face_boundaries, grid, near_plane,
+                                       key_defines, key_capacity, num_faces)
+    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
+    return generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
+                         bounds.num_tiles_overlapped, grid, key_defines)
 
 
 @record_function("sort_keys")
@@ -759,10 +800,9 @@ def render_fused(extrinsics, intrinsics, image_shape, vertices, faces, shell_fac
     key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
                                      ("shell", num_shell_bits))
     positions, depths = project_vertices(vertices, extrinsics, intrinsics)
-    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
-    paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
-                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
-    del bounds, depths
+    paired = _keys(positions, depths, faces, shell_face_boundaries, grid, near_plane, num_faces, key_defines,
+                   key_capacity)
+    del depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.num_tiles_per_image, key_count=paired.count)
     paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
@@ -809,10 +849,9 @@ def render_cameras(extrinsics, intrinsics, image_shapes, vertices, faces, shell_
     key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
                                      ("shell", num_shell_bits))
     positions, depths = project_vertices(vertices, extrinsics, intrinsics)
-    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
-    paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
-                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
-    del bounds, depths
+    paired = _keys(positions, depths, faces, shell_face_boundaries, grid, near_plane, num_faces, key_defines,
+                   key_capacity)
+    del depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
     paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)
@@ -849,10 +888,9 @@ def render_fused_loss(extrinsics, intrinsics, image_shape, vertices, faces, shel
     key_defines = create_key_defines(("camera", num_camera_bits), ("tile", num_tile_bits), ("depth", 32),
                                      ("shell", num_shell_bits))
     positions, depths = project_vertices(vertices, extrinsics, intrinsics)
-    bounds = bound_triangles(positions, depths, faces, grid, near_plane, num_faces)
-    paired = generate_keys(depths, faces, shell_face_boundaries, bounds.tile_minima, bounds.tile_maxima,
-                           bounds.num_tiles_overlapped, grid, key_defines, key_capacity)
-    del bounds, depths
+    paired = _keys(positions, depths, faces, shell_face_boundaries, grid, near_plane, num_faces, key_defines,
+                   key_capacity)
+    del depths
     LAST_RENDER_STATS.update(num_keys=paired.num_keys, num_tiles=grid.camera_tiles, key_count=paired.count)
     paired, tile_boundaries = _sort_and_delineate(paired, grid, key_defines, False)
     colors = evaluate_spherical_harmonics(vertices, spherical_harmonics, extrinsics, sh_degree)

@@ -468,3 +468,73 @@ def test_tile_sort_falls_back_when_a_camera_sets_the_sign_bit(cuda_device):
     want = tr.sort_keys(paired, grid)
     np.testing.assert_array_equal(_n(got.keys), _n(want.keys))
     np.testing.assert_array_equal(_n(got_bounds), _n(tr.delineate_tiles(want, grid, kd, False)))
+
+
+# ---------------------------------------------------------------------------
+# Fused bound + scan + keys (capacity mode)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", list(SCENES))
+def test_bound_and_generate_keys_matches_oracle(cuda_device, name):
+    scene = make_scene(**SCENES[name])
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, cuda_device)
+    want = oracle.render_fused(scene.extrinsics, scene.intrinsics, scene.image_shape, scene.vertices, scene.faces,
+                               scene.face_boundaries, scene.sdf, scene.sh, scene.sh_degree, scene.sharpness,
+                               scene.background)
+    faces, sfb = _t(scene.faces, cuda_device), _t(scene.face_boundaries, cuda_device)
+    n = want.keys.size
+    for capacity in (n, n + 1000, n // 2, 0):
+        got = tr.bound_and_generate_keys(xy, depth, faces, sfb, grid, 0.2, kd, capacity)
+        assert int(got.count.item()) == n
+        m = min(n, capacity)
+        np.testing.assert_array_equal(_n(got.keys)[:m], want.keys[:m])
+        np.testing.assert_array_equal(_n(got.triangle_indices)[:m], want.tri[:m])
+
+
+def _random_front(rng, b, f, v, grid):
+    h, w = grid.image_shape
+    xy = np.stack([rng.uniform(-40, w + 40, (b, v)), rng.uniform(-40, h + 40, (b, v))], -1).astype(np.float32)
+    # Small triangles mostly, a few that span many tiles.
+    centre = rng.integers(0, v, f)
+    spread = rng.integers(1, 40, f)
+    spread[rng.random(f) < 0.01] = v
+    faces = np.stack([centre, (centre + rng.integers(0, 1 + spread)) % v, (centre + rng.integers(0, 1 + spread)) % v],
+                     -1).astype(np.int32)
+    depth = rng.uniform(0.1, 5.0, (b, v)).astype(np.float32)  # some corners before the near plane
+    return xy, depth, faces
+
+
+@pytest.mark.parametrize("b,f,ragged,live", [
+    (1, 1, False, None),
+    (1, 1023, False, None),
+    (2, 1025, False, 700),
+    (4, 200_000, False, None),
+    (3, 150_001, True, None),
+    (8, 90_000, True, 61_234),
+])
+def test_bound_and_generate_keys_matches_three_stage_chain(cuda_device, b, f, ragged, live):
+    d = cuda_device
+    rng = np.random.default_rng(b * 7 + f)
+    s = 5
+    if ragged:
+        shapes = [(int(rng.integers(40, 400)), int(rng.integers(40, 500))) for _ in range(b)]
+        grid = tr.TileGrid.for_cameras((16, 16), shapes, s)
+    else:
+        grid = tr.TileGrid((16, 16), (300, 420), b, s)
+    xy, depth, faces = _random_front(rng, b, f, max(f // 2, 3), grid)
+    kd = tr.create_key_defines(*FUSED_KEYS)
+    sfb = np.sort(rng.integers(0, f + 1, s)).astype(np.int32)
+    sfb[-1] = f
+    xy_t, depth_t, faces_t, sfb_t = _t(xy, d), _t(depth, d), _t(faces, d), _t(sfb, d)
+    nf = torch.tensor(live, dtype=torch.int32, device=d) if live is not None else None
+    bounds = tr.bound_triangles(xy_t, depth_t, faces_t, grid, 0.2, nf)
+    want = tr.generate_keys(depth_t, faces_t, sfb_t, bounds.tile_minima, bounds.tile_maxima,
+                            bounds.num_tiles_overlapped, grid, kd)
+    n = want.num_keys
+    assert n > 0 or f < 100
+    for capacity in (n, n + 333, (2 * n) // 3):
+        got = tr.bound_and_generate_keys(xy_t, depth_t, faces_t, sfb_t, grid, 0.2, kd, capacity, nf)
+        assert int(got.count.item()) == n
+        m = min(n, capacity)
+        np.testing.assert_array_equal(_n(got.keys)[:m], _n(want.keys)[:m])
+        np.testing.assert_array_equal(_n(got.triangle_indices)[:m], _n(want.triangle_indices)[:m])
+    assert nt.workspace(torch.device(d)).status() == 0
