@@ -294,7 +294,7 @@ def run_ours(args, rank, world, local):
 
     # The training step as one CUDA graph (capacity-sized buffers, no host
     # reads); the timed region. L2 flushed between steps, outside the events.
-    step = graph.CapturedTrainingStep(w)
+    step = graph.CapturedTrainingStep(w, input_sets=2)  # set 1: the e2e pipeline's second input buffer
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize(device)
@@ -334,20 +334,18 @@ def run_ours(args, rank, world, local):
     launches_per_step = step.launches_per_replay
 
     # End to end through the public API: every step copies its parameters,
-    # target and cameras from pinned host memory, replays the step and reads
-    # its loss back, as a training loop with an input pipeline does: the
-    # copy of step i + 1's inputs (into one of two staging sets, on a copy
-    # stream) overlaps step i's compute; the compute stream waits for it,
-    # moves the staged inputs into place, flushes L2 and replays; each
-    # step's loss is read on the host one step later. The wall clock runs
-    # from the first copy to the last loss read.
-    host = {k: v.detach().cpu().pin_memory() for k, v in
-            (("sdf", w.grid_sdf), ("sh", w.grid_sh), ("target", w.target), ("ext", w.extrinsics),
-             ("intr", w.intrinsics))}
-    inputs = {"sdf": w.grid_sdf, "sh": w.grid_sh, "target": w.target, "ext": w.extrinsics, "intr": w.intrinsics}
+    # target and cameras from pinned host memory into the inputs the step
+    # reads, replays the step and reads its loss back, as a training loop
+    # with an input pipeline does. The step holds two input sets (one graph
+    # each, both reading their set in place): the copy of step i + 1's inputs
+    # into one set (on a copy stream, once that set's previous replay is
+    # done) overlaps step i's replay on the other; the compute stream waits
+    # for the copy, flushes L2 and replays; each step's loss is read on the
+    # host one step later. The wall clock runs from the first copy to the
+    # last loss read.
+    host = {k: v.detach().cpu().pin_memory() for k, v in step.inputs[0].items()}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     copy_stream = torch.cuda.Stream(device)
-    staging = [{k: torch.empty_like(v) for k, v in inputs.items()} for _ in range(2)]
     copied = [torch.cuda.Event() for _ in range(2)]
     consumed = [torch.cuda.Event() for _ in range(2)]
     loss_host = [torch.empty((), dtype=torch.float32).pin_memory() for _ in range(2)]
@@ -356,8 +354,9 @@ def run_ours(args, rank, world, local):
     def issue_copy(b):
         with torch.cuda.stream(copy_stream):
             copy_stream.wait_event(consumed[b])
-            for k, t in host.items():
-                staging[b][k].copy_(t, non_blocking=True)
+            with torch.no_grad():
+                for k, t in host.items():
+                    step.inputs[b][k].copy_(t, non_blocking=True)
             copied[b].record(copy_stream)
 
     def run_e2e(n):
@@ -368,12 +367,9 @@ def run_ours(args, rank, world, local):
             if i + 1 < n:
                 issue_copy(1 - b)
             stream.wait_event(copied[b])
-            with torch.no_grad():
-                for k, t in inputs.items():
-                    t.copy_(staging[b][k], non_blocking=True)
-            consumed[b].record(stream)
             flush.fill_(float(i))
-            loss_host[b].copy_(step(), non_blocking=True)
+            loss_host[b].copy_(step(b), non_blocking=True)
+            consumed[b].record(stream)
             loss_ready[b].record(stream)
             if i > 0:
                 loss_ready[1 - b].synchronize()
@@ -461,9 +457,10 @@ def run_ours(args, rank, world, local):
             "launch_ms": dom_ms,
         },
         "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
-                "form": "per step: pinned-host copy of parameters, target and cameras on a copy stream (double "
-                        "buffered, overlapping the previous step), staged copy into place, L2 flush, graph "
-                        "replay, loss read on the host one step later; wall clock over all steps"},
+                "form": "per step: pinned-host copy of parameters, target and cameras on a copy stream into "
+                        "one of the step's two input sets (one graph per set, each reading its set in place; "
+                        "the copy overlaps the other set's replay), L2 flush, graph replay, loss read on the "
+                        "host one step later; wall clock over all steps"},
         "clocks": clock_info,
     }
     if not args.no_cameras and world == 1:

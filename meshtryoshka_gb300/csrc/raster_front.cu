@@ -19,32 +19,32 @@ namespace {
 // Camera centres: inverse(extrinsics)[:, :3, 3]
 // (triangle_rasterization/evaluate_spherical_harmonics.py:38), in fp64.
 // ---------------------------------------------------------------------------
+// One warp per camera: column 3 of the inverse is C[3][r] / det with
+// det = sum_c m[0][c] C[0][c], so only seven cofactors are needed; lanes
+// 0-3 compute C[0][c], lanes 4-6 C[3][r] (one 3x3 minor each).
 __global__ void camera_positions_kernel(const float* __restrict__ ext, int B, float* __restrict__ out) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  double m[16];
-  for (int i = 0; i < 16; ++i) m[i] = (double)ext[16 * b + i];
-  // Column 3 of the inverse via cofactors: inv[r][3] = C[3][r] / det.
-  auto det3 = [&](int r0, int r1, int r2, int c0, int c1, int c2) {
-    return m[4 * r0 + c0] * (m[4 * r1 + c1] * m[4 * r2 + c2] - m[4 * r1 + c2] * m[4 * r2 + c1]) -
-           m[4 * r0 + c1] * (m[4 * r1 + c0] * m[4 * r2 + c2] - m[4 * r1 + c2] * m[4 * r2 + c0]) +
-           m[4 * r0 + c2] * (m[4 * r1 + c0] * m[4 * r2 + c1] - m[4 * r1 + c1] * m[4 * r2 + c0]);
-  };
-  double cof[4][4];
-  for (int r = 0; r < 4; ++r) {
-    for (int c = 0; c < 4; ++c) {
-      int rs[3], cs[3], ri = 0, ci = 0;
-      for (int k = 0; k < 4; ++k) {
-        if (k != r) rs[ri++] = k;
-        if (k != c) cs[ci++] = k;
-      }
-      const double minor = det3(rs[0], rs[1], rs[2], cs[0], cs[1], cs[2]);
-      cof[r][c] = ((r + c) & 1) ? -minor : minor;
+  const int cam = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (cam >= B) return;  // whole warps exit together
+  const float* E = ext + 16 * cam;
+  double cof = 0.0;
+  if (lane < 7) {
+    const int skip_r = lane < 4 ? 0 : 3, skip_c = lane < 4 ? lane : lane - 4;
+    int rs[3], cs[3], ri = 0, ci = 0;
+    for (int k = 0; k < 4; ++k) {
+      if (k != skip_r) rs[ri++] = k;
+      if (k != skip_c) cs[ci++] = k;
     }
+    auto m = [&](int r, int c) { return (double)E[4 * r + c]; };
+    const double minor =
+        m(rs[0], cs[0]) * (m(rs[1], cs[1]) * m(rs[2], cs[2]) - m(rs[1], cs[2]) * m(rs[2], cs[1])) -
+        m(rs[0], cs[1]) * (m(rs[1], cs[0]) * m(rs[2], cs[2]) - m(rs[1], cs[2]) * m(rs[2], cs[0])) +
+        m(rs[0], cs[2]) * (m(rs[1], cs[0]) * m(rs[2], cs[1]) - m(rs[1], cs[1]) * m(rs[2], cs[0]));
+    cof = ((skip_r + skip_c) & 1) ? -minor : minor;
   }
-  double det = 0;
-  for (int c = 0; c < 4; ++c) det += m[c] * cof[0][c];
-  for (int r = 0; r < 3; ++r) out[3 * b + r] = (float)(cof[3][r] / det);
+  double det = 0.0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) det += (double)E[c] * __shfl_sync(0xffffffffu, cof, c);
+  if (lane >= 4 && lane < 7) out[3 * cam + (lane - 4)] = (float)(cof / det);
 }
 
 // ---------------------------------------------------------------------------
@@ -639,7 +639,7 @@ int mt_camera_positions(const float* extrinsics, int32_t B, float* out, mt_strea
   MT_REQUIRE(B >= 0);
   if (B == 0) return MT_OK;
   MT_REQUIRE(extrinsics && out);
-  camera_positions_kernel<<<grid_1d(B, 64), 64, 0, as_stream(stream)>>>(extrinsics, B, out);
+  camera_positions_kernel<<<grid_1d((int64_t)B * 32, 128), 128, 0, as_stream(stream)>>>(extrinsics, B, out);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

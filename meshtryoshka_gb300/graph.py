@@ -24,6 +24,8 @@ between replays.
 
 from __future__ import annotations
 
+import dataclasses
+
 import torch
 from torch import Tensor
 
@@ -32,15 +34,31 @@ from . import pipeline
 from . import triangle_rasterization as tr
 
 
+# The per-step inputs a graph reads in place.
+INPUTS = ("grid_sdf", "grid_sh", "target", "extrinsics", "intrinsics")
+
+
 class CapturedTrainingStep:
-    """Fused forward + backward of ``pipeline.Workload`` as one CUDA graph."""
+    """Fused forward + backward of ``pipeline.Workload`` as one CUDA graph.
+
+    ``input_sets`` > 1 captures one graph per set of inputs (``INPUTS``):
+    set 0 is the workload's own tensors, the others are device copies
+    (``self.inputs[i]``), and ``step(i)`` replays the graph that reads set i
+    in place. A host pipeline can then copy the next step's inputs into one
+    set while the other set's graph runs, with no device-side copy between
+    them. Each graph has its own memory pool, so the outputs of one set's
+    replay stay valid across replays of the others."""
 
     def __init__(self, workload: pipeline.Workload, gradient_mode: str | None = None, margin: float = 1.25,
-                 capacities: pipeline.Capacities | None = None, warmup: int = 2):
+                 capacities: pipeline.Capacities | None = None, warmup: int = 2, input_sets: int = 1):
         self.w = workload
         self.gradient_mode = gradient_mode
         self.margin = margin
         self.warmup = warmup
+        self.inputs = [{k: getattr(workload, k) for k in INPUTS}]
+        for _ in range(1, max(int(input_sets), 1)):
+            self.inputs.append({k: getattr(workload, k).detach().clone() for k in INPUTS})
+        self._views = [dataclasses.replace(workload, **{k: v for k, v in s.items()}) for s in self.inputs]
         if capacities is None:
             capacities = pipeline.Capacities.around(self._measure(), margin)
         self.capacities = capacities
@@ -53,15 +71,15 @@ class CapturedTrainingStep:
             _, stats = pipeline.forward(self.w, "fused", self.gradient_mode)
         return stats
 
-    def _step(self) -> tuple[Tensor, Tensor, Tensor, Tensor]:
+    def _step(self, slot: int = 0) -> tuple[Tensor, Tensor, Tensor, Tensor]:
         # The graph differentiates with respect to aliases of the parameters
         # (same storage, fresh autograd leaves made on the capture stream) and
         # returns the gradients instead of accumulating them: autograd state
         # left on the parameters by eager steps on another stream would
         # otherwise make the capture wait on that stream.
-        loss, overflow = pipeline.forward_counted(self.w, self.capacities, self.gradient_mode,
-                                                  self._sdf, self._sh)
-        grad_sdf, grad_sh = torch.autograd.grad(loss, (self._sdf, self._sh))
+        loss, overflow = pipeline.forward_counted(self._views[slot], self.capacities, self.gradient_mode,
+                                                  self._sdf[slot], self._sh[slot])
+        grad_sdf, grad_sh = torch.autograd.grad(loss, (self._sdf[slot], self._sh[slot]))
         return loss.detach(), overflow, grad_sdf, grad_sh
 
     def _capture(self) -> None:
@@ -70,43 +88,58 @@ class CapturedTrainingStep:
         self.stream = torch.cuda.Stream(device)
         self.stream.wait_stream(torch.cuda.current_stream(device))
         with torch.cuda.stream(self.stream):
-            self._sdf = w.grid_sdf.detach().requires_grad_(True)
-            self._sh = w.grid_sh.detach().requires_grad_(True)
+            self._sdf = [s["grid_sdf"].detach().requires_grad_(True) for s in self.inputs]
+            self._sh = [s["grid_sh"].detach().requires_grad_(True) for s in self.inputs]
             # Warm-up on the capture stream: allocates this stream's library
             # workspace and raises kernel shared-memory limits outside capture.
             for _ in range(self.warmup):
                 self._step()
-            self._workspace = nt.workspace(device).buffer  # kept alive for the graph
+            self._workspace = nt.workspace(device).buffer  # kept alive for the graphs
         torch.cuda.current_stream(device).wait_stream(self.stream)
-        self.graph = torch.cuda.CUDAGraph()
+        self.graphs, self._outputs = [], []
         with nt.record_launches() as rec:
-            with torch.cuda.graph(self.graph, stream=self.stream):
-                # Gradient tensors written by every replay (graph-owned memory).
-                self.loss, self.overflow, self.grad_sdf, self.grad_sh = self._step()
-        self.launches_per_replay = rec.launches
+            for slot in range(len(self.inputs)):
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=self.stream):
+                    # Loss, overflow flag and gradients written by every replay
+                    # (graph-owned memory).
+                    self._outputs.append(self._step(slot))
+                self.graphs.append(g)
+        self.launches_per_replay = rec.launches // len(self.inputs)
+        self.graph = self.graphs[0]
+        self._select(0)
         # Device tables the graph reads (ragged camera grids) stay alive with it.
         self._tables = list(tr._CAMERA_TABLES.values())
 
-    def __call__(self) -> Tensor:
-        """Replay one step on the current stream; returns the (device) loss.
-        The parameters' ``.grad`` point at the graph's gradient tensors."""
-        self.graph.replay()
-        self.w.grid_sdf.grad = self.grad_sdf
-        self.w.grid_sh.grad = self.grad_sh
+    def _select(self, slot: int) -> None:
+        self.slot = slot
+        self.loss, self.overflow, self.grad_sdf, self.grad_sh = self._outputs[slot]
+
+    def __call__(self, slot: int = 0) -> Tensor:
+        """Replay one step (reading input set ``slot``) on the current stream;
+        returns the (device) loss. ``self.grad_sdf`` / ``self.grad_sh`` are
+        that replay's gradients; for set 0 the workload parameters' ``.grad``
+        point at them too."""
+        self.graphs[slot].replay()
+        self._select(slot)
+        if slot == 0:
+            self.w.grid_sdf.grad = self.grad_sdf
+            self.w.grid_sh.grad = self.grad_sh
         return self.loss
 
-    def run_uncaptured(self) -> Tensor:
+    def run_uncaptured(self, slot: int = 0) -> Tensor:
         """The captured function run once outside the graph, on the capture
         stream: the same library kernels with the same capacities, each
         launched from the host (for per-kernel timing). Returns the loss."""
         with torch.cuda.stream(self.stream):
-            loss = self._step()[0]
+            loss = self._step(slot)[0]
         return loss
 
     def check(self) -> bool:
-        """True when the last replay fit its capacities. Otherwise re-captures
-        with capacities grown to the measured sizes (times the margin) and
-        returns False: the step must be replayed again. Synchronizes."""
+        """True when the last replay (of the last replayed input set) fit its
+        capacities. Otherwise re-captures with capacities grown to the
+        measured sizes (times the margin) and returns False: the step must be
+        replayed again. Synchronizes."""
         if not bool(self.overflow.item()):
             return True
         grown = pipeline.Capacities.around(self._measure(), self.margin)

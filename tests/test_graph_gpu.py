@@ -104,3 +104,31 @@ def test_captured_step_follows_parameter_updates(cuda_device):
     assert step.check()
     loss_e, gsdf_e, gsh_e, _ = _eager(w)
     assert abs(float(loss) - loss_e) <= LOSS_RTOL * abs(loss_e)
+
+
+def test_captured_step_input_sets_read_their_own_inputs(cuda_device):
+    """With two input sets, each graph reads its own set in place; a replay of
+    one set leaves the other set's outputs as they were."""
+    w = pipeline.build_workload("small", cuda_device)
+    step = graph.CapturedTrainingStep(w, input_sets=2)
+    assert len(step.graphs) == 2 and step.launches_per_replay >= 15
+    with torch.no_grad():
+        step.inputs[1]["grid_sh"].mul_(0.5)
+        step.inputs[1]["target"].mul_(0.75)
+    loss0 = float(step(0))
+    g0 = step.grad_sh.clone()
+    loss1 = float(step(1))
+    assert step.check()
+    torch.cuda.synchronize()
+    # Set 0's outputs survive the replay of set 1.
+    torch.testing.assert_close(step._outputs[0][3], g0, rtol=0, atol=0)
+    loss_e0, _, gsh_e0, _ = _eager(w)
+    assert abs(loss0 - loss_e0) <= LOSS_RTOL * abs(loss_e0)
+    _close(g0, gsh_e0)
+    with torch.no_grad():
+        w.grid_sh.mul_(0.5)
+        w.target.mul_(0.75)
+    loss_e1, gsdf_e1, gsh_e1, _ = _eager(w)
+    assert abs(loss1 - loss_e1) <= LOSS_RTOL * abs(loss_e1)
+    _close(step.grad_sdf, gsdf_e1)
+    _close(step.grad_sh, gsh_e1)
