@@ -428,7 +428,11 @@ MT_API int mt_delineate_tiles(const int64_t* sorted_keys, int64_t K,
  * sort's order. Same outputs as mt_sort_pairs_i64_i32 + mt_delineate_tiles.
  * Applicable when mt_sort_keys_by_tile_supported() returns 1 (the key
  * layout is the fused or explicit one, no camera sets the key's sign bit,
- * and the composite of low bits and index fits in 63 bits). */
+ * and the composite of low bits and index fits in 63 bits). Part of the work
+ * runs on a helper stream that this library keeps per (device, stream); it
+ * is forked from `stream` and joined back to it with events, so the outputs
+ * are ordered on `stream` as usual (and the call can be graph-captured once
+ * it has run on that stream outside capture). */
 MT_API int mt_sort_keys_by_tile_supported(const int32_t* layout, int32_t separate_shells,
                                    int32_t B, int64_t K);
 MT_API size_t mt_sort_keys_by_tile_workspace_bytes(int64_t K, int64_t num_bins);

@@ -21,6 +21,16 @@
 // Valid only when the bin order equals the signed key order (the camera
 // field's top bit is clear for every camera) and the composite fits in 63
 // bits; the caller checks both and otherwise uses the radix sort.
+//
+// The three bin sorts touch disjoint bins, so the large-bin sort (whose
+// longest bins set the tail) runs on a helper stream forked from the caller's
+// stream and joined back with events; the tiny and small sorts fill the SMs
+// beside it. Fork and join are ordinary stream dependencies, so the call
+// stays capturable in a CUDA graph.
+
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "mt_common.cuh"
 
@@ -439,6 +449,40 @@ int mt_sort_keys_by_tile_supported(const int32_t* layout, int32_t separate_shell
   return low_bits + idx_bits <= 63 ? 1 : 0;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Helper stream and fork / join events of one (device, caller stream),
+// created on first use and kept for the process.
+struct ForkJoin {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+int fork_join_for(cudaStream_t caller, ForkJoin& out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, cudaStream_t>, ForkJoin> table;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return MT_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = table.find({device, caller});
+  if (it == table.end()) {
+    ForkJoin f;
+    if (cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming) != cudaSuccess)
+      return MT_ERR_CUDA;
+    it = table.emplace(std::make_pair(device, caller), f).first;
+  }
+  out = it->second;
+  return MT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t K, const int64_t* num_keys,
                          const int32_t* layout, int32_t separate_shells, int32_t B, int32_t shell_dim,
                          int64_t num_tiles, int64_t* sorted_keys, int32_t* sorted_triangles, int64_t* boundaries,
@@ -480,7 +524,19 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
   bin_scatter_kernel<<<grid_stride_blocks(K, kThreads), kThreads, 0, s>>>(k64, K, num_keys, m, w.counts, w.cursors,
                                                                         idx_bits, low_mask_host, w.tmp);
   MT_CHECK_LAUNCH();
-  // As many CTAs as are resident at once; each takes listed bins in turn.
+  // Large bins on the helper stream, the rest on the caller's; as many CTAs
+  // as are resident at once, each taking listed bins in turn.
+  const size_t large_smem = 2 * (size_t)kChunk * sizeof(uint64_t);
+  if (set_smem<bin_sort_large_kernel>(large_smem) != MT_OK) return MT_ERR_CUDA;
+  ForkJoin fj;
+  if (fork_join_for(s, fj) != MT_OK) return MT_ERR_CUDA;
+  if (cudaEventRecord(fj.fork, s) != cudaSuccess || cudaStreamWaitEvent(fj.side, fj.fork, 0) != cudaSuccess)
+    return MT_ERR_CUDA;
+  const unsigned large_ctas = (unsigned)(nbins < (int64_t)kSmCount * 2 ? nbins : (int64_t)kSmCount * 2);
+  bin_sort_large_kernel<<<large_ctas, kLargeThreads, large_smem, fj.side>>>(
+      w.tmp, w.alt, w.lists + 2 * nbins, w.list_sizes + 2, idx_mask, k64, triangles,
+      reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
+  MT_CHECK_LAUNCH();
   const unsigned tiny_ctas = (unsigned)(nbins < (int64_t)kSmCount * 5 ? nbins : (int64_t)kSmCount * 5);
   bin_sort_tiny_kernel<<<tiny_ctas, 32 * kTinyWarps, 0, s>>>(w.tmp, w.lists, w.list_sizes, idx_mask, k64, triangles,
                                                              reinterpret_cast<uint64_t*>(sorted_keys),
@@ -492,13 +548,8 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
                                                              reinterpret_cast<uint64_t*>(sorted_keys),
                                                              sorted_triangles);
   MT_CHECK_LAUNCH();
-  const size_t large_smem = 2 * (size_t)kChunk * sizeof(uint64_t);
-  if (set_smem<bin_sort_large_kernel>(large_smem) != MT_OK) return MT_ERR_CUDA;
-  const unsigned large_ctas = (unsigned)(nbins < (int64_t)kSmCount * 2 ? nbins : (int64_t)kSmCount * 2);
-  bin_sort_large_kernel<<<large_ctas, kLargeThreads, large_smem, s>>>(
-      w.tmp, w.alt, w.lists + 2 * nbins, w.list_sizes + 2, idx_mask, k64, triangles,
-      reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
-  MT_CHECK_LAUNCH();
+  if (cudaEventRecord(fj.join, fj.side) != cudaSuccess || cudaStreamWaitEvent(s, fj.join, 0) != cudaSuccess)
+    return MT_ERR_CUDA;
   return MT_OK;
 }
 
