@@ -290,6 +290,26 @@ MT_API int mt_count_triangle_faces(const float* signed_distances,
                             int32_t* face_counts, uint8_t* cell_codes,
                             mt_stream_t stream);
 
+/* The shell boundaries of triangle_extraction/__init__.py:145-146 from the
+ * two scanned count arrays (vertex_offsets: S*G + 1 entries, face_offsets:
+ * S*Nv + 1): vertex_boundaries[s] = vertex_offsets[(s + 1) G],
+ * face_boundaries[s] = face_offsets[(s + 1) Nv] / 3, and (num_faces
+ * nullable) *num_faces = face_offsets[S Nv] / 3 (:131). One launch for what
+ * the reference does with four tensor ops. */
+MT_API int mt_shell_boundaries(const int32_t* vertex_offsets, int64_t G,
+                               const int32_t* face_offsets, int64_t Nv, int32_t S,
+                               int32_t* vertex_boundaries, int32_t* face_boundaries,
+                               int32_t* num_faces, mt_stream_t stream);
+
+/* Not in the reference (capacity-sized buffers of a captured step):
+ * *overflow = 1 when a live count exceeds its capacity (num_vertices >
+ * vertex_capacity, num_faces > face_capacity or num_keys > key_capacity;
+ * a NULL count is skipped), else 0. Device scalars in, one byte out. */
+MT_API int mt_capacity_overflow(const int32_t* num_vertices, int64_t vertex_capacity,
+                                const int32_t* num_faces, int64_t face_capacity,
+                                const int64_t* num_keys, int64_t key_capacity,
+                                uint8_t* overflow, mt_stream_t stream);
+
 /* triangle_extraction/create_triangle_faces.slang:5-78. face_offsets is the
  * exclusive scan of face_counts. Outputs faces [F,3] int32 (reversed slot
  * order as in the reference) and voxel_indices [F]. V is the length of

@@ -67,6 +67,8 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
         I32,
         [P, P, I64, I64, I64, P, P, P, I32, P, I64, P, P, P],
     ),
+    "mt_shell_boundaries": (I32, [P, I64, P, I64, I32, P, P, P, P]),
+    "mt_capacity_overflow": (I32, [P, I64, P, I64, P, I64, P, P]),
     "mt_sort_pairs_workspace_bytes": (c_size_t, [I64]),
     "mt_sort_pairs_i64_i32": (I32, [P, P, P, P, I64, P, I32, I32, P, c_size_t, P]),
     "mt_camera_positions": (I32, [P, I32, P, P]),

@@ -954,6 +954,31 @@ __global__ void sdf_regularizers_backward_kernel(const float* __restrict__ sdf,
   }
 }
 
+// Last entry of every shell's block of an exclusive scan: the vertex and face
+// boundaries of triangle_extraction/__init__.py:145-146 (faces / 3, floor),
+// plus the face total of :131 (offsets are non-negative, so / is floor).
+__global__ void shell_boundaries_kernel(const int32_t* __restrict__ voff, int64_t G,
+                                        const int32_t* __restrict__ foff, int64_t Nv, int S,
+                                        int32_t* __restrict__ vb, int32_t* __restrict__ fb,
+                                        int32_t* __restrict__ num_faces) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < S) {
+    vb[s] = G > 0 ? voff[(int64_t)(s + 1) * G] : 0;
+    fb[s] = Nv > 0 ? foff[(int64_t)(s + 1) * Nv] / 3 : 0;
+  }
+  if (s == 0 && num_faces) *num_faces = foff[(int64_t)S * Nv] / 3;
+}
+
+__global__ void capacity_overflow_kernel(const int32_t* __restrict__ nv, int64_t cv, const int32_t* __restrict__ nf,
+                                         int64_t cf, const int64_t* __restrict__ nk, int64_t ck,
+                                         uint8_t* __restrict__ overflow) {
+  bool over = false;
+  if (nv) over |= (int64_t)*nv > cv;
+  if (nf) over |= (int64_t)*nf > cf;
+  if (nk) over |= *nk > ck;
+  *overflow = over ? 1 : 0;
+}
+
 }  // namespace
 }  // namespace mt
 
@@ -1164,6 +1189,29 @@ int mt_compute_sdf_regularizers_backward(const float* grid_signed_distances, con
   sdf_regularizers_backward_kernel<<<grid_stride_blocks(Nv, 256), 256, 0, st>>>(
       grid_signed_distances, voxel_neighbors, voxel_lower_corners, G, voxel_upper_corners, Nv, voxel_x, voxel_y,
       voxel_z, grad_eikonal_loss_pos, grad_eikonal_loss_neg, grad_curvature_loss, grad_grid_signed_distances);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_shell_boundaries(const int32_t* vertex_offsets, int64_t G, const int32_t* face_offsets, int64_t Nv, int32_t S,
+                        int32_t* vertex_boundaries, int32_t* face_boundaries, int32_t* num_faces,
+                        mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && Nv >= 0 && S >= 0);
+  if (S == 0 && !num_faces) return MT_OK;
+  MT_REQUIRE(vertex_offsets && face_offsets);
+  MT_REQUIRE(S == 0 || (vertex_boundaries && face_boundaries));
+  shell_boundaries_kernel<<<grid_1d(S > 0 ? S : 1, 128), 128, 0, as_stream(stream)>>>(
+      vertex_offsets, G, face_offsets, Nv, S, vertex_boundaries, face_boundaries, num_faces);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_capacity_overflow(const int32_t* num_vertices, int64_t vertex_capacity, const int32_t* num_faces,
+                         int64_t face_capacity, const int64_t* num_keys, int64_t key_capacity, uint8_t* overflow,
+                         mt_stream_t stream) {
+  MT_REQUIRE(overflow);
+  capacity_overflow_kernel<<<1, 1, 0, as_stream(stream)>>>(num_vertices, vertex_capacity, num_faces, face_capacity,
+                                                          num_keys, key_capacity, overflow);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

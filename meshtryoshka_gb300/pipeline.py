@@ -15,6 +15,7 @@ import numpy as np
 import torch
 from torch import Tensor
 
+from . import _native as nt
 from . import synthetic
 from . import triangle_extraction as te
 from . import triangle_rasterization as tr
@@ -134,6 +135,21 @@ class Capacities:
         return Capacities(grow(stats["V"]), grow(stats["F"]), grow(stats["K"]))
 
 
+_AFFINE: dict = {}
+
+
+def uncontract_stand_in(vertices: Tensor) -> Tensor:
+    """2 v - 1, the linear stand-in for the trainer's uncontract(), as one
+    elementwise kernel (-1 + v * 2: v * 2 is exact, so the value is that of
+    2.0 * v - 1.0)."""
+    key = str(vertices.device)
+    consts = _AFFINE.get(key)
+    if consts is None:
+        consts = (torch.tensor(-1.0, device=vertices.device), torch.tensor(2.0, device=vertices.device))
+        _AFFINE[key] = consts
+    return torch.addcmul(consts[0], vertices, consts[1])
+
+
 def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = None,
                     grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None) -> tuple[Tensor, Tensor]:
     """The fused step's forward with capacity-sized buffers and no
@@ -146,16 +162,16 @@ def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = N
         grid_sdf, w.voxels.vertices, grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
         w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces)
     with torch.no_grad():
-        vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
+        vertices = uncontract_stand_in(tri.vertices)
     counted = dict(num_faces=counts.num_faces, key_capacity=caps.keys)
     if w.fused_loss:
         loss = _fused_loss(w, tri, vertices, gradient_mode, **counted)
     else:
         loss = _loss(w, _render(w, tri, vertices, gradient_mode, **counted))
     key_count = tr.LAST_RENDER_STATS["key_count"]
-    with torch.no_grad():
-        overflow = ((counts.num_vertices > caps.vertices) | (counts.num_faces > caps.faces)
-                    | (key_count > caps.keys))
+    overflow = torch.empty((), dtype=torch.bool, device=loss.device)
+    nt.call("mt_capacity_overflow", counts.num_vertices.data_ptr(), caps.vertices, counts.num_faces.data_ptr(),
+            caps.faces, key_count.data_ptr(), caps.keys, overflow.data_ptr(), nt.stream(loss.device))
     return loss, overflow
 
 
@@ -168,7 +184,7 @@ def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
     tri = te.tessellate_voxels(grid_sdf, w.voxels.vertices, grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
                                w.voxels.upper_corners, w.voxels.indices, w.level_sets)
     with torch.no_grad():
-        vertices = 2.0 * tri.vertices - 1.0  # linear stand-in for uncontract()
+        vertices = uncontract_stand_in(tri.vertices)
     if mode == "fused" and w.fused_loss and target is w.target:
         loss = _fused_loss(w, tri, vertices, gradient_mode)
     else:
@@ -204,7 +220,7 @@ def per_camera_training_step(w: Workload, gradient_mode: str | None = None) -> T
     tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
                                w.voxels.upper_corners, w.voxels.indices, w.level_sets)
     with torch.no_grad():
-        vertices = 2.0 * tri.vertices - 1.0
+        vertices = uncontract_stand_in(tri.vertices)
     shapes = w.image_shapes or ((w.image_shape,) * w.extrinsics.shape[0])
     total = 0.0
     for b, ((h, wd), target) in enumerate(zip(shapes, w.targets())):

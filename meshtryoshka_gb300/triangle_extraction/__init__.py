@@ -753,7 +753,7 @@ def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lowe
             counts = None
         else:
             num_vertices, num_faces = capacity
-            counts = TessellationCounts(vertex_offsets[-1], torch.div(face_offsets[-1], 3, rounding_mode="floor"))
+            counts = TessellationCounts(vertex_offsets[-1], torch.empty((), dtype=torch.int32, device=device))
 
     triangle_vertices, triangle_sdf, triangle_sh, triangle_types = create_triangle_vertices(
         vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets,
@@ -765,14 +765,13 @@ def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lowe
             signed_distances, neighbors, indices, vertex_offsets, triangle_types, voxel_cell_codes, level_sets,
             face_offsets, num_faces if capacity is None else None, None if capacity is None else num_faces,
         )
-        if g > 0 and num_level_sets > 0:
-            vertex_boundaries = vertex_offsets[1:].view(num_level_sets, -1)[:, -1].clone()
-        else:
-            vertex_boundaries = torch.zeros((num_level_sets,), dtype=torch.int32, device=device)
-        if nv > 0 and num_level_sets > 0:
-            face_boundaries = face_offsets[1:].view(num_level_sets, -1)[:, -1].clone() // 3
-        else:
-            face_boundaries = torch.zeros((num_level_sets,), dtype=torch.int32, device=device)
+        # vertex_offsets[1:].view(S, -1)[:, -1] and face_offsets[...] // 3 (and
+        # the counted face total) in one launch.
+        vertex_boundaries = torch.empty((num_level_sets,), dtype=torch.int32, device=device)
+        face_boundaries = torch.empty((num_level_sets,), dtype=torch.int32, device=device)
+        nt.call("mt_shell_boundaries", vertex_offsets.data_ptr(), g, face_offsets.data_ptr(), nv, num_level_sets,
+                vertex_boundaries.data_ptr(), face_boundaries.data_ptr(),
+                counts.num_faces.data_ptr() if counts is not None else None, nt.stream(device))
 
     logging.debug(f"Created {num_vertices} vertices and {num_faces} faces.")
     return Triangles(triangle_vertices, triangle_sdf, triangle_sh, faces, voxel_indices, vertex_boundaries,
