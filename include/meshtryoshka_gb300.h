@@ -223,7 +223,9 @@ MT_API int mt_count_triangle_vertices(const float* signed_distances,
  * vertex_sources [3,V] int32: origin corner, axis corner and the float bits
  * of the (detached) weight t of every vertex. num_vertices: NULL, or a
  * device int32 (the last vertex offset); V is then the buffers' capacity
- * (the row stride of spherical_harmonics) and vertices past it are dropped. */
+ * (the row stride of spherical_harmonics) and vertices past it are dropped.
+ * spherical_harmonics NULL (grid_sh may then be NULL too): the SH rows are
+ * not formed (mt_grid_sh_colors evaluates colours from the grid directly). */
 MT_API int mt_create_triangle_vertices(const float* grid_vertices,
                                 const float* grid_signed_distances,
                                 const float* grid_spherical_harmonics,
@@ -257,6 +259,64 @@ MT_API int mt_create_triangle_vertices_backward(
  * NULL or smaller workspace the single-pass gather runs instead; both give
  * the same results. */
 MT_API size_t mt_create_triangle_vertices_backward_workspace_bytes(int64_t G, int64_t V);
+
+/* ------------------------------------------------------------------------
+ * Grid SH straight to vertex colours (not in the reference, which forms the
+ * per-vertex SH rows [C,V,3] in create_triangle_vertices.slang:145-199 and
+ * evaluates them in evaluate_spherical_harmonics.slang:4-270; these entry
+ * points give the same bits without the rows, forward and backward).
+ * ---------------------------------------------------------------------- */
+
+/* The backward of create_triangle_vertices.slang:201-291 as a gather needs,
+ * per grid vertex, the list of its contributions (vertex, t, origin or axis
+ * corner), enumerated in a fixed order. This builds it ahead of the
+ * backward: corner_inverse [4,G] (scratch), list_offsets [G+1] (CSR offsets)
+ * and list [2V, 2] int32 (vertex | origin flag << 31, float bits of t). At
+ * most mt_vertex_grad_list_max_shells() level sets and V < 2^31
+ * (MT_ERR_TOO_LARGE otherwise). */
+MT_API int mt_vertex_grad_list_max_shells(void);
+MT_API size_t mt_build_vertex_grad_list_workspace_bytes(int64_t G);
+MT_API int mt_build_vertex_grad_list(const float* grid_signed_distances,
+                                     const int32_t* lower_corners, int64_t G,
+                                     const float* level_sets, int32_t S,
+                                     const int32_t* vertex_offsets, int64_t V,
+                                     int32_t* corner_inverse, int32_t* list_offsets,
+                                     int32_t* list, void* workspace,
+                                     size_t workspace_bytes, mt_stream_t stream);
+
+/* create_triangle_vertices.slang:201-291 (backward) for the vertex positions
+ * and signed distances from a prebuilt list: the same sums, in the same
+ * order, as mt_create_triangle_vertices_backward. Every grid entry written. */
+MT_API int mt_vertex_grads_from_list(const int32_t* list_offsets, const int32_t* list,
+                                     int64_t G, const float* grad_vertices,
+                                     const float* grad_signed_distances,
+                                     float* grad_grid_vertices,
+                                     float* grad_grid_signed_distances,
+                                     mt_stream_t stream);
+
+/* out_colors [B,V,3] = evaluate_spherical_harmonics(vertices, the SH rows
+ * that mt_create_triangle_vertices would interpolate from grid_sh [C,G,3]
+ * with vertex_sources [3,V]), rows in registers. num_vertices: NULL or the
+ * device live count; rows past it are not written. */
+MT_API int mt_grid_sh_colors(const float* grid_spherical_harmonics, int32_t C, int64_t G,
+                             const int32_t* vertex_sources, int64_t V,
+                             const int32_t* num_vertices, const float* vertices,
+                             int32_t sh_degree, const float* camera_positions,
+                             int32_t B, float* out_colors, mt_stream_t stream);
+
+/* Backward of mt_grid_sh_colors: grad_grid_sh [C,G,3] (every entry written)
+ * from grad_colors [B,V,3] through the list of mt_build_vertex_grad_list;
+ * the per-vertex SH gradient of
+ * mt_evaluate_spherical_harmonics_backward is formed on the fly, so the
+ * result equals that call followed by mt_create_triangle_vertices_backward
+ * bit for bit. */
+MT_API int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list,
+                                      int64_t G, int64_t V, const float* vertices,
+                                      int32_t C, int32_t sh_degree,
+                                      const float* camera_positions, int32_t B,
+                                      const float* out_colors, const float* grad_colors,
+                                      float* grad_grid_spherical_harmonics,
+                                      mt_stream_t stream);
 
 /* triangle_extraction/compute_sdf_regularizers.slang:18-128 (forward) and its
  * automatic derivative (backward). Per voxel: eikonal_loss_pos / _neg [Nv]

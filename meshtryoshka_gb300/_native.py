@@ -68,6 +68,12 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
         [P, P, I64, I64, I64, P, P, P, I32, P, I64, P, P, P],
     ),
     "mt_shell_boundaries": (I32, [P, I64, P, I64, I32, P, P, P, P]),
+    "mt_vertex_grad_list_max_shells": (I32, []),
+    "mt_build_vertex_grad_list_workspace_bytes": (c_size_t, [I64]),
+    "mt_build_vertex_grad_list": (I32, [P, P, I64, P, I32, P, I64, P, P, P, P, c_size_t, P]),
+    "mt_vertex_grads_from_list": (I32, [P, P, I64, P, P, P, P, P]),
+    "mt_grid_sh_colors": (I32, [P, I32, I64, P, I64, P, P, I32, P, I32, P, P]),
+    "mt_grid_sh_colors_backward": (I32, [P, P, I64, I64, P, I32, I32, P, I32, P, P, P, P]),
     "mt_capacity_overflow": (I32, [P, I64, P, I64, P, I64, P, P]),
     "mt_sort_pairs_workspace_bytes": (c_size_t, [I64]),
     "mt_sort_pairs_i64_i32": (I32, [P, P, P, P, I64, P, I32, I32, P, c_size_t, P]),
@@ -138,11 +144,12 @@ def library_path() -> str:
 KERNELS_PER_CALL = {
     "mt_sort_pairs_i64_i32": 11,  # histogram, plan, 8 digit passes, copy
     "mt_create_voxels": 1,
-    "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows
+    "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows (1 without the rows)
     "mt_create_triangle_vertices_backward": 5,  # corner inverse, count, scan, list + grads, SH gather
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
     "mt_sort_keys_by_tile": 6,
-    "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
+    "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys
+    "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
 }
 
 
@@ -174,12 +181,14 @@ def record_launches(timed: bool = False):
         _recorder = previous
 
 
-def call(name: str, *args) -> None:
-    """Call an entry point and raise RuntimeError on a non-zero status."""
+def call(name: str, *args, launches: int | None = None) -> None:
+    """Call an entry point and raise RuntimeError on a non-zero status.
+    ``launches``: kernels this call enqueues, when it differs from the entry
+    point's usual count (``KERNELS_PER_CALL``)."""
     lib = _load()
     rec = _recorder
     if rec is not None:
-        rec.launches += KERNELS_PER_CALL.get(name, 1)
+        rec.launches += KERNELS_PER_CALL.get(name, 1) if launches is None else launches
         rec.calls[name] = rec.calls.get(name, 0) + 1
         if rec.timed:
             start = torch.cuda.Event(enable_timing=True)

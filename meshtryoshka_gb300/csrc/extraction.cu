@@ -14,6 +14,7 @@
 
 #include "mc_tables.h"
 #include "mt_common.cuh"
+#include "sh.cuh"
 
 namespace mt {
 namespace {
@@ -624,7 +625,7 @@ __global__ void vertex_grad_list_kernel(const float* __restrict__ gsdf, const in
           for (int ch = 0; ch < 3; ++ch) p[ch] += weighted(__ldg(dv + 3 * vi + ch), t, origin);
         }
       });
-      gdsdf[x] = d;
+      if (gdsdf) gdsdf[x] = d;
       if (gdv) {
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) gdv[3 * x + ch] = p[ch];
@@ -658,6 +659,184 @@ __global__ void vertex_sh_gather_kernel(const float* __restrict__ dsh, int C, in
     dst[0] = a0;
     dst[1] = a1;
     dst[2] = a2;
+  }
+}
+
+// The signed-distance and position gradients of the list (pass 2's sums,
+// in list order, so the same bits), for a list built ahead of the backward.
+__global__ void vertex_grads_from_list_kernel(const int32_t* __restrict__ offsets, const int2* __restrict__ list,
+                                              int64_t G, const float* __restrict__ dv, const float* __restrict__ dsdf,
+                                              float* __restrict__ gdv, float* __restrict__ gdsdf) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < G; x += (int64_t)gridDim.x * blockDim.x) {
+    float d = 0.f, p[3] = {0.f, 0.f, 0.f};
+    const int32_t end = __ldg(offsets + x + 1);
+    for (int32_t q = __ldg(offsets + x); q < end; ++q) {
+      const int2 e = __ldg(list + q);
+      const int64_t vi = e.x & 0x7fffffff;
+      const bool origin = e.x < 0;
+      const float t = __int_as_float(e.y);
+      if (dsdf) d += weighted(__ldg(dsdf + vi), t, origin);
+      if (dv) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) p[ch] += weighted(__ldg(dv + 3 * vi + ch), t, origin);
+      }
+    }
+    gdsdf[x] = d;
+    if (gdv) {
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) gdv[3 * x + ch] = p[ch];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Grid SH -> vertex colours without per-vertex SH rows: the interpolation of
+// create_triangle_vertices.slang:145-199 (coefficients of vertex v from its
+// two grid corners with weight t) followed by
+// evaluate_spherical_harmonics.slang:4-270 for every camera, the coefficients
+// kept in registers. Same operations as interpolate_vertex_sh_kernel then
+// sh_forward_kernel, so the same bits. Vertices at or past the live count are
+// not touched.
+// ---------------------------------------------------------------------------
+template <int kCoeff>
+__device__ __forceinline__ void grid_sh_vertex(const float* __restrict__ gsh, int64_t G,
+                                               const int32_t* __restrict__ sources, int64_t V,
+                                               const float* __restrict__ verts, const float* __restrict__ campos,
+                                               int B, int64_t v, float* __restrict__ out) {
+  const int32_t i0 = __ldg(sources + v), i1 = __ldg(sources + V + v);
+  const float t = __int_as_float(__ldg(sources + 2 * V + v));
+  float coef[kCoeff][3];
+#pragma unroll
+  for (int k = 0; k < kCoeff; ++k) {
+    const float* p0 = gsh + ((int64_t)k * G + i0) * 3;
+    const float* p1 = gsh + ((int64_t)k * G + i1) * 3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) coef[k][c] = lerp_ref(__ldg(p0 + c), __ldg(p1 + c), t);
+  }
+  sh_colors<kCoeff>(verts, V, coef, campos, B, v, out);
+}
+
+__global__ void grid_sh_colors_kernel(const float* __restrict__ gsh, int64_t G, const int32_t* __restrict__ sources,
+                                      int64_t V, const int32_t* __restrict__ count, const float* __restrict__ verts,
+                                      int n_coeff, const float* __restrict__ campos, int B, float* __restrict__ out) {
+  const int64_t n = count ? min((int64_t)max(*count, 0), V) : V;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    switch (n_coeff) {
+      case 1: grid_sh_vertex<1>(gsh, G, sources, V, verts, campos, B, v, out); break;
+      case 4: grid_sh_vertex<4>(gsh, G, sources, V, verts, campos, B, v, out); break;
+      case 9: grid_sh_vertex<9>(gsh, G, sources, V, verts, campos, B, v, out); break;
+      default: grid_sh_vertex<16>(gsh, G, sources, V, verts, campos, B, v, out); break;
+    }
+  }
+}
+
+// Backward: grid vertex x's SH gradient is sum over its list entries (v, t)
+// of weighted(d sh_v), with d sh_v[k] = sum_b basis_k(dir_bv) d rgb_bv
+// [rgb_bv > 0] formed on the fly (the sums of sh_backward_kernel, cameras in
+// order, then of vertex_sh_gather_kernel, entries in list order: the same
+// bits without the [C, V, 3] rows). One thread per (group of kRowsPerThread
+// rows, grid vertex); consecutive threads write consecutive grid vertices of
+// each row. Rows k >= n_coeff (up to C) are written as zeros.
+// A CTA takes kShX consecutive grid vertices; their list entries are
+// contiguous. In rounds of kShThreads entries, thread i forms entry i's
+// weighted SH gradient (all rows: the per-vertex d sh_v of sh_backward_kernel,
+// cameras in order, then weighted by the entry's (t, origin)) in shared
+// memory; then thread (row half h, grid vertex x) adds x's entries of the
+// round to its 8 rows in list order, carrying its sums across rounds. The
+// same sums in the same order as sh_backward_kernel + vertex_sh_gather_kernel.
+constexpr int kShThreads = 128;
+constexpr int kShX = 64;
+constexpr int kShStride = 49;  // 48 values per entry; odd stride spreads rows over banks
+
+__device__ __forceinline__ void entry_sh_gradient(int2 e, int64_t V, const float* __restrict__ verts, int n_coeff,
+                                                  const float* __restrict__ campos, int B,
+                                                  const float* __restrict__ colors,
+                                                  const float* __restrict__ dcolors, float* __restrict__ out) {
+  const int64_t vi = e.x & 0x7fffffff;
+  const bool origin = e.x < 0;
+  const float t = __int_as_float(e.y);
+  const float px = __ldg(verts + 3 * vi), py = __ldg(verts + 3 * vi + 1), pz = __ldg(verts + 3 * vi + 2);
+  float d[16][3];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
+#pragma unroll 2
+  for (int b = 0; b < B; ++b) {
+    const int64_t ob = ((int64_t)b * V + vi) * 3;
+    float col[3], dcol[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      col[c] = __ldg(colors + ob + c);
+      dcol[c] = __ldg(dcolors + ob + c);
+    }
+    float g[3];
+    bool any = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      g[c] = col[c] > 0.0f ? dcol[c] : 0.0f;
+      any |= g[c] != 0.0f;
+    }
+    if (!any) continue;
+    float dx, dy, dz;
+    view_dir_at(px, py, pz, campos + 3 * b, dx, dy, dz);
+    float basis[16];
+    sh_basis(dx, dy, dz, n_coeff, basis);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      if (k < n_coeff) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[3 * k + c] = weighted(d[k][c], t, origin);
+  }
+}
+
+__global__ void __launch_bounds__(kShThreads)
+    grid_sh_colors_backward_kernel(const int32_t* __restrict__ offsets, const int2* __restrict__ list, int64_t G,
+                                   int64_t V, const float* __restrict__ verts, int C, int n_coeff,
+                                   const float* __restrict__ campos, int B, const float* __restrict__ colors,
+                                   const float* __restrict__ dcolors, float* __restrict__ gdsh) {
+  __shared__ float s_grad[kShThreads * kShStride];
+  const int tid = threadIdx.x;
+  const int half = tid / kShX, xl = tid % kShX;  // rows 8*half .. 8*half+7 of grid vertex x0 + xl
+  for (int64_t x0 = (int64_t)blockIdx.x * kShX; x0 < G; x0 += (int64_t)gridDim.x * kShX) {
+    const int64_t x = x0 + xl;
+    const int32_t e_begin = __ldg(offsets + x0), e_end = __ldg(offsets + min(x0 + kShX, G));
+    const int32_t my_begin = x < G ? __ldg(offsets + x) : 0, my_end = x < G ? __ldg(offsets + x + 1) : 0;
+    float acc[8][3];
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) acc[kk][0] = acc[kk][1] = acc[kk][2] = 0.f;
+    for (int32_t base = e_begin; base < e_end; base += kShThreads) {
+      if (base + tid < e_end)
+        entry_sh_gradient(__ldg(list + base + tid), V, verts, n_coeff, campos, B, colors, dcolors,
+                          s_grad + tid * kShStride);
+      __syncthreads();
+      const int32_t lo = max(my_begin, base), hi = min(my_end, base + kShThreads);
+      for (int32_t q = lo; q < hi; ++q) {
+        const float* src = s_grad + (q - base) * kShStride + 24 * half;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[kk][c] += src[3 * kk + c];
+        }
+      }
+      __syncthreads();
+    }
+    if (x < G) {
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const int k = 8 * half + kk;
+        if (k < C) {
+          float* dst = gdsh + ((int64_t)k * G + x) * 3;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) dst[c] = k < n_coeff ? acc[kk][c] : 0.f;
+        }
+      }
+    }
   }
 }
 
@@ -1062,13 +1241,14 @@ int mt_create_triangle_vertices(const float* grid_vertices, const float* grid_si
                                 mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && S >= 0 && C >= 1 && V >= 0);
   if (G == 0 || S == 0 || V == 0) return MT_OK;
-  MT_REQUIRE(grid_vertices && grid_signed_distances && grid_spherical_harmonics && lower_corners && level_sets &&
-             vertex_offsets && vertices && signed_distances && spherical_harmonics && vertex_types &&
-             vertex_sources);
+  MT_REQUIRE(grid_vertices && grid_signed_distances && lower_corners && level_sets && vertex_offsets && vertices &&
+             signed_distances && vertex_types && vertex_sources);
   create_vertices_kernel<<<grid_stride_blocks(G, 128), 128, 0, as_stream(stream)>>>(
       grid_vertices, grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, V, vertices,
       signed_distances, vertex_types, vertex_sources);
   MT_CHECK_LAUNCH();
+  if (spherical_harmonics == nullptr) return MT_OK;  // rows left to mt_grid_sh_colors
+  MT_REQUIRE(grid_spherical_harmonics);
   interpolate_vertex_sh_kernel<<<grid_stride_blocks((int64_t)C * V, 256), 256, 0, as_stream(stream)>>>(
       grid_spherical_harmonics, C, G, vertex_sources, V, num_vertices, spherical_harmonics);
   MT_CHECK_LAUNCH();
@@ -1212,6 +1392,91 @@ int mt_capacity_overflow(const int32_t* num_vertices, int64_t vertex_capacity, c
   MT_REQUIRE(overflow);
   capacity_overflow_kernel<<<1, 1, 0, as_stream(stream)>>>(num_vertices, vertex_capacity, num_faces, face_capacity,
                                                           num_keys, key_capacity, overflow);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_vertex_grad_list_max_shells(void) { return kShellsPerChunk; }
+
+size_t mt_build_vertex_grad_list_workspace_bytes(int64_t G) { return 256 + mt_scan_workspace_bytes(G + 1); }
+
+int mt_build_vertex_grad_list(const float* grid_signed_distances, const int32_t* lower_corners, int64_t G,
+                              const float* level_sets, int32_t S, const int32_t* vertex_offsets, int64_t V,
+                              int32_t* corner_inverse, int32_t* list_offsets, int32_t* list, void* workspace,
+                              size_t workspace_bytes, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && S >= 0 && V >= 0);
+  if (S > kShellsPerChunk || V >= (int64_t)0x7fffffff) return MT_ERR_TOO_LARGE;
+  if (G == 0) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && lower_corners && corner_inverse && list_offsets && workspace);
+  MT_REQUIRE(S == 0 || (level_sets && vertex_offsets));
+  MT_REQUIRE(V == 0 || list);
+  if (workspace_bytes < mt_build_vertex_grad_list_workspace_bytes(G)) return MT_ERR_WORKSPACE_TOO_SMALL;
+  cudaStream_t st = as_stream(stream);
+  if (cudaMemsetAsync(corner_inverse, 0xff, (size_t)G * 4 * sizeof(int32_t), st) != cudaSuccess) return MT_ERR_CUDA;
+  invert_corners_kernel<<<grid_stride_blocks(G, 256), 256, 0, st>>>(lower_corners, G, corner_inverse);
+  MT_CHECK_LAUNCH();
+  vertex_grad_list_kernel<false><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, list_offsets,
+      nullptr, nullptr, nullptr, nullptr, nullptr);
+  MT_CHECK_LAUNCH();
+  char* ws = static_cast<char*>(workspace);
+  const int rc = mt_exclusive_scan_i32(list_offsets, G + 1, ws + 256, workspace_bytes - 256, stream);
+  if (rc != MT_OK) return rc;
+  vertex_grad_list_kernel<true><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, list_offsets,
+      reinterpret_cast<int2*>(list), nullptr, nullptr, nullptr, nullptr);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_vertex_grads_from_list(const int32_t* list_offsets, const int32_t* list, int64_t G,
+                              const float* grad_vertices, const float* grad_signed_distances,
+                              float* grad_grid_vertices, float* grad_grid_signed_distances, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0);
+  if (G == 0) return MT_OK;
+  MT_REQUIRE(list_offsets && grad_grid_signed_distances);
+  MT_REQUIRE(grad_vertices == nullptr || grad_grid_vertices != nullptr);
+  vertex_grads_from_list_kernel<<<grid_stride_blocks(G, 256), 256, 0, as_stream(stream)>>>(
+      list_offsets, reinterpret_cast<const int2*>(list), G, grad_vertices, grad_signed_distances, grad_grid_vertices,
+      grad_grid_signed_distances);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_grid_sh_colors(const float* grid_spherical_harmonics, int32_t C, int64_t G, const int32_t* vertex_sources,
+                      int64_t V, const int32_t* num_vertices, const float* vertices, int32_t sh_degree,
+                      const float* camera_positions, int32_t B, float* out_colors, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+  MT_REQUIRE(C >= n);
+  if (V == 0 || B == 0) return MT_OK;
+  MT_REQUIRE(grid_spherical_harmonics && vertex_sources && vertices && camera_positions && out_colors);
+  grid_sh_colors_kernel<<<grid_stride_blocks(V, 256), 256, 0, as_stream(stream)>>>(
+      grid_spherical_harmonics, G, vertex_sources, V, num_vertices, vertices, n, camera_positions, B, out_colors);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list, int64_t G, int64_t V,
+                               const float* vertices, int32_t C, int32_t sh_degree, const float* camera_positions,
+                               int32_t B, const float* out_colors, const float* grad_colors,
+                               float* grad_grid_spherical_harmonics, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
+  const int n = (sh_degree + 1) * (sh_degree + 1);
+  MT_REQUIRE(C >= n);
+  if (G == 0) return MT_OK;
+  MT_REQUIRE(list_offsets && grad_grid_spherical_harmonics);
+  // No cameras or vertices: every list sum is empty and the rows are zeros.
+  const int Bn = V > 0 ? B : 0;
+  MT_REQUIRE(Bn == 0 || (list && vertices && camera_positions && out_colors && grad_colors));
+  cudaStream_t st = as_stream(stream);
+  if (C > 16 && cudaMemsetAsync(grad_grid_spherical_harmonics + (size_t)16 * G * 3, 0,
+                                (size_t)(C - 16) * G * 3 * sizeof(float), st) != cudaSuccess)
+    return MT_ERR_CUDA;  // rows past degree 3's sixteen are zeros
+  const int64_t xblocks = (G + kShX - 1) / kShX;
+  grid_sh_colors_backward_kernel<<<(unsigned)min(xblocks, (int64_t)152 * 32), kShThreads, 0, st>>>(
+      list_offsets, reinterpret_cast<const int2*>(list), G, V, vertices, C, n, camera_positions, Bn, out_colors,
+      grad_colors, grad_grid_spherical_harmonics);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

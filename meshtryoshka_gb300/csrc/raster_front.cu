@@ -11,6 +11,7 @@
 // operation by operation in IEEE-754 single precision.
 
 #include "lookback.cuh"  // warp_sum, warp_inclusive_sum
+#include "sh.cuh"
 
 namespace mt {
 namespace {
@@ -78,52 +79,6 @@ __global__ void project_kernel(const float* __restrict__ verts, int64_t V, const
   }
 }
 
-// ---------------------------------------------------------------------------
-// evaluate_spherical_harmonics.slang:4-270. Real SH up to degree 3;
-// rgb = max(sum_k basis_k(dir) sh_k + 0.5, 0).
-// ---------------------------------------------------------------------------
-__constant__ float kShC0 = 0.28209479177387814f;
-__constant__ float kShC1 = 0.4886025119029199f;
-__constant__ float kShC2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f,
-                               -1.0925484305920792f, 0.5462742152960396f};
-__constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f,
-                               0.3731763325901154f,  -0.4570457994644658f, 1.445305721320277f,
-                               -0.5900435899266435f};
-
-__device__ __forceinline__ void sh_basis(float x, float y, float z, int n, float (&basis)[16]) {
-  basis[0] = kShC0;
-  if (n <= 1) return;
-  basis[1] = -kShC1 * y;
-  basis[2] = kShC1 * z;
-  basis[3] = -kShC1 * x;
-  if (n <= 4) return;
-  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
-  basis[4] = kShC2[0] * xy;
-  basis[5] = kShC2[1] * yz;
-  basis[6] = kShC2[2] * (2.0f * zz - xx - yy);
-  basis[7] = kShC2[3] * xz;
-  basis[8] = kShC2[4] * (xx - yy);
-  if (n <= 9) return;
-  basis[9] = kShC3[0] * y * (3.0f * xx - yy);
-  basis[10] = kShC3[1] * xy * z;
-  basis[11] = kShC3[2] * y * (4.0f * zz - xx - yy);
-  basis[12] = kShC3[3] * z * (2.0f * zz - 3.0f * xx - 3.0f * yy);
-  basis[13] = kShC3[4] * x * (4.0f * zz - xx - yy);
-  basis[14] = kShC3[5] * z * (xx - yy);
-  basis[15] = kShC3[6] * x * (xx - 3.0f * yy);
-}
-
-__device__ __forceinline__ void view_dir(const float* __restrict__ verts, int64_t v, const float* __restrict__ cam,
-                                         float& x, float& y, float& z) {
-  // normalize(vertex - camera) = d / sqrt(dot(d, d))
-  const float dx = __fsub_rn(verts[3 * v], cam[0]), dy = __fsub_rn(verts[3 * v + 1], cam[1]),
-              dz = __fsub_rn(verts[3 * v + 2], cam[2]);
-  const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-  x = __fdiv_rn(dx, len);
-  y = __fdiv_rn(dy, len);
-  z = __fdiv_rn(dz, len);
-}
-
 // The vertex's coefficients are read once into registers and serve every
 // camera.
 template <int kCoeff>
@@ -138,23 +93,7 @@ __device__ __forceinline__ void sh_forward_vertex(const float* __restrict__ vert
     coef[k][1] = __ldg(s + 1);
     coef[k][2] = __ldg(s + 2);
   }
-  for (int b = 0; b < B; ++b) {
-    float x, y, z;
-    view_dir(verts, v, campos + 3 * b, x, y, z);
-    float basis[16];
-    sh_basis(x, y, z, kCoeff, basis);
-    float rgb[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) rgb[c] = __fmul_rn(basis[0], coef[0][c]);
-#pragma unroll
-    for (int k = 1; k < kCoeff; ++k) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) rgb[c] = __fadd_rn(rgb[c], __fmul_rn(basis[k], coef[k][c]));
-    }
-    float* o = out + ((int64_t)b * V + v) * 3;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) o[c] = fmaxf(__fadd_rn(rgb[c], 0.5f), 0.0f);
-  }
+  sh_colors<kCoeff>(verts, V, coef, campos, B, v, out);
 }
 
 __global__ void sh_forward_kernel(const float* __restrict__ verts, int64_t V, const float* __restrict__ sh,

@@ -151,16 +151,18 @@ def uncontract_stand_in(vertices: Tensor) -> Tensor:
 
 
 def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = None,
-                    grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None) -> tuple[Tensor, Tensor]:
+                    grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None,
+                    defer_sh: bool = True) -> tuple[Tensor, Tensor]:
     """The fused step's forward with capacity-sized buffers and no
     device->host reads (capturable in a CUDA graph). Returns the loss and a
     device flag that is true when a live vertex, face or key count exceeded
-    its capacity (the step's result is then incomplete)."""
+    its capacity (the step's result is then incomplete). ``defer_sh``: vertex
+    colours straight from the grid SH (no per-vertex SH rows; same values)."""
     grid_sdf = w.grid_sdf if grid_sdf is None else grid_sdf
     grid_sh = w.grid_sh if grid_sh is None else grid_sh
     tri, counts = te.tessellate_voxels_counted(
         grid_sdf, w.voxels.vertices, grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
-        w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces)
+        w.voxels.upper_corners, w.voxels.indices, w.level_sets, caps.vertices, caps.faces, defer_sh=defer_sh)
     with torch.no_grad():
         vertices = uncontract_stand_in(tri.vertices)
     counted = dict(num_faces=counts.num_faces, key_capacity=caps.keys)

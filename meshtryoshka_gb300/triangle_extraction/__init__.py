@@ -27,6 +27,7 @@ from .. import _native as nt
 __all__ = [
     "Voxels",
     "Triangles",
+    "DeferredSH",
     "extract_voxels",
     "tessellate_voxels",
     "compute_sdf_regularizers",
@@ -435,6 +436,76 @@ def count_triangle_vertices(signed_distances: Tensor, lower_corners: Tensor, lev
     return counts
 
 
+class DeferredSH:
+    """Per-vertex SH coefficients that are never formed (not in the
+    reference): stands where ``Triangles.spherical_harmonics`` holds the
+    [C, V, 3] rows, and renders evaluate vertex colours straight from the
+    grid coefficients through it (``evaluate``), forward and backward, with
+    the same bits as the rows would give. Filled by ``CreateTriangleVertices``
+    with ``defer_sh``: the vertices' source records and the per-grid-vertex
+    contribution list that both backward passes use."""
+
+    def __init__(self, grid_spherical_harmonics: Tensor):
+        self.grid_spherical_harmonics = grid_spherical_harmonics
+        self.vertex_sources: Tensor | None = None  # [3, V] int32 (origin, axis corner, bits of t)
+        self.num_vertices: Tensor | None = None  # device int32 live count (capacity mode) or None
+        self.list_offsets: Tensor | None = None  # [G + 1] int32
+        self.contributions: Tensor | None = None  # [2V, 2] int32
+
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        c = self.grid_spherical_harmonics.shape[0]
+        v = self.vertex_sources.shape[1] if self.vertex_sources is not None else 0
+        return (c, v, 3)
+
+    def evaluate(self, vertices: Tensor, extrinsics: Tensor, sh_degree: int) -> Tensor:
+        """evaluate_spherical_harmonics(vertices, rows, extrinsics, sh_degree)."""
+        return GridSHColors.apply(self.grid_spherical_harmonics, vertices, extrinsics, sh_degree, self)
+
+
+class GridSHColors(torch.autograd.Function):
+    """Vertex colours [B, V, 3] from the grid SH (create_triangle_vertices.py's
+    SH interpolation followed by evaluate_spherical_harmonics.py:23-111, fused);
+    the gradient goes straight to the grid SH."""
+
+    @staticmethod
+    def forward(ctx, grid_spherical_harmonics, vertices, extrinsics, sh_degree, deferred):
+        with record_function("grid_sh_colors_forward"):
+            gsh = _f32(grid_spherical_harmonics, "grid_spherical_harmonics")
+            vertices = _f32(vertices, "vertices")
+            extrinsics = _f32(extrinsics, "extrinsics")
+            device = nt.require_cuda(gsh, vertices, extrinsics)
+            c, g, _ = gsh.shape
+            b = extrinsics.shape[0]
+            v = vertices.shape[0]
+            if deferred.vertex_sources.shape[1] != v:
+                raise ValueError("vertices must have one row per deferred SH vertex")
+            campos = torch.empty((b, 3), dtype=torch.float32, device=device)
+            nt.call("mt_camera_positions", nt.ptr(extrinsics), b, nt.ptr(campos), nt.stream(device))
+            colors = torch.empty((b, v, 3), dtype=torch.float32, device=device)
+            nt.call("mt_grid_sh_colors", nt.ptr(gsh), c, g, nt.ptr(deferred.vertex_sources), v,
+                    nt.ptr(deferred.num_vertices), nt.ptr(vertices), int(sh_degree), nt.ptr(campos), b,
+                    nt.ptr(colors), nt.stream(device))
+            ctx.save_for_backward(vertices, campos, colors)
+            ctx.deferred = deferred
+            ctx.gsh_shape = gsh.shape
+            ctx.sh_degree = int(sh_degree)
+            return colors
+
+    @staticmethod
+    def backward(ctx, grad_colors):
+        with record_function("grid_sh_colors_backward"):
+            vertices, campos, colors = ctx.saved_tensors
+            d = ctx.deferred
+            c, g, _ = ctx.gsh_shape
+            device = vertices.device
+            grad_gsh = torch.empty(ctx.gsh_shape, dtype=torch.float32, device=device)  # fully written
+            nt.call("mt_grid_sh_colors_backward", nt.ptr(d.list_offsets), nt.ptr(d.contributions), g,
+                    vertices.shape[0], nt.ptr(vertices), c, ctx.sh_degree, nt.ptr(campos), campos.shape[0],
+                    nt.ptr(colors), nt.ptr(grad_colors.contiguous()), nt.ptr(grad_gsh), nt.stream(device))
+            return grad_gsh, None, None, None, None
+
+
 class CreateTriangleVerticesResult(NamedTuple):
     vertices: Tensor
     signed_distances: Tensor
@@ -448,7 +519,7 @@ class CreateTriangleVertices(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners,
-                level_sets, vertex_offsets, num_vertices=None, capacity=None):
+                level_sets, vertex_offsets, num_vertices=None, capacity=None, deferred=None):
         with record_function("create_triangle_vertices_forward"):
             grid_vertices = _f32(grid_vertices, "grid_vertices")
             grid_signed_distances = _f32(grid_signed_distances, "grid_signed_distances")
@@ -472,15 +543,35 @@ class CreateTriangleVertices(torch.autograd.Function):
             kw = dict(dtype=torch.float32, device=device)
             vertices = torch.empty((v, 3), **kw)
             sdf = torch.empty((v,), **kw)
-            sh = torch.empty((c, v, 3), **kw)
+            # Deferred SH: no rows (a [C, 0, 3] placeholder); colours come from
+            # the grid through `deferred`.
+            sh = torch.empty((c, 0 if deferred is not None else v, 3), **kw)
             types = torch.empty((v,), dtype=torch.uint8, device=device)
             sources = torch.empty((3, v), dtype=torch.int32, device=device)
             nt.call(
                 "mt_create_triangle_vertices",
                 nt.ptr(grid_vertices), nt.ptr(grid_signed_distances), nt.ptr(grid_spherical_harmonics), c,
                 nt.ptr(voxel_lower_corners), g, nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v, count_ptr,
-                nt.ptr(vertices), nt.ptr(sdf), nt.ptr(sh), nt.ptr(types), nt.ptr(sources), nt.stream(device),
+                nt.ptr(vertices), nt.ptr(sdf), None if deferred is not None else nt.ptr(sh), nt.ptr(types),
+                nt.ptr(sources), nt.stream(device), launches=1 if deferred is not None else None,
             )
+            ctx.deferred = deferred is not None
+            if deferred is not None:
+                # The contribution list of the backward gather, built now so that
+                # the colour backward and this Function's backward share it.
+                inverse = torch.empty((4, g), dtype=torch.int32, device=device)
+                offsets = torch.empty((g + 1,), dtype=torch.int32, device=device)
+                contributions = torch.empty((2 * v, 2), dtype=torch.int32, device=device)
+                ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_build_vertex_grad_list_workspace_bytes(g))
+                nt.call("mt_build_vertex_grad_list", nt.ptr(grid_signed_distances), nt.ptr(voxel_lower_corners), g,
+                        nt.ptr(level_sets), s, nt.ptr(vertex_offsets), v, nt.ptr(inverse), nt.ptr(offsets),
+                        nt.ptr(contributions), ws_ptr, ws_bytes, nt.stream(device))
+                deferred.vertex_sources = sources
+                deferred.num_vertices = (vertex_offsets[-1:].view(()) if capacity is not None else None)
+                deferred.list_offsets = offsets
+                deferred.contributions = contributions
+                ctx.list = (offsets, contributions)
+                ctx.mark_non_differentiable(sh)
             ctx.save_for_backward(grid_signed_distances, voxel_lower_corners, level_sets, vertex_offsets)
             ctx.shapes = (grid_vertices.shape, grid_spherical_harmonics.shape, v)
             ctx.mark_non_differentiable(types)
@@ -502,6 +593,14 @@ class CreateTriangleVertices(torch.autograd.Function):
                 raise ValueError("grid_signed_distances must have one value per voxel-lower-corner entry")
             grad_grid_vertices = torch.empty(gv_shape, dtype=torch.float32, device=device)
             grad_grid_sdf = torch.empty_like(grid_signed_distances)
+            if ctx.deferred:
+                # The SH gradient comes from the colour Function (GridSHColors).
+                offsets, contributions = ctx.list
+                gv = grad_vertices.contiguous() if grad_vertices is not None else None
+                gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
+                nt.call("mt_vertex_grads_from_list", nt.ptr(offsets), nt.ptr(contributions), g, nt.ptr(gv),
+                        nt.ptr(gd), nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.stream(device))
+                return grad_grid_vertices, grad_grid_sdf, None, None, None, None, None, None, None
             grad_grid_sh = torch.empty(gsh_shape, dtype=torch.float32, device=device)
             inverse = torch.empty((4, g), dtype=torch.int32, device=device)
             gv = grad_vertices.contiguous() if grad_vertices is not None else None
@@ -516,7 +615,7 @@ class CreateTriangleVertices(torch.autograd.Function):
                 nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), ws_ptr, ws_bytes,
                 nt.stream(device),
             )
-            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None
+            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None, None
 
 
 def create_triangle_vertices(
@@ -528,14 +627,18 @@ def create_triangle_vertices(
     vertex_offsets: Tensor,
     num_vertices: int | None = None,
     capacity: int | None = None,
+    deferred: DeferredSH | None = None,
 ) -> CreateTriangleVerticesResult:
     """``num_vertices`` (optional, not in the reference signature) skips the
     device->host read of ``vertex_offsets[-1]`` when the caller knows it.
     ``capacity`` (optional) sizes the outputs to a fixed row count instead and
-    keeps the live count on the device; rows past it are unused."""
+    keeps the live count on the device; rows past it are unused.
+    ``deferred`` (optional): the SH rows are not formed; ``deferred`` is filled
+    for colour evaluation from the grid, and the result's
+    ``spherical_harmonics`` is a [C, 0, 3] placeholder."""
     result = CreateTriangleVertices.apply(
         grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners, level_sets,
-        vertex_offsets, num_vertices, capacity,
+        vertex_offsets, num_vertices, capacity, deferred,
     )
     return CreateTriangleVerticesResult(*result)
 
@@ -718,6 +821,7 @@ def tessellate_voxels_counted(
     level_sets: Tensor,
     vertex_capacity: int,
     face_capacity: int,
+    defer_sh: bool = False,
 ) -> tuple[Triangles, TessellationCounts]:
     """tessellate_voxels without any device->host read, for CUDA-graph capture.
 
@@ -726,13 +830,20 @@ def tessellate_voxels_counted(
     counts are unused (faces never name them). When a live count exceeds its
     capacity the extra vertices / faces are dropped; callers compare the counts
     with the capacities (see ``meshtryoshka_gb300.graph``).
+
+    ``defer_sh``: ``Triangles.spherical_harmonics`` is a ``DeferredSH`` instead
+    of the [C, V, 3] rows; the render entry points evaluate colours from the
+    grid through it (same values, no rows written or read). Applies when the
+    level sets are at most ``mt_vertex_grad_list_max_shells()``; otherwise the
+    rows are formed as usual.
     """
+    defer = defer_sh and level_sets.shape[0] <= nt.library().mt_vertex_grad_list_max_shells()
     return _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners, upper_corners,
-                       indices, level_sets, (int(vertex_capacity), int(face_capacity)))
+                       indices, level_sets, (int(vertex_capacity), int(face_capacity)), defer)
 
 
 def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners, upper_corners, indices,
-                level_sets, capacity):
+                level_sets, capacity, defer_sh=False):
     (num_level_sets,) = level_sets.shape
     device = nt.require_cuda(signed_distances, lower_corners, level_sets)
     logging.debug(f"Tessellating {neighbors.shape[1]} voxels with {num_level_sets} level sets.")
@@ -755,10 +866,13 @@ def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lowe
             num_vertices, num_faces = capacity
             counts = TessellationCounts(vertex_offsets[-1], torch.empty((), dtype=torch.int32, device=device))
 
+    deferred = DeferredSH(spherical_harmonics) if defer_sh else None
     triangle_vertices, triangle_sdf, triangle_sh, triangle_types = create_triangle_vertices(
         vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets,
-        num_vertices if capacity is None else None, None if capacity is None else num_vertices,
+        num_vertices if capacity is None else None, None if capacity is None else num_vertices, deferred,
     )
+    if deferred is not None:
+        triangle_sh = deferred
 
     with torch.no_grad():
         faces, voxel_indices = create_triangle_faces(

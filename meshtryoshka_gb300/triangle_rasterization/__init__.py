@@ -476,6 +476,11 @@ class EvaluateSphericalHarmonics(torch.autograd.Function):
 
 def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, extrinsics: Tensor,
                                  sh_degree: int) -> Tensor:
+    """``spherical_harmonics``: the [C, V, 3] rows, or (not in the reference)
+    a deferred-SH object of the tessellation (``triangle_extraction.DeferredSH``)
+    whose ``evaluate`` gives the same colours from the grid coefficients."""
+    if not isinstance(spherical_harmonics, Tensor) and hasattr(spherical_harmonics, "evaluate"):
+        return spherical_harmonics.evaluate(vertices, extrinsics, sh_degree)
     return EvaluateSphericalHarmonics.apply(vertices, spherical_harmonics, extrinsics, sh_degree)
 
 

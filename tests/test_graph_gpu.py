@@ -18,6 +18,7 @@ import torch
 
 from meshtryoshka_gb300 import graph, pipeline
 from meshtryoshka_gb300 import triangle_extraction as te
+from meshtryoshka_gb300 import triangle_rasterization as tr
 
 pytestmark = pytest.mark.gpu
 
@@ -132,3 +133,40 @@ def test_captured_step_input_sets_read_their_own_inputs(cuda_device):
     assert abs(loss1 - loss_e1) <= LOSS_RTOL * abs(loss_e1)
     _close(step.grad_sdf, gsdf_e1)
     _close(step.grad_sh, gsh_e1)
+
+
+@pytest.mark.parametrize("config", ["small", "mid"])
+def test_deferred_sh_matches_rows_bit_for_bit(cuda_device, config):
+    """Colours from the grid SH (no per-vertex rows) equal the rows path, and
+    so do the grid gradients: SH through the colours, signed distances and
+    positions through the shared contribution list."""
+    w = pipeline.build_workload(config, cuda_device)
+    args = (w.voxels.vertices, None, w.voxels.neighbors, w.voxels.lower_corners, w.voxels.upper_corners,
+            w.voxels.indices, w.level_sets)
+    with torch.no_grad():
+        _, stats = pipeline.forward(w)
+    caps = pipeline.Capacities.around(stats)
+    out = {}
+    for defer in (False, True):
+        gsdf = w.grid_sdf.detach().clone().requires_grad_(True)
+        gsh = w.grid_sh.detach().clone().requires_grad_(True)
+        a = list(args)
+        a[1] = gsh
+        tri, counts = te.tessellate_voxels_counted(gsdf, *a, caps.vertices, caps.faces, defer_sh=defer)
+        assert isinstance(tri.spherical_harmonics, te.DeferredSH) == defer
+        n = int(counts.num_vertices)
+        verts = pipeline.uncontract_stand_in(tri.vertices.detach())
+        colors = tr.evaluate_spherical_harmonics(verts, tri.spherical_harmonics, w.extrinsics, w.sh_degree)
+        gen = torch.Generator(device=cuda_device).manual_seed(5)
+        dcol = torch.randn(colors.shape, generator=gen, device=cuda_device)
+        dcol[:, n:] = 0
+        dsdf = torch.randn(tri.signed_distances.shape, generator=gen, device=cuda_device)
+        dpos = torch.randn(tri.vertices.shape, generator=gen, device=cuda_device)
+        dsdf[n:] = 0
+        dpos[n:] = 0
+        (g_sh,) = torch.autograd.grad(colors, gsh, dcol, retain_graph=True)
+        g_sdf, = torch.autograd.grad((tri.signed_distances * dsdf).sum() + (tri.vertices * dpos).sum(), gsdf)
+        out[defer] = (colors[:, :n].clone(), g_sh, g_sdf)
+    for got, want in zip(out[True], out[False]):
+        torch.testing.assert_close(got, want, rtol=0, atol=0)
+    assert float(out[True][1].abs().max()) > 0
