@@ -551,7 +551,16 @@ MT_API int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, i
  * loss_scale x sum over pixels and channels of
  * (clip(rgb + T * background, 0, 1) - target)^2, and the backward takes
  * d L / d loss from the device scalar grad_loss instead of grad_out.
+ * hit_bits (not in the reference; NULL = off): uint32 scratch of
+ * mt_composite_hit_bits_words(camera_tiles, tile_h, tile_w) words. The
+ * forward stores there, for the first batches of triangles each warp walks,
+ * the bits of the triangles each pixel hits; a backward on the same inputs
+ * given the same buffer reads them instead of testing those batches again
+ * (same bits, same gradients). camera_tiles: the total tiles over cameras
+ * (B * rows * cols for a uniform grid).
  * ---------------------------------------------------------------------- */
+MT_API int64_t mt_composite_hit_bits_words(int64_t camera_tiles, int32_t tile_h, int32_t tile_w);
+
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
     const int32_t* faces, const float* sharpness, const int64_t* sorted_keys,
@@ -560,7 +569,8 @@ MT_API int mt_intersect_and_composite_forward(
     int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H, int32_t W,
     const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
     uint32_t* warp_masks, uint64_t* work_counter, float* out, const float* target,
-    const float* background, float loss_scale, float* loss_sum, mt_stream_t stream);
+    const float* background, float loss_scale, float* loss_sum, uint32_t* hit_bits,
+    mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
@@ -577,7 +587,8 @@ MT_API int mt_intersect_and_composite_backward(
     uint64_t* work_counter, const float* out, const float* grad_out,
     const float* target, const float* background, float loss_scale,
     const float* grad_loss, float* grad_colors, float* grad_signed_distances,
-    float* grad_sharpness, int32_t exact_adjoint, mt_stream_t stream);
+    float* grad_sharpness, int32_t exact_adjoint, const uint32_t* hit_bits,
+    mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Explicit mode (triangle_rasterization/__init__.py:22-164).

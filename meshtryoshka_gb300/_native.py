@@ -95,12 +95,13 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_intersect_and_composite_forward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
-         c_float, P, P],
+         c_float, P, P, P],
     ),
+    "mt_composite_hit_bits_words": (I64, [I64, I32, I32]),
     "mt_intersect_and_composite_backward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P,
-         c_float, P, P, P, P, I32, P],
+         c_float, P, P, P, P, I32, P, P],
     ),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),

@@ -47,6 +47,10 @@ constexpr int kQueue = 64;   // queued key offsets per warp
 constexpr int kRing = 64;    // gradient slots per warp (two batches)
 constexpr int kSavedFwd = 4;  // hits per lane per batch whose (u, v, w) the test phase keeps (forward)
 constexpr int kSavedBwd = 3;  // same, backward (its shared memory is tighter)
+// Batches per work item whose per-lane hit bits the forward stores for the
+// backward (which then skips their test phase); later batches are tested
+// again.
+constexpr int kHitBatches = 8;
 
 // The (u, v, w) of the first K hits each lane finds in a batch, so that the
 // hit phase does not solve them again (later hits are re-solved).
@@ -369,7 +373,8 @@ __device__ __forceinline__ const float* target_of(const CompositeArgs& a, const 
 
 // Returns the pixel's sum of squared errors when the epilogue is on.
 __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
-                                              float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane) {
+                                              float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane,
+                                              int64_t item, uint32_t* __restrict__ hit_bits) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -384,6 +389,7 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   const int64_t end = a.bounds[2 * ((int64_t)px.cam * T + px.tile) + 1];
   int64_t next = start;
   int queued = 0;
+  int batch = 0;
   while (__any_sync(0xffffffffu, active)) {
     queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
     const int nb = min(queued, kBatch);
@@ -391,8 +397,10 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
     if (lane < nb) gather(a, px.cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
+    uint32_t hits = active ? batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane) : 0u;
+    if (hit_bits && batch < kHitBatches) __stcs(hit_bits + (item * kHitBatches + batch) * 32 + lane, hits);
+    ++batch;
     if (active) {
-      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
       int n = 0;
       while (hits) {
         const int i = __ffs(hits) - 1;
@@ -444,16 +452,17 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   return sq;
 }
 
-__global__ void __launch_bounds__(kCtaThreads)
+__global__ void __launch_bounds__(kCtaThreads, 4)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
-                             unsigned long long* __restrict__ counter, float* __restrict__ loss_sum) {
+                             unsigned long long* __restrict__ counter, float* __restrict__ loss_sum,
+                             uint32_t* __restrict__ hit_bits) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   float sq = 0.0f;
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane);
+    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hit_bits);
   if (a.target) {  // one atomic per warp for the whole launch
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
@@ -510,7 +519,8 @@ __device__ __forceinline__ void flush_half(const CompositeArgs& a, const Composi
 }
 
 __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
-                                              const CompositeGrads& gr, WarpBackward& ws, const Pixel& px, int lane) {
+                                              const CompositeGrads& gr, WarpBackward& ws, const Pixel& px, int lane,
+                                              int64_t item, const uint32_t* __restrict__ hit_bits) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -575,8 +585,15 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
     if (lane < nb) ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
+    // The forward's hit bits for this batch when it stored them (the same
+    // walk, so the same bits); otherwise the test phase runs again.
+    const bool stored = hit_bits != nullptr && batch < kHitBatches;
+    uint32_t hits = 0;
+    if (stored)
+      hits = __ldcs(hit_bits + (item * kHitBatches + batch) * 32 + lane);
+    else if (active)
+      hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
     if (active) {
-      uint32_t hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
       int n = 0;
       while (hits) {
         const int i = __ffs(hits) - 1;
@@ -585,7 +602,10 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
-        hit_weights(ws.saved, k, lane, g, px.fx, px.fy, u, v, w);
+        if (stored)
+          hit_test(g, px.fx, px.fy, u, v, w);  // a hit: the solve gives the forward's (u, v, w)
+        else
+          hit_weights(ws.saved, k, lane, g, px.fx, px.fy, u, v, w);
         const TriAttr& t = ws.attr[i];
         const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
         float e_in;
@@ -674,13 +694,13 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
 
 __global__ void __launch_bounds__(kCtaThreads)
     composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr,
-                              unsigned long long* __restrict__ counter) {
+                              unsigned long long* __restrict__ counter, const uint32_t* __restrict__ hit_bits) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    backward_item(a, masks, gr, ws, pixel_of(a, item), lane);
+    backward_item(a, masks, gr, ws, pixel_of(a, item), lane, item, hit_bits);
 }
 
 int check_args(const CompositeArgs& a) {
@@ -762,6 +782,11 @@ using namespace mt;
 
 extern "C" {
 
+int64_t mt_composite_hit_bits_words(int64_t camera_tiles, int32_t tile_h, int32_t tile_w) {
+  if (camera_tiles <= 0 || tile_h <= 0 || tile_w <= 0) return 0;
+  return camera_tiles * (((int64_t)tile_h * tile_w + 31) / 32) * kHitBatches * 32;
+}
+
 int mt_intersect_and_composite_forward(const float* xy, const float* colors, const float* signed_distances,
                                        int64_t V, const int32_t* faces, const float* sharpness,
                                        const int64_t* sorted_keys, const int32_t* sorted_triangles, int64_t K,
@@ -771,7 +796,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
                                        uint64_t* work_counter, float* out, const float* target,
                                        const float* background, float loss_scale, float* loss_sum,
-                                       mt_stream_t stream) {
+                                       uint32_t* hit_bits, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
@@ -799,7 +824,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   composite_forward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum);
+      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hit_bits);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -814,7 +839,7 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         const float* out, const float* grad_out, const float* target,
                                         const float* background, float loss_scale, const float* grad_loss,
                                         float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
-                                        int32_t exact_adjoint, mt_stream_t stream) {
+                                        int32_t exact_adjoint, const uint32_t* hit_bits, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out,
@@ -839,7 +864,7 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   composite_backward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter));
+      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hit_bits);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

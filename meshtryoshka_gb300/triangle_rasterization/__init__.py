@@ -487,6 +487,15 @@ def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, 
 # ---------------------------------------------------------------------------
 # Fused compositing (intersect_and_composite.py:24-175)
 # ---------------------------------------------------------------------------
+def _hit_bits(ctx, grid: TileGrid, device) -> Tensor | None:
+    """Scratch for the hit bits the forward stores for its backward (only
+    when a gradient will be asked for)."""
+    if not any(ctx.needs_input_grad):
+        return None
+    words = nt.library().mt_composite_hit_bits_words(grid.camera_tiles, grid.tile_shape[0], grid.tile_shape[1])
+    return torch.empty((max(int(words), 1),), dtype=torch.int32, device=device)
+
+
 class IntersectAndComposite(torch.autograd.Function):
     @staticmethod
     def forward(ctx, vertices, colors, signed_distances, faces, sharpness, sorted_keys, sorted_triangle_indices,
@@ -507,11 +516,13 @@ class IntersectAndComposite(torch.autograd.Function):
             # Uniform cameras: [B, 4, H, W]; ragged: every camera's [4, h, w] back to back.
             out = torch.empty((grid.output_numel,) if grid.ragged else (b, 4, h, w), dtype=torch.float32,
                               device=device)
+            hits = _hit_bits(ctx, grid, device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
-                    0.0, None, nt.stream(device))
+                    0.0, None, nt.ptr(hits), nt.stream(device))
+            ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness))
@@ -536,7 +547,7 @@ class IntersectAndComposite(torch.autograd.Function):
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, nt.ptr(grad_colors), nt.ptr(grad_sdf),
-                    nt.ptr(grad_sharp), int(mode == "exact"), nt.stream(device))
+                    nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
 
@@ -571,11 +582,13 @@ class IntersectCompositeLoss(torch.autograd.Function):
                               device=device)
             loss = torch.empty((), dtype=torch.float32, device=device)
             scale = 1.0 / target.numel()
+            hits = _hit_bits(ctx, grid, device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), nt.ptr(target),
-                    nt.ptr(background), scale, loss.data_ptr(), nt.stream(device))
+                    nt.ptr(background), scale, loss.data_ptr(), nt.ptr(hits), nt.stream(device))
+            ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness), scale)
@@ -601,7 +614,7 @@ class IntersectCompositeLoss(torch.autograd.Function):
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(),
                     nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp), int(mode == "exact"),
-                    nt.stream(device))
+                    nt.ptr(ctx.hits), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None, None, None)
 

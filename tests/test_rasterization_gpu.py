@@ -538,3 +538,34 @@ def test_bound_and_generate_keys_matches_three_stage_chain(cuda_device, b, f, ra
         np.testing.assert_array_equal(_n(got.keys)[:m], _n(want.keys)[:m])
         np.testing.assert_array_equal(_n(got.triangle_indices)[:m], _n(want.triangle_indices)[:m])
     assert nt.workspace(torch.device(d)).status() == 0
+
+
+@pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside"])
+def test_backward_with_and_without_stored_hit_bits(cuda_device, name, monkeypatch):
+    """The backward reads the forward's hit bits for a warp's first batches;
+    without them it tests those batches again. Both give the same gradients
+    (up to the order of the compositing atomics)."""
+    d = cuda_device
+    scene = make_scene(**SCENES[name])
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
+    colors_np = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
+    b, s, t = grid.num_cameras, grid.num_shells, grid.num_tiles_per_image
+    g = None
+    grads = []
+    for stored in (True, False):
+        if not stored:
+            monkeypatch.setattr(tr, "_hit_bits", lambda ctx, grid, device: None)
+        colors = _t(colors_np, d).requires_grad_(True)
+        sdf = _t(scene.sdf, d).requires_grad_(True)
+        sharp = torch.tensor(scene.sharpness, device=d).requires_grad_(True)
+        out = tr.intersect_and_composite(xy, colors, sdf, _t(scene.faces, d), sharp, sorted_.keys,
+                                         sorted_.triangle_indices, tb.view(b, t, 2), s, grid, kd)
+        if g is None:
+            g = _t(np.random.default_rng(2).normal(0, 1, tuple(out.shape)).astype(np.float32), d)
+        out.backward(g)
+        grads.append((_n(colors.grad), _n(sdf.grad), float(sharp.grad)))
+    (c1, s1, h1), (c0, s0, h0) = grads
+    _close_grad(c1, c0, 1e-5)
+    _close_grad(s1, s0, 1e-5)
+    assert abs(h1 - h0) <= 1e-5 * max(abs(h0), 1e-12)
+    assert np.abs(c0).max() > 0
