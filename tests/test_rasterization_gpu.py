@@ -540,13 +540,28 @@ def test_bound_and_generate_keys_matches_three_stage_chain(cuda_device, b, f, ra
     assert nt.workspace(torch.device(d)).status() == 0
 
 
-@pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside"])
+# A whole 8-shell sphere in a few tiles: warps walk far more than the 8
+# batches whose hit bits the forward stores, so the backward mixes stored
+# and re-tested batches.
+DENSE = dict(cameras=((0.0, 0.0, 5.0),), image_shape=(40, 48), fov=20.0,
+             levels=tuple(float(x) for x in np.linspace(0.03, -0.03, 8)), sh_degree=1)
+
+
+def test_fused_backward_past_the_stored_batches(cuda_device):
+    scene = make_scene(**DENSE)
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, cuda_device)
+    counts = _n(tb)[..., 1] - _n(tb)[..., 0]
+    assert counts.max() > 8 * 32 * 4  # tiles far longer than the stored batches
+    _check_fused_backward(scene, cuda_device, "reference", (16, 16))
+
+
+@pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside", "dense"])
 def test_backward_with_and_without_stored_hit_bits(cuda_device, name, monkeypatch):
     """The backward reads the forward's hit bits for a warp's first batches;
     without them it tests those batches again. Both give the same gradients
     (up to the order of the compositing atomics)."""
     d = cuda_device
-    scene = make_scene(**SCENES[name])
+    scene = make_scene(**(DENSE if name == "dense" else SCENES[name]))
     grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
     colors_np = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
     b, s, t = grid.num_cameras, grid.num_shells, grid.num_tiles_per_image
