@@ -582,17 +582,18 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
     const int half = batch & 1;
     // The half being overwritten held batch - 2: flush it first.
     if (batch >= 2) flush_half(a, gr, cam, ws, half, lane);
-    if (lane < nb) ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
+    // The forward's hit bits for this batch when it stored them (the same
+    // walk, so the same bits); otherwise the test phase runs again. With
+    // stored bits only the triangles that some pixel of the warp hits are
+    // gathered (the other slots are never read).
+    const bool stored = hit_bits != nullptr && batch < kHitBatches;
+    uint32_t hits = stored ? __ldcs(hit_bits + (item * kHitBatches + batch) * 32 + lane) : 0u;
+    const uint32_t needed = stored ? __reduce_or_sync(0xffffffffu, hits) : 0xffffffffu;
+    if (lane < nb && ((needed >> lane) & 1u))
+      ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
-    // The forward's hit bits for this batch when it stored them (the same
-    // walk, so the same bits); otherwise the test phase runs again.
-    const bool stored = hit_bits != nullptr && batch < kHitBatches;
-    uint32_t hits = 0;
-    if (stored)
-      hits = __ldcs(hit_bits + (item * kHitBatches + batch) * 32 + lane);
-    else if (active)
-      hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
+    if (!stored && active) hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
     if (active) {
       int n = 0;
       while (hits) {
