@@ -153,6 +153,50 @@ __device__ __forceinline__ void warp_block_rect(int w, int tile_w, int tile_h, i
   y1 = (float)(ty * tile_h + ly1) + 0.5f;
 }
 
+// Exact block exclusion by the barycentric numerators. hit_test computes
+// each numerator N(p) = A (q . eX) - C (q . eY), q = p - P, in single
+// precision and rejects p when N(p) < thr. The exact value is affine in p,
+// N(p) = a qx + b qy with a = A eXx - C eYx, b = A eXy - C eYy, and the
+// single-precision evaluation errs by at most 5 u S(p), u = 2^-24, with
+// S(p) = |qx| sx + |qy| sy, sx = |A eXx| + |C eYx|, sy = |A eXy| + |C eYy|.
+// Over the rectangle of pixel centres [x0, x1] x [y0, y1] the affine part and
+// S are largest at corners and separate in x and y, so with E = 32 u (room
+// for the rounding of a, b, sx, sy and of this evaluation, at most 10 u S):
+//   max_x (a qx + E sx |qx|) + max_y (b qy + E sy |qy|) + E max S < thr
+// means every pixel centre of the rectangle is rejected by hit_test.
+// Non-finite values compare false: no exclusion.
+struct EdgeBound {
+  float a, b, sx, sy, px, py;
+};
+
+__device__ __forceinline__ EdgeBound edge_bound(float A, float C, float Px, float Py, float eXx, float eXy,
+                                                float eYx, float eYy) {
+  return EdgeBound{A * eXx - C * eYx, A * eXy - C * eYy, fabsf(A * eXx) + fabsf(C * eYx),
+                   fabsf(A * eXy) + fabsf(C * eYy), Px, Py};
+}
+
+__device__ __forceinline__ bool edge_excludes(const EdgeBound& e, float thr, float x0, float x1, float y0,
+                                              float y1) {
+  constexpr float kErr = 0x1p-19f;  // 32 u
+  const float qx0 = x0 - e.px, qx1 = x1 - e.px, qy0 = y0 - e.py, qy1 = y1 - e.py;
+  const float tx = fmaxf(e.a * qx0 + kErr * e.sx * fabsf(qx0), e.a * qx1 + kErr * e.sx * fabsf(qx1));
+  const float ty = fmaxf(e.b * qy0 + kErr * e.sy * fabsf(qy0), e.b * qy1 + kErr * e.sy * fabsf(qy1));
+  const float bm = kErr * (e.sx * fmaxf(fabsf(qx0), fabsf(qx1)) + e.sy * fmaxf(fabsf(qy0), fabsf(qy1)));
+  return tx + ty + bm < thr;
+}
+
+// The three numerator bounds of a staged triangle (vn and wn from corner 1,
+// un from corner 2, as hit_test forms them).
+struct TriangleBounds3 {
+  EdgeBound v, w, u;
+};
+
+__device__ __forceinline__ TriangleBounds3 triangle_bounds(const TriGeom& g) {
+  return TriangleBounds3{edge_bound(g.d1313, g.d1213, g.p1x, g.p1y, g.e12x, g.e12y, g.e13x, g.e13y),
+                         edge_bound(g.d1212, g.d1213, g.p1x, g.p1y, g.e13x, g.e13y, g.e12x, g.e12y),
+                         edge_bound(g.d1223, g.d1323, g.p2x, g.p2y, g.e13x, g.e13y, g.e12x, g.e12y)};
+}
+
 // One mask per sorted key: bit w = warp w of the key's tile may be covered.
 // Keys past num_keys (a device value; all K when NULL) get no mask: no tile
 // range reaches them.
@@ -176,10 +220,18 @@ __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int6
       setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
       const CullBox box = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
       const int tx = tile % cols_b, ty = tile / cols_b;
+      // Exclusion needs the fast reject, finite coordinates and a
+      // well-conditioned triangle: exactly the triangles with a finite box.
+      const bool exact_cull = box.x0 > -__int_as_float(0x7f800000);
+      const TriangleBounds3 tb = triangle_bounds(g);
       for (int w = 0; w < warps; ++w) {
         float x0, x1, y0, y1;
         warp_block_rect(w, a.tile_w, a.tile_h, tx, ty, x0, x1, y0, y1);
-        if (box_overlaps(box, x0, x1, y0, y1)) m |= 1u << w;
+        if (!box_overlaps(box, x0, x1, y0, y1)) continue;
+        if (exact_cull && (edge_excludes(tb.v, g.thr, x0, x1, y0, y1) || edge_excludes(tb.w, g.thr, x0, x1, y0, y1) ||
+                           edge_excludes(tb.u, g.thr, x0, x1, y0, y1)))
+          continue;
+        m |= 1u << w;
       }
     }
     masks[k] = m;
