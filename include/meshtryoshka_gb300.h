@@ -305,18 +305,23 @@ MT_API int mt_grid_sh_colors(const float* grid_spherical_harmonics, int32_t C, i
                              int32_t B, float* out_colors, mt_stream_t stream);
 
 /* Backward of mt_grid_sh_colors: grad_grid_sh [C,G,3] (every entry written)
- * from grad_colors [B,V,3] through the list of mt_build_vertex_grad_list;
- * the per-vertex SH gradient of
- * mt_evaluate_spherical_harmonics_backward is formed on the fly, so the
- * result equals that call followed by mt_create_triangle_vertices_backward
- * bit for bit. */
+ * from grad_colors [B,V,3] through the list of mt_build_vertex_grad_list.
+ * The per-vertex SH gradient of mt_evaluate_spherical_harmonics_backward is
+ * formed once per vertex into workspace (at least
+ * mt_grid_sh_colors_backward_workspace_bytes(V) bytes, 16-byte aligned) and
+ * summed per grid vertex, or, with workspace NULL, on the fly per list
+ * entry; either way the result equals that call followed by
+ * mt_create_triangle_vertices_backward bit for bit. num_vertices: NULL or the
+ * device live vertex count. */
+MT_API size_t mt_grid_sh_colors_backward_workspace_bytes(int64_t V);
 MT_API int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list,
                                       int64_t G, int64_t V, const float* vertices,
                                       int32_t C, int32_t sh_degree,
                                       const float* camera_positions, int32_t B,
                                       const float* out_colors, const float* grad_colors,
                                       float* grad_grid_spherical_harmonics,
-                                      mt_stream_t stream);
+                                      const int32_t* num_vertices, void* workspace,
+                                      size_t workspace_bytes, mt_stream_t stream);
 
 /* triangle_extraction/compute_sdf_regularizers.slang:18-128 (forward) and its
  * automatic derivative (backward). Per voxel: eikonal_loss_pos / _neg [Nv]

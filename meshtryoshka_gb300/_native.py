@@ -73,7 +73,8 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_build_vertex_grad_list": (I32, [P, P, I64, P, I32, P, I64, P, P, P, P, c_size_t, P]),
     "mt_vertex_grads_from_list": (I32, [P, P, I64, P, P, P, P, P]),
     "mt_grid_sh_colors": (I32, [P, I32, I64, P, I64, P, P, I32, P, I32, P, P]),
-    "mt_grid_sh_colors_backward": (I32, [P, P, I64, I64, P, I32, I32, P, I32, P, P, P, P]),
+    "mt_grid_sh_colors_backward_workspace_bytes": (c_size_t, [I64]),
+    "mt_grid_sh_colors_backward": (I32, [P, P, I64, I64, P, I32, I32, P, I32, P, P, P, P, P, c_size_t, P]),
     "mt_capacity_overflow": (I32, [P, I64, P, I64, P, I64, P, P]),
     "mt_sort_pairs_workspace_bytes": (c_size_t, [I64]),
     "mt_sort_pairs_i64_i32": (I32, [P, P, P, P, I64, P, I32, I32, P, c_size_t, P]),
@@ -150,7 +151,8 @@ KERNELS_PER_CALL = {
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
     "mt_sort_keys_by_tile": 6,
     "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys
-    "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
+    "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill
+    "mt_grid_sh_colors_backward": 2,  # per-vertex SH gradients, per-grid-vertex sums  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
 }
 
 

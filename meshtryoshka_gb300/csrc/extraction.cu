@@ -840,6 +840,98 @@ __global__ void __launch_bounds__(kShThreads)
   }
 }
 
+// Two-pass form of the same backward (with scratch): pass 1, one thread per
+// live vertex v, forms d sh_v (cameras in order, as sh_backward_kernel) once
+// into a vertex-major array [V][16][3]; pass 2, one thread per (8-row half h,
+// grid vertex x), sums x's list entries of rows 8h .. 8h + 7 (96 contiguous
+// bytes per entry) weighted, in list order. The same bits as the one-pass
+// kernel, with each vertex's gradient formed once instead of once per entry.
+__global__ void vertex_sh_grad_kernel(const float* __restrict__ verts, int64_t V, const int32_t* __restrict__ count,
+                                      int n_coeff, const float* __restrict__ campos, int B,
+                                      const float* __restrict__ colors, const float* __restrict__ dcolors,
+                                      float4* __restrict__ out) {
+  const int64_t n = count ? min((int64_t)max(*count, 0), V) : V;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const float px = __ldg(verts + 3 * v), py = __ldg(verts + 3 * v + 1), pz = __ldg(verts + 3 * v + 2);
+    float d[16][3];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
+    for (int b = 0; b < B; ++b) {
+      const int64_t ob = ((int64_t)b * V + v) * 3;
+      float col[3], dcol[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        col[c] = __ldg(colors + ob + c);
+        dcol[c] = __ldg(dcolors + ob + c);
+      }
+      float g[3];
+      bool any = false;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        g[c] = col[c] > 0.0f ? dcol[c] : 0.0f;
+        any |= g[c] != 0.0f;
+      }
+      if (!any) continue;
+      float dx, dy, dz;
+      view_dir_at(px, py, pz, campos + 3 * b, dx, dy, dz);
+      float basis[16];
+      sh_basis(dx, dy, dz, n_coeff, basis);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k < n_coeff) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+        }
+      }
+    }
+    float4* o = out + v * 12;
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      const int j = 4 * q;
+      o[q] = make_float4(d[j / 3][j % 3], d[(j + 1) / 3][(j + 1) % 3], d[(j + 2) / 3][(j + 2) % 3],
+                         d[(j + 3) / 3][(j + 3) % 3]);
+    }
+  }
+}
+
+__global__ void grid_sh_gather_kernel(const int32_t* __restrict__ offsets, const int2* __restrict__ list, int64_t G,
+                                      const float4* __restrict__ dsh, int C, int n_coeff,
+                                      float* __restrict__ gdsh) {
+  const int64_t total = 2 * G;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
+    const int half = (int)(o / G);
+    const int64_t x = o - (int64_t)half * G;
+    float acc[24];
+#pragma unroll
+    for (int j = 0; j < 24; ++j) acc[j] = 0.f;
+    const int32_t end = __ldg(offsets + x + 1);
+    for (int32_t q = __ldg(offsets + x); q < end; ++q) {
+      const int2 e = __ldg(list + q);
+      const int64_t vi = e.x & 0x7fffffff;
+      const bool origin = e.x < 0;
+      const float t = __int_as_float(e.y);
+      const float4* src = dsh + vi * 12 + 6 * half;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const float4 val = __ldg(src + r);
+        acc[4 * r + 0] += weighted(val.x, t, origin);
+        acc[4 * r + 1] += weighted(val.y, t, origin);
+        acc[4 * r + 2] += weighted(val.z, t, origin);
+        acc[4 * r + 3] += weighted(val.w, t, origin);
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      const int k = 8 * half + kk;
+      if (k < C) {
+        float* dst = gdsh + ((int64_t)k * G + x) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dst[c] = k < n_coeff ? acc[3 * kk + c] : 0.f;
+      }
+    }
+  }
+}
+
 size_t vertex_grad_bytes(int64_t G, int64_t V, int32_t** counts, int2** list, void** scan_ws, size_t* scan_bytes,
                          char* base) {
   size_t off = 256;  // the workspace status word
@@ -1457,10 +1549,15 @@ int mt_grid_sh_colors(const float* grid_spherical_harmonics, int32_t C, int64_t 
   return MT_OK;
 }
 
+size_t mt_grid_sh_colors_backward_workspace_bytes(int64_t V) {
+  return 256 + (size_t)(V > 0 ? V : 0) * 48 * sizeof(float);
+}
+
 int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list, int64_t G, int64_t V,
                                const float* vertices, int32_t C, int32_t sh_degree, const float* camera_positions,
                                int32_t B, const float* out_colors, const float* grad_colors,
-                               float* grad_grid_spherical_harmonics, mt_stream_t stream) {
+                               float* grad_grid_spherical_harmonics, const int32_t* num_vertices, void* workspace,
+                               size_t workspace_bytes, mt_stream_t stream) {
   MT_REQUIRE(G >= 0 && V >= 0 && B >= 0 && sh_degree >= 0 && sh_degree <= 3);
   const int n = (sh_degree + 1) * (sh_degree + 1);
   MT_REQUIRE(C >= n);
@@ -1473,6 +1570,17 @@ int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list,
   if (C > 16 && cudaMemsetAsync(grad_grid_spherical_harmonics + (size_t)16 * G * 3, 0,
                                 (size_t)(C - 16) * G * 3 * sizeof(float), st) != cudaSuccess)
     return MT_ERR_CUDA;  // rows past degree 3's sixteen are zeros
+  if (workspace && workspace_bytes >= mt_grid_sh_colors_backward_workspace_bytes(V) && Bn > 0) {
+    float4* dsh = reinterpret_cast<float4*>(static_cast<char*>(workspace) + 256);
+    MT_REQUIRE((reinterpret_cast<uintptr_t>(dsh) & 15) == 0);
+    vertex_sh_grad_kernel<<<grid_stride_blocks(V, 128), 128, 0, st>>>(vertices, V, num_vertices, n, camera_positions,
+                                                                      Bn, out_colors, grad_colors, dsh);
+    MT_CHECK_LAUNCH();
+    grid_sh_gather_kernel<<<grid_stride_blocks(2 * G, 256), 256, 0, st>>>(
+        list_offsets, reinterpret_cast<const int2*>(list), G, dsh, C, n, grad_grid_spherical_harmonics);
+    MT_CHECK_LAUNCH();
+    return MT_OK;
+  }
   const int64_t xblocks = (G + kShX - 1) / kShX;
   grid_sh_colors_backward_kernel<<<(unsigned)min(xblocks, (int64_t)152 * 32), kShThreads, 0, st>>>(
       list_offsets, reinterpret_cast<const int2*>(list), G, V, vertices, C, n, camera_positions, Bn, out_colors,

@@ -500,9 +500,12 @@ class GridSHColors(torch.autograd.Function):
             c, g, _ = ctx.gsh_shape
             device = vertices.device
             grad_gsh = torch.empty(ctx.gsh_shape, dtype=torch.float32, device=device)  # fully written
-            nt.call("mt_grid_sh_colors_backward", nt.ptr(d.list_offsets), nt.ptr(d.contributions), g,
-                    vertices.shape[0], nt.ptr(vertices), c, ctx.sh_degree, nt.ptr(campos), campos.shape[0],
-                    nt.ptr(colors), nt.ptr(grad_colors.contiguous()), nt.ptr(grad_gsh), nt.stream(device))
+            v = vertices.shape[0]
+            ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_grid_sh_colors_backward_workspace_bytes(v))
+            nt.call("mt_grid_sh_colors_backward", nt.ptr(d.list_offsets), nt.ptr(d.contributions), g, v,
+                    nt.ptr(vertices), c, ctx.sh_degree, nt.ptr(campos), campos.shape[0], nt.ptr(colors),
+                    nt.ptr(grad_colors.contiguous()), nt.ptr(grad_gsh), nt.ptr(d.num_vertices), ws_ptr, ws_bytes,
+                    nt.stream(device))
             return grad_gsh, None, None, None, None
 
 
