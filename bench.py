@@ -337,17 +337,18 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(statistics.mean(step_ms), world)
     launches_per_step = step.launches_per_replay
 
-    # End to end through the public API: every step copies its parameters,
-    # target and cameras from pinned host memory into the inputs the step
+    # End to end through the public API: every step copies its batch (target
+    # images and cameras) from pinned host memory into the inputs the step
     # reads, replays the step and reads its loss back, as a training loop
-    # with an input pipeline does. The step holds two input sets (one graph
-    # each, both reading their set in place): the copy of step i + 1's inputs
-    # into one set (on a copy stream, once that set's previous replay is
-    # done) overlaps step i's replay on the other; the compute stream waits
-    # for the copy, flushes L2 and replays; each step's loss is read on the
-    # host one step later. The wall clock runs from the first copy to the
-    # last loss read.
-    host = {k: v.detach().cpu().pin_memory() for k, v in step.inputs[0].items()}
+    # with an input pipeline does (the parameters stay resident on the
+    # device, where an optimizer updates them in place). The step holds two
+    # input sets (one graph each, both reading their set in place): the copy
+    # of step i + 1's batch into one set (on a copy stream, once that set's
+    # previous replay is done) overlaps step i's replay on the other; the
+    # compute stream waits for the copy, flushes L2 and replays; each step's
+    # loss is read on the host one step later. The wall clock runs from the
+    # first copy to the last loss read.
+    host = {k: step.inputs[0][k].detach().cpu().pin_memory() for k in graph.DATA}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     copy_stream = torch.cuda.Stream(device)
     copied = [torch.cuda.Event() for _ in range(2)]
@@ -463,10 +464,11 @@ def run_ours(args, rank, world, local):
             "launch_ms": dom_ms,
         },
         "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
-                "form": "per step: pinned-host copy of parameters, target and cameras on a copy stream into "
-                        "one of the step's two input sets (one graph per set, each reading its set in place; "
-                        "the copy overlaps the other set's replay), L2 flush, graph replay, loss read on the "
-                        "host one step later; wall clock over all steps"},
+                "form": "per step: pinned-host copy of the batch (target images and cameras) on a copy stream "
+                        "into one of the step's two input sets (one graph per set, each reading its set in "
+                        "place; parameters resident and shared; the copy overlaps the other set's replay), "
+                        "L2 flush, graph replay, loss read on the host one step later; wall clock over all "
+                        "steps"},
         "clocks": clock_info,
     }
     if not args.no_cameras and world == 1:

@@ -34,20 +34,25 @@ from . import pipeline
 from . import triangle_rasterization as tr
 
 
-# The per-step inputs a graph reads in place.
-INPUTS = ("grid_sdf", "grid_sh", "target", "extrinsics", "intrinsics")
+# The tensors a graph reads in place: the parameters, and the per-step data
+# (the batch a training loop feeds every step).
+PARAMETERS = ("grid_sdf", "grid_sh")
+DATA = ("target", "extrinsics", "intrinsics")
+INPUTS = PARAMETERS + DATA
 
 
 class CapturedTrainingStep:
     """Fused forward + backward of ``pipeline.Workload`` as one CUDA graph.
 
-    ``input_sets`` > 1 captures one graph per set of inputs (``INPUTS``):
-    set 0 is the workload's own tensors, the others are device copies
-    (``self.inputs[i]``), and ``step(i)`` replays the graph that reads set i
-    in place. A host pipeline can then copy the next step's inputs into one
-    set while the other set's graph runs, with no device-side copy between
-    them. Each graph has its own memory pool, so the outputs of one set's
-    replay stay valid across replays of the others."""
+    ``input_sets`` > 1 captures one graph per set of per-step data (``DATA``:
+    target and cameras): set 0 is the workload's own tensors, the others are
+    device copies (``self.inputs[i]``), and ``step(i)`` replays the graph that
+    reads set i in place. The parameters are shared by every set (each graph
+    reads the workload's parameters in place). A host pipeline can then copy
+    the next step's batch into one set while the other set's graph runs, with
+    no device-side copy between them. Each graph has its own memory pool, so
+    the outputs of one set's replay stay valid across replays of the
+    others."""
 
     def __init__(self, workload: pipeline.Workload, gradient_mode: str | None = None, margin: float = 1.25,
                  capacities: pipeline.Capacities | None = None, warmup: int = 2, input_sets: int = 1):
@@ -57,7 +62,8 @@ class CapturedTrainingStep:
         self.warmup = warmup
         self.inputs = [{k: getattr(workload, k) for k in INPUTS}]
         for _ in range(1, max(int(input_sets), 1)):
-            self.inputs.append({k: getattr(workload, k).detach().clone() for k in INPUTS})
+            data = {k: getattr(workload, k).detach().clone() for k in DATA}
+            self.inputs.append({**{k: getattr(workload, k) for k in PARAMETERS}, **data})
         self._views = [dataclasses.replace(workload, **{k: v for k, v in s.items()}) for s in self.inputs]
         if capacities is None:
             capacities = pipeline.Capacities.around(self._measure(), margin)

@@ -108,13 +108,14 @@ def test_captured_step_follows_parameter_updates(cuda_device):
 
 
 def test_captured_step_input_sets_read_their_own_inputs(cuda_device):
-    """With two input sets, each graph reads its own set in place; a replay of
-    one set leaves the other set's outputs as they were."""
+    """With two input sets, each graph reads its own batch in place and the
+    shared parameters; a replay of one set leaves the other set's outputs as
+    they were."""
     w = pipeline.build_workload("small", cuda_device)
     step = graph.CapturedTrainingStep(w, input_sets=2)
     assert len(step.graphs) == 2 and step.launches_per_replay >= 15
+    assert step.inputs[1]["grid_sh"] is w.grid_sh  # parameters are shared
     with torch.no_grad():
-        step.inputs[1]["grid_sh"].mul_(0.5)
         step.inputs[1]["target"].mul_(0.75)
     loss0 = float(step(0))
     g0 = step.grad_sh.clone()
@@ -127,7 +128,6 @@ def test_captured_step_input_sets_read_their_own_inputs(cuda_device):
     assert abs(loss0 - loss_e0) <= LOSS_RTOL * abs(loss_e0)
     _close(g0, gsh_e0)
     with torch.no_grad():
-        w.grid_sh.mul_(0.5)
         w.target.mul_(0.75)
     loss_e1, gsdf_e1, gsh_e1, _ = _eager(w)
     assert abs(loss1 - loss_e1) <= LOSS_RTOL * abs(loss_e1)
