@@ -1,5 +1,6 @@
-// Decoupled look-back (Merrill & Garland, 2016) shared by the single-pass
-// scans (scan.cu) and the fused tile-bound / key kernel (raster_front.cu).
+// Decoupled look-back (Merrill & Garland, 2016) of the single-pass scans
+// (scan.cu), and the warp sums they use (also used by the capacity-mode key
+// kernels of raster_front.cu).
 //
 // Tiles are claimed in launch order through an atomic counter, so every
 // predecessor of a tile has already started when the tile looks back and the
