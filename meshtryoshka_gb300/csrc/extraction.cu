@@ -899,8 +899,10 @@ __global__ void grid_sh_gather_kernel(const int32_t* __restrict__ offsets, const
                                       float* __restrict__ gdsh) {
   const int64_t total = 2 * G;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total; o += (int64_t)gridDim.x * blockDim.x) {
-    const int half = (int)(o / G);
-    const int64_t x = o - (int64_t)half * G;
+    // Adjacent threads take the two halves of one grid vertex, so a vertex's
+    // 192-byte gradient row is read by neighbouring lanes together.
+    const int half = (int)(o & 1);
+    const int64_t x = o >> 1;
     float acc[24];
 #pragma unroll
     for (int j = 0; j < 24; ++j) acc[j] = 0.f;
