@@ -856,31 +856,40 @@ __global__ void vertex_sh_grad_kernel(const float* __restrict__ verts, int64_t V
     float d[16][3];
 #pragma unroll
     for (int k = 0; k < 16; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
-    for (int b = 0; b < B; ++b) {
-      const int64_t ob = ((int64_t)b * V + v) * 3;
-      float col[3], dcol[3];
+    // Cameras two at a time: both cameras' colours and colour gradients are
+    // loaded together, then the cameras are added in order.
+    for (int b0 = 0; b0 < B; b0 += 2) {
+      float col[2][3], dcol[2][3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        col[c] = __ldg(colors + ob + c);
-        dcol[c] = __ldg(dcolors + ob + c);
+      for (int j = 0; j < 2; ++j) {
+        const bool in = b0 + j < B;
+        const int64_t ob = ((int64_t)(b0 + j) * V + v) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          col[j][c] = in ? __ldg(colors + ob + c) : 0.0f;
+          dcol[j][c] = in ? __ldg(dcolors + ob + c) : 0.0f;
+        }
       }
-      float g[3];
-      bool any = false;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        g[c] = col[c] > 0.0f ? dcol[c] : 0.0f;
-        any |= g[c] != 0.0f;
-      }
-      if (!any) continue;
-      float dx, dy, dz;
-      view_dir_at(px, py, pz, campos + 3 * b, dx, dy, dz);
-      float basis[16];
-      sh_basis(dx, dy, dz, n_coeff, basis);
+      for (int j = 0; j < 2; ++j) {
+        float g[3];
+        bool any = false;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        if (k < n_coeff) {
+        for (int c = 0; c < 3; ++c) {
+          g[c] = col[j][c] > 0.0f ? dcol[j][c] : 0.0f;
+          any |= g[c] != 0.0f;
+        }
+        if (!any) continue;  // also every camera past B (its g is zero)
+        float dx, dy, dz;
+        view_dir_at(px, py, pz, campos + 3 * (b0 + j), dx, dy, dz);
+        float basis[16];
+        sh_basis(dx, dy, dz, n_coeff, basis);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+        for (int k = 0; k < 16; ++k) {
+          if (k < n_coeff) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+          }
         }
       }
     }
