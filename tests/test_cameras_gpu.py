@@ -115,9 +115,9 @@ def test_uneven_workload_batched_equals_per_camera(cuda_device):
         w.grid_sh.grad = None
         return out
 
-    loss_plain = float(pipeline.per_camera_training_step(w))
+    loss_plain = float(pipeline.per_camera_training_step(w).detach())
     g_plain = grads()
-    loss_batched = float(pipeline.training_step(w))
+    loss_batched = float(pipeline.training_step(w).detach())
     g_batched = grads()
     # The loss is a float32 sum of ~3e7 squared errors, accumulated by
     # per-warp atomics in scheduling order: the two forms agree to the

@@ -91,7 +91,7 @@ def test_training_step_fused_loss_equals_unfused(cuda_device, config):
     results = []
     for fused in (False, True):
         w.fused_loss = fused
-        loss = float(pipeline.training_step(w))
+        loss = float(pipeline.training_step(w).detach())
         results.append((loss, w.grid_sdf.grad.clone(), w.grid_sh.grad.clone()))
         w.grid_sdf.grad = None
         w.grid_sh.grad = None
