@@ -521,7 +521,7 @@ def run_cameras(device, steps):
     with torch.no_grad():
         tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors,
                                    w.voxels.lower_corners, w.voxels.upper_corners, w.voxels.indices, w.level_sets)
-        vertices = 2.0 * tri.vertices - 1.0
+        vertices = pipeline.uncontract_stand_in(tri.vertices)
         args = (vertices, tri.faces, tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics, w.sh_degree,
                 w.sharpness, w.background)
         images = tr.render_cameras(w.extrinsics, w.intrinsics, w.image_shapes, *args, tile_shape=tile)
@@ -590,7 +590,7 @@ def run_large(device, steps):
     with torch.no_grad():
         tri = te.tessellate_voxels(w.grid_sdf, w.voxels.vertices, w.grid_sh, w.voxels.neighbors,
                                    w.voxels.lower_corners, w.voxels.upper_corners, w.voxels.indices, w.level_sets)
-        vertices = 2.0 * tri.vertices - 1.0
+        vertices = pipeline.uncontract_stand_in(tri.vertices)
         fused = pipeline._render(w, tri, vertices, None, "fused")
         explicit = pipeline._render(w, tri, vertices, None, "explicit")
         diff = float((fused - explicit).abs().max())

@@ -42,7 +42,7 @@ import numpy as np
 import torch
 from torch import Tensor
 
-from . import synthetic
+from . import pipeline, synthetic
 from . import triangle_extraction as te
 from . import triangle_rasterization as tr
 
@@ -78,7 +78,7 @@ class Scene:
         v = self.voxels
         tri = te.tessellate_voxels(grid_sdf, v.vertices, grid_sh, v.neighbors, v.lower_corners, v.upper_corners,
                                    v.indices, self.level_sets)
-        return (2.0 * tri.vertices - 1.0).detach(), tri
+        return pipeline.uncontract_stand_in(tri.vertices).detach(), tri
 
     def refresh_mesh(self) -> None:
         """Re-tessellates the cached mesh (after the scene's parameters change)."""
