@@ -162,6 +162,20 @@ struct TileBounds {
   int r0, c0, r1, c1;
 };
 
+// ymax / tile as the reference divides it: for a power-of-two tile the
+// product with the exact reciprocal is the same correctly rounded quotient.
+__device__ __forceinline__ float div_by_tile(float x, int tile) {
+  if ((tile & (tile - 1)) == 0) return __fmul_rn(x, __int_as_float((127 - (__ffs(tile) - 1)) << 23));
+  return __fdiv_rn(x, (float)tile);
+}
+
+// max(v / tile, 0) with C's truncating division; for a power-of-two tile a
+// shift (flooring) differs only for negative v, where both clamp to 0.
+__device__ __forceinline__ int first_tile(int v, int tile) {
+  if ((tile & (tile - 1)) == 0) return max(v >> (__ffs(tile) - 1), 0);
+  return max(v / tile, 0);
+}
+
 // Tile rectangle of one projected triangle; mean_depth receives
 // (ad + bd + cd) / 3 (keys.slang's key depth) when the face is not culled.
 __device__ __forceinline__ TileBounds bounds_from_corners(float ax, float ay, float ad, float bx, float by, float bd,
@@ -175,10 +189,10 @@ __device__ __forceinline__ TileBounds bounds_from_corners(float ax, float ay, fl
   mean_depth = __fdiv_rn(__fadd_rn(__fadd_rn(ad, bd), cd), 3.0f);
   const float ymin = fminf(fminf(ay, by), cy), ymax = fmaxf(fmaxf(ay, by), cy);
   const float xmin = fminf(fminf(ax, bx), cx), xmax = fmaxf(fmaxf(ax, bx), cx);
-  t.r0 = min(max(f2i_rz(ymin) / tile_h, 0), rows);
-  t.r1 = min(max(f2i_rz(ceilf(__fdiv_rn(ymax, (float)tile_h))), 0), rows);
-  t.c0 = min(max(f2i_rz(xmin) / tile_w, 0), cols);
-  t.c1 = min(max(f2i_rz(ceilf(__fdiv_rn(xmax, (float)tile_w))), 0), cols);
+  t.r0 = min(first_tile(f2i_rz(ymin), tile_h), rows);
+  t.r1 = min(max(f2i_rz(ceilf(div_by_tile(ymax, tile_h))), 0), rows);
+  t.c0 = min(first_tile(f2i_rz(xmin), tile_w), cols);
+  t.c1 = min(max(f2i_rz(ceilf(div_by_tile(xmax, tile_w))), 0), cols);
   return t;
 }
 
