@@ -1047,6 +1047,7 @@ __global__ void __launch_bounds__(256)
     const int span = __shfl_sync(0xffffffffu, incl, 31);
     if (span == 0) continue;
     const int64_t first_slot = __ldg(foff + base);
+    const int64_t s_base = base / Nv;  // shell of the warp's first item (one division per warp step)
     for (int start = 0; start < span; start += 32) {
       const int r = start + lane;
       int src = 0;  // item holding slot r: smallest src with incl[src] > r
@@ -1060,8 +1061,12 @@ __global__ void __launch_bounds__(256)
       if (r >= span) continue;
       const int e = r - before;
       const int64_t item = base + src;
-      const int s = (int)(item / Nv);
-      const int64_t v = item - (int64_t)s * Nv;
+      int s = (int)s_base;
+      int64_t v = item - s_base * Nv;
+      while (v >= Nv) {  // at most ceil(32 / Nv) steps
+        v -= Nv;
+        ++s;
+      }
       const int eid = (int)((s_edges[c] >> (4 * e)) & 15u);
       const int owner = s_owner[eid];
       const uint8_t axis = s_axis[eid];
