@@ -1,0 +1,172 @@
+"""CPU checks of the exactness arguments behind two compositing and key
+speed-ups, with every float32 operation emulated one by one in numpy (IEEE
+single precision, round to nearest, no fused multiply-add):
+
+* warp-block edge exclusion: a block of pixel centres whose warp bit the
+  mask kernel clears is rejected by the barycentric test's fast reject at
+  every pixel centre (adversarial triangles: slivers, sub-pixel, repeated
+  vertices, vertices on pixel centres, huge);
+* tile bounds with power-of-two tiles: division by 2^k equals multiplication
+  by 2^-k for every float32, and the shifted integer division agrees with
+  C's truncating one under max(., 0).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+f32 = np.float32
+INF = f32(np.inf)
+
+
+def _dot2(ax, ay, bx, by):
+    return f32(f32(ax * bx) + f32(ay * by))
+
+
+def _setup(p1, p2, p3):
+    """Triangle-only part of the barycentric solve (setup_geometry)."""
+    e12x, e12y = f32(p2[0] - p1[0]), f32(p2[1] - p1[1])
+    e13x, e13y = f32(p3[0] - p1[0]), f32(p3[1] - p1[1])
+    e23x, e23y = f32(p3[0] - p2[0]), f32(p3[1] - p2[1])
+    d1212 = _dot2(e12x, e12y, e12x, e12y)
+    d1223 = _dot2(e12x, e12y, e23x, e23y)
+    d1213 = _dot2(e12x, e12y, e13x, e13y)
+    d1313 = _dot2(e13x, e13y, e13x, e13y)
+    d1323 = _dot2(e13x, e13y, e23x, e23y)
+    d2323 = _dot2(e23x, e23y, e23x, e23y)
+    a, b, c = abs(d1213), abs(d1223), abs(d1323)
+    if a <= b and a <= c:
+        denom = f32(f32(d1212 * d1313) - f32(d1213 * d1213))
+    elif b <= a and b <= c:
+        denom = f32(f32(d1212 * d2323) - f32(d1223 * d1223))
+    elif c <= a and c <= b:
+        denom = f32(f32(d1313 * d2323) - f32(d1323 * d1323))
+    else:
+        denom = f32(np.nan)
+    dd = f32(denom + f32(1e-8))
+    fast = dd > f32(2.0 ** -20) and dd < INF
+    thr = -f32(dd * f32(2.0 ** -100)) if fast else -INF
+    return dict(p1=p1, p2=p2, e12=(e12x, e12y), e13=(e13x, e13y), d1212=d1212, d1213=d1213, d1313=d1313,
+                d1223=d1223, d1323=d1323, thr=thr)
+
+
+def _numerators(g, px, py):
+    """The three numerators of the barycentric test at pixel centres (arrays)."""
+    q1x, q1y = (px - g["p1"][0]).astype(f32), (py - g["p1"][1]).astype(f32)
+    q2x, q2y = (px - g["p2"][0]).astype(f32), (py - g["p2"][1]).astype(f32)
+    e12x, e12y = g["e12"]
+    e13x, e13y = g["e13"]
+
+    def dot(ax, ay, bx, by):
+        return ((ax * bx).astype(f32) + (ay * by).astype(f32)).astype(f32)
+
+    d1x12, d1x13 = dot(q1x, q1y, e12x, e12y), dot(q1x, q1y, e13x, e13y)
+    d2x12, d2x13 = dot(q2x, q2y, e12x, e12y), dot(q2x, q2y, e13x, e13y)
+
+    def dop(a, x, c, y):
+        return ((a * x).astype(f32) - (c * y).astype(f32)).astype(f32)
+
+    vn = dop(g["d1313"], d1x12, g["d1213"], d1x13)
+    wn = dop(g["d1212"], d1x13, g["d1213"], d1x12)
+    un = dop(g["d1223"], d2x13, g["d1323"], d2x12)
+    return un, vn, wn
+
+
+def _edge_excludes(A, C, P, eX, eY, thr, x0, x1, y0, y1):
+    """The mask kernel's exclusion by one numerator (edge_bound, edge_excludes)."""
+    k = f32(2.0 ** -19)
+    a = f32(f32(A * eX[0]) - f32(C * eY[0]))
+    b = f32(f32(A * eX[1]) - f32(C * eY[1]))
+    sx = f32(abs(f32(A * eX[0])) + abs(f32(C * eY[0])))
+    sy = f32(abs(f32(A * eX[1])) + abs(f32(C * eY[1])))
+    qx0, qx1 = f32(x0 - P[0]), f32(x1 - P[0])
+    qy0, qy1 = f32(y0 - P[1]), f32(y1 - P[1])
+
+    def term(c, s, q):
+        return f32(f32(c * q) + f32(f32(k * s) * abs(q)))
+
+    tx = max(term(a, sx, qx0), term(a, sx, qx1))
+    ty = max(term(b, sy, qy0), term(b, sy, qy1))
+    bm = f32(k * f32(f32(sx * max(abs(qx0), abs(qx1))) + f32(sy * max(abs(qy0), abs(qy1)))))
+    hi = f32(f32(tx + ty) + bm)
+    return bool(hi < thr)
+
+
+def _block_excluded(g, x0, x1, y0, y1):
+    if not g["thr"] > -INF:
+        return False
+    e12, e13 = g["e12"], g["e13"]
+    return (_edge_excludes(g["d1313"], g["d1213"], g["p1"], e12, e13, g["thr"], x0, x1, y0, y1)
+            or _edge_excludes(g["d1212"], g["d1213"], g["p1"], e13, e12, g["thr"], x0, x1, y0, y1)
+            or _edge_excludes(g["d1223"], g["d1323"], g["p2"], e13, e12, g["thr"], x0, x1, y0, y1))
+
+
+def _triangles(rng, n):
+    out = []
+    for kind in rng.integers(0, 6, n):
+        c = rng.uniform(0, 200, 2)
+        if kind == 0:  # small, well shaped
+            p = c + rng.normal(0, 3, (3, 2))
+        elif kind == 1:  # sliver
+            d = rng.normal(0, 1, 2)
+            d /= np.linalg.norm(d)
+            p = c + rng.uniform(-20, 20, 3)[:, None] * d + rng.normal(0, 1e-3, (3, 2))
+        elif kind == 2:  # repeated vertex
+            p = np.stack((c, c + rng.normal(0, 5, 2), c))
+        elif kind == 3:  # sub-pixel
+            p = c + rng.normal(0, 0.3, (3, 2))
+        elif kind == 4:  # large
+            p = c + rng.normal(0, 60, (3, 2))
+        else:  # vertices on pixel centres
+            p = np.floor(c) + 0.5 + rng.integers(-4, 5, (3, 2)).astype(float)
+        p = p.astype(f32)
+        # Counter-clockwise in the sense of the back-face test (both orders
+        # are exercised by the exclusion, which does not depend on it).
+        out.append(p)
+    return out
+
+
+def test_excluded_blocks_are_fast_rejected_everywhere():
+    rng = np.random.default_rng(0)
+    checked = excluded = 0
+    lx, ly = np.meshgrid(np.arange(8), np.arange(4))
+    for p in _triangles(rng, 1500):
+        g = _setup(p[0], p[1], p[2])
+        lo = np.floor(p.min(0)).astype(int) - 9
+        hi = np.floor(p.max(0)).astype(int) + 9
+        for bx in range(lo[0] - lo[0] % 8, hi[0] + 1, 8):
+            for by in range(lo[1] - lo[1] % 4, hi[1] + 1, 4):
+                x0, x1 = f32(bx + 0.5), f32(bx + 7.5)
+                y0, y1 = f32(by + 0.5), f32(by + 3.5)
+                checked += 1
+                if not _block_excluded(g, x0, x1, y0, y1):
+                    continue
+                excluded += 1
+                px = (bx + lx + 0.5).astype(f32).ravel()
+                py = (by + ly + 0.5).astype(f32).ravel()
+                un, vn, wn = _numerators(g, px, py)
+                rejected = (un < g["thr"]) | (vn < g["thr"]) | (wn < g["thr"])
+                assert rejected.all(), (p, bx, by)
+    assert checked > 10000 and excluded > checked // 4  # the exclusion is exercised
+
+
+def test_power_of_two_tile_division_is_a_multiply():
+    rng = np.random.default_rng(1)
+    bits = rng.integers(0, 2 ** 32, 2_000_000, dtype=np.uint64).astype(np.uint32)
+    x = bits.view(f32)
+    x = x[np.isfinite(x)]
+    extra = np.array([0.0, -0.0, 1e-45, -1e-45, 1.17549435e-38, 3.4028235e38, 7.5, -7.5, 8.0, 1023.9999],
+                     dtype=f32)
+    x = np.concatenate([x, extra])
+    for k in range(0, 11):
+        div = (x / f32(2 ** k)).astype(f32)
+        mul = (x * f32(2.0 ** -k)).astype(f32)
+        np.testing.assert_array_equal(div.view(np.uint32), mul.view(np.uint32))
+
+
+def test_power_of_two_first_tile_shift():
+    v = np.arange(-70000, 70000, dtype=np.int64)
+    for k in range(0, 11):
+        t = 1 << k
+        trunc = np.where(v >= 0, v // t, -((-v) // t))  # C's truncating division
+        np.testing.assert_array_equal(np.maximum(trunc, 0), np.maximum(v >> k, 0))
