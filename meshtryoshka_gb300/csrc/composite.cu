@@ -1,14 +1,17 @@
 // Fused multi-shell intersect + composite, forward and backward, for sm_103a.
 //
-// Follows triangle_rasterization/intersect_and_composite.slang:1-564. One CTA
-// per (camera, tile) and one thread per pixel, as in the reference, but the
-// warps of a CTA never wait for each other:
+// Follows triangle_rasterization/intersect_and_composite.slang:1-564. One
+// thread per pixel, as in the reference, but warps are independent: persistent
+// warps pull (camera, tile, warp-in-tile) work items from a device counter and
+// never wait for each other:
 //
 //   * a pre-pass (warp_mask_kernel) gives every sorted key a bitmask of the
 //     warps of its tile whose pixels the triangle can cover. Warps own compact
 //     8x4 pixel blocks, and the bit is set unless the triangle's conservative
-//     accept box (bary.cuh: cull_box) misses the block, so culling changes
-//     no hit decision;
+//     accept box (bary.cuh: cull_box) misses the block or one barycentric
+//     numerator is provably below the fast-reject threshold at every pixel
+//     centre of the block (edge exclusion), so culling changes no hit
+//     decision;
 //   * each warp walks its tile's key list on its own: it scans 32 masks per
 //     step (one coalesced load + ballot), queues the keys that concern it,
 //     and whenever 32 are queued its lanes gather those triangles (one each)
@@ -21,7 +24,10 @@
 // Per pixel, the three barycentric numerators reject most triangles before
 // any division (bary.cuh: hit_test).
 //
-// Backward re-walks the same way, recomputes hits and applies the suffix
+// The forward stores each lane's hit bits for a warp's first kHitBatches
+// batches (optional hit_bits scratch); the backward re-walks the same way,
+// reads those bits instead of testing again (gathering only the triangles
+// some pixel hits), re-solves each hit's barycentrics and applies the suffix
 // trick of the reference. Per-triangle gradient sums live in a per-warp ring
 // of 64 shared-memory slots (the current and the previous batch); a slot is
 // flushed to global memory with one atomic per non-zero scalar when its batch
