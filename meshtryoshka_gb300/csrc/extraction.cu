@@ -11,6 +11,13 @@
 // with lane = bit, turning the reference's serial 32-bit walk into warp-ballot
 // stream compaction (popcount of the lanes below); all [*, G] / [*, Nv] tables
 // are read one row at a time so every row read is coalesced.
+//
+// For the captured training step the per-vertex SH rows can be skipped: the
+// grid-SH colour kernels evaluate vertex colours straight from the grid
+// coefficients (evaluate_spherical_harmonics.slang with the interpolation of
+// create_triangle_vertices.slang) and send the SH gradient straight back to
+// the grid through the per-grid-vertex contribution list, with the same bits
+// as the row path.
 
 #include "mc_tables.h"
 #include "mt_common.cuh"
