@@ -149,7 +149,7 @@ KERNELS_PER_CALL = {
     "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows (1 without the rows)
     "mt_create_triangle_vertices_backward": 5,  # corner inverse, count, scan, list + grads, SH gather
     "mt_intersect_and_composite_forward": 2,  # warp masks, composite
-    "mt_sort_keys_by_tile": 6,
+    "mt_sort_keys_by_tile": 7,  # count, scan, tile ranges, scatter, tiny / medium / small / large bin sorts
     "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys
     "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill
     "mt_grid_sh_colors_backward": 2,  # per-vertex SH gradients, per-grid-vertex sums  # count, scan, tile ranges, scatter, small-bin and large-bin sorts

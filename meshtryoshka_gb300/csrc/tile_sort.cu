@@ -12,7 +12,8 @@
 //      (low bits << index bits) | original index;
 //   4. sort each bin's composites: the original index breaks ties, so the
 //      order is the stable sort's. Bins of up to 256 keys are sorted by one
-//      warp, up to 1024 by 128-thread CTAs, larger ones by 512-thread CTAs
+//      warp, up to 512 by 64-thread CTAs, up to 1024 by 128-thread CTAs,
+//      larger ones by 512-thread CTAs
 //      (4096 keys in shared memory; beyond that, sorted 4096-key chunks
 //      merged pairwise in global memory). In shared memory each thread sorts
 //      8 values in registers, then sorted runs are merged (merge path);
@@ -59,8 +60,11 @@ __device__ __forceinline__ int64_t live_keys(int64_t capacity, const int64_t* co
 
 constexpr int kThreads = 256;       // counting, scatter and tile-range kernels
 constexpr int kTinyCap = 256;       // keys per bin sorted by one warp
+constexpr int kMediumThreads = 64;
+constexpr int kMediumCap = 512;     // keys per bin sorted by a 64-thread CTA
 constexpr int kSmallThreads = 128;
 constexpr int kSmallCap = 1024;     // keys per bin sorted by a 128-thread CTA
+constexpr int kTiers = 4;           // tiny, medium, small, large
 constexpr int kLargeThreads = 512;
 constexpr int kChunk = 4096;        // keys per shared-memory sort of a 512-thread CTA
 
@@ -93,7 +97,7 @@ __global__ void bin_bounds_kernel(const int32_t* __restrict__ offsets, int64_t n
     bounds[2 * b + 1] = e > s ? e : 0;
     if (e > s) {
       const int n = e - s;
-      const int which = n <= kTinyCap ? 0 : (n <= kSmallCap ? 1 : 2);
+      const int which = n <= kTinyCap ? 0 : n <= kMediumCap ? 1 : n <= kSmallCap ? 2 : 3;
       lists[which * nbins + atomicAdd(list_sizes + which, 1)] = make_int2(s, n);
     }
   }
@@ -279,18 +283,22 @@ __global__ void __launch_bounds__(32 * kTinyWarps)
   }
 }
 
-// 4 + 5 for the listed bins of more than kTinyCap and at most kSmallCap keys.
-__global__ void __launch_bounds__(kSmallThreads)
-    bin_sort_small_kernel(const uint64_t* __restrict__ tmp, const int2* __restrict__ list,
-                          const int32_t* __restrict__ list_size, uint64_t idx_mask,
-                          const uint64_t* __restrict__ keys_in, const int32_t* __restrict__ tri_in,
-                          uint64_t* __restrict__ keys_out, int32_t* __restrict__ tri_out) {
-  __shared__ uint64_t s[kSmallCap], s2[kSmallCap];
+// 4 + 5 for the listed bins of at most kCtaThreads * 8 keys (and more than
+// the tier below): one CTA per bin. Instantiated for the medium (64 threads,
+// <= 512 keys) and small (128 threads, <= 1024 keys) tiers, so that a bin's
+// idle threads stay few.
+template <int kCtaThreads>
+__global__ void __launch_bounds__(kCtaThreads)
+    bin_sort_cta_kernel(const uint64_t* __restrict__ tmp, const int2* __restrict__ list,
+                        const int32_t* __restrict__ list_size, uint64_t idx_mask,
+                        const uint64_t* __restrict__ keys_in, const int32_t* __restrict__ tri_in,
+                        uint64_t* __restrict__ keys_out, int32_t* __restrict__ tri_out) {
+  __shared__ uint64_t s[kCtaThreads * kPerThread], s2[kCtaThreads * kPerThread];
   const int count = *list_size;
   for (int l = blockIdx.x; l < count; l += gridDim.x) {
     const int2 e = list[l];
-    const uint64_t* sorted = block_merge_sort<kSmallThreads>(tmp + e.x, e.y, s, s2, threadIdx.x);
-    write_sorted<kSmallThreads, true>(sorted, e.y, e.x, idx_mask, keys_in, tri_in, keys_out, tri_out, threadIdx.x);
+    const uint64_t* sorted = block_merge_sort<kCtaThreads>(tmp + e.x, e.y, s, s2, threadIdx.x);
+    write_sorted<kCtaThreads, true>(sorted, e.y, e.x, idx_mask, keys_in, tri_in, keys_out, tri_out, threadIdx.x);
     __syncthreads();
   }
 }
@@ -371,8 +379,8 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 struct TileSortWorkspace {
   int32_t* counts;   // nbins + 1 (scanned in place into offsets)
   int32_t* cursors;  // nbins
-  int2* lists;       // 3 x nbins (start, count): tiny, small and large non-empty bins
-  int32_t* list_sizes;  // 3
+  int2* lists;       // kTiers x nbins (start, count): tiny, medium, small and large non-empty bins
+  int32_t* list_sizes;  // kTiers
   uint64_t* tmp;     // K
   uint64_t* alt;     // K
   void* scan_ws;
@@ -388,8 +396,8 @@ size_t tile_sort_bytes(int64_t K, int64_t nbins, TileSortWorkspace* w, char* bas
   };
   char* counts = take((size_t)(nbins + 1) * sizeof(int32_t));
   char* cursors = take((size_t)nbins * sizeof(int32_t));
-  char* lists = take((size_t)3 * nbins * sizeof(int2));
-  char* list_sizes = take(3 * sizeof(int32_t));
+  char* lists = take((size_t)kTiers * nbins * sizeof(int2));
+  char* list_sizes = take(kTiers * sizeof(int32_t));
   char* tmp = take((size_t)K * sizeof(uint64_t));
   char* alt = take((size_t)K * sizeof(uint64_t));
   const size_t scan_bytes = mt_scan_workspace_bytes(nbins + 1);
@@ -509,7 +517,7 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
   const uint64_t idx_mask = (1ull << idx_bits) - 1ull;
   if (cudaMemsetAsync(w.counts, 0, (size_t)(nbins + 1) * sizeof(int32_t), s) != cudaSuccess) return MT_ERR_CUDA;
   if (cudaMemsetAsync(w.cursors, 0, (size_t)nbins * sizeof(int32_t), s) != cudaSuccess) return MT_ERR_CUDA;
-  if (cudaMemsetAsync(w.list_sizes, 0, 3 * sizeof(int32_t), s) != cudaSuccess) return MT_ERR_CUDA;
+  if (cudaMemsetAsync(w.list_sizes, 0, kTiers * sizeof(int32_t), s) != cudaSuccess) return MT_ERR_CUDA;
   const uint64_t* k64 = reinterpret_cast<const uint64_t*>(keys);
   // A key outside every bin (never made by mt_generate_keys) is recorded in
   // the workspace status word; it is left out of the output.
@@ -534,7 +542,7 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
     return MT_ERR_CUDA;
   const unsigned large_ctas = (unsigned)(nbins < (int64_t)kSmCount * 2 ? nbins : (int64_t)kSmCount * 2);
   bin_sort_large_kernel<<<large_ctas, kLargeThreads, large_smem, fj.side>>>(
-      w.tmp, w.alt, w.lists + 2 * nbins, w.list_sizes + 2, idx_mask, k64, triangles,
+      w.tmp, w.alt, w.lists + 3 * nbins, w.list_sizes + 3, idx_mask, k64, triangles,
       reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
   MT_CHECK_LAUNCH();
   const unsigned tiny_ctas = (unsigned)(nbins < (int64_t)kSmCount * 5 ? nbins : (int64_t)kSmCount * 5);
@@ -542,11 +550,15 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
                                                              reinterpret_cast<uint64_t*>(sorted_keys),
                                                              sorted_triangles);
   MT_CHECK_LAUNCH();
+  const unsigned medium_ctas = (unsigned)(nbins < (int64_t)kSmCount * 22 ? nbins : (int64_t)kSmCount * 22);
+  bin_sort_cta_kernel<kMediumThreads><<<medium_ctas, kMediumThreads, 0, s>>>(
+      w.tmp, w.lists + nbins, w.list_sizes + 1, idx_mask, k64, triangles, reinterpret_cast<uint64_t*>(sorted_keys),
+      sorted_triangles);
+  MT_CHECK_LAUNCH();
   const unsigned small_ctas = (unsigned)(nbins < (int64_t)kSmCount * 11 ? nbins : (int64_t)kSmCount * 11);
-  bin_sort_small_kernel<<<small_ctas, kSmallThreads, 0, s>>>(w.tmp, w.lists + nbins, w.list_sizes + 1, idx_mask,
-                                                             k64, triangles,
-                                                             reinterpret_cast<uint64_t*>(sorted_keys),
-                                                             sorted_triangles);
+  bin_sort_cta_kernel<kSmallThreads><<<small_ctas, kSmallThreads, 0, s>>>(
+      w.tmp, w.lists + 2 * nbins, w.list_sizes + 2, idx_mask, k64, triangles,
+      reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
   MT_CHECK_LAUNCH();
   if (cudaEventRecord(fj.join, fj.side) != cudaSuccess || cudaStreamWaitEvent(s, fj.join, 0) != cudaSuccess)
     return MT_ERR_CUDA;

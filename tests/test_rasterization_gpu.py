@@ -421,6 +421,8 @@ EXPLICIT_KEYS = (("camera", 6), ("shell", 6), ("tile", 20), ("depth", 32))
     (1, 1, 1, 1, 1, None),
     (5000, 4, 3, 7, 9, None),
     (300_000, 32, 8, 40, 50, None),
+    (200_000, 2, 1, 10, 20, None),  # ~500 keys per bin: the 64- and 128-thread tiers
+    (150_000, 1, 2, 15, 20, None),
     (100_000, 2, 4, 3, 3, 4),  # one tile of 50k keys per camera: chunks and merge rounds
     (20_000, 3, 2, 60, 70, 0),
 ])
