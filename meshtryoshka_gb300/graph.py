@@ -72,9 +72,14 @@ class CapturedTrainingStep:
         self._capture()
 
     def _measure(self) -> dict:
-        """Live sizes of one eager forward (no autograd graph is kept)."""
+        """Live sizes of one eager forward per input set (no autograd graph is
+        kept), the largest of each over the sets: the key count depends on
+        each set's cameras."""
+        stats = None
         with torch.no_grad():
-            _, stats = pipeline.forward(self.w, "fused", self.gradient_mode)
+            for view in self._views:
+                _, st = pipeline.forward(view, "fused", self.gradient_mode)
+                stats = st if stats is None else {k: max(stats[k], st[k]) for k in st}
         return stats
 
     def _step(self, slot: int = 0) -> tuple[Tensor, Tensor, Tensor, Tensor]:
