@@ -38,7 +38,7 @@ def _eager(w):
     w.grid_sh.grad = None
     loss, stats = pipeline.forward(w, "fused")
     loss.backward()
-    out = float(loss), w.grid_sdf.grad.clone(), w.grid_sh.grad.clone(), stats
+    out = float(loss.detach()), w.grid_sdf.grad.clone(), w.grid_sh.grad.clone(), stats
     w.grid_sdf.grad = None
     w.grid_sh.grad = None
     return out
@@ -170,3 +170,29 @@ def test_deferred_sh_matches_rows_bit_for_bit(cuda_device, config):
     for got, want in zip(out[True], out[False]):
         torch.testing.assert_close(got, want, rtol=0, atol=0)
     assert float(out[True][1].abs().max()) > 0
+
+
+def test_captured_step_input_set_with_other_cameras(cuda_device):
+    """A batch with other cameras in set 1 (more keys): the step detects an
+    overflow if there is one, re-captures with capacities measured over every
+    set, and then matches the eager step on that batch."""
+    w = pipeline.build_workload("small", cuda_device)
+    step = graph.CapturedTrainingStep(w, input_sets=2, margin=1.0)
+    closer = w.extrinsics.clone()
+    closer[:, 2, 3] *= 0.8  # cameras moved towards the scene: larger images of it, more keys
+    with torch.no_grad():
+        step.inputs[1]["extrinsics"].copy_(closer)
+    for _ in range(3):
+        loss1 = step(1)
+        torch.cuda.synchronize()
+        if step.check():
+            break
+    assert step.check()
+    loss1 = float(loss1)
+    g_sdf, g_sh = step.grad_sdf.clone(), step.grad_sh.clone()
+    with torch.no_grad():
+        w.extrinsics.copy_(closer)
+    loss_e, gsdf_e, gsh_e, _ = _eager(w)
+    assert abs(loss1 - loss_e) <= LOSS_RTOL * abs(loss_e)
+    _close(g_sdf, gsdf_e)
+    _close(g_sh, gsh_e)
