@@ -285,7 +285,7 @@ def upscale_occupancy(occupancy: Tensor, target_shape: tuple[int, int, int]) -> 
 
 class UpscaledParameters(NamedTuple):
     signed_distances: Tensor  # [vertex] float32
-    spherical_harmonics: Tensor  # [sh, vertex, 3] float32
+    spherical_harmonics: Tensor  # [sh, vertex, 3]; a DeferredSH from tessellate_voxels_counted(defer_sh=True) float32
     occupancy: Tensor  # [i, j, k_packed] int32
 
 
