@@ -56,7 +56,7 @@ constexpr int kSavedBwd = 3;  // same, backward (its shared memory is tighter)
 // Batches per work item whose per-lane hit bits the forward stores for the
 // backward (which then skips their test phase); later batches are tested
 // again.
-constexpr int kHitBatches = 8;
+constexpr int kHitBatches = 32;
 
 // The (u, v, w) of the first K hits each lane finds in a batch, so that the
 // hit phase does not solve them again (later hits are re-solved).

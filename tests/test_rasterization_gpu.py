@@ -542,10 +542,10 @@ def test_bound_and_generate_keys_matches_three_stage_chain(cuda_device, b, f, ra
     assert nt.workspace(torch.device(d)).status() == 0
 
 
-# A whole 8-shell sphere in a few tiles: warps walk far more than the 8
+# A whole 8-shell sphere in a few tiles: warps walk far more than the 32
 # batches whose hit bits the forward stores, so the backward mixes stored
 # and re-tested batches.
-DENSE = dict(cameras=((0.0, 0.0, 5.0),), image_shape=(40, 48), fov=20.0,
+DENSE = dict(cameras=((0.0, 0.0, 8.0),), image_shape=(32, 32), fov=20.0,
              levels=tuple(float(x) for x in np.linspace(0.03, -0.03, 8)), sh_degree=1)
 
 
@@ -553,7 +553,7 @@ def test_fused_backward_past_the_stored_batches(cuda_device):
     scene = make_scene(**DENSE)
     grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, cuda_device)
     counts = _n(tb)[..., 1] - _n(tb)[..., 0]
-    assert counts.max() > 8 * 32 * 4  # tiles far longer than the stored batches
+    assert counts.max() > 32 * 32 * 4  # tiles far longer than the stored batches
     _check_fused_backward(scene, cuda_device, "reference", (16, 16))
 
 
