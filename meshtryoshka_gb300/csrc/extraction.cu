@@ -416,14 +416,20 @@ __global__ void interpolate_vertex_sh_kernel(const float* __restrict__ gsh, int 
 // Crossings are packed 3 bits per shell into 64-bit masks, shells taken in
 // chunks of 21; the first chunk writes, later chunks add.
 // ---------------------------------------------------------------------------
-__global__ void invert_corners_kernel(const int32_t* __restrict__ lower, int64_t G, int32_t* __restrict__ inverse) {
+// `zero0` [G+1] and `zero1` [G] (either may be NULL) are cleared on the way,
+// for the per-entry list passes that follow.
+__global__ void invert_corners_kernel(const int32_t* __restrict__ lower, int64_t G, int32_t* __restrict__ inverse,
+                                      int32_t* __restrict__ zero0 = nullptr, uint32_t* __restrict__ zero1 = nullptr) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G; e += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const int32_t x = __ldg(lower + r * G + e);
       if (x >= 0 && x < G) inverse[r * G + x] = (int32_t)e;
     }
+    if (zero0) zero0[e] = 0;
+    if (zero1) zero1[e] = 0u;
   }
+  if (zero0 && blockIdx.x == 0 && threadIdx.x == 0) zero0[G] = 0;
 }
 
 constexpr int kShellsPerChunk = 21;
@@ -692,6 +698,94 @@ __global__ void vertex_grads_from_list_kernel(const int32_t* __restrict__ offset
     if (gdv) {
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) gdv[3 * x + ch] = p[ch];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same contribution list built per grid entry (mt_build_vertex_grad_list).
+//
+// Grid vertex x's list is four segments: the vertices of the entry whose
+// origin x is, then the axis-0, axis-1 and axis-2 vertices of the entries
+// whose axis-a corner x is, each in shell order (the order of
+// for_each_contribution). Entry e owns segment r of x = lower[r][e] when the
+// corner inverse names e there (so exactly the entries the per-vertex
+// enumeration visits, also for inputs where two entries share a corner).
+// Pass 1 adds each owned segment's length to x's count and stores it in byte
+// r of x's segment word; pass 2 writes the segment at x's scanned offset plus
+// the lengths of x's earlier segments. Each entry loads its own corners once
+// (the per-vertex passes load four entries' corners per grid vertex).
+// Counts and segment words start at zero (cleared by invert_corners_kernel).
+// ---------------------------------------------------------------------------
+template <bool kFill>
+__global__ void entry_list_kernel(const float* __restrict__ gsdf, const int32_t* __restrict__ lower, int64_t G,
+                                  const float* __restrict__ level_sets, int S, const int32_t* __restrict__ voff,
+                                  const int32_t* __restrict__ inverse, int64_t V, int32_t* __restrict__ counts,
+                                  uint32_t* __restrict__ segments, int2* __restrict__ list) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G; e += (int64_t)gridDim.x * blockDim.x) {
+    const Corners4 c = load_corners(gsdf, lower, G, e);
+    const uint64_t bits = crossing_bits(c, level_sets, 0, S);
+    if (bits == 0) continue;
+    int64_t x[4];
+    x[0] = __ldg(lower + e);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x[a + 1] = c.idx[a];
+    bool owns[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) owns[r] = x[r] >= 0 && x[r] < G && __ldg(inverse + r * G + x[r]) == (int32_t)e;
+    if (!(owns[0] || owns[1] || owns[2] || owns[3])) continue;
+    if (!kFill) {
+      int n[4] = {0, 0, 0, 0};
+      for (int s = 0; s < S; ++s) {
+        const uint32_t m = (uint32_t)(bits >> (3 * s)) & 7u;
+        if (m == 0) continue;
+        const int64_t base = __ldg(voff + (int64_t)s * G + e);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (!((m >> a) & 1u) || base + __popc(m & ((1u << a) - 1u)) >= V) continue;
+          ++n[0];
+          ++n[a + 1];
+        }
+      }
+      uint8_t* seg = reinterpret_cast<uint8_t*>(segments);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (owns[r] && n[r] > 0) {
+          atomicAdd(counts + x[r], n[r]);
+          seg[4 * x[r] + r] = (uint8_t)n[r];  // n[0] <= 3 * 21, n[a + 1] <= 21
+        }
+      }
+    } else {
+      const int64_t cap = 2 * V;
+      int64_t pos[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        pos[r] = 0;
+        if (owns[r]) {
+          const uint32_t w = __ldg(segments + x[r]);
+          uint32_t earlier = 0;
+#pragma unroll
+          for (int q = 0; q < r; ++q) earlier += (w >> (8 * q)) & 0xffu;
+          pos[r] = (int64_t)__ldg(counts + x[r]) + earlier;  // counts = scanned offsets here
+        }
+      }
+      for (int s = 0; s < S; ++s) {
+        const uint32_t m = (uint32_t)(bits >> (3 * s)) & 7u;
+        if (m == 0) continue;
+        const float iso = __ldg(level_sets + s);
+        const int64_t base = __ldg(voff + (int64_t)s * G + e);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          if (!((m >> a) & 1u)) continue;
+          const int64_t vi = base + __popc(m & ((1u << a) - 1u));
+          if (vi >= V) continue;
+          const int tb = __float_as_int(mc_weight(c.d0, c.d[a], iso));
+          if (owns[0] && pos[0] < cap) list[pos[0]] = make_int2((int)vi | (int)0x80000000, tb);
+          ++pos[0];
+          if (owns[a + 1] && pos[a + 1] < cap) list[pos[a + 1]] = make_int2((int)vi, tb);
+          ++pos[a + 1];
+        }
+      }
     }
   }
 }
@@ -1513,7 +1607,12 @@ int mt_capacity_overflow(const int32_t* num_vertices, int64_t vertex_capacity, c
 
 int mt_vertex_grad_list_max_shells(void) { return kShellsPerChunk; }
 
-size_t mt_build_vertex_grad_list_workspace_bytes(int64_t G) { return 256 + mt_scan_workspace_bytes(G + 1); }
+// Workspace: status word, the segment words [G], the scan's scratch.
+static size_t segment_bytes(int64_t G) { return ((size_t)G * sizeof(uint32_t) + 255) & ~(size_t)255; }
+
+size_t mt_build_vertex_grad_list_workspace_bytes(int64_t G) {
+  return 256 + segment_bytes(G) + mt_scan_workspace_bytes(G + 1);
+}
 
 int mt_build_vertex_grad_list(const float* grid_signed_distances, const int32_t* lower_corners, int64_t G,
                               const float* level_sets, int32_t S, const int32_t* vertex_offsets, int64_t V,
@@ -1527,19 +1626,22 @@ int mt_build_vertex_grad_list(const float* grid_signed_distances, const int32_t*
   MT_REQUIRE(V == 0 || list);
   if (workspace_bytes < mt_build_vertex_grad_list_workspace_bytes(G)) return MT_ERR_WORKSPACE_TOO_SMALL;
   cudaStream_t st = as_stream(stream);
-  if (cudaMemsetAsync(corner_inverse, 0xff, (size_t)G * 4 * sizeof(int32_t), st) != cudaSuccess) return MT_ERR_CUDA;
-  invert_corners_kernel<<<grid_stride_blocks(G, 256), 256, 0, st>>>(lower_corners, G, corner_inverse);
-  MT_CHECK_LAUNCH();
-  vertex_grad_list_kernel<false><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
-      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, list_offsets,
-      nullptr, nullptr, nullptr, nullptr, nullptr);
-  MT_CHECK_LAUNCH();
   char* ws = static_cast<char*>(workspace);
-  const int rc = mt_exclusive_scan_i32(list_offsets, G + 1, ws + 256, workspace_bytes - 256, stream);
-  if (rc != MT_OK) return rc;
-  vertex_grad_list_kernel<true><<<grid_stride_blocks(G, 128), 128, 0, st>>>(
+  uint32_t* segments = reinterpret_cast<uint32_t*>(ws + 256);
+  const size_t scan_off = 256 + segment_bytes(G);
+  if (cudaMemsetAsync(corner_inverse, 0xff, (size_t)G * 4 * sizeof(int32_t), st) != cudaSuccess) return MT_ERR_CUDA;
+  invert_corners_kernel<<<grid_stride_blocks(G, 256), 256, 0, st>>>(lower_corners, G, corner_inverse, list_offsets,
+                                                                    segments);
+  MT_CHECK_LAUNCH();
+  entry_list_kernel<false><<<grid_stride_blocks(G, 256), 256, 0, st>>>(
       grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, list_offsets,
-      reinterpret_cast<int2*>(list), nullptr, nullptr, nullptr, nullptr);
+      segments, nullptr);
+  MT_CHECK_LAUNCH();
+  const int rc = mt_exclusive_scan_i32(list_offsets, G + 1, ws + scan_off, workspace_bytes - scan_off, stream);
+  if (rc != MT_OK) return rc;
+  entry_list_kernel<true><<<grid_stride_blocks(G, 256), 256, 0, st>>>(
+      grid_signed_distances, lower_corners, G, level_sets, S, vertex_offsets, corner_inverse, V, list_offsets,
+      segments, reinterpret_cast<int2*>(list));
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

@@ -58,7 +58,7 @@ def test_fused_loss_equals_unfused(cuda_device, name, mode):
     loss.backward()
     want = _grads(args)
     fused = tr.render_fused_loss(ext, intr, scene.image_shape, **args, target=target, gradient_mode=mode)
-    assert abs(float(fused) - float(loss)) <= 1e-5 * float(loss)
+    assert abs(float(fused.detach()) - float(loss.detach())) <= 1e-5 * float(loss.detach())
     fused.backward()
     for got, ref in zip(_grads(args), want):
         _close(got, ref)
@@ -79,7 +79,7 @@ def test_fused_loss_cameras_of_different_sizes(cuda_device):
     want = _grads(args)
     flat = torch.cat([t.reshape(-1) for t in targets])
     fused = tr.render_fused_loss(ext, intr, None, **args, target=flat, camera_shapes=shapes)
-    assert abs(float(fused) - float(loss)) <= 1e-5 * float(loss)
+    assert abs(float(fused.detach()) - float(loss.detach())) <= 1e-5 * float(loss.detach())
     fused.backward()
     for got, ref in zip(_grads(args), want):
         _close(got, ref)
