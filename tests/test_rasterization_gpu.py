@@ -174,7 +174,7 @@ def test_fused_backward(cuda_device, name, mode):
     _check_fused_backward(make_scene(**SCENES[name]), cuda_device, mode, (16, 16))
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (32, 32), (16, 8), (12, 20)])
+@pytest.mark.parametrize("tile", [(8, 8), (32, 32), (16, 8), (12, 20), (4, 8)])
 def test_fused_backward_tile_shapes(cuda_device, tile):
     """8x4-block tiles use per-triangle coverage; other shapes per-pixel tests."""
     _check_fused_backward(make_scene(**SCENES["three_cams_odd"]), cuda_device, "reference", tile)
@@ -217,7 +217,7 @@ def test_reference_and_exact_routing_differ_only_with_multiple_hits(cuda_device)
     _close_grad(grads["reference"], grads["exact"], rtol=1e-6)
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 32), (16, 8), (12, 20)])
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 32), (16, 8), (12, 20), (4, 8)])
 def test_fused_tile_shapes(cuda_device, tile):
     scene = make_scene(**SCENES["three_cams_odd"])
     inputs = _fused_inputs(scene, cuda_device)
