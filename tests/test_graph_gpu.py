@@ -135,7 +135,7 @@ def test_captured_step_input_sets_read_their_own_inputs(cuda_device):
     _close(step.grad_sh, gsh_e1)
 
 
-@pytest.mark.parametrize("config", ["small", "mid"])
+@pytest.mark.parametrize("config", ["small", "mid", "large"])
 def test_deferred_sh_matches_rows_bit_for_bit(cuda_device, config):
     """Colours from the grid SH (no per-vertex rows) equal the rows path, and
     so do the grid gradients: SH through the colours, signed distances and
