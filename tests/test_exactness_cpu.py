@@ -8,7 +8,9 @@ single precision, round to nearest, no fused multiply-add):
   vertices, vertices on pixel centres, huge);
 * tile bounds with power-of-two tiles: division by 2^k equals multiplication
   by 2^-k for every float32, and the shifted integer division agrees with
-  C's truncating one under max(., 0).
+  C's truncating one under max(., 0);
+* the contribution list of the vertex-interpolation backward built per grid
+  entry is the per-grid-vertex enumeration's list, written inside its bounds.
 """
 
 from __future__ import annotations
@@ -170,3 +172,102 @@ def test_power_of_two_first_tile_shift():
         t = 1 << k
         trunc = np.where(v >= 0, v // t, -((-v) // t))  # C's truncating division
         np.testing.assert_array_equal(np.maximum(trunc, 0), np.maximum(v >> k, 0))
+
+
+def _crossings(sdf, lower, levels):
+    """[S, 3, G] edge crossings of every grid entry (crossing_mask)."""
+    d0 = sdf[lower[0]]
+    out = np.zeros((len(levels), 3, lower.shape[1]), bool)
+    for a in range(3):
+        da = np.where(lower[a + 1] >= 0, sdf[np.maximum(lower[a + 1], 0)], d0)
+        for s, iso in enumerate(levels):
+            out[s, a] = (d0 < iso) != (da < iso)
+    return out
+
+
+def _lists(lower, cross, capacity):
+    """The contribution list enumerated per grid vertex (vertex_grad_list_kernel)
+    and built per grid entry (entry_list_kernel: counts and segment lengths,
+    scan, fill at offset + earlier segments); entries are (vertex, origin)."""
+    S, _, G = cross.shape
+    voff = np.concatenate([[0], np.cumsum(cross.sum(1).reshape(-1))])[:-1].reshape(S, G)
+    inverse = np.full((4, G), -1, np.int64)
+    for r in range(4):
+        for e in range(G):
+            if 0 <= lower[r, e] < G:
+                inverse[r, lower[r, e]] = e
+
+    def vertices(e):  # (shell, axis, vertex) of entry e in shell-then-axis order, capacity-checked
+        out = []
+        for s in range(S):
+            for a in range(3):
+                if cross[s, a, e]:
+                    v = voff[s, e] + int(cross[s, :a, e].sum())
+                    if v < capacity:
+                        out.append((a, v))
+        return out
+
+    per_vertex = []
+    for x in range(G):
+        if inverse[0, x] >= 0:
+            per_vertex += [(v, 1) for _, v in vertices(inverse[0, x])]
+        for a in range(3):
+            if inverse[a + 1, x] >= 0:
+                per_vertex += [(v, 0) for b, v in vertices(inverse[a + 1, x]) if b == a]
+
+    counts = np.zeros(G + 1, np.int64)
+    segments = np.zeros((G, 4), np.int64)
+    owners = []
+    for e in range(G):
+        xs = lower[:, e]
+        owns = [0 <= xs[r] < G and inverse[r, xs[r]] == e for r in range(4)]
+        owners.append((xs, owns))
+        n = [0, 0, 0, 0]
+        for a, _ in vertices(e):
+            n[0] += 1
+            n[a + 1] += 1
+        for r in range(4):
+            if owns[r] and n[r]:
+                counts[xs[r]] += n[r]
+                segments[xs[r], r] = n[r]
+    assert segments.max() < 256  # one byte per segment
+    offsets = np.concatenate([[0], np.cumsum(counts)])[:-1]
+    per_entry = [None] * (2 * capacity)
+    for e, (xs, owns) in enumerate(owners):
+        pos = [offsets[xs[r]] + segments[xs[r], :r].sum() if owns[r] else 0 for r in range(4)]
+        for a, v in vertices(e):
+            for r, flag in ((0, 1), (a + 1, 0)):
+                if owns[r]:
+                    assert 0 <= pos[r] < 2 * capacity and per_entry[pos[r]] is None
+                    per_entry[pos[r]] = (v, flag)
+                pos[r] += 1
+    assert offsets[-1] == len(per_vertex) <= 2 * capacity
+    return per_vertex, per_entry[:len(per_vertex)]
+
+
+def test_contribution_list_per_entry_equals_per_vertex():
+    """The captured step builds the contribution list per grid entry; it is
+    the per-vertex enumeration's list entry for entry, at full and at half
+    vertex capacity, and with two entries sharing a corner (an input the
+    corner inverse resolves to one owner), every write inside the list."""
+    from oracle import oracle
+    from tests import semantics
+
+    n = 32
+    coords = -1 + (np.arange(n) + 0.5) * 2 / n
+    z, y, x = np.meshgrid(coords, coords, coords, indexing="ij")
+    d = np.sqrt(x * x + y * y + z * z) - 0.5
+    vox = oracle.extract_voxels(semantics.pack(np.abs(d) < 2.5 * 2 / n))
+    p = 2 * vox.vertices.astype(np.float64) - 1
+    sdf = (np.linalg.norm(p, axis=1) - 0.5 + np.random.default_rng(0).normal(0, 0.002, len(p))).astype(f32)
+    lower = vox.lower_corners.astype(np.int64)
+    levels = np.array([0.04, 0.0, -0.04], f32)
+    shared = lower.copy()
+    shared[2, 10:20] = shared[2, 30:40]  # axis-1 corners shared by two entries
+    shared[0, 50] = shared[0, 60]        # an origin shared by two entries
+    for topology in (lower, shared):
+        cross = _crossings(sdf, topology, levels)
+        total = int(cross.sum())
+        for capacity in (total, total // 2):
+            per_vertex, per_entry = _lists(topology, cross, capacity)
+            assert per_entry == per_vertex and len(per_vertex) > 1000
