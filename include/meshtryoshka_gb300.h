@@ -80,6 +80,16 @@ MT_API int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t
                                  void* workspace, size_t workspace_bytes,
                                  mt_stream_t stream);
 
+/* Test support for the bounded device waits (no counterpart in the
+ * reference): one warp looks back from tile 1 of a scan whose tile 0 never
+ * publishes, gives up after spin_limit polls (1..2^20), records
+ * MT_ERR_DEVICE_TIMEOUT in the workspace status word (byte 0, as every scan
+ * does) and writes the prefix it fell back to (0) to prefix_out[0] (device).
+ * The workspace needs at least 272 bytes. */
+MT_API int mt_test_lookback_timeout(int32_t spin_limit, int64_t* prefix_out, void* workspace,
+                             size_t workspace_bytes, mt_stream_t stream);
+
+
 /* Allocation-free exclusive scan (no counterpart in the reference). Same
  * result as mt_exclusive_scan_i32, for callers that cannot allocate device
  * memory for scratch: a plain C/C++ host with no device allocator of its own,
@@ -88,11 +98,20 @@ MT_API int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t
  * every GPU that loads it until the process exits. Limits: n <=
  * mt_exclusive_scan_i32_static_max_elements() (2^26); larger n returns
  * MT_ERR_TOO_LARGE. All calls on a device share the array, so calls whose
- * work overlaps on the GPU race; issue them on one stream. The first call on
- * a device (with that device current) looks up the array's address; make it
- * before any stream capture on that device. data must live on the current
- * device. */
+ * work overlaps on the GPU race; issue them on one stream. The first call in
+ * a CUDA context (that context current) looks up the array's address and
+ * caches it under the context's id, so a device reset or another context
+ * gets a fresh lookup; make that first call before any stream capture in the
+ * context. data and stream must belong to the current context. A look-back
+ * wait that gave up leaves MT_ERR_DEVICE_TIMEOUT in the array's status word
+ * (read it with mt_exclusive_scan_i32_static_status); each call clears it. */
 MT_API int mt_exclusive_scan_i32_static(int32_t* data, int64_t n, mt_stream_t stream);
+
+/* Copies the status word of the last mt_exclusive_scan_i32_static call in the
+ * current context (MT_OK or MT_ERR_DEVICE_TIMEOUT, 4 bytes) to status_out,
+ * device or host memory, in stream order; read host memory after the stream
+ * has been synchronised. Allocates nothing. */
+MT_API int mt_exclusive_scan_i32_static_status(int32_t* status_out, mt_stream_t stream);
 
 /* Largest n accepted by mt_exclusive_scan_i32_static. */
 MT_API int64_t mt_exclusive_scan_i32_static_max_elements(void);

@@ -37,6 +37,8 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_inclusive_scan_i32_to_i64": (I32, [P, P, I64, P, c_size_t, P]),
     "mt_exclusive_scan_i32_static": (I32, [P, I64, P]),
     "mt_exclusive_scan_i32_static_max_elements": (I64, []),
+    "mt_exclusive_scan_i32_static_status": (I32, [P, P]),
+    "mt_test_lookback_timeout": (I32, [I32, P, P, c_size_t, P]),
     "mt_compute_vertex_occupancy": (I32, [P, I32, I32, I32, P, P, P]),
     "mt_count_occupancy": (I32, [P, I32, I32, I32, P, P]),
     "mt_create_voxels": (I32, [P, P, P, P, I32, I32, I32, I64, I64, P, P, P, P, P, P]),

@@ -55,9 +55,10 @@ __device__ __forceinline__ T warp_sum(T x) {
 // Called by all 32 lanes of one warp of tile `tile` with the tile's total.
 // Publishes the tile's aggregate, gathers the exclusive prefix of all earlier
 // tiles, publishes the inclusive prefix and returns the exclusive prefix (in
-// every lane).
+// every lane). `spin_limit` bounds the polls of one descriptor.
 template <typename T>
-__device__ __forceinline__ T lookback_prefix(uint64_t* desc, int64_t tile, T block_total, int* status) {
+__device__ __forceinline__ T lookback_prefix(uint64_t* desc, int64_t tile, T block_total, int* status,
+                                             int spin_limit = kSpinLimit) {
   const int lane = threadIdx.x & 31;
   if (tile == 0) {
     if (lane == 0) st_relaxed(&desc[0], pack_desc((int64_t)block_total, kFlagPrefix));
@@ -74,7 +75,7 @@ __device__ __forceinline__ T lookback_prefix(uint64_t* desc, int64_t tile, T blo
       int spins = 0;
       d = ld_relaxed(&desc[pred]);
       while ((d & 3) == 0) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           timed_out = true;
           d = pack_desc(0, kFlagPrefix);
           break;

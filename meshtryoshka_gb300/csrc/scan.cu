@@ -142,6 +142,15 @@ int launch_scan(const TI* in, TO* out, int64_t n, void* ws, size_t ws_bytes, cud
   return MT_OK;
 }
 
+// One warp looks back from tile 1 over a descriptor array whose tile 0 never
+// publishes: the wait gives up after `spin_limit` polls, records
+// MT_ERR_DEVICE_TIMEOUT in the status word and treats the missing tile as an
+// empty prefix; out[0] receives the prefix the look-back returned.
+__global__ void lookback_timeout_kernel(uint64_t* desc, int* status, int spin_limit, int64_t* out) {
+  const int64_t prefix = lookback_prefix<int64_t>(desc, 1, (int64_t)5, status, spin_limit);
+  if (threadIdx.x == 0) out[0] = prefix;
+}
+
 }  // namespace
 
 int scan_exclusive_i32(int32_t* data, int64_t n, void* ws, size_t ws_bytes, cudaStream_t s) {
@@ -171,6 +180,20 @@ int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, voi
   return mt::launch_scan<int32_t, int64_t, true>(in, out, n, ws, ws_bytes, mt::as_stream(stream));
 }
 
+int mt_test_lookback_timeout(int32_t spin_limit, int64_t* prefix_out, void* ws, size_t ws_bytes,
+                             mt_stream_t stream) {
+  MT_REQUIRE(spin_limit >= 1 && spin_limit <= (1 << 20) && prefix_out != nullptr && ws != nullptr);
+  if (ws_bytes < mt::kScanHeader + 16) return MT_ERR_WORKSPACE_TOO_SMALL;
+  char* base = static_cast<char*>(ws);
+  cudaStream_t s = mt::as_stream(stream);
+  // Tile 0's descriptor stays zero ("not ready"): nothing ever publishes it.
+  if (cudaMemsetAsync(base + mt::kScanHeader, 0, 16, s) != cudaSuccess) return MT_ERR_CUDA;
+  mt::lookback_timeout_kernel<<<1, 32, 0, s>>>(reinterpret_cast<uint64_t*>(base + mt::kScanHeader),
+                                               reinterpret_cast<int*>(base), spin_limit, prefix_out);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -192,9 +215,15 @@ int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, voi
 //   * every call on a device shares the same array and re-initialises the
 //     parts that must start at zero, so calls whose work overlaps on the GPU
 //     (two streams at once) race and must not be issued;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress, with that device current, and caches it; make
-//     that first call before any stream capture on that device.
+//   * the first call in a CUDA context (with that context current) looks up
+//     the array's device address with cudaGetSymbolAddress and caches it
+//     under the context's unique id, so a device reset (which destroys the
+//     primary context) or a driver-API context of the caller's own gets its
+//     own lookup; make the first call in a context before any stream capture
+//     in it;
+//   * a look-back that gave up waiting (MT_ERR_DEVICE_TIMEOUT) leaves its
+//     code in the array's status word, which the next call clears;
+//     mt_exclusive_scan_i32_static_status copies that word out.
 // ---------------------------------------------------------------------------
 namespace mt {
 namespace {
@@ -202,28 +231,88 @@ namespace {
 constexpr int64_t kStaticScanMaxElements = (int64_t)1 << 26;
 constexpr size_t kStaticScanBytes =
     kScanHeader + (size_t)((kStaticScanMaxElements + kScanTile - 1) / kScanTile) * 8;
-constexpr int kStaticScanMaxDevices = 64;
+constexpr int kStaticScanMaxContexts = 64;
 
 static __device__ __align__(256) unsigned char g_static_scan_scratch[kStaticScanBytes];
 
-// Host-side cache of each device's address of the array above. The symbol
-// itself is only a host-side stand-in and must never be passed to a kernel.
-std::atomic<void*> g_static_scan_address[kStaticScanMaxDevices];
+// Host-side cache of the array's device address per CUDA context (keyed by
+// the driver's context id, which is never reused within a process). The
+// symbol itself is only a host-side stand-in and must never be passed to a
+// kernel.
+struct StaticScanEntry {
+  unsigned long long context_id;
+  void* address;
+};
+StaticScanEntry g_static_scan_cache[kStaticScanMaxContexts];
+int g_static_scan_entries = 0;
 std::mutex g_static_scan_setup;
 
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+
+// The current context's id through the driver entry points the runtime
+// hands out (this library links only the runtime). *none is set when no
+// context is current on this thread yet.
+int current_context_id(unsigned long long* id, bool* none) {
+  static std::atomic<CtxGetCurrentFn> get_current{nullptr};
+  static std::atomic<CtxGetIdFn> get_id{nullptr};
+  *none = false;
+  CtxGetCurrentFn fc = get_current.load(std::memory_order_acquire);
+  CtxGetIdFn fi = get_id.load(std::memory_order_acquire);
+  if (fc == nullptr || fi == nullptr) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+        qa != cudaDriverEntryPointSuccess || a == nullptr)
+      return MT_ERR_CUDA;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+        qb != cudaDriverEntryPointSuccess || b == nullptr)
+      return MT_ERR_CUDA;
+    fc = reinterpret_cast<CtxGetCurrentFn>(a);
+    fi = reinterpret_cast<CtxGetIdFn>(b);
+    get_current.store(fc, std::memory_order_release);
+    get_id.store(fi, std::memory_order_release);
+  }
+  void* ctx = nullptr;
+  if (fc(&ctx) != 0) return MT_ERR_CUDA;
+  if (ctx == nullptr) {
+    *none = true;
+    return MT_OK;
+  }
+  if (fi(ctx, id) != 0) return MT_ERR_CUDA;
+  return MT_OK;
+}
+
 int static_scan_scratch(void** out) {
-  int device = 0;
-  if (cudaGetDevice(&device) != cudaSuccess) return MT_ERR_CUDA;
-  if (device < 0 || device >= kStaticScanMaxDevices) return MT_ERR_INVALID_ARGUMENT;
-  void* p = g_static_scan_address[device].load(std::memory_order_acquire);
-  if (p == nullptr) {
-    std::lock_guard<std::mutex> lock(g_static_scan_setup);
-    p = g_static_scan_address[device].load(std::memory_order_relaxed);
-    if (p == nullptr) {
-      if (cudaGetSymbolAddress(&p, g_static_scan_scratch) != cudaSuccess || p == nullptr) return MT_ERR_CUDA;
-      g_static_scan_address[device].store(p, std::memory_order_release);
+  unsigned long long id = 0;
+  bool none = false;
+  int rc = current_context_id(&id, &none);
+  if (rc != MT_OK) return rc;
+  std::lock_guard<std::mutex> lock(g_static_scan_setup);
+  if (!none) {
+    for (int i = 0; i < g_static_scan_entries; ++i) {
+      if (g_static_scan_cache[i].context_id == id) {
+        *out = g_static_scan_cache[i].address;
+        return MT_OK;
+      }
     }
   }
+  // Set-up for this context (with no context current yet, this binds the
+  // runtime to the current device's primary context first).
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_static_scan_scratch) != cudaSuccess || p == nullptr) return MT_ERR_CUDA;
+  if (none) {
+    rc = current_context_id(&id, &none);
+    if (rc != MT_OK || none) return MT_ERR_CUDA;
+  }
+  // A full table forgets its oldest context (contexts that old are long gone
+  // in every realistic process).
+  if (g_static_scan_entries == kStaticScanMaxContexts) {
+    for (int i = 1; i < kStaticScanMaxContexts; ++i) g_static_scan_cache[i - 1] = g_static_scan_cache[i];
+    --g_static_scan_entries;
+  }
+  g_static_scan_cache[g_static_scan_entries++] = StaticScanEntry{id, p};
   *out = p;
   return MT_OK;
 }
@@ -247,6 +336,16 @@ int mt_exclusive_scan_i32_static(int32_t* data, int64_t n, mt_stream_t stream) {
   if (cudaMemsetAsync(scratch, 0, 4, mt::as_stream(stream)) != cudaSuccess) return MT_ERR_CUDA;
   return mt::launch_scan<int32_t, int32_t, false>(data, data, n, scratch, mt::kStaticScanBytes,
                                                   mt::as_stream(stream));
+}
+
+int mt_exclusive_scan_i32_static_status(int32_t* status_out, mt_stream_t stream) {
+  MT_REQUIRE(status_out != nullptr);
+  void* scratch = nullptr;
+  const int rc = mt::static_scan_scratch(&scratch);
+  if (rc != MT_OK) return rc;
+  if (cudaMemcpyAsync(status_out, scratch, 4, cudaMemcpyDefault, mt::as_stream(stream)) != cudaSuccess)
+    return MT_ERR_CUDA;
+  return MT_OK;
 }
 
 }  // extern "C"

@@ -43,6 +43,42 @@ def test_static_scan_matches_workspace_scan_on_consecutive_calls(cuda_device):
         np.testing.assert_array_equal(without.cpu().numpy(), expect)
 
 
+def test_static_scan_at_its_maximum_size(cuda_device):
+    """n equal to the limit uses the last descriptor slot of the fixed array."""
+    from meshtryoshka_gb300 import _native as nt
+
+    lib = nt.library()
+    n = lib.mt_exclusive_scan_i32_static_max_elements()
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    gen = torch.Generator(device=cuda_device).manual_seed(3)
+    x = torch.randint(0, 4, (n,), dtype=torch.int32, device=cuda_device, generator=gen)
+    host_in = x.cpu().numpy()
+    without = x.clone()
+    assert lib.mt_exclusive_scan_i32_static(without.data_ptr(), n, stream) == 0
+    ws = torch.zeros(lib.mt_scan_workspace_bytes(n), dtype=torch.uint8, device=cuda_device)
+    assert lib.mt_exclusive_scan_i32(x.data_ptr(), n, ws.data_ptr(), ws.numel(), stream) == 0  # in place
+    torch.cuda.synchronize(cuda_device)
+    assert torch.equal(x, without)
+    del x, ws
+    expect = np.cumsum(host_in, dtype=np.int64)
+    expect = np.concatenate(([0], expect[:-1])).astype(np.int32)
+    np.testing.assert_array_equal(without.cpu().numpy(), expect)
+
+
+def test_static_scan_status_word_reads_ok(cuda_device):
+    from meshtryoshka_gb300 import _native as nt
+
+    lib = nt.library()
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    x = torch.ones(100_000, dtype=torch.int32, device=cuda_device)
+    assert lib.mt_exclusive_scan_i32_static(x.data_ptr(), x.numel(), stream) == 0
+    status = torch.full((1,), -1, dtype=torch.int32, device=cuda_device)
+    assert lib.mt_exclusive_scan_i32_static_status(status.data_ptr(), stream) == 0
+    torch.cuda.synchronize(cuda_device)
+    assert int(status) == 0
+    assert int(x[-1]) == x.numel() - 1
+
+
 def test_static_scan_rejects_sizes_beyond_its_limit(cuda_device):
     from meshtryoshka_gb300 import _native as nt
 
