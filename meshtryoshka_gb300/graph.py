@@ -32,6 +32,7 @@ from torch import Tensor
 from . import _native as nt
 from . import pipeline
 from . import triangle_rasterization as tr
+from .record import recording
 
 
 # The tensors a graph reads in place: the parameters, and the per-step data
@@ -55,8 +56,13 @@ class CapturedTrainingStep:
     others."""
 
     def __init__(self, workload: pipeline.Workload, gradient_mode: str | None = None, margin: float = 1.25,
-                 capacities: pipeline.Capacities | None = None, warmup: int = 2, input_sets: int = 1):
+                 capacities: pipeline.Capacities | None = None, warmup: int = 2, input_sets: int = 1,
+                 record: bool = False):
         self.w = workload
+        # record: keep references to each graph's intermediate buffers
+        # (meshtryoshka_gb300.record) in self.records[set].
+        self.record = record
+        self.records: list[dict] = []
         self.gradient_mode = gradient_mode
         self.margin = margin
         self.warmup = warmup
@@ -107,15 +113,21 @@ class CapturedTrainingStep:
                 self._step()
             self._workspace = nt.workspace(device).buffer  # kept alive for the graphs
         torch.cuda.current_stream(device).wait_stream(self.stream)
-        self.graphs, self._outputs = [], []
+        self.graphs, self._outputs, self.records = [], [], []
         with nt.record_launches() as rec:
             for slot in range(len(self.inputs)):
                 g = torch.cuda.CUDAGraph()
+                store: dict = {}
                 with torch.cuda.graph(g, stream=self.stream):
                     # Loss, overflow flag and gradients written by every replay
                     # (graph-owned memory).
-                    self._outputs.append(self._step(slot))
+                    if self.record:
+                        with recording(store):
+                            self._outputs.append(self._step(slot))
+                    else:
+                        self._outputs.append(self._step(slot))
                 self.graphs.append(g)
+                self.records.append(store)
         self.launches_per_replay = rec.launches // len(self.inputs)
         self.graph = self.graphs[0]
         self._select(0)

@@ -23,6 +23,7 @@ from torch import Tensor
 from torch.profiler import record_function
 
 from .. import _native as nt
+from ..record import note
 
 __all__ = [
     "Voxels",
@@ -891,5 +892,8 @@ def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lowe
                 counts.num_faces.data_ptr() if counts is not None else None, nt.stream(device))
 
     logging.debug(f"Created {num_vertices} vertices and {num_faces} faces.")
+    note(vertex_offsets=vertex_offsets, face_offsets=face_offsets, faces=faces, voxel_indices=voxel_indices,
+         vertex_boundaries=vertex_boundaries, face_boundaries=face_boundaries, triangle_vertices=triangle_vertices,
+         triangle_signed_distances=triangle_sdf)
     return Triangles(triangle_vertices, triangle_sdf, triangle_sh, faces, voxel_indices, vertex_boundaries,
                      face_boundaries), counts

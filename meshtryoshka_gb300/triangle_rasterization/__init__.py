@@ -30,6 +30,7 @@ from torch import Tensor
 from torch.profiler import record_function
 
 from .. import _native as nt
+from ..record import note
 
 __all__ = [
     "render",
@@ -419,7 +420,10 @@ def _sort_and_delineate(paired_keys: PairedKeys, grid: TileGrid, key_defines,
     lib = nt.library()
     if n == 0 or not lib.mt_sort_keys_by_tile_supported(layout, int(separate_shells), b, n):
         paired = sort_keys(paired_keys, grid)
-        return paired, delineate_tiles(paired, grid, key_defines, separate_shells)
+        bounds = delineate_tiles(paired, grid, key_defines, separate_shells)
+        note(sorted_keys=paired.keys, sorted_triangles=paired.triangle_indices, tile_boundaries=bounds,
+             key_count=paired.count)
+        return paired, bounds
     device = nt.require_cuda(keys, tri)
     out_keys = torch.empty_like(keys)
     out_tri = torch.empty_like(tri)
@@ -428,6 +432,7 @@ def _sort_and_delineate(paired_keys: PairedKeys, grid: TileGrid, key_defines,
     nt.call("mt_sort_keys_by_tile", keys.data_ptr(), tri.data_ptr(), n, nt.ptr(paired_keys.count), layout,
             int(separate_shells), b, sd, t, out_keys.data_ptr(), out_tri.data_ptr(), bounds.data_ptr(), ws_ptr,
             ws_bytes, nt.stream(device))
+    note(sorted_keys=out_keys, sorted_triangles=out_tri, tile_boundaries=bounds, key_count=paired_keys.count)
     return PairedKeys(out_keys, out_tri, paired_keys.count), bounds
 
 
@@ -522,6 +527,7 @@ class IntersectAndComposite(torch.autograd.Function):
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
                     0.0, None, nt.ptr(hits), nt.stream(device))
+            note(composite=out)
             ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
@@ -588,6 +594,7 @@ class IntersectCompositeLoss(torch.autograd.Function):
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), nt.ptr(target),
                     nt.ptr(background), scale, loss.data_ptr(), nt.ptr(hits), nt.stream(device))
+            note(composite=out, loss=loss)
             ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,

@@ -20,9 +20,10 @@ The reference's module-level helpers in ``common.slang`` (64-bit indexing,
 DiffTensorView load/store) are replaced by equivalents in the shim; every
 kernel body is the reference's own code.
 
-Usage: ``python oracle/build_ref.py [reference root]`` (default: the mounted
-reference at /root/reference). Returns without building when the reference
-tree is absent.
+Usage: ``python oracle/build_ref.py [reference root]`` (default: the
+``MESHTRYOSHKA_REFERENCE`` environment variable, else a ``reference``
+checkout beside this repository). Returns without building when the
+reference tree is absent.
 """
 
 from __future__ import annotations
@@ -37,7 +38,8 @@ ORACLE_DIR = Path(__file__).resolve().parent
 OUT_DIR = ORACLE_DIR / "_ref"
 SHIM_DIR = ORACLE_DIR / "ref_shim"
 LIBRARY = OUT_DIR / "libref.so"
-DEFAULT_ROOT = Path("/root/reference")
+# A checkout of the reference next to this repository, when there is one.
+DEFAULT_ROOT = ORACLE_DIR.parent.parent / "reference"
 
 # (package, file) -> functions to drop (backward passes need Slang autodiff).
 SOURCES = {

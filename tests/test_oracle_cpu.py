@@ -13,7 +13,9 @@ import pytest
 from oracle import oracle
 from tests import semantics
 
-REFERENCE_CONSTANTS = "/root/reference/triangle_extraction/constants.slang"
+from oracle import build_ref
+
+REFERENCE_CONSTANTS = str(build_ref.reference_root() / "triangle_extraction" / "constants.slang")
 
 # FNV-1a checksums of the reference's FIRST_MARCHING_CUBES_ID[257] and
 # MARCHING_CUBES_IDS[2460] (triangle_extraction/constants.slang:1-142),
