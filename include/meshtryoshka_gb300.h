@@ -89,7 +89,6 @@ MT_API int mt_inclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t
 MT_API int mt_test_lookback_timeout(int32_t spin_limit, int64_t* prefix_out, void* workspace,
                              size_t workspace_bytes, mt_stream_t stream);
 
-
 /* Allocation-free exclusive scan (no counterpart in the reference). Same
  * result as mt_exclusive_scan_i32, for callers that cannot allocate device
  * memory for scratch: a plain C/C++ host with no device allocator of its own,
@@ -272,6 +271,25 @@ MT_API int mt_create_triangle_vertices_backward(
     int64_t V, int32_t* corner_inverse, float* grad_grid_vertices,
     float* grad_grid_signed_distances, float* grad_grid_spherical_harmonics,
     void* workspace, size_t workspace_bytes, mt_stream_t stream);
+
+/* Opt-in live marching-cubes weight (not in the reference, which detaches t
+ * at create_triangle_vertices.slang:92-96). Adds (+=) to
+ * grad_grid_signed_distances [G] the gradient that flows through
+ * t = (iso - d0) / (d1 - d0) when t is live: for every vertex with
+ * 0 < t < 1 and d0 != d1, dL/dt = grad_vertices . (p1 - p0) +
+ * sum_k grad_spherical_harmonics[k] . (sh1_k - sh0_k), scattered as
+ * -dL/dt (1 - t) / (d1 - d0) to the origin corner and -dL/dt t / (d1 - d0) to
+ * the axis corner. vertex_sources: the [3, V] (origin, axis corner, t bits)
+ * record written by mt_create_triangle_vertices; num_vertices: optional
+ * device count of live rows (NULL = V). Either gradient may be NULL. With t
+ * live the vertex SDF is the level set itself, so a caller combining this
+ * with mt_create_triangle_vertices_backward passes it no SDF gradient. */
+MT_API int mt_create_triangle_vertices_live_t_backward(
+    const float* grid_vertices, const float* grid_signed_distances,
+    const float* grid_spherical_harmonics, int32_t C, int64_t G,
+    const int32_t* vertex_sources, int64_t V, const int32_t* num_vertices,
+    const float* grad_vertices, const float* grad_spherical_harmonics,
+    float* grad_grid_signed_distances, mt_stream_t stream);
 
 /* Workspace for mt_create_triangle_vertices_backward's list form (S <= 21:
  * per-grid-vertex contribution lists, then a coalesced SH gather). With a
@@ -575,15 +593,21 @@ MT_API int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, i
  * loss_scale x sum over pixels and channels of
  * (clip(rgb + T * background, 0, 1) - target)^2, and the backward takes
  * d L / d loss from the device scalar grad_loss instead of grad_out.
- * hit_bits (not in the reference; NULL = off): uint32 scratch of
- * mt_composite_hit_bits_words(camera_tiles, tile_h, tile_w) words. The
- * forward stores there, for the first batches of triangles each warp walks,
- * the bits of the triangles each pixel hits; a backward on the same inputs
- * given the same buffer reads them instead of testing those batches again
- * (same bits, same gradients). camera_tiles: the total tiles over cameras
- * (B * rows * cols for a uniform grid).
+ * hit_bits (not in the reference; NULL = off): a hit-bit store of
+ * hit_bits_bytes bytes, 128-byte aligned; mt_composite_hit_bits_bytes gives
+ * the size that holds a number of batches. Each warp work item of the
+ * forward counts the keys it will walk, reserves ceil(count / 32) batches of
+ * the store and writes, per batch, the bits of the triangles each of its
+ * pixels hits, as long as the store has room (a 128-byte line per batch); a
+ * backward on the same inputs given the same buffer reads them instead of
+ * testing those batches again, and tests the rest (same bits, same
+ * gradients). Batches for K keys never exceed
+ * K * ceil(tile_h * tile_w / 32) / 32 + camera_tiles * ceil(tile_h * tile_w / 32).
+ * camera_tiles: the total tiles over cameras (B * rows * cols for a uniform
+ * grid).
  * ---------------------------------------------------------------------- */
-MT_API int64_t mt_composite_hit_bits_words(int64_t camera_tiles, int32_t tile_h, int32_t tile_w);
+MT_API size_t mt_composite_hit_bits_bytes(int64_t camera_tiles, int32_t tile_h, int32_t tile_w,
+                                          int64_t batches);
 
 MT_API int mt_intersect_and_composite_forward(
     const float* xy, const float* colors, const float* signed_distances, int64_t V,
@@ -593,12 +617,14 @@ MT_API int mt_intersect_and_composite_forward(
     int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H, int32_t W,
     const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
     uint32_t* warp_masks, uint64_t* work_counter, float* out, const float* target,
-    const float* background, float loss_scale, float* loss_sum, uint32_t* hit_bits,
+    const float* background, float loss_scale, float* loss_sum, void* hit_bits, size_t hit_bits_bytes,
     mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
- * same keys. exact_adjoint = 0 reproduces the reference's gradient routing
+ * same keys. ssaa (1 = none): with ssaa > 1 (uniform cameras, H and W
+ * multiples of ssaa) target is the factor written by mt_ssaa_loss and every
+ * sub-pixel takes 1 / ssaa^2 of its output pixel's d L / d image. exact_adjoint = 0 reproduces the reference's gradient routing
  * (the outer hit's deferred gradient is scattered with the current hit's
  * barycentric weights); 1 uses the outer hit's own weights. */
 MT_API int mt_intersect_and_composite_backward(
@@ -610,9 +636,21 @@ MT_API int mt_intersect_and_composite_backward(
     const int64_t* cameras, int64_t camera_tiles, const uint32_t* warp_masks,
     uint64_t* work_counter, const float* out, const float* grad_out,
     const float* target, const float* background, float loss_scale,
-    const float* grad_loss, float* grad_colors, float* grad_signed_distances,
-    float* grad_sharpness, int32_t exact_adjoint, const uint32_t* hit_bits,
+    const float* grad_loss, int32_t ssaa, float* grad_colors, float* grad_signed_distances,
+    float* grad_sharpness, int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
     mt_stream_t stream);
+
+/* MSE epilogue with SSAA (not in the reference, where the trainer applies
+ * triangle_rasterization/__init__.py:274-287 and the loss as tensor ops):
+ * raw [B,4,H,W] compositing output at the supersampled size; per output
+ * pixel of [B,3,H/ssaa,W/ssaa], the mean of rgb + T * background over its
+ * ssaa x ssaa sub-pixels, clipped to [0,1], against target. Sets the device
+ * scalar *loss = loss_scale x sum of squared errors and writes factor
+ * [B,3,H/ssaa,W/ssaa] = 2 (image - target) where the clip passes the
+ * gradient (else 0), for the compositing backward's ssaa mode. */
+MT_API int mt_ssaa_loss(const float* raw, int32_t B, int32_t H, int32_t W, int32_t ssaa,
+                        const float* background, const float* target, float loss_scale, float* loss,
+                        float* factor, mt_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Explicit mode (triangle_rasterization/__init__.py:22-164).

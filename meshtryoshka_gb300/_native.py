@@ -57,6 +57,7 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
         I32,
         [P, P, P, I32, P, I64, P, I32, P, I64, P, P, P, P, P, P, P],
     ),
+    "mt_create_triangle_vertices_live_t_backward": (I32, [P, P, P, I32, I64, P, I64, P, P, P, P, P]),
     "mt_create_triangle_vertices_backward": (
         I32,
         [P, I32, P, I64, P, I32, P, P, P, P, I64, P, P, P, P, P, c_size_t, P],
@@ -98,14 +99,15 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_intersect_and_composite_forward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
-         c_float, P, P, P],
+         c_float, P, P, c_size_t, P],
     ),
-    "mt_composite_hit_bits_words": (I64, [I64, I32, I32]),
+    "mt_composite_hit_bits_bytes": (c_size_t, [I64, I32, I32, I64]),
     "mt_intersect_and_composite_backward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P,
-         c_float, P, P, P, P, I32, P, P],
+         c_float, P, I32, P, P, P, I32, P, c_size_t, P],
     ),
+    "mt_ssaa_loss": (I32, [P, I32, I32, I32, I32, P, P, c_float, P, P, P]),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),
     "mt_interpolate_backward": (I32, [P, P, I32, I32, I32, I32, P, I64, P, P, P, P, P]),
@@ -154,7 +156,7 @@ KERNELS_PER_CALL = {
     "mt_sort_keys_by_tile": 7,  # count, scan, tile ranges, scatter, tiny / medium / small / large bin sorts
     "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys
     "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill
-    "mt_grid_sh_colors_backward": 2,  # per-vertex SH gradients, per-grid-vertex sums  # count, scan, tile ranges, scatter, small-bin and large-bin sorts
+    "mt_grid_sh_colors_backward": 2,  # per-vertex SH gradients, per-grid-vertex sums
 }
 
 

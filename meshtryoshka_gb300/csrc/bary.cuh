@@ -13,13 +13,26 @@
 
 namespace mt {
 
-struct TriGeom {
+// 64 bytes, 16-byte aligned: a staged triangle loads as four 16-byte words.
+struct alignas(16) TriGeom {
   float p1x, p1y, p2x, p2y;    // first two corners
   float e12x, e12y, e13x, e13y;  // edge vectors p2 - p1, p3 - p1
   float d1212, d1213, d1313, d1223;
   float d1323, dd, thr;  // dd = denom + 1e-8; thr = fast-reject threshold (or -inf)
   int shell;
 };
+
+// A staged triangle read from shared memory as four 16-byte loads.
+__device__ __forceinline__ TriGeom load_geom(const TriGeom* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 a = q[0], b = q[1], c = q[2], d = q[3];
+  TriGeom g;
+  g.p1x = a.x; g.p1y = a.y; g.p2x = a.z; g.p2y = a.w;
+  g.e12x = b.x; g.e12y = b.y; g.e13x = b.z; g.e13y = b.w;
+  g.d1212 = c.x; g.d1213 = c.y; g.d1313 = c.z; g.d1223 = c.w;
+  g.d1323 = d.x; g.dd = d.y; g.thr = d.z; g.shell = __float_as_int(d.w);
+  return g;
+}
 
 __device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) {
   return __fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by));
@@ -73,26 +86,46 @@ __device__ __forceinline__ void setup_geometry(float p1x, float p1y, float p2x, 
   g.thr = fast ? -__fmul_rn(dd, 0x1p-100f) : __int_as_float(0xff800000);
 }
 
-// Barycentric solve and acceptance test (intersect_and_composite.slang:65-136).
-__device__ __forceinline__ bool hit_test(const TriGeom& g, float px, float py, float& u, float& v, float& w) {
+// The three barycentric numerators of pixel (px, py)
+// (intersect_and_composite.slang:65-106).
+__device__ __forceinline__ void numerators(const TriGeom& g, float px, float py, float& un, float& vn, float& wn) {
   const float q1x = __fsub_rn(px, g.p1x), q1y = __fsub_rn(py, g.p1y);
   const float q2x = __fsub_rn(px, g.p2x), q2y = __fsub_rn(py, g.p2y);
   const float d1x12 = dot2(q1x, q1y, g.e12x, g.e12y);
   const float d1x13 = dot2(q1x, q1y, g.e13x, g.e13y);
   const float d2x12 = dot2(q2x, q2y, g.e12x, g.e12y);
   const float d2x13 = dot2(q2x, q2y, g.e13x, g.e13y);
-  const float vn = diff_of_products(g.d1313, d1x12, g.d1213, d1x13);
-  const float wn = diff_of_products(g.d1212, d1x13, g.d1213, d1x12);
-  const float un = diff_of_products(g.d1223, d2x13, g.d1323, d2x12);
-  if (un < g.thr || vn < g.thr || wn < g.thr) return false;
-  u = __fdiv_rn(un, g.dd);
-  v = __fdiv_rn(vn, g.dd);
-  w = __fdiv_rn(wn, g.dd);
+  vn = diff_of_products(g.d1313, d1x12, g.d1213, d1x13);
+  wn = diff_of_products(g.d1212, d1x13, g.d1213, d1x12);
+  un = diff_of_products(g.d1223, d2x13, g.d1323, d2x12);
+}
+
+// The fast reject: false when a numerator proves the quotient negative.
+// NaN numerators pass (the divisions below reject them).
+__device__ __forceinline__ bool numerators_pass(const TriGeom& g, float un, float vn, float wn) {
+  return !(un < g.thr || vn < g.thr || wn < g.thr);
+}
+
+// The divisions and the acceptance test of a pixel whose numerators passed
+// (intersect_and_composite.slang:107-136).
+__device__ __forceinline__ bool solve_and_accept(float un, float vn, float wn, float dd, float& u, float& v,
+                                                 float& w) {
+  u = __fdiv_rn(un, dd);
+  v = __fdiv_rn(vn, dd);
+  w = __fdiv_rn(wn, dd);
   const float sum = __fadd_rn(__fadd_rn(u, v), w);
   if (isnan(u) || isnan(v) || isnan(w)) return false;
   if (u < 0.0f || u > 1.0f || v < 0.0f || v > 1.0f || w < 0.0f || w > 1.0f) return false;
   if (sum < 0.999f || sum > 1.001f) return false;
   return true;
+}
+
+// Barycentric solve and acceptance test (intersect_and_composite.slang:65-136).
+__device__ __forceinline__ bool hit_test(const TriGeom& g, float px, float py, float& u, float& v, float& w) {
+  float un, vn, wn;
+  numerators(g, px, py, un, vn, wn);
+  if (!numerators_pass(g, un, vn, wn)) return false;
+  return solve_and_accept(un, vn, wn, g.dd, u, v, w);
 }
 
 // u * a + v * b + w * c, left to right (intersect_and_composite.slang:141-146).

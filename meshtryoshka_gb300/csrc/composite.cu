@@ -24,11 +24,13 @@
 // Per pixel, the three barycentric numerators reject most triangles before
 // any division (bary.cuh: hit_test).
 //
-// The forward stores each lane's hit bits for a warp's first kHitBatches
-// batches (optional hit_bits scratch); the backward re-walks the same way,
-// reads those bits instead of testing again (gathering only the triangles
-// some pixel hits), re-solves each hit's barycentrics and applies the suffix
-// trick of the reference. Per-triangle gradient sums live in a per-warp ring
+// The forward stores each lane's hit bits (optional hit-bit store): every
+// work item counts the keys its warp will walk, reserves exactly that many
+// batches (a bump allocator) and writes one 32-word line per batch while the
+// store's capacity lasts; the backward re-walks the same way, reads those
+// bits instead of testing again (gathering only the triangles some pixel
+// hits), re-solves each hit's barycentrics and applies the suffix trick of
+// the reference. Batches past the capacity are tested again. Per-triangle gradient sums live in a per-warp ring
 // of 64 shared-memory slots (the current and the previous batch); a slot is
 // flushed to global memory with one atomic per non-zero scalar when its batch
 // retires, and gradients for older triangles go to global memory directly.
@@ -53,10 +55,19 @@ constexpr int kQueue = 64;   // queued key offsets per warp
 constexpr int kRing = 64;    // gradient slots per warp (two batches)
 constexpr int kSavedFwd = 4;  // hits per lane per batch whose (u, v, w) the test phase keeps (forward)
 constexpr int kSavedBwd = 3;  // same, backward (its shared memory is tighter)
-// Batches per work item whose per-lane hit bits the forward stores for the
-// backward (which then skips their test phase); later batches are tested
-// again.
-constexpr int kHitBatches = 32;
+// Hit-bit store (bytes): [0, 8) batch allocator, [8, 8 + 4 items) first
+// stored batch of each work item (int32, -1 = none), then from a 128-byte
+// boundary `capacity` batches of 32 words (one per lane).
+struct HitStore {
+  unsigned long long* next;
+  int32_t* item_base;
+  uint32_t* batches;  // NULL: no store
+  int64_t capacity;
+};
+
+__host__ __device__ constexpr size_t hit_store_header(int64_t items) {
+  return ((size_t)(8 + 4 * items) + 127) / 128 * 128;
+}
 
 // The (u, v, w) of the first K hits each lane finds in a batch, so that the
 // hit phase does not solve them again (later hits are re-solved).
@@ -65,10 +76,18 @@ struct SavedHits {
   float u[K][32], v[K][32], w[K][32];
 };
 
-struct TriAttr {
+struct alignas(16) TriAttr {
   float ca[3], cb[3], cc[3];
   float sa, sb, sc;
 };
+
+// A (pixel, triangle) pair of the forward's test phase whose numerators
+// passed the fast reject; its divisions and acceptance test are pending.
+struct alignas(16) Candidate {
+  int id;  // pixel lane | triangle << 5 | the lane's candidate ordinal << 10
+  float un, vn, wn;
+};
+constexpr int kCandRing = 64;  // ring of pending candidates per warp (solved 32 at a time)
 
 struct CompositeArgs {
   const float* xy;      // [B, V, 2]
@@ -97,6 +116,10 @@ struct CompositeArgs {
   const float* target;
   const float* background;
   float loss_scale;
+  // SSAA factor of the epilogue's backward (1: none). With ssaa > 1 the
+  // backward's `target` is the per-output-pixel factor written by
+  // ssaa_loss_kernel, [B, 3, H / ssaa, W / ssaa].
+  int ssaa;
 };
 
 struct CompositeGrads {
@@ -113,6 +136,8 @@ struct WarpForward {
   TriGeom geo[kBatch];
   TriAttr attr[kBatch];
   SavedHits<kSavedFwd> saved;
+  Candidate cand[kCandRing];
+  uint32_t rejected[32];  // per lane: candidates that failed the full test
   int queue[kQueue];
 };
 
@@ -330,6 +355,71 @@ __device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float
   return hits;
 }
 
+// Solves `count` (<= 32) pending candidates starting at ring position
+// `head`, one per lane: the divisions and the acceptance test of hit_test. A
+// rejected candidate sets its triangle's bit in its pixel's `rejected` word;
+// an accepted one among its pixel's first K candidates keeps its (u, v, w).
+template <int K>
+__device__ __forceinline__ void solve_candidates(WarpForward& ws, int head, int count, int lane) {
+  if (lane < count) {
+    const Candidate c = ws.cand[(head + lane) & (kCandRing - 1)];
+    const int pl = c.id & 31, i = (c.id >> 5) & 31, n = c.id >> 10;
+    float u, v, w;
+    if (solve_and_accept(c.un, c.vn, c.wn, ws.geo[i].dd, u, v, w)) {
+      if (n < K) {
+        ws.saved.u[n][pl] = u;
+        ws.saved.v[n][pl] = v;
+        ws.saved.w[n][pl] = w;
+      }
+    } else {
+      atomicOr(&ws.rejected[pl], 1u << i);
+    }
+  }
+}
+
+// Test phase of a batch with the divisions dealt across the warp. Every lane
+// evaluates the numerators of every staged triangle (the whole warp busy);
+// the (pixel, triangle) pairs that pass the fast reject are queued in a ring
+// and solved 32 at a time, one per lane, instead of by the few lanes whose
+// pixels a triangle covers while the others idle. Triangles of shells the
+// pixel has already passed are skipped, as in batch_hits. Returns the lane's
+// candidate bits (bit i: triangle i passed the fast reject) and sets `hits`
+// to those that passed the full test: the decisions and (u, v, w) of
+// hit_test, the (u, v, w) kept by candidate ordinal.
+__device__ __forceinline__ uint32_t dealt_batch_hits(WarpForward& ws, int nb, float fx, float fy, int last_shell,
+                                                     bool active, int lane, uint32_t& hits) {
+  const uint32_t lt = lanemask_lt();
+  ws.rejected[lane] = 0u;
+  uint32_t cand = 0;
+  int n = 0, head = 0, tail = 0;
+  for (int i = 0; i < nb; ++i) {
+    const TriGeom g = load_geom(&ws.geo[i]);
+    float un, vn, wn;
+    numerators(g, fx, fy, un, vn, wn);
+    const bool pass = active && g.shell > last_shell && numerators_pass(g, un, vn, wn);
+    const uint32_t m = __ballot_sync(0xffffffffu, pass);
+    if (pass) {
+      ws.cand[(tail + __popc(m & lt)) & (kCandRing - 1)] = Candidate{lane | (i << 5) | (n << 10), un, vn, wn};
+      cand |= 1u << i;
+      ++n;
+    }
+    tail += __popc(m);
+    if (tail - head >= 32) {  // at most 63 pending: one round empties below 32
+      __syncwarp();
+      solve_candidates<kSavedFwd>(ws, head, 32, lane);
+      head += 32;
+      __syncwarp();
+    }
+  }
+  if (tail > head) {
+    __syncwarp();
+    solve_candidates<kSavedFwd>(ws, head, tail - head, lane);
+  }
+  __syncwarp();
+  hits = cand & ~ws.rejected[lane];
+  return cand;
+}
+
 // (u, v, w) of the lane's n-th hit in the batch (triangle g): kept by the
 // test phase, or solved again.
 template <int K>
@@ -430,9 +520,29 @@ __device__ __forceinline__ const float* target_of(const CompositeArgs& a, const 
 }
 
 // Returns the pixel's sum of squared errors when the epilogue is on.
+// Reserves the work item's batches in the hit-bit store: the number of keys
+// of the tile whose mask has this warp's bit, in batches of kBatch (the walk
+// forms exactly that many batches or stops earlier). Returns the item's first
+// stored batch, or -1 when nothing is stored; records it for the backward.
+__device__ __forceinline__ int64_t reserve_hit_batches(const HitStore& hs, const uint32_t* __restrict__ masks,
+                                                       int64_t start, int64_t end, int wt, int64_t item, int lane) {
+  int keys = 0;
+  for (int64_t k0 = start; k0 < end; k0 += 32) {
+    const int64_t k = k0 + lane;
+    keys += __popc(__ballot_sync(0xffffffffu, k < end && ((__ldg(masks + k) >> wt) & 1u)));
+  }
+  const unsigned long long batches = (unsigned long long)((keys + kBatch - 1) / kBatch);
+  unsigned long long base = 0;
+  if (lane == 0 && batches > 0) base = atomicAdd(hs.next, batches);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const int64_t first = (batches > 0 && base < (unsigned long long)hs.capacity) ? (int64_t)base : -1;
+  if (lane == 0) hs.item_base[item] = (int32_t)first;
+  return first;
+}
+
 __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
                                               float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane,
-                                              int64_t item, uint32_t* __restrict__ hit_bits) {
+                                              int64_t item, const HitStore& hs) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -448,6 +558,7 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   int64_t next = start;
   int queued = 0;
   int batch = 0;
+  const int64_t hit_base = hs.batches ? reserve_hit_batches(hs, masks, start, end, px.wt, item, lane) : -1;
   while (__any_sync(0xffffffffu, active)) {
     queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
     const int nb = min(queued, kBatch);
@@ -455,15 +566,17 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
     if (lane < nb) gather(a, px.cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
-    uint32_t hits = active ? batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane) : 0u;
-    if (hit_bits && batch < kHitBatches) __stcs(hit_bits + (item * kHitBatches + batch) * 32 + lane, hits);
+    uint32_t hits = 0;
+    uint32_t cand = dealt_batch_hits(ws, nb, px.fx, px.fy, last_shell, active, lane, hits);
+    if (hit_base >= 0 && hit_base + batch < hs.capacity) __stcs(hs.batches + (hit_base + batch) * 32 + lane, hits);
     ++batch;
     if (active) {
       int n = 0;
-      while (hits) {
-        const int i = __ffs(hits) - 1;
-        hits &= hits - 1;
-        const int k = n++;
+      while (cand) {
+        const int i = __ffs(cand) - 1;
+        cand &= cand - 1;
+        const int k = n++;  // candidate ordinal: the index of kept (u, v, w)
+        if (!((hits >> i) & 1u)) continue;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
         float u, v, w;
@@ -513,14 +626,14 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
 __global__ void __launch_bounds__(kCtaThreads, 4)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
                              unsigned long long* __restrict__ counter, float* __restrict__ loss_sum,
-                             uint32_t* __restrict__ hit_bits) {
+                             HitStore hs) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   float sq = 0.0f;
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hit_bits);
+    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs);
   if (a.target) {  // one atomic per warp for the whole launch
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
@@ -578,7 +691,7 @@ __device__ __forceinline__ void flush_half(const CompositeArgs& a, const Composi
 
 __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
                                               const CompositeGrads& gr, WarpBackward& ws, const Pixel& px, int lane,
-                                              int64_t item, const uint32_t* __restrict__ hit_bits) {
+                                              int64_t item, const HitStore& hs) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -590,7 +703,20 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
 #pragma unroll
     for (int c = 0; c < 3; ++c) final_rgb[c] = a.out[o + c * px.plane];
     final_T = a.out[o + 3 * px.plane];
-    if (a.target) {
+    if (a.target && a.ssaa > 1) {
+      // SSAA: every sub-pixel gets 1 / ssaa^2 of its output pixel's
+      // d loss / d image, through the background blend.
+      const int f = a.ssaa;
+      const int64_t wo = px.width / f, plane_out = (int64_t)(px.plane / ((int64_t)f * f));
+      const float* g = a.target + (int64_t)px.cam * 3 * plane_out + (int64_t)(px.py / f) * wo + px.px / f;
+      const float gscale = a.loss_scale * *gr.grad_loss / (float)(f * f);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float x = gscale * g[c * plane_out];
+        dL_rgb[c] = x;
+        dL_T += x * a.background[c];
+      }
+    } else if (a.target) {
       // d loss / d image = 2 (image - target) loss_scale, through the clip
       // and the background blend.
       const float gscale = 2.0f * a.loss_scale * *gr.grad_loss;
@@ -633,6 +759,7 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
   int64_t next = start;
   int queued = 0;
   int batch = 0;
+  const int64_t hit_base = hs.batches ? (int64_t)hs.item_base[item] : -1;
   while (__any_sync(0xffffffffu, active)) {
     queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
     const int nb = min(queued, kBatch);
@@ -644,8 +771,8 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
     // walk, so the same bits); otherwise the test phase runs again. With
     // stored bits only the triangles that some pixel of the warp hits are
     // gathered (the other slots are never read).
-    const bool stored = hit_bits != nullptr && batch < kHitBatches;
-    uint32_t hits = stored ? __ldcs(hit_bits + (item * kHitBatches + batch) * 32 + lane) : 0u;
+    const bool stored = hit_base >= 0 && hit_base + batch < hs.capacity;
+    uint32_t hits = stored ? __ldcs(hs.batches + (hit_base + batch) * 32 + lane) : 0u;
     const uint32_t needed = stored ? __reduce_or_sync(0xffffffffu, hits) : 0xffffffffu;
     if (lane < nb && ((needed >> lane) & 1u))
       ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
@@ -753,13 +880,58 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
 
 __global__ void __launch_bounds__(kCtaThreads)
     composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr,
-                              unsigned long long* __restrict__ counter, const uint32_t* __restrict__ hit_bits) {
+                              unsigned long long* __restrict__ counter, HitStore hs) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    backward_item(a, masks, gr, ws, pixel_of(a, item), lane, item, hit_bits);
+    backward_item(a, masks, gr, ws, pixel_of(a, item), lane, item, hs);
+}
+
+// The MSE epilogue with SSAA (triangle_rasterization/__init__.py:274-287
+// followed by the trainer's MSE): per output pixel, the mean over its
+// ssaa x ssaa sub-pixels of rgb + T * background, clipped to [0, 1], against
+// the target; loss += loss_scale x sum of squared errors (one atomic per CTA),
+// and factor = 2 (image - target) where the clip passes the gradient, else 0
+// (the backward scales it by loss_scale x d L / d loss / ssaa^2).
+__global__ void ssaa_loss_kernel(const float* __restrict__ raw, int B, int H, int W, int f,
+                                 const float* __restrict__ background, const float* __restrict__ target,
+                                 float loss_scale, float* __restrict__ loss, float* __restrict__ factor) {
+  const int ho = H / f, wo = W / f;
+  const int64_t plane = (int64_t)H * W, plane_out = (int64_t)ho * wo;
+  const int64_t n = (int64_t)B * plane_out;
+  const float inv = 1.0f / (float)(f * f);
+  float sq = 0.0f;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = o / plane_out, r = o - b * plane_out;
+    const int y = (int)(r / wo), x = (int)(r - (int64_t)y * wo);
+    const float* src = raw + b * 4 * plane;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float acc = 0.0f;
+      for (int dy = 0; dy < f; ++dy) {
+        const int64_t row = (int64_t)(y * f + dy) * W + (int64_t)x * f;
+        for (int dx = 0; dx < f; ++dx)
+          acc += __fadd_rn(src[c * plane + row + dx], __fmul_rn(src[3 * plane + row + dx], background[c]));
+      }
+      const float mean = acc * inv;
+      const bool inside = mean >= 0.0f && mean <= 1.0f;
+      const float d = fminf(fmaxf(mean, 0.0f), 1.0f) - target[(b * 3 + c) * plane_out + r];
+      sq += d * d;
+      factor[(b * 3 + c) * plane_out + r] = inside ? 2.0f * d : 0.0f;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  __shared__ float part[8];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sq;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    if (t != 0.0f) atomicAdd(loss, t * loss_scale);
+  }
 }
 
 int check_args(const CompositeArgs& a) {
@@ -796,12 +968,30 @@ int persistent_ctas(const CompositeArgs& a, size_t smem, int64_t& ctas) {
 }
 
 
+// The hit-bit store of `bytes` bytes at `base` for the launch's work items
+// (NULL base or too few bytes for one batch: no store).
+int make_hit_store(const CompositeArgs& a, void* base, size_t bytes, HitStore& hs) {
+  hs = HitStore{nullptr, nullptr, nullptr, 0};
+  if (base == nullptr) return MT_OK;
+  if ((reinterpret_cast<uintptr_t>(base) & 127) != 0) return MT_ERR_INVALID_ARGUMENT;
+  const int64_t items = a.total_tiles * ((a.tile_h * a.tile_w + 31) / 32);
+  const size_t header = hit_store_header(items);
+  if (bytes < header + 128) return MT_OK;
+  int64_t cap = (int64_t)((bytes - header) / 128);
+  if (cap > 0x7fffffff) cap = 0x7fffffff;  // item bases are int32
+  char* p = static_cast<char*>(base);
+  hs = HitStore{reinterpret_cast<unsigned long long*>(p), reinterpret_cast<int32_t*>(p + 8),
+                reinterpret_cast<uint32_t*>(p + header), cap};
+  return MT_OK;
+}
+
 CompositeArgs make_args(const float* xy, const float* colors, const float* sdf, int64_t V, const int32_t* faces,
                         const float* sharpness, const int64_t* keys, const int32_t* tri, const int64_t* bounds,
                         int32_t B, int32_t S, int32_t rows, int32_t cols, int32_t tile_h, int32_t tile_w, int32_t H,
                         int32_t W, const int32_t* layout, const float* out, const int64_t* cameras,
                         int64_t camera_tiles) {
   CompositeArgs a{};
+  a.ssaa = 1;
   a.target = nullptr;
   a.background = nullptr;
   a.loss_scale = 0.0f;
@@ -841,9 +1031,11 @@ using namespace mt;
 
 extern "C" {
 
-int64_t mt_composite_hit_bits_words(int64_t camera_tiles, int32_t tile_h, int32_t tile_w) {
-  if (camera_tiles <= 0 || tile_h <= 0 || tile_w <= 0) return 0;
-  return camera_tiles * (((int64_t)tile_h * tile_w + 31) / 32) * kHitBatches * 32;
+size_t mt_composite_hit_bits_bytes(int64_t camera_tiles, int32_t tile_h, int32_t tile_w, int64_t batches) {
+  if (camera_tiles <= 0 || tile_h <= 0 || tile_w <= 0 || batches <= 0) return 0;
+  if (batches > 0x7fffffff) batches = 0x7fffffff;
+  const int64_t items = camera_tiles * (((int64_t)tile_h * tile_w + 31) / 32);
+  return hit_store_header(items) + (size_t)batches * 128;
 }
 
 int mt_intersect_and_composite_forward(const float* xy, const float* colors, const float* signed_distances,
@@ -855,7 +1047,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
                                        uint64_t* work_counter, float* out, const float* target,
                                        const float* background, float loss_scale, float* loss_sum,
-                                       uint32_t* hit_bits, mt_stream_t stream) {
+                                       void* hit_bits, size_t hit_bits_bytes, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
@@ -871,6 +1063,10 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
+  HitStore hs;
+  rc = make_hit_store(a, hit_bits, hit_bits_bytes, hs);
+  if (rc != MT_OK) return rc;
+  if (hs.next && cudaMemsetAsync(hs.next, 0, 8, s) != cudaSuccess) return MT_ERR_CUDA;
   if (K > 0) {
     warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
     MT_CHECK_LAUNCH();
@@ -883,7 +1079,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
   if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   composite_forward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hit_bits);
+      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hs);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }
@@ -897,8 +1093,10 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         int64_t camera_tiles, const uint32_t* warp_masks, uint64_t* work_counter,
                                         const float* out, const float* grad_out, const float* target,
                                         const float* background, float loss_scale, const float* grad_loss,
-                                        float* grad_colors, float* grad_signed_distances, float* grad_sharpness,
-                                        int32_t exact_adjoint, const uint32_t* hit_bits, mt_stream_t stream) {
+                                        int32_t ssaa, float* grad_colors, float* grad_signed_distances,
+                                        float* grad_sharpness,
+                                        int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
+                                        mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out,
@@ -906,14 +1104,19 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   a.target = target;
   a.background = background;
   a.loss_scale = loss_scale;
+  a.ssaa = ssaa;
   int rc = check_args(a);
   if (rc != MT_OK) return rc;
+  MT_REQUIRE(ssaa >= 1 && (ssaa == 1 || (target && !cameras && H % ssaa == 0 && W % ssaa == 0)));
   if (a.total_tiles == 0 || H == 0 || W == 0) return MT_OK;
   MT_REQUIRE(xy && colors && signed_distances && faces && sharpness && tile_boundaries && out);
   MT_REQUIRE(target ? (background && grad_loss) : grad_out != nullptr);
   MT_REQUIRE(grad_colors && grad_signed_distances && grad_sharpness && work_counter);
   MT_REQUIRE(K == 0 || (sorted_keys && sorted_triangles && warp_masks));
   CompositeGrads gr{grad_loss, grad_out, grad_colors, grad_signed_distances, grad_sharpness, exact_adjoint ? 1 : 0};
+  HitStore hs;
+  rc = make_hit_store(a, const_cast<void*>(hit_bits), hit_bits_bytes, hs);
+  if (rc != MT_OK) return rc;
   const size_t smem = sizeof(WarpBackward) * kWarpsPerCta;
   cudaStream_t s = as_stream(stream);
   rc = set_smem<composite_backward_kernel>(smem);
@@ -923,7 +1126,21 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   composite_backward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hit_bits);
+      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hs);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_ssaa_loss(const float* raw, int32_t B, int32_t H, int32_t W, int32_t ssaa, const float* background,
+                 const float* target, float loss_scale, float* loss, float* factor, mt_stream_t stream) {
+  MT_REQUIRE(B >= 0 && H >= 0 && W >= 0 && ssaa >= 1 && H % ssaa == 0 && W % ssaa == 0 && loss != nullptr);
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess) return MT_ERR_CUDA;
+  const int64_t n = (int64_t)B * (H / ssaa) * (W / ssaa);
+  if (n == 0) return MT_OK;
+  MT_REQUIRE(raw && background && target && factor);
+  ssaa_loss_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(raw, B, H, W, ssaa, background, target, loss_scale,
+                                                              loss, factor);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

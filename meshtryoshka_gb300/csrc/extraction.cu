@@ -405,6 +405,51 @@ __global__ void interpolate_vertex_sh_kernel(const float* __restrict__ gsh, int 
 }
 
 // ---------------------------------------------------------------------------
+// Live marching-cubes weight (not in the reference, which detaches t at
+// create_triangle_vertices.slang:92-96). With t = (iso - d0) / (d1 - d0) live,
+// a vertex's position and SH depend on its two corner SDFs through t:
+//   dL/dt = g_pos . (p1 - p0) + sum_k g_sh_k . (sh1_k - sh0_k),
+//   dt/dd0 = -(1 - t) / (d1 - d0),  dt/dd1 = -t / (d1 - d0),
+// and its SDF, d0 + t (d1 - d0) = iso, does not depend on them at all. t is
+// constant where the reference clamps it or sets it to 0.5 (d0 == d1), so
+// only 0 < t < 1 contributes. One thread per vertex adds the two corner
+// terms to the grid SDF gradient with atomics. Rows have stride V; only the
+// first `count` vertices (device value; all V when NULL) are real.
+// ---------------------------------------------------------------------------
+__global__ void live_t_backward_kernel(const float* __restrict__ gv, const float* __restrict__ gsdf,
+                                       const float* __restrict__ gsh, int C, int64_t G,
+                                       const int32_t* __restrict__ sources, int64_t V,
+                                       const int32_t* __restrict__ count, const float* __restrict__ grad_v,
+                                       const float* __restrict__ grad_sh, float* __restrict__ grad_gsdf) {
+  const int64_t n = count ? min((int64_t)max(*count, 0), V) : V;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i0 = __ldg(sources + v), i1 = __ldg(sources + V + v);
+    const float t = __int_as_float(__ldg(sources + 2 * V + v));
+    const float d0 = __ldg(gsdf + i0), d1 = __ldg(gsdf + i1);
+    if (!(t > 0.0f && t < 1.0f) || d0 == d1) continue;
+    float dldt = 0.0f;
+    if (grad_v) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        dldt += __ldg(grad_v + 3 * v + c) * (__ldg(gv + 3 * (int64_t)i1 + c) - __ldg(gv + 3 * (int64_t)i0 + c));
+    }
+    if (grad_sh) {
+      for (int k = 0; k < C; ++k) {
+        const float* g = grad_sh + ((int64_t)k * V + v) * 3;
+        const float* p0 = gsh + ((int64_t)k * G + i0) * 3;
+        const float* p1 = gsh + ((int64_t)k * G + i1) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dldt += __ldg(g + c) * (__ldg(p1 + c) - __ldg(p0 + c));
+      }
+    }
+    if (dldt == 0.0f) continue;
+    const float q = dldt / (d1 - d0);
+    atomicAdd(grad_gsdf + i0, -q * (1.0f - t));
+    atomicAdd(grad_gsdf + i1, -q * t);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // create_triangle_vertices.slang:201-291 (backward) as a gather. The detached
 // weight t routes d(vertex) to the origin corner with (1 - t) and to the axis
 // corner with t. Grid vertex x receives from the vertices of the one entry
@@ -1438,6 +1483,23 @@ int mt_count_triangle_vertices(const float* signed_distances, const int32_t* low
   MT_REQUIRE(S == 0 || level_sets);
   count_vertices_kernel<<<grid_stride_blocks(G, 256), 256, 0, as_stream(stream)>>>(signed_distances, lower_corners, G,
                                                                                   level_sets, S, counts);
+  MT_CHECK_LAUNCH();
+  return MT_OK;
+}
+
+int mt_create_triangle_vertices_live_t_backward(const float* grid_vertices, const float* grid_signed_distances,
+                                                const float* grid_spherical_harmonics, int32_t C, int64_t G,
+                                                const int32_t* vertex_sources, int64_t V, const int32_t* num_vertices,
+                                                const float* grad_vertices, const float* grad_spherical_harmonics,
+                                                float* grad_grid_signed_distances, mt_stream_t stream) {
+  MT_REQUIRE(G >= 0 && V >= 0 && C >= 1);
+  if (V == 0 || G == 0 || (grad_vertices == nullptr && grad_spherical_harmonics == nullptr)) return MT_OK;
+  MT_REQUIRE(grid_signed_distances && vertex_sources && grad_grid_signed_distances);
+  MT_REQUIRE(grad_vertices == nullptr || grid_vertices != nullptr);
+  MT_REQUIRE(grad_spherical_harmonics == nullptr || grid_spherical_harmonics != nullptr);
+  live_t_backward_kernel<<<grid_stride_blocks(V, 256), 256, 0, as_stream(stream)>>>(
+      grid_vertices, grid_signed_distances, grid_spherical_harmonics, C, G, vertex_sources, V, num_vertices,
+      grad_vertices, grad_spherical_harmonics, grad_grid_signed_distances);
   MT_CHECK_LAUNCH();
   return MT_OK;
 }

@@ -37,6 +37,7 @@ class Workload:
     image_shapes: tuple[tuple[int, int], ...] | None = None  # cameras of different sizes
     tile_shape: tuple[int, int] = (16, 16)
     fused_loss: bool = True  # fused render: blend, clip and MSE inside the compositing kernels
+    ssaa: int = 1  # supersampling factor of the render (the trainer's train_ssaa)
 
     @property
     def sh_degree(self) -> int:
@@ -104,7 +105,7 @@ def _fused_loss(w: Workload, tri, vertices, gradient_mode, **counted) -> Tensor:
     return tr.render_fused_loss(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
                                 tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness,
                                 w.background, w.target, tile_shape=w.tile_shape, gradient_mode=gradient_mode,
-                                camera_shapes=w.image_shapes, **counted)
+                                camera_shapes=w.image_shapes, ssaa=w.ssaa, **counted)
 
 
 def _render(w: Workload, tri, vertices, gradient_mode, mode="fused", **counted):
@@ -118,7 +119,7 @@ def _render(w: Workload, tri, vertices, gradient_mode, mode="fused", **counted):
                                tile_shape=w.tile_shape, gradient_mode=gradient_mode, **counted)
     return tr.render(w.extrinsics, w.intrinsics, w.image_shape, vertices, tri.faces, tri.face_boundaries,
                      tri.signed_distances, tri.spherical_harmonics, w.sh_degree, w.sharpness, w.background,
-                     tile_shape=w.tile_shape, mode=mode, gradient_mode=gradient_mode)
+                     tile_shape=w.tile_shape, mode=mode, gradient_mode=gradient_mode, ssaa=w.ssaa)
 
 
 @dataclass(frozen=True)
@@ -235,9 +236,11 @@ def per_camera_training_step(w: Workload, gradient_mode: str | None = None) -> T
     return loss
 
 
-def algorithmic_bytes(stats: dict) -> dict[str, float]:
-    """Compulsory traffic per stage (each input read once, each output
-    written once, gathers counted once per consumer), from the measured sizes."""
+def reference_algorithm_bytes(stats: dict) -> dict[str, float]:
+    """Compulsory traffic per stage of the reference's algorithm (eight radix
+    passes over 24-byte key pairs, per-vertex SH rows formed and read back,
+    delineation as its own pass), from the measured sizes. Each input read
+    once, each output written once, gathers counted once per consumer."""
     G, Nv, V, F, C, S, B, P, K, T = (stats[k] for k in ("G", "Nv", "V", "F", "C", "S", "B", "P", "K", "T"))
     passes = 8
     return {
@@ -255,6 +258,43 @@ def algorithmic_bytes(stats: dict) -> dict[str, float]:
         "composite_bwd": K * 96 + 32 * P + 16 * V * B,
         "sh_bwd": 12 * B * V + 24 * C * V,
         "create_vertices_bwd": V * (16 + 12 * C) + G * 4 * (4 + 12 + 12 * C),
+    }
+
+
+def step_bytes(stats: dict) -> dict[str, float]:
+    """Compulsory traffic of the kernels the captured training step runs
+    (``graph.CapturedTrainingStep``: deferred SH, the contribution list, the
+    capacity-mode keys, the tile-bucketed sort, warp masks, the compositing
+    kernels with the MSE epilogue), from the measured sizes. Each input read
+    once, each output written once, gathers counted once per consumer;
+    scratch that only speeds a kernel up (stored hit bits) is not counted."""
+    G, Nv, V, F, C, S, B, P, K, T = (stats[k] for k in ("G", "Nv", "V", "F", "C", "S", "B", "P", "K", "T"))
+    return {
+        # tessellation
+        "count_vertices": G * (16 + 16) + 4 * S * G,
+        "scans": 8 * S * G + 8 * S * Nv,
+        # per entry: 4 corner ids, 4 SDFs, 4 positions, its offsets; per
+        # vertex: position, SDF, type, source record (origin, corner, t)
+        "create_vertices": G * (16 + 4 * (4 + 12) + 4 * S) + V * (12 + 4 + 1 + 12),
+        # corner inverse, per-entry list counts, their scan, list fill
+        "contribution_list": G * (16 + 16) + G * (16 + 4) + 8 * G + G * 16 + 16 * V,
+        "count_faces": Nv * (32 + 32) + 5 * S * Nv,
+        "create_faces": Nv * (28 + 4 + S) + 8 * S * Nv + 16 * F,
+        # render front end
+        "uncontract": 24 * V,
+        "project": 12 * V + 12 * B * V,
+        "grid_sh_colors": V * (12 + 12) + 2 * 12 * C * V + 12 * B * V,
+        "keys": B * F * (12 + 36 + 20) + B * F * 20 + 12 * K,
+        "tile_sort": 60 * K + 16 * B * T,
+        "warp_masks": K * (8 + 4 + 12 + 24) + 4 * K,
+        # compositing with the MSE epilogue (target read, output written)
+        "composite_fwd": K * 96 + 16 * P + 12 * P,
+        "gradient_zero_fill": 12 * B * V + 4 * V,
+        "composite_bwd": K * 96 + 16 * P + 12 * P + 16 * V * B,
+        # grid SH gradient: per-vertex SH gradient once, then per grid vertex
+        # the weighted sum over its list entries
+        "grid_sh_bwd": 12 * B * V + 24 * V + 12 * C * V + 16 * V + 2 * 12 * C * V + 12 * C * G,
+        "grid_sdf_bwd": 16 * V + 4 * V + 16 * G,
     }
 
 

@@ -519,11 +519,15 @@ class CreateTriangleVerticesResult(NamedTuple):
 
 class CreateTriangleVertices(torch.autograd.Function):
     """create_triangle_vertices.py:30-170: vertices on crossing edges, with the
-    MC weight t detached (gradients reach both edge corners with (1-t, t))."""
+    MC weight t detached (gradients reach both edge corners with (1-t, t)).
+
+    ``live_t`` (not in the reference): t = (iso - d0) / (d1 - d0) is
+    differentiated too, so the positions and SH of a vertex also depend on
+    its corner SDFs through t, and its SDF (= the level set) on nothing."""
 
     @staticmethod
     def forward(ctx, grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners,
-                level_sets, vertex_offsets, num_vertices=None, capacity=None, deferred=None):
+                level_sets, vertex_offsets, num_vertices=None, capacity=None, deferred=None, live_t=False):
         with record_function("create_triangle_vertices_forward"):
             grid_vertices = _f32(grid_vertices, "grid_vertices")
             grid_signed_distances = _f32(grid_signed_distances, "grid_signed_distances")
@@ -578,6 +582,11 @@ class CreateTriangleVertices(torch.autograd.Function):
                 ctx.mark_non_differentiable(sh)
             ctx.save_for_backward(grid_signed_distances, voxel_lower_corners, level_sets, vertex_offsets)
             ctx.shapes = (grid_vertices.shape, grid_spherical_harmonics.shape, v)
+            ctx.live_t = None
+            if live_t:
+                if deferred is not None:
+                    raise ValueError("a live marching-cubes weight needs the per-vertex SH rows (no deferred SH)")
+                ctx.live_t = (grid_vertices, grid_spherical_harmonics, sources, count_ptr is not None)
             ctx.mark_non_differentiable(types)
             ctx.set_materialize_grads(False)
             return vertices, sdf, sh, types
@@ -604,12 +613,14 @@ class CreateTriangleVertices(torch.autograd.Function):
                 gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
                 nt.call("mt_vertex_grads_from_list", nt.ptr(offsets), nt.ptr(contributions), g, nt.ptr(gv),
                         nt.ptr(gd), nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.stream(device))
-                return grad_grid_vertices, grad_grid_sdf, None, None, None, None, None, None, None
+                return grad_grid_vertices, grad_grid_sdf, None, None, None, None, None, None, None, None
             grad_grid_sh = torch.empty(gsh_shape, dtype=torch.float32, device=device)
             inverse = torch.empty((4, g), dtype=torch.int32, device=device)
             gv = grad_vertices.contiguous() if grad_vertices is not None else None
             gd = grad_signed_distances.contiguous() if grad_signed_distances is not None else None
             gs = grad_spherical_harmonics.contiguous() if grad_spherical_harmonics is not None else None
+            if ctx.live_t is not None:
+                gd = None  # with t live, the vertex SDF is the level set: no gradient reaches the corners
             ws_ptr, ws_bytes = nt.workspace(device).get(
                 nt.library().mt_create_triangle_vertices_backward_workspace_bytes(g, v))
             nt.call(
@@ -619,7 +630,13 @@ class CreateTriangleVertices(torch.autograd.Function):
                 nt.ptr(grad_grid_vertices), nt.ptr(grad_grid_sdf), nt.ptr(grad_grid_sh), ws_ptr, ws_bytes,
                 nt.stream(device),
             )
-            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None, None
+            if ctx.live_t is not None:
+                grid_vertices, grid_sh, sources, counted = ctx.live_t
+                count_ptr = vertex_offsets.data_ptr() + 4 * (vertex_offsets.numel() - 1) if counted else None
+                nt.call("mt_create_triangle_vertices_live_t_backward", nt.ptr(grid_vertices),
+                        nt.ptr(grid_signed_distances), nt.ptr(grid_sh), c, g, nt.ptr(sources), v, count_ptr,
+                        nt.ptr(gv), nt.ptr(gs), nt.ptr(grad_grid_sdf), nt.stream(device))
+            return grad_grid_vertices, grad_grid_sdf, grad_grid_sh, None, None, None, None, None, None, None
 
 
 def create_triangle_vertices(
@@ -632,6 +649,7 @@ def create_triangle_vertices(
     num_vertices: int | None = None,
     capacity: int | None = None,
     deferred: DeferredSH | None = None,
+    t_gradient: str = "detached",
 ) -> CreateTriangleVerticesResult:
     """``num_vertices`` (optional, not in the reference signature) skips the
     device->host read of ``vertex_offsets[-1]`` when the caller knows it.
@@ -639,10 +657,15 @@ def create_triangle_vertices(
     keeps the live count on the device; rows past it are unused.
     ``deferred`` (optional): the SH rows are not formed; ``deferred`` is filled
     for colour evaluation from the grid, and the result's
-    ``spherical_harmonics`` is a [C, 0, 3] placeholder."""
+    ``spherical_harmonics`` is a [C, 0, 3] placeholder.
+    ``t_gradient`` (not in the reference): "detached" (the reference's
+    gradients) or "live" (the marching-cubes weight is differentiated as a
+    function of the edge's two corner SDFs; needs the SH rows)."""
+    if t_gradient not in ("detached", "live"):
+        raise ValueError(f"t_gradient must be 'detached' or 'live', not {t_gradient!r}")
     result = CreateTriangleVertices.apply(
         grid_vertices, grid_signed_distances, grid_spherical_harmonics, voxel_lower_corners, level_sets,
-        vertex_offsets, num_vertices, capacity, deferred,
+        vertex_offsets, num_vertices, capacity, deferred, t_gradient == "live",
     )
     return CreateTriangleVerticesResult(*result)
 
@@ -802,15 +825,21 @@ def tessellate_voxels(
     upper_corners: Tensor,
     indices: Tensor,
     level_sets: Tensor,
+    t_gradient: str = "detached",
 ) -> Triangles:
     """Marching cubes over every level set (triangle_extraction/__init__.py:75-157).
 
     Differentiable with respect to ``signed_distances`` and
     ``spherical_harmonics`` (and ``vertices``) through the triangle vertices'
     signed distances / colours, exactly as the reference.
+
+    ``t_gradient`` (not in the reference): "live" also differentiates each
+    vertex's edge-crossing weight t = (iso - d0) / (d1 - d0) as a function of
+    its two corner SDFs (topology stays fixed); the default "detached" gives
+    the reference's gradients.
     """
     triangles, _ = _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners,
-                               upper_corners, indices, level_sets, None)
+                               upper_corners, indices, level_sets, None, t_gradient=t_gradient)
     return triangles
 
 
@@ -847,7 +876,7 @@ def tessellate_voxels_counted(
 
 
 def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners, upper_corners, indices,
-                level_sets, capacity, defer_sh=False):
+                level_sets, capacity, defer_sh=False, t_gradient="detached"):
     (num_level_sets,) = level_sets.shape
     device = nt.require_cuda(signed_distances, lower_corners, level_sets)
     logging.debug(f"Tessellating {neighbors.shape[1]} voxels with {num_level_sets} level sets.")
@@ -874,6 +903,7 @@ def _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lowe
     triangle_vertices, triangle_sdf, triangle_sh, triangle_types = create_triangle_vertices(
         vertices, signed_distances, spherical_harmonics, lower_corners, level_sets, vertex_offsets,
         num_vertices if capacity is None else None, None if capacity is None else num_vertices, deferred,
+        t_gradient=t_gradient,
     )
     if deferred is not None:
         triangle_sh = deferred

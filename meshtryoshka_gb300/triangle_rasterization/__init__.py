@@ -217,6 +217,10 @@ def _f32(t: Tensor) -> Tensor:
     return t.contiguous()
 
 
+def _numel(t: Tensor | None) -> int:
+    return 0 if t is None else t.numel() * t.element_size()
+
+
 def _i32(t: Tensor) -> Tensor:
     if t.dtype != torch.int32:
         raise TypeError(f"expected int32, got {t.dtype}")
@@ -492,13 +496,31 @@ def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, 
 # ---------------------------------------------------------------------------
 # Fused compositing (intersect_and_composite.py:24-175)
 # ---------------------------------------------------------------------------
-def _hit_bits(ctx, grid: TileGrid, device) -> Tensor | None:
-    """Scratch for the hit bits the forward stores for its backward (only
-    when a gradient will be asked for)."""
-    if not any(ctx.needs_input_grad):
+# Byte budget of the compositing hit-bit store, per pixel of the render (not
+# in the reference). The forward stores, per warp and batch of 32 triangles,
+# the bits of the triangles each pixel hits, so that the backward need not
+# test them again; batches beyond the budget are tested again by the
+# backward (same gradients). 16 B per pixel is a sixth of the explicit
+# mode's 12 * num_shells B per pixel at 8 shells; 0 turns the store off.
+HIT_BITS_BYTES_PER_PIXEL = 16
+
+
+def _hit_bits(ctx, grid: TileGrid, num_keys: int, device) -> Tensor | None:
+    """The hit-bit store for the forward and its backward (only when a
+    gradient will be asked for): the batches num_keys keys can form at most,
+    capped by HIT_BITS_BYTES_PER_PIXEL."""
+    if not any(ctx.needs_input_grad) or HIT_BITS_BYTES_PER_PIXEL <= 0:
         return None
-    words = nt.library().mt_composite_hit_bits_words(grid.camera_tiles, grid.tile_shape[0], grid.tile_shape[1])
-    return torch.empty((max(int(words), 1),), dtype=torch.int32, device=device)
+    th, tw = grid.tile_shape
+    warps = (th * tw + 31) // 32
+    items = grid.camera_tiles * warps
+    most = int(num_keys) * warps // 32 + items
+    budget = HIT_BITS_BYTES_PER_PIXEL * grid.camera_tiles * th * tw // 128
+    batches = min(most, budget)
+    if batches <= 0:
+        return None
+    nbytes = int(nt.library().mt_composite_hit_bits_bytes(grid.camera_tiles, th, tw, batches))
+    return torch.empty((nbytes,), dtype=torch.uint8, device=device)
 
 
 class IntersectAndComposite(torch.autograd.Function):
@@ -521,12 +543,12 @@ class IntersectAndComposite(torch.autograd.Function):
             # Uniform cameras: [B, 4, H, W]; ragged: every camera's [4, h, w] back to back.
             out = torch.empty((grid.output_numel,) if grid.ragged else (b, 4, h, w), dtype=torch.float32,
                               device=device)
-            hits = _hit_bits(ctx, grid, device)
+            hits = _hit_bits(ctx, grid, k, device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
-                    0.0, None, nt.ptr(hits), nt.stream(device))
+                    0.0, None, nt.ptr(hits), _numel(hits), nt.stream(device))
             note(composite=out)
             ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
@@ -552,22 +574,26 @@ class IntersectAndComposite(torch.autograd.Function):
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
-                    nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, nt.ptr(grad_colors), nt.ptr(grad_sdf),
-                    nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), nt.stream(device))
+                    nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, 1, nt.ptr(grad_colors), nt.ptr(grad_sdf),
+                    nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), _numel(ctx.hits), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
 
 
 class IntersectCompositeLoss(torch.autograd.Function):
-    """Fused compositing with the MSE epilogue in the same kernels (not in the
-    reference): returns mean((clip(rgb + T * background, 0, 1) - target)^2)
-    over every pixel and channel; the image is never materialised and the
-    backward forms d loss / d (rgb, T) inside the compositing adjoint."""
+    """Fused compositing with the MSE epilogue (not in the reference): returns
+    mean((clip(rgb + T * background, 0, 1) - target)^2) over every pixel and
+    channel; the backward forms d loss / d (rgb, T) inside the compositing
+    adjoint. Without SSAA the epilogue runs inside the compositing kernel and
+    the image is never materialised; with ``ssaa`` > 1 the compositing output
+    is at the supersampled size and one kernel averages each ssaa x ssaa block
+    (after the background blend, before the clip, as the render entry points
+    do) and takes the loss, keeping a per-pixel factor for the backward."""
 
     @staticmethod
     def forward(ctx, vertices, colors, signed_distances, faces, sharpness, sorted_keys, sorted_triangle_indices,
                 tile_boundaries, num_shells, grid, key_defines, target, background, gradient_mode=None,
-                num_keys=None):
+                num_keys=None, ssaa=1):
         with record_function("intersect_composite_loss_forward"):
             xy, colors, sdf, faces = _f32(vertices), _f32(colors), _f32(signed_distances), _i32(faces)
             target, background = _f32(target), _f32(background)
@@ -579,7 +605,10 @@ class IntersectCompositeLoss(torch.autograd.Function):
             k = keys.numel()
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
-            if target.numel() * 4 != grid.output_numel * 3:
+            ssaa = int(ssaa)
+            if ssaa > 1 and (grid.ragged or h % ssaa or w % ssaa):
+                raise ValueError("SSAA needs cameras of one image size, a multiple of ssaa")
+            if target.numel() * 4 * ssaa * ssaa != grid.output_numel * 3:
                 raise ValueError("target must hold 3 channels of every camera's image")
             masks = torch.empty((k,), dtype=torch.int32, device=device)
             counter = torch.empty((1,), dtype=torch.int64, device=device)
@@ -588,24 +617,31 @@ class IntersectCompositeLoss(torch.autograd.Function):
                               device=device)
             loss = torch.empty((), dtype=torch.float32, device=device)
             scale = 1.0 / target.numel()
-            hits = _hit_bits(ctx, grid, device)
+            hits = _hit_bits(ctx, grid, k, device)
+            in_kernel = ssaa == 1
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
-                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), nt.ptr(target),
-                    nt.ptr(background), scale, loss.data_ptr(), nt.ptr(hits), nt.stream(device))
+                    nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out),
+                    nt.ptr(target) if in_kernel else None, nt.ptr(background) if in_kernel else None, scale,
+                    loss.data_ptr() if in_kernel else None, nt.ptr(hits), _numel(hits), nt.stream(device))
+            factor = target
+            if not in_kernel:
+                factor = torch.empty_like(target)
+                nt.call("mt_ssaa_loss", out.data_ptr(), b, h, w, ssaa, nt.ptr(background), nt.ptr(target), scale,
+                        loss.data_ptr(), factor.data_ptr(), nt.stream(device))
             note(composite=out, loss=loss)
             ctx.hits = hits
-            ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background)
+            ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, factor, background)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
-                        torch.is_tensor(sharpness), scale)
+                        torch.is_tensor(sharpness), scale, ssaa)
             return loss
 
     @staticmethod
     def backward(ctx, grad_loss):
         with record_function("intersect_composite_loss_backward"):
             xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, target, background = ctx.saved_tensors
-            num_shells, grid, key_defines, mode, sharp_is_tensor, scale = ctx.meta
+            num_shells, grid, key_defines, mode, sharp_is_tensor, scale, ssaa = ctx.meta
             device = xy.device
             grad_loss = grad_loss.to(torch.float32).contiguous()
             grad_colors = torch.zeros_like(colors)
@@ -619,11 +655,11 @@ class IntersectCompositeLoss(torch.autograd.Function):
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
-                    nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(),
+                    nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(), ssaa,
                     nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp), int(mode == "exact"),
-                    nt.ptr(ctx.hits), nt.stream(device))
+                    nt.ptr(ctx.hits), _numel(ctx.hits), nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
-                    None, None, None, None, None, None, None)
+                    None, None, None, None, None, None, None, None)
 
 
 def intersect_and_composite(vertices, colors, signed_distances, faces, sharpness, sorted_keys,
@@ -893,15 +929,24 @@ def render_fused_loss(extrinsics, intrinsics, image_shape, vertices, faces, shel
                       spherical_harmonics, sh_degree, sharpness, background, target, tile_shape=(16, 16),
                       near_plane=0.2, num_camera_bits=6, num_shell_bits=6, num_tile_bits=20, gradient_mode=None,
                       num_faces: Tensor | None = None, key_capacity: int | None = None,
-                      camera_shapes=None) -> Tensor:
+                      camera_shapes=None, ssaa: int = 1) -> Tensor:
     """mean((render_fused(...) - target)^2) with the background blend, clip and
     MSE inside the compositing kernels (not in the reference, where the
     trainer applies them as separate tensor ops). Same loss and gradients as
     the unfused composition. target: [B, 3, H, W]; with ``camera_shapes``
     (one (h, w) per camera, as ``render_cameras``) every camera's [3, h, w]
-    back to back. SSAA is not part of this form."""
+    back to back. ``ssaa`` > 1 (cameras of one size): rendered at ssaa times
+    the size and averaged per pixel after the background blend and before the
+    clip, as ``render_fused`` does."""
     b = extrinsics.shape[0]
     (s,) = shell_face_boundaries.shape
+    if ssaa > 1:
+        if camera_shapes is not None:
+            raise ValueError("SSAA needs cameras of one image size")
+        if vertices.numel() == 0 or faces.numel() == 0:
+            image = background.reshape(1, 3, 1, 1).expand(b, 3, *image_shape)
+            return ((image - target) ** 2).mean()
+        image_shape, intrinsics = _ssaa(intrinsics, image_shape, ssaa)
     grid = (TileGrid.for_cameras(tile_shape, camera_shapes, s) if camera_shapes is not None
             else TileGrid(tuple(tile_shape), tuple(image_shape), b, s))
     if vertices.numel() == 0 or faces.numel() == 0:
@@ -922,7 +967,7 @@ def render_fused_loss(extrinsics, intrinsics, image_shape, vertices, faces, shel
     t = tile_boundaries.shape[2]
     return IntersectCompositeLoss.apply(positions, colors, signed_distances, faces, sharpness, paired.keys,
                                         paired.triangle_indices, tile_boundaries.view(b, t, 2), s, grid, key_defines,
-                                        target, background, gradient_mode, paired.count)
+                                        target, background, gradient_mode, paired.count, ssaa)
 
 
 def render(extrinsics, intrinsics, image_shape, vertices, faces, shell_face_boundaries, signed_distances,

@@ -99,3 +99,43 @@ def test_training_step_fused_loss_equals_unfused(cuda_device, config):
     assert abs(l1 - l0) <= 1e-5 * l0
     _close(s1, s0)
     _close(h1, h0)
+
+
+@pytest.mark.parametrize("ssaa", [2, 3])
+@pytest.mark.parametrize("name", ["three_cams_odd", "close_up"])
+def test_fused_loss_with_ssaa_equals_unfused(cuda_device, name, ssaa):
+    """SSAA (the trainer's train_ssaa): the image rendered at ssaa times the
+    size, blended, averaged per ssaa x ssaa block and clipped, against the
+    fused loss whose compositing backward takes 1 / ssaa^2 of each output
+    pixel's gradient."""
+    scene = make_scene(**SCENES[name])
+    d = cuda_device
+    args = _inputs(scene, d)
+    ext, intr = _t(scene.extrinsics, d), _t(scene.intrinsics, d)
+    b = scene.extrinsics.shape[0]
+    target = _t(np.random.default_rng(ssaa).uniform(0, 1, (b, 3, *scene.image_shape)).astype(np.float32), d)
+    image = tr.render_fused(ext, intr, scene.image_shape, **args, ssaa=ssaa, tile_shape=(8, 8))
+    loss = ((image - target) ** 2).mean()
+    loss.backward()
+    want = _grads(args)
+    fused = tr.render_fused_loss(ext, intr, scene.image_shape, **args, target=target, ssaa=ssaa, tile_shape=(8, 8))
+    assert abs(float(fused.detach()) - float(loss.detach())) <= 1e-5 * float(loss.detach())
+    fused.backward()
+    for got, ref in zip(_grads(args), want):
+        _close(got, ref)
+
+
+def test_training_step_with_ssaa_uses_the_fused_loss(cuda_device):
+    w = pipeline.build_workload("small", cuda_device)
+    w.ssaa = 2
+    results = []
+    for fused in (False, True):
+        w.fused_loss = fused
+        loss = float(pipeline.training_step(w).detach())
+        results.append((loss, w.grid_sdf.grad.clone(), w.grid_sh.grad.clone()))
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+    (l0, s0, h0), (l1, s1, h1) = results
+    assert abs(l1 - l0) <= 1e-5 * l0
+    _close(s1, s0)
+    _close(h1, h0)

@@ -284,3 +284,89 @@ def test_oracle_sdf_regularizers_adjoint_matches_fd():
     fd = [m.central_difference(loss64, sdf64, i, STEP) for i in idx]
     assert np.linalg.norm(fd) > 0
     assert _rel([grad[i] for i in idx], fd) <= FD_RTOL
+
+
+@pytest.mark.gpu
+def test_gpu_live_t_vertex_gradients_match_fd(cuda_device):
+    """t_gradient="live": the marching-cubes weight t = (iso - d0) / (d1 - d0)
+    is differentiated as a function of the edge's two corner SDFs (topology
+    held fixed). Loss = <vertices, Gp> + <sdf, Gs> + <sh, Gsh> of the
+    tessellation; its gradients with respect to the grid SDF, SH and
+    positions against FP64 central differences (relative error <= 1e-3), on
+    corners whose vertices all sit strictly inside their edges. The default
+    mode stays the reference's (detached t) on the same inputs."""
+    import torch
+
+    from meshtryoshka_gb300 import triangle_extraction as te
+
+    d = cuda_device
+    rng = np.random.default_rng(11)
+    n = 32
+    coords = -1 + (np.arange(n) + 0.5) * 2 / n
+    z, y, x = np.meshgrid(coords, coords, coords, indexing="ij")
+    occ = semantics.pack(np.abs(np.sqrt(x * x + y * y + z * z) - 0.5) < 2.5 * 2 / n)
+    vox = oracle.extract_voxels(occ)
+    p = 2 * vox.vertices.astype(np.float64) - 1
+    gsdf = (np.linalg.norm(p, axis=1) - 0.5 + rng.normal(0, 0.002, len(p))).astype(np.float32)
+    gsh = np.concatenate([rng.uniform(0, 1, (1, len(p), 3)), rng.normal(0, 0.1, (3, len(p), 3))]).astype(np.float32)
+    ls = np.array([0.02, 0.0, -0.02], np.float32)
+    otri = oracle.tessellate_voxels(gsdf, vox.vertices, gsh, vox.neighbors, vox.lower_corners, vox.upper_corners,
+                                    vox.indices, ls)
+    v = otri.vertices.shape[0]
+    gp = rng.normal(0, 1, (v, 3)).astype(np.float32)
+    gs = rng.normal(0, 1, (v,)).astype(np.float32)
+    gh = rng.normal(0, 1, (4, v, 3)).astype(np.float32)
+
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(d)  # noqa: E731
+    grads = {}
+    for mode in ("live", "detached"):
+        sdf_d = t(gsdf).requires_grad_(True)
+        sh_d = t(gsh).requires_grad_(True)
+        pos_d = t(vox.vertices).requires_grad_(True)
+        tri = te.tessellate_voxels(sdf_d, pos_d, sh_d, t(vox.neighbors), t(vox.lower_corners),
+                                   t(vox.upper_corners), t(vox.indices), t(ls), t_gradient=mode)
+        loss = (tri.vertices * t(gp)).sum() + (tri.signed_distances * t(gs)).sum() + \
+            (tri.spherical_harmonics * t(gh)).sum()
+        loss.backward()
+        grads[mode] = (sdf_d.grad.cpu().numpy(), sh_d.grad.cpu().numpy(), pos_d.grad.cpu().numpy())
+
+    # Detached mode: the reference's adjoint (the oracle's restatement).
+    want_pos, want_sdf, want_sh = oracle.create_triangle_vertices_backward(
+        gsdf, gsh.shape, vox.lower_corners, ls, otri.vertex_offsets, gp, gs, gh)
+    for got, want in zip(grads["detached"], (want_sdf, want_sh, want_pos)):
+        assert np.abs(got - want).max() <= 1e-5 * max(np.abs(want).max(), 1e-30)
+
+    # FP64 model with t live.
+    i0, i1, tw = oracle.triangle_vertex_sources(gsdf, vox.lower_corners, ls, otri.vertex_offsets, v)
+    shell = np.searchsorted(otri.vertex_boundaries, np.arange(v), side="right")
+    iso = ls.astype(np.float64)[shell]
+    sdf64, sh64, pos64 = gsdf.astype(np.float64), gsh.astype(np.float64), vox.vertices.astype(np.float64)
+
+    def loss64():
+        d0, d1 = sdf64[i0], sdf64[i1]
+        tt = np.clip((iso - d0) / (d1 - d0), 0.0, 1.0)
+        verts = pos64[i0] + tt[:, None] * (pos64[i1] - pos64[i0])
+        vsdf = d0 + tt * (d1 - d0)
+        vsh = sh64[:, i0] + tt[None, :, None] * (sh64[:, i1] - sh64[:, i0])
+        return float((verts * gp).sum() + (vsdf * gs).sum() + (vsh * gh).sum())
+
+    inside = (tw > 1e-3) & (tw < 1 - 1e-3) & (gsdf[i0] != gsdf[i1])
+    bad = np.zeros(len(gsdf), bool)
+    bad[i0[~inside]] = True
+    bad[i1[~inside]] = True
+    used = np.zeros(len(gsdf), bool)
+    used[i0] = True
+    used[i1] = True
+    corners = np.nonzero(used & ~bad)[0]
+    sdf_idx = [(int(c),) for c in rng.choice(corners, N_ENTRIES, replace=False)]
+    sh_idx = [(int(k), int(c), int(ch)) for k, c, ch in
+              zip(rng.integers(0, 4, N_ENTRIES), rng.choice(corners, N_ENTRIES), rng.integers(0, 3, N_ENTRIES))]
+    pos_idx = [(int(c), int(ch)) for c, ch in zip(rng.choice(corners, N_ENTRIES), rng.integers(0, 3, N_ENTRIES))]
+    g_sdf, g_sh, g_pos = grads["live"]
+    for grid, idx, got in ((sdf64, sdf_idx, g_sdf), (sh64, sh_idx, g_sh), (pos64, pos_idx, g_pos)):
+        fd = [m.central_difference(loss64, grid, i, STEP) for i in idx]
+        assert np.linalg.norm(fd) > 0
+        assert _rel([got[i] for i in idx], fd) <= FD_RTOL
+    # The live weight changes the SDF gradient (and nothing else).
+    assert _rel(g_sdf[[i[0] for i in sdf_idx]], want_sdf[[i[0] for i in sdf_idx]]) > 1e-2
+    np.testing.assert_allclose(g_sh, want_sh, rtol=0, atol=1e-5 * np.abs(want_sh).max())

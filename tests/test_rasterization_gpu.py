@@ -542,26 +542,53 @@ def test_bound_and_generate_keys_matches_three_stage_chain(cuda_device, b, f, ra
     assert nt.workspace(torch.device(d)).status() == 0
 
 
-# A whole 8-shell sphere in a few tiles: warps walk far more than the 32
-# batches whose hit bits the forward stores, so the backward mixes stored
-# and re-tested batches.
+# A whole 8-shell sphere in a few tiles: warps walk hundreds of batches, so
+# a small hit-bit budget runs out inside a work item and the backward mixes
+# stored and re-tested batches.
 DENSE = dict(cameras=((0.0, 0.0, 8.0),), image_shape=(32, 32), fov=20.0,
              levels=tuple(float(x) for x in np.linspace(0.03, -0.03, 8)), sh_degree=1)
 
 
-def test_fused_backward_past_the_stored_batches(cuda_device):
+@pytest.mark.parametrize("budget", [16, 1])
+def test_fused_backward_past_the_stored_batches(cuda_device, budget, monkeypatch):
+    """Against the oracle with the default hit-bit budget and with 1 byte per
+    pixel, which runs out part-way through the dense tiles' walks."""
+    monkeypatch.setattr(tr, "HIT_BITS_BYTES_PER_PIXEL", budget)
     scene = make_scene(**DENSE)
     grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, cuda_device)
     counts = _n(tb)[..., 1] - _n(tb)[..., 0]
-    assert counts.max() > 32 * 32 * 4  # tiles far longer than the stored batches
+    assert counts.max() > 32 * 32 * 4  # tiles of hundreds of batches
     _check_fused_backward(scene, cuda_device, "reference", (16, 16))
+
+
+def test_hit_bit_store_size_follows_the_work(cuda_device):
+    """The store holds the batches the keys can form, not a fixed number of
+    batches per warp: at most K * warps / 32 + work items batches, and never
+    more than the byte budget."""
+    lib = nt.library()
+    header = lib.mt_composite_hit_bits_bytes(1000, 8, 8, 1) - 128
+    assert header == (8 + 4 * 2000 + 127) // 128 * 128
+    assert lib.mt_composite_hit_bits_bytes(1000, 8, 8, 10) == header + 10 * 128
+    assert lib.mt_composite_hit_bits_bytes(0, 8, 8, 10) == 0
+
+    class Ctx:
+        needs_input_grad = (True,)
+
+    grid = tr.TileGrid((8, 8), (800, 800), 4, 8)
+    hits = tr._hit_bits(Ctx(), grid, 2_500_000, cuda_device)
+    most = 2_500_000 * 2 // 32 + grid.camera_tiles * 2
+    assert hits.numel() == lib.mt_composite_hit_bits_bytes(grid.camera_tiles, 8, 8, most)
+    assert hits.numel() < 12 * 4 * 8 * 800 * 800 / 6  # far below the explicit mode's buffers
+    dense = tr._hit_bits(Ctx(), grid, 100_000_000, cuda_device)  # capped by the budget
+    budget = tr.HIT_BITS_BYTES_PER_PIXEL * grid.camera_tiles * 64 // 128
+    assert dense.numel() == lib.mt_composite_hit_bits_bytes(grid.camera_tiles, 8, 8, budget)
 
 
 @pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside", "dense"])
 def test_backward_with_and_without_stored_hit_bits(cuda_device, name, monkeypatch):
-    """The backward reads the forward's hit bits for a warp's first batches;
-    without them it tests those batches again. Both give the same gradients
-    (up to the order of the compositing atomics)."""
+    """The backward reads the forward's hit bits for the batches the store
+    holds; without them it tests every batch again. Both give the same
+    gradients (up to the order of the compositing atomics)."""
     d = cuda_device
     scene = make_scene(**(DENSE if name == "dense" else SCENES[name]))
     grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
@@ -571,7 +598,7 @@ def test_backward_with_and_without_stored_hit_bits(cuda_device, name, monkeypatc
     grads = []
     for stored in (True, False):
         if not stored:
-            monkeypatch.setattr(tr, "_hit_bits", lambda ctx, grid, device: None)
+            monkeypatch.setattr(tr, "HIT_BITS_BYTES_PER_PIXEL", 0)
         colors = _t(colors_np, d).requires_grad_(True)
         sdf = _t(scene.sdf, d).requires_grad_(True)
         sharp = torch.tensor(scene.sharpness, device=d).requires_grad_(True)
