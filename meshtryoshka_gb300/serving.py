@@ -12,15 +12,16 @@ against a target image.
 * admits the requests that have arrived into a FIFO queue;
 * retires finished batches (a CUDA event per batch, polled without blocking)
   and stamps their requests' completion times;
-* while a stream slot and the in-flight memory budget allow, and either
-  nothing is in flight or requests have queued up (``overlap_backlog``;
-  overlapping batches slow each other, which only pays when requests wait),
-  forms the next batch from the head of the queue: render-only requests of
-  the head's scene
-  (in arrival order, up to ``max_batch`` and a pixel budget) go into one
-  ``render_cameras`` call for cameras of any size; a gradient request runs
-  on its own (its gradient is with respect to the scene's parameters, so it
-  cannot share a loss with other requests);
+* while a stream slot is free and the estimated device bytes of the batches
+  in flight leave room (``hbm_budget``; ``Scene.request_bytes`` estimates a
+  request from its pixels, its scene's tile keys per pixel and, for a
+  gradient request, the tessellation and gradient buffers), forms the next
+  batch from the head of the queue: render-only requests of the head's scene
+  (in arrival order, up to ``max_batch``) go into one ``render_cameras`` call
+  for cameras of any size; render + gradient requests of the head's scene
+  (up to ``max_gradient_batch``) share one tessellation and each get the
+  gradient of their own loss; a batch starts while another is in flight once
+  ``overlap_backlog`` requests wait;
 * launches the batch on its own CUDA stream, so batches overlap on the GPU.
 
 ``run_plain`` is the per-request form at the same arrival times: one request
@@ -28,7 +29,8 @@ at a time, rendered and completed before the next starts.
 
 Every request's result is the same alone and in a batch: a camera rendered
 in ``render_cameras`` equals its ``render_fused`` image bit for bit, and a
-gradient request is computed alone either way (tests/test_serving_gpu.py).
+gradient request's loss and gradient involve its own camera only (the shared
+tessellation is deterministic) (tests/test_serving_gpu.py).
 """
 
 from __future__ import annotations
@@ -58,6 +60,10 @@ class Scene:
     sharpness: Tensor  # []
     background: Tensor  # [3]
     mesh: tuple = ()  # (vertices, faces, shell face boundaries, sdf, sh) for render-only requests
+    # Tessellated [0, 1]^3 vertices -> renderer positions (None: the 2 v - 1
+    # stand-in of the synthetic scenes; a checkpoint scene uses its
+    # contraction's inverse, as the reference's model does).
+    vertex_map: object = None
 
     @staticmethod
     def build(config: str, device, seed: int = 0) -> "Scene":
@@ -74,17 +80,70 @@ class Scene:
         scene.refresh_mesh()
         return scene
 
+    @staticmethod
+    def from_checkpoint(path, layout, contraction, level_sets: Tensor, device, name: str | None = None,
+                        sdf_offset=None, sharpness: float = 400.0) -> "Scene":
+        """A resident scene from a reference trainer checkpoint
+        (meshtryoshka_gb300.checkpoint): its tesseract voxels, signed
+        distances and SH; positions through ``contraction.uncontract``."""
+        from . import checkpoint
+
+        loaded = checkpoint.load_tesseract_checkpoint(path, layout, device, sdf_offset)
+        scene = Scene(name or str(path), loaded.voxels, loaded.signed_distances, loaded.spherical_harmonics,
+                      level_sets.to(device=device, dtype=torch.float32).contiguous(), loaded.sh_degree,
+                      torch.tensor(sharpness, dtype=torch.float32, device=device),
+                      torch.zeros(3, dtype=torch.float32, device=device), vertex_map=contraction.uncontract)
+        scene.refresh_mesh()
+        return scene
+
     def tessellate(self, grid_sdf: Tensor, grid_sh: Tensor):
         v = self.voxels
         tri = te.tessellate_voxels(grid_sdf, v.vertices, grid_sh, v.neighbors, v.lower_corners, v.upper_corners,
                                    v.indices, self.level_sets)
-        return pipeline.uncontract_stand_in(tri.vertices).detach(), tri
+        positions = self.vertex_map(tri.vertices) if self.vertex_map is not None else \
+            pipeline.uncontract_stand_in(tri.vertices)
+        return positions.detach().contiguous(), tri
 
     def refresh_mesh(self) -> None:
         """Re-tessellates the cached mesh (after the scene's parameters change)."""
         with torch.no_grad():
             vertices, tri = self.tessellate(self.grid_sdf, self.grid_sh)
         self.mesh = (vertices, tri.faces, tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics)
+        self.keys_per_pixel = None
+
+    def measure_keys_per_pixel(self, shape=(512, 512)) -> float:
+        """Tile keys per pixel of a render of this scene (a probe from the
+        first request camera direction the scene's layout uses), for the
+        server's memory estimates."""
+        if getattr(self, "keys_per_pixel", None) is None:
+            eye = np.array([0.0, 0.1, 0.6 if self._inside() else 2.2])
+            ext = torch.from_numpy(synthetic.look_at(eye)[None]).to(self.grid_sdf.device)
+            intr = torch.from_numpy(synthetic.pinhole(shape[0], shape[1], 55.0)[None]).to(self.grid_sdf.device)
+            with torch.no_grad():
+                tr.render_fused(ext, intr, shape, *self.mesh, self.sh_degree, self.sharpness, self.background)
+            self.keys_per_pixel = max(tr.LAST_RENDER_STATS.get("num_keys", 0) / float(shape[0] * shape[1]), 1.0)
+        return self.keys_per_pixel
+
+    def _inside(self) -> bool:
+        cfg = synthetic.CONFIGS.get(self.name)
+        return cfg is not None and cfg.background_radius is not None
+
+    def request_bytes(self, r: "Request") -> int:
+        """Estimated device bytes a request holds while in flight: the
+        compositing output and image (28 B per pixel), its tile keys (sort
+        buffers and masks, 40 B per key), and for a gradient request also the
+        tessellation with its autograd state, the grid gradients, the target
+        and the hit-bit store (16 B per pixel)."""
+        kpp = self.measure_keys_per_pixel()
+        p = r.pixels
+        total = 28 * p + int(40 * kpp * p)
+        if r.gradient:
+            v = self.mesh[0].shape[0]
+            f = self.mesh[1].shape[0]
+            c = self.grid_sh.shape[0]
+            g = self.grid_sdf.shape[0]
+            total += v * (12 + 4 + 12 * c + 1 + 12) + f * 16 + g * (4 + 12 * c) + v * 24 + (12 + 16) * p
+        return total
 
 
 @dataclass
@@ -134,6 +193,27 @@ def render_alone(scene: Scene, r: Request, tile_shape=(16, 16)) -> Completed:
     return Completed(r, image.detach(), grad_sdf, grad_sh)
 
 
+def render_gradient_batch(scene: Scene, batch: list[Request], tile_shape=(16, 16)) -> list[Completed]:
+    """Render + gradient requests of one scene: one tessellation of the
+    scene's parameters shared by every request, then per request its render,
+    its MSE and the gradient of that loss alone (the same results as each
+    request alone: the tessellation is deterministic)."""
+    if len(batch) == 1:
+        return [render_alone(scene, batch[0], tile_shape)]
+    sdf = scene.grid_sdf.detach().requires_grad_(True)
+    sh = scene.grid_sh.detach().requires_grad_(True)
+    vertices, tri = scene.tessellate(sdf, sh)
+    out = []
+    for i, r in enumerate(batch):
+        image = tr.render_fused(r.extrinsics[None], r.intrinsics[None], r.shape, vertices, tri.faces,
+                                tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics, scene.sh_degree,
+                                scene.sharpness, scene.background, tile_shape=tile_shape)[0]
+        loss = ((image - r.target) ** 2).mean()
+        grad_sdf, grad_sh = torch.autograd.grad(loss, (sdf, sh), retain_graph=i + 1 < len(batch))
+        out.append(Completed(r, image.detach(), grad_sdf, grad_sh))
+    return out
+
+
 def render_batch(scene: Scene, batch: list[Request], tile_shape=(16, 16)) -> list[Completed]:
     """Render-only requests of one scene in one pass over cameras of any size."""
     if len(batch) == 1:
@@ -151,7 +231,7 @@ class _InFlight:
     results: list[Completed]
     event: torch.cuda.Event
     stream: torch.cuda.Stream
-    pixels: int
+    bytes: int
 
 
 @dataclass
@@ -159,30 +239,42 @@ class Server:
     scenes: list[Scene]
     streams: int = 4  # batches in flight at once
     max_batch: int = 16  # requests per render batch
-    max_pixels: int = 16 * 1920 * 1080  # in-flight pixel budget (bounds the HBM in use)
-    overlap_backlog: int = 2  # queued requests needed to start a batch while another is in flight
+    max_gradient_batch: int = 4  # render + gradient requests per batch (one shared tessellation)
+    hbm_budget: int = 8 << 30  # estimated device bytes of the batches in flight (Scene.request_bytes)
+    overlap_backlog: int = 1  # queued requests needed to start a batch while another is in flight
     tile_shape: tuple[int, int] = (16, 16)
     batches: int = field(default=0, init=False)
+    peak_inflight_bytes: int = field(default=0, init=False)
 
-    def _form_batch(self, queue: deque, budget: int) -> list[Request]:
+    def __post_init__(self):
+        for scene in self.scenes:  # the per-scene key density of the byte estimates, measured up front
+            scene.measure_keys_per_pixel()
+
+    def _bytes(self, r: Request) -> int:
+        return self.scenes[r.scene].request_bytes(r)
+
+    def _form_batch(self, queue: deque, budget: int, idle: bool) -> tuple[list[Request], int]:
+        """The next batch from the head of the queue: requests of the head's
+        scene and kind (render-only, or render + gradient), in arrival order,
+        while their estimated bytes fit ``budget``. With nothing in flight
+        (``idle``) the head goes alone even if it exceeds the budget."""
         head = queue[0]
-        if head.gradient:
-            return [queue.popleft()] if head.pixels <= budget or budget == self.max_pixels else []
-        batch, pixels, keep = [], 0, deque()
-        while queue and len(batch) < self.max_batch:
+        limit = self.max_gradient_batch if head.gradient else self.max_batch
+        batch, used, keep = [], 0, deque()
+        while queue and len(batch) < limit:
             r = queue.popleft()
-            if r.scene == head.scene and not r.gradient and (pixels + r.pixels <= budget or not batch):
+            b = self._bytes(r)
+            if r.scene == head.scene and r.gradient == head.gradient and (used + b <= budget or (not batch and idle)):
                 batch.append(r)
-                pixels += r.pixels
+                used += b
             else:
                 keep.append(r)
-                if len(keep) > 4 * self.max_batch:  # look ahead a bounded distance
+                if len(keep) > 4 * self.max_batch or not batch:  # look ahead a bounded distance
                     break
         queue.extendleft(reversed(keep))
-        if pixels > budget and budget < self.max_pixels:  # head alone does not fit yet
-            queue.extendleft(reversed(batch))
-            return []
-        return batch
+        if not batch:
+            return [], 0
+        return batch, used
 
     def run(self, requests: list[Request]) -> list[Completed]:
         """Serves ``requests`` (sorted by arrival) in real time; returns them
@@ -216,18 +308,19 @@ class Server:
             while queue and free:
                 if inflight and len(queue) < self.overlap_backlog:
                     break
-                budget = self.max_pixels - sum(f.pixels for f in inflight)
-                batch = self._form_batch(queue, budget)
+                held = sum(f.bytes for f in inflight)
+                batch, used = self._form_batch(queue, self.hbm_budget - held, not inflight)
                 if not batch:
                     break
                 stream = free.pop()
                 with torch.cuda.stream(stream):
                     scene = self.scenes[batch[0].scene]
                     results = (render_batch(scene, batch, self.tile_shape) if not batch[0].gradient
-                               else [render_alone(scene, batch[0], self.tile_shape)])
+                               else render_gradient_batch(scene, batch, self.tile_shape))
                     event = torch.cuda.Event()
                     event.record(stream)
-                inflight.append(_InFlight(results, event, stream, sum(r.pixels for r in batch)))
+                inflight.append(_InFlight(results, event, stream, used))
+                self.peak_inflight_bytes = max(self.peak_inflight_bytes, held + used)
                 self.batches += 1
                 launched = True
             if not launched and not inflight and pending and not queue:

@@ -197,6 +197,120 @@ def subdivision_fixture(ref) -> dict[str, np.ndarray]:
 
 
 # ---------------------------------------------------------------------------
+# Tesseract assembly of a trainer checkpoint (meshtryoshka/model/tesseract.py)
+# ---------------------------------------------------------------------------
+def _reference_tesseract(ref):
+    """The reference's tesseract module, imported with stand-ins for its
+    package-relative imports (initializer, utils, scene type) and for the
+    CUDA triangle_extraction package; its component geometry, voxel
+    concatenation and duplicate re-indexing are plain torch and run as they
+    are. index_vertices is the reference's own Python (stable sort)."""
+    import importlib.util
+    import types
+
+    import torch
+
+    from meshtryoshka_gb300 import triangle_extraction as ours
+
+    index_module = ref.python_module("triangle_extraction/index_vertices.py")
+    sort = torch.Tensor.sort
+
+    def index_vertices(points, tol):
+        torch.Tensor.sort = lambda self, *a, **k: sort(self, *a, **{**k, "stable": True})
+        try:
+            return index_module.index_vertices(points, tol)
+        finally:
+            torch.Tensor.sort = sort
+
+    stubs = {
+        "refpkg": {}, "refpkg.model": {},
+        "refpkg.initializer": {"Initializer": object},
+        "refpkg.utils": {"get_value_for_step": lambda step, schedule: schedule[max(k for k in schedule if k <= step)]},
+        "refpkg.model.common": {"Scene": object},
+        "triangle_extraction": {"UpscaledParameters": object, "Voxels": ours.Voxels, "dilate_occupancy": None,
+                                "extract_voxels": None, "get_occupancy_mesh": None, "index_vertices": index_vertices,
+                                "upscale_parameters": None, "write_occupancy": None},
+    }
+    saved = {name: sys.modules.get(name) for name in stubs}
+    for name, attrs in stubs.items():
+        module = types.ModuleType(name)
+        if name in ("refpkg", "refpkg.model"):
+            module.__path__ = []
+        for key, value in attrs.items():
+            setattr(module, key, value)
+        sys.modules[name] = module
+    try:
+        path = ref.build_ref.reference_root() / "meshtryoshka" / "model" / "tesseract.py"
+        spec = importlib.util.spec_from_file_location("refpkg.model.tesseract", path)
+        module = importlib.util.module_from_spec(spec)
+        module.__package__ = "refpkg.model"
+        spec.loader.exec_module(module)
+    finally:
+        for name, old in saved.items():
+            if old is None:
+                sys.modules.pop(name, None)
+            else:
+                sys.modules[name] = old
+    return module
+
+
+TESSERACT = dict(center=32, arm=32, center_extent=0.5)
+
+
+def tesseract_fixture(ref) -> dict[str, np.ndarray]:
+    """A small tesseract (central cube 32^3, six arms 32 voxels deep) assembled
+    by the reference's code from a seeded flat occupancy: per component the
+    oracle's extract_voxels (pinned to the reference kernels), then the
+    reference's corner mapping, concatenation and duplicate re-indexing; and
+    the reference's contraction inverse on seeded points."""
+    import torch
+
+    from meshtryoshka_gb300 import triangle_extraction as ours
+    from oracle import oracle
+
+    tm = _reference_tesseract(ref)
+    cm = ref.python_module("meshtryoshka/model/contraction.py")
+    cfg = tm.TesseractCfg(center_resolution={0: TESSERACT["center"]}, arm_resolution={0: TESSERACT["arm"]},
+                          center_extent=TESSERACT["center_extent"], parameter_init_seed=0, active_sh_degree={0: 0},
+                          sh_lr_scale=1.0, disable_spherical_harmonics=False, disable_sparsity=False,
+                          disable_tesseract=False)
+    components = [tm.TesseractCenter(cfg)] + [tm.TesseractArm(cfg, d, s) for d in range(3) for s in range(2)]
+    rng = np.random.default_rng(23)
+    words, parts, out = [], [], {}
+    for index, component in enumerate(components):
+        i, j, k = component.shape(0)
+        # A shell around the component's centre plus sparse noise, so voxels,
+        # subvoxels and shared faces all occur.
+        z, y, x = np.meshgrid(*(np.arange(n) + 0.5 for n in (i, j, k)), indexing="ij")
+        r = np.sqrt(((x / k - 0.5) * 2) ** 2 + ((y / j - 0.5) * 2) ** 2 + ((z / i - 0.5) * 2) ** 2)
+        bits = (np.abs(r - 0.8) < 0.05) | (rng.random((i, j, k)) < 0.002)
+        occ = _pack(bits)
+        words.append(occ.reshape(-1))
+        v = oracle.extract_voxels(occ)
+        t = ours.Voxels(*(torch.from_numpy(np.ascontiguousarray(a)) for a in
+                          (v.vertices, v.neighbors, v.lower_corners, v.upper_corners, v.indices)), v.grid_shape)
+        parts.append(t._replace(vertices=component.interpolate(t.vertices)))
+        out[f"corners_{index}"] = component.corners.numpy()
+    voxels = tm.Tesseract.concatenate_voxels(parts)
+    voxels = tm.Tesseract.reindex_duplicate_vertices(voxels)
+    out.update({"occupancy": np.concatenate(words).astype(np.int32), "vertices": voxels.vertices.numpy(),
+                "neighbors": voxels.neighbors.numpy(), "lower_corners": voxels.lower_corners.numpy(),
+                "upper_corners": voxels.upper_corners.numpy(), "indices": voxels.indices.numpy(),
+                "layout": np.array([TESSERACT["center"], TESSERACT["arm"]], np.int32),
+                "center_extent": np.array(TESSERACT["center_extent"], np.float32)})
+    points = rng.uniform(-0.05, 1.05, (4000, 3)).astype(np.float32)
+    contraction = cm.Contraction(cm.ContractionCfg(center_radius=0.6, arm_ratio=0.5, disable_exponential=False),
+                                 TESSERACT["center_extent"])
+    out["contraction_points"] = points
+    out["uncontracted"] = contraction.uncontract(torch.from_numpy(points)).numpy()
+    weights = rng.uniform(0, 1, (500, 3)).astype(np.float32)
+    out["map_points"] = weights
+    for index, component in enumerate(components):
+        out[f"mapped_{index}"] = component.interpolate(torch.from_numpy(weights)).numpy()
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Rasterization: a tessellated sphere seen by a few cameras
 # ---------------------------------------------------------------------------
 SCENES = {
@@ -285,7 +399,8 @@ def generate(reference: str | None = None) -> dict[str, dict[str, np.ndarray]]:
 
     if not ref.available():
         raise SystemExit("reference tree not found; cannot build its kernels")
-    fixtures = {"extraction": extraction_fixture(ref), "subdivision": subdivision_fixture(ref)}
+    fixtures = {"extraction": extraction_fixture(ref), "subdivision": subdivision_fixture(ref),
+                "tesseract": tesseract_fixture(ref)}
     for name, kw in SCENES.items():
         fixtures[f"raster_{name}"] = raster_fixture(ref, **kw)
     return fixtures

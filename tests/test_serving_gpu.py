@@ -3,9 +3,12 @@
 Requests for two resident scenes (render-only and render + gradient, images
 of 256-1920 x 256-1080 px) arrive faster than they are served, so the server
 batches render-only requests of a scene into one pass over cameras of
-different sizes and overlaps batches on several streams. Each completed
+different sizes, batches render + gradient requests of a scene over one
+shared tessellation, and overlaps batches on several streams. Each completed
 request is then recomputed on its own: images must be identical, gradients
-within 1e-4 of the largest entry (atomic accumulation order).
+within 1e-4 of the largest entry (atomic accumulation order). The in-flight
+byte estimate never exceeds the server's HBM budget (except for a request
+served alone that exceeds it by itself).
 """
 
 from __future__ import annotations
@@ -32,11 +35,11 @@ def scenes(cuda_device):
 def test_results_same_alone_and_in_the_mix(scenes):
     requests = serving.poisson_requests(scenes, rate=4000.0, duration=0.02, seed=11, gradient_fraction=0.25)
     assert len(requests) > 40 and any(r.gradient for r in requests)
-    server = serving.Server(scenes, streams=3, max_batch=8)
+    server = serving.Server(scenes, streams=3, max_batch=8, overlap_backlog=2)
     done = server.run(requests)
     torch.cuda.synchronize()
     assert sorted(c.request.id for c in done) == [r.id for r in requests]
-    assert server.batches < len(requests)  # render-only requests were batched
+    assert server.batches < len(requests)  # requests were batched
     for c in done:
         assert c.done >= c.request.arrival
         alone = serving.render_alone(scenes[c.request.scene], c.request)
@@ -57,9 +60,31 @@ def test_plain_form_serves_everything(scenes):
     assert summary["requests"] == len(requests) and summary["p99_ms"] >= summary["p50_ms"] > 0
 
 
-def test_memory_budget_limits_inflight_pixels(scenes):
-    """A pixel budget of one large image still serves every request."""
-    requests = serving.poisson_requests(scenes, rate=4000.0, duration=0.01, seed=2, gradient_fraction=0.0)
-    server = serving.Server(scenes, streams=4, max_batch=16, max_pixels=1920 * 1080)
+def test_gradient_requests_share_one_tessellation(scenes):
+    """A batch of render + gradient requests of one scene gives each
+    request's own gradients."""
+    requests = [r for r in serving.poisson_requests(scenes, rate=4000.0, duration=0.05, seed=8,
+                                                    gradient_fraction=1.0) if r.scene == 0][:3]
+    assert len(requests) == 3
+    batch = serving.render_gradient_batch(scenes[0], requests)
+    for c in batch:
+        alone = serving.render_alone(scenes[0], c.request)
+        torch.testing.assert_close(c.image, alone.image, rtol=0, atol=0)
+        _close(c.grad_sdf, alone.grad_sdf)
+        _close(c.grad_sh, alone.grad_sh)
+
+
+def test_memory_budget_bounds_the_bytes_in_flight(scenes):
+    """With a budget of a few requests' worth of bytes, the in-flight
+    estimate stays within it and every request is served."""
+    requests = serving.poisson_requests(scenes, rate=4000.0, duration=0.02, seed=2, gradient_fraction=0.2)
+    sizes = [scenes[r.scene].request_bytes(r) for r in requests]
+    budget = 3 * max(sizes)
+    server = serving.Server(scenes, streams=4, max_batch=16, hbm_budget=budget)
     done = server.run(requests)
     assert len(done) == len(requests)
+    assert 0 < server.peak_inflight_bytes <= budget
+    # A budget below one request still serves (one request at a time).
+    tight = serving.Server(scenes, streams=4, max_batch=16, hbm_budget=min(sizes) // 2)
+    assert len(tight.run(requests[:10])) == 10
+    assert tight.peak_inflight_bytes <= max(sizes[:10])
