@@ -42,16 +42,20 @@ CONFIG_NAME = "mid"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default: 200 on the GPU, 5 for the host-core reference arm)")
+    p.add_argument("--warmup", type=int, default=None, help="warm-up steps (default: 5 on the GPU, 3 on the host)")
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
     p.add_argument("--config", default=CONFIG_NAME)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-cameras", action="store_true", help="skip the uneven-camera batching comparison")
     p.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
-    p.add_argument("--serve-seconds", type=float, default=0.5, help="arrival window per request rate")
+    p.add_argument("--serve-requests", type=int, default=2000, help="requests per arrival rate of the serving sweep")
     p.add_argument("--no-subdivision", action="store_true", help="skip the subdivision step measurement")
     p.add_argument("--no-large", action="store_true", help="skip the large-configuration step in both modes")
+    p.add_argument("--tile", default=None, help="tile shape HxW for the step (default: autotuned)")
+    p.add_argument("--no-reference-cub", action="store_true",
+                   help="skip timing the reference's CUB scan and sort extensions")
     return p.parse_args()
 
 
@@ -136,6 +140,31 @@ class ClockSampler:
         }
 
 
+def profiled_traffic(entry: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    of an entry point's kernels from the ncu capture summarised in
+    profiles/traffic.json, used only while the kernels' sources are the ones
+    captured (their SHA-256 is recorded beside the figure)."""
+    import hashlib
+
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            table = json.load(f)
+    except (OSError, ValueError):
+        return None, "no capture"
+    rec = table.get(entry)
+    if not isinstance(rec, dict):
+        return None, "no capture of this entry point"
+    digest = hashlib.sha256()
+    for name in rec.get("sources", []):
+        with open(os.path.join(ROOT, "meshtryoshka_gb300", "csrc", name), "rb") as f:
+            digest.update(f.read())
+    if digest.hexdigest() != rec.get("sha256"):
+        return None, "capture predates the current kernel sources"
+    return rec.get("bytes_per_launch"), rec.get("capture")
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -149,9 +178,13 @@ def measured_peaks():
 # ---------------------------------------------------------------------------
 # CPU leg: the oracle (restatement of the reference algorithm) on host cores.
 # ---------------------------------------------------------------------------
-def cpu_sample(w, camera: int):
-    """Tessellation of the whole grid plus fused render fwd+bwd of one camera on
-    the host cores; returns (tessellate_s, render_s)."""
+def cpu_step(w, tile_shape=(16, 16)):
+    """One whole training step of the workload on the host cores with the
+    oracle (the restatement of the reference's kernels): tessellation of every
+    shell, fused render of every camera, the MSE loss through the background
+    blend and the clip, the compositing backward, the SH backward and the
+    vertex-interpolation backward into the grid SDF and SH. Returns
+    (seconds, sizes)."""
     import numpy as np
 
     from oracle import oracle
@@ -162,33 +195,48 @@ def cpu_sample(w, camera: int):
     sdf = w.grid_sdf.detach().cpu().numpy()
     sh = w.grid_sh.detach().cpu().numpy()
     ls = w.level_sets.cpu().numpy()
+    ext = w.extrinsics.cpu().numpy()
+    intr = w.intrinsics.cpu().numpy()
+    bg = w.background.cpu().numpy()
+    target = w.target.detach().cpu().numpy()
+    b = ext.shape[0]
     t0 = time.perf_counter()
     tri = oracle.tessellate_voxels(sdf, np_vox[0], sh, np_vox[1], np_vox[2], np_vox[3], np_vox[4], ls)
-    rng = np.random.default_rng(0)
-    g_sdf = rng.normal(0, 1e-3, tri.signed_distances.shape).astype(np.float32)
-    g_sh = rng.normal(0, 1e-3, tri.spherical_harmonics.shape).astype(np.float32)
-    oracle.create_triangle_vertices_backward(sdf, sh.shape, np_vox[2], ls, tri.vertex_offsets, None, g_sdf, g_sh)
-    t1 = time.perf_counter()
-    ext = w.extrinsics[camera:camera + 1].cpu().numpy()
-    intr = w.intrinsics[camera:camera + 1].cpu().numpy()
-    verts = (2.0 * tri.vertices - 1.0).astype(np.float32)
+    verts = (np.float32(2.0) * tri.vertices - np.float32(1.0)).astype(np.float32)
     r = oracle.render_fused(ext, intr, w.image_shape, verts, tri.faces, tri.face_boundaries, tri.signed_distances,
-                            tri.spherical_harmonics, w.sh_degree, float(w.sharpness), w.background.cpu().numpy())
-    grad = (2.0 / r.image.size) * (r.image - w.target[camera:camera + 1].cpu().numpy())
-    h, wd = w.image_shape
-    rows, cols = -(-h // 16), -(-wd // 16)
-    kd = oracle.fused_key_defines()
+                            tri.spherical_harmonics, w.sh_degree, float(w.sharpness), bg, tile_shape=tile_shape)
+    bgc = bg[None, :, None, None]
+    x = r.raw[:, :3] + r.raw[:, 3:4] * bgc
+    grad = np.where((x >= 0) & (x <= 1), (2.0 / target.size) * (r.image - target), 0.0).astype(np.float32)
     graw = np.zeros_like(r.raw)
     graw[:, :3] = grad
-    graw[:, 3] = (grad * w.background.cpu().numpy()[None, :, None, None]).sum(1)
+    graw[:, 3] = (grad * bgc).sum(1)
     gcol, gsdf, _ = oracle.intersect_and_composite_backward(
         r.xy, r.colors, tri.signed_distances, tri.faces, float(w.sharpness), r.sorted_keys, r.sorted_tri,
-        r.tile_boundaries.reshape(1, rows * cols, 2), tri.face_boundaries.shape[0], (16, 16), w.image_shape, kd,
-        r.raw, graw)
-    oracle.evaluate_spherical_harmonics_backward(verts, tri.spherical_harmonics.shape, ext, w.sh_degree, r.colors,
-                                                 gcol)
-    t2 = time.perf_counter()
-    return t1 - t0, t2 - t1
+        r.tile_boundaries.reshape(b, -1, 2), tri.face_boundaries.shape[0], tile_shape, w.image_shape,
+        oracle.fused_key_defines(), r.raw, graw)
+    gsh = oracle.evaluate_spherical_harmonics_backward(verts, tri.spherical_harmonics.shape, ext, w.sh_degree,
+                                                       r.colors, gcol)
+    oracle.create_triangle_vertices_backward(sdf, sh.shape, np_vox[2], ls, tri.vertex_offsets, None, gsdf, gsh)
+    seconds = time.perf_counter() - t0
+    h, wd = w.image_shape
+    sizes = {"G": int(np_vox[2].shape[1]), "Nv": int(np_vox[3].shape[1]), "V": int(tri.vertices.shape[0]),
+             "F": int(tri.faces.shape[0]), "P": int(b * h * wd)}
+    return seconds, sizes
+
+
+def workload_config(w, sizes: dict) -> dict:
+    """The `config` object of both arms' bench lines (identical for the same
+    workload): what is computed, on which sizes, and how L2 is handled."""
+    h, wd = w.image_shape
+    cfg = w.config
+    return {
+        "workload": f"{cfg.name}: {cfg.resolution}^3 band around {cfg.num_spheres} spheres, SH deg {cfg.sh_degree}, "
+                    f"{len(cfg.level_sets)} shells, {w.extrinsics.shape[0]}x{h}x{wd}, fused fwd+bwd training step",
+        "sizes": {k: int(sizes[k]) for k in ("G", "Nv", "V", "F", "P")},
+        "l2": "GPU arm: flushed by a 256 MB write between timed steps; host arm: inputs far larger than the "
+              "host caches",
+    }
 
 
 def cpu_threads():
@@ -228,29 +276,33 @@ def host_workload(name: str):
 
 def run_reference(args, rank, world):
     """CPU restatement of the reference path on the host cores (rank 0 only;
-    under torchrun the other ranks return without work)."""
+    under torchrun the other ranks return without work). Every timed step is
+    one whole training step of the workload: all cameras, forward and
+    backward."""
     if rank != 0:
         return
     w = host_workload(args.config)
-    b = w.extrinsics.shape[0]
     times = []
+    sizes = None
     for i in range(args.warmup + args.steps):
-        tess_s, render_s = cpu_sample(w, i % b)
+        seconds, sizes = cpu_step(w)
         if i >= args.warmup:
-            times.append(tess_s + b * render_s)
+            times.append(seconds)
     ms = 1000.0 * statistics.mean(times)
-    h, wd = w.image_shape
+    b = w.extrinsics.shape[0]
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.config}: {w.config.resolution}^3 band, {w.config.num_spheres} spheres, "
-                               f"SH deg {w.sh_degree}, {w.level_sets.numel()} shells, {b}x{h}x{wd} fused fwd+bwd",
-                   "parallelism": "host threads"},
+        "config": workload_config(w, sizes),
         "impl": "reference",
+        "parallelism": f"host threads ({cpu_threads()})",
+        "tile_shape": [16, 16],
+        "timed_region_s": sum(times),
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": cpu_threads(), "kind": "port",
-                         "sample": f"per step: full tessellation fwd+bwd + fused render fwd+bwd of 1 of {b} cameras "
-                                   f"(round robin), render time x{b}"},
+                         "sample": f"each step: the whole training step on the host (tessellation of every shell, "
+                                   f"fused render of all {b} cameras, MSE through blend and clip, compositing, SH "
+                                   f"and vertex-interpolation backward into the grid)"},
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -272,7 +324,12 @@ def run_ours(args, rank, world, local):
     # The tile shape only splits the work (every pixel walks the same
     # triangles in the same order, so images and gradients are the same):
     # the step uses the fastest of a few shapes, timed as captured steps.
-    tile, tile_ms = autotune.tune_tile_shape(w, candidates=((8, 8), (16, 8), (16, 16)), repeats=5)
+    if args.tile:
+        tile = tuple(int(x) for x in args.tile.lower().split("x"))
+        w.tile_shape = tile
+        tile_ms = {}
+    else:
+        tile, tile_ms = autotune.tune_tile_shape(w, repeats=5)
 
     def eager_step():
         w.grid_sdf.grad = None
@@ -394,28 +451,26 @@ def run_ours(args, rank, world, local):
     if rank != 0:
         return
 
-    # Roofline of the dominant kernel (largest share of device time).
+    # Roofline of the dominant entry point (largest share of device time).
     peak, peak_kind = measured_peaks()
-    bytes_by_stage = pipeline.algorithmic_bytes(stats)
-    stage_of = {
-        "mt_intersect_and_composite_backward": "composite_bwd",
-        "mt_intersect_and_composite_forward": "composite_fwd",
-        "mt_sort_pairs_i64_i32": "sort",
-        "mt_create_triangle_vertices_backward": "create_vertices_bwd",
-        "mt_create_triangle_vertices": "create_vertices",
-        "mt_evaluate_spherical_harmonics_backward": "sh_bwd",
+    bytes_by_stage = pipeline.step_bytes(stats)
+    # Library entry point -> the step_bytes stages its kernels cover.
+    stages_of = {
+        "mt_intersect_and_composite_backward": ("composite_bwd",),
+        "mt_intersect_and_composite_forward": ("composite_fwd", "warp_masks"),
+        "mt_sort_keys_by_tile": ("tile_sort",),
+        "mt_bound_and_generate_keys": ("keys",),
+        "mt_grid_sh_colors": ("grid_sh_colors",),
+        "mt_create_triangle_faces": ("create_faces",),
     }
     totals = {k: sum(v) for k, v in per_call.items()}
     dominant = max(totals, key=totals.get)
     dom_ms = statistics.mean(per_call[dominant])
-    dom_bytes = bytes_by_stage.get(stage_of.get(dominant, ""), None)
+    dom_stages = stages_of.get(dominant)
+    dom_bytes = sum(bytes_by_stage[x] for x in dom_stages) if dom_stages else None
     achieved = (dom_bytes / (dom_ms * 1e-3) / 1e9) if dom_bytes else None
     total_bytes = sum(bytes_by_stage.values())
-    traffic = None
-    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_path):
-        with open(traffic_path) as f:
-            traffic = json.load(f).get(dominant)
+    traffic, traffic_note = profiled_traffic(dominant)
 
     b = stats["B"]
     h, wd = w.image_shape
@@ -432,16 +487,15 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": f"{args.config}: {w.config.resolution}^3 band around {w.config.num_spheres} spheres, "
-                        f"SH deg {w.sh_degree}, {stats['S']} shells, {b}x{h}x{wd}, fused fwd+bwd training step",
-            "sizes": {k: stats[k] for k in ("G", "Nv", "V", "F", "K", "P")},
-            "l2": "flushed (256 MB write) between timed steps",
-            "parallelism": "replicas" if world > 1 else "single GPU",
-            "tile_shape": list(tile),
-            "tile_autotune_ms": {f"{k[0]}x{k[1]}": v for k, v in tile_ms.items()},
-        },
+        "config": workload_config(w, stats),
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "tile_shape": list(tile),
+        "tile_autotune_ms": {"x".join(str(x) for x in k): v for k, v in tile_ms.items()},
+        "keys": stats["K"],
         "hbm_gbs": total_bytes / (ms * 1e-3) / 1e9,
+        "hbm_bytes_per_step": total_bytes,
+        "hbm_bytes_form": "compulsory bytes of the kernels the captured step runs (pipeline.step_bytes)",
+        "reference_algorithm_bytes_per_step": sum(pipeline.reference_algorithm_bytes(stats).values()),
         "step_ms_median": statistics.median(step_ms),
         "step_ms_p90": sorted(step_ms)[int(0.9 * (len(step_ms) - 1))],
         "wall_s_timed_region": wall,
@@ -460,7 +514,9 @@ def run_ours(args, rank, world, local):
             "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None,
             "traffic": traffic,
+            "traffic_source": traffic_note,
             "algorithmic_bytes_per_launch": dom_bytes,
+            "algorithmic_stages": list(dom_stages) if dom_stages else None,
             "launch_ms": dom_ms,
         },
         "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
@@ -474,17 +530,20 @@ def run_ours(args, rank, world, local):
     if not args.no_cameras and world == 1:
         line["cameras_batched"] = run_cameras(device, min(args.steps, 20))
     if not args.no_serving and world == 1:
-        line["serving"] = run_serving(device, args.serve_seconds)
+        line["serving"] = run_serving(device, args.serve_requests)
     if not args.no_large and world == 1:
         line["large"] = run_large(device, min(args.steps, 10))
     if not args.no_subdivision and world == 1:
         line["subdivision"] = run_subdivision(device, min(args.steps, 20), cpu=not args.no_cpu_baseline)
+    if not args.no_reference_cub and world == 1:
+        line["reference_cub"] = run_reference_cub(w)
     if not args.no_cpu_baseline and world == 1:
-        tess_s, render_s = cpu_sample(w, 0)
-        cpu_ms = 1000.0 * (tess_s + b * render_s)
+        cpu_s = [cpu_step(w)[0] for _ in range(3)]
+        cpu_ms = 1000.0 * statistics.median(cpu_s[1:])
         line["cpu_baseline"] = {
             "value": cpu_ms, "unit": "ms", "cores": cpu_threads(), "kind": "port",
-            "sample": f"full tessellation fwd+bwd + fused render fwd+bwd of 1 of {b} cameras, render time x{b}",
+            "sample": f"3 whole training steps of the workload on the host (tessellation of every shell, fused "
+                      f"render of all {b} cameras, MSE, every backward), median of the last 2",
         }
     print(json.dumps(line))
 
@@ -534,7 +593,7 @@ def run_cameras(device, steps):
                     f"{len(w.image_shapes)} cameras of 200-1600 px per side ({w.num_pixels} pixels), "
                     "fused fwd+bwd training step",
         "tile": list(tile),
-        "tile_ms": {f"{a}x{b}": v for (a, b), v in tile_ms.items()},
+        "tile_ms": {"x".join(str(x) for x in k): v for k, v in tile_ms.items()},
         "batched_graph_ms": batched_graph,
         "batched_eager_ms": eager_ms,
         "per_camera_eager_ms": plain_ms,
@@ -554,6 +613,8 @@ def run_large(device, steps):
 
     from meshtryoshka_gb300 import autotune, graph, pipeline
     from meshtryoshka_gb300 import triangle_extraction as te
+
+    from meshtryoshka_gb300 import triangle_rasterization as tr
 
     w = pipeline.build_workload("large", device)
     out = {}
@@ -575,15 +636,37 @@ def run_large(device, steps):
         peak = torch.cuda.max_memory_allocated(device) - resident
         out[mode] = {"eager_ms": autotune.time_ms(step, repeats=steps), "peak_hbm_gb": peak / 1e9,
                      "resident_gb": resident / 1e9}
+        if mode == "fused":  # the same step with no hit bits kept for the backward
+            budget = tr.HIT_BITS_BYTES_PER_PIXEL
+            tr.HIT_BITS_BYTES_PER_PIXEL = 0
+            w.grid_sdf.grad = None
+            w.grid_sh.grad = None
+            torch.cuda.empty_cache()
+            torch.cuda.reset_peak_memory_stats(device)
+            step()
+            torch.cuda.synchronize(device)
+            out[mode]["peak_hbm_gb_without_hit_bits"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
+            tr.HIT_BITS_BYTES_PER_PIXEL = budget
     w.grid_sdf.grad = None
     w.grid_sh.grad = None
-    captured = graph.CapturedTrainingStep(w)
+    with torch.no_grad():
+        _, stats = pipeline.forward(w, "fused")
+    # The captured step's footprint: its capacity-sized buffers, deferred SH,
+    # the contribution list and the hit bits, from the warm-up through the
+    # capture and one replay (peak above the resident scene).
+    torch.cuda.empty_cache()
+    resident = torch.cuda.memory_allocated(device)
+    torch.cuda.reset_peak_memory_stats(device)
+    captured = graph.CapturedTrainingStep(w, capacities=pipeline.Capacities.around(stats))
+    captured()
+    torch.cuda.synchronize(device)
+    out["fused"]["graph_peak_hbm_gb"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
     out["fused"]["graph_ms"] = autotune.time_ms(captured, repeats=steps)
-    _, stats = pipeline.forward(w, "fused")
     del captured
     # The captured step at the fastest tile shape (same images; the eager and
     # memory figures above stay at the reference's 16x16 tiles).
-    tile, tile_ms = autotune.tune_tile_shape(w, candidates=((8, 8), (16, 8), (16, 16)), repeats=steps)
+    tile, tile_ms = autotune.tune_tile_shape(w, candidates=((8, 8, 256), (8, 8, 512), (16, 8, 256), (16, 16, 256)),
+                                             repeats=steps)
     out["fused"]["graph_ms_tuned"] = tile_ms[tile]
     out["fused"]["graph_tile_shape"] = list(tile)
     w.tile_shape = (16, 16)
@@ -668,16 +751,97 @@ def run_subdivision(device, steps, cpu=True, config="mid"):
     return result
 
 
+def run_reference_cub(w, repeats=20):
+    """The reference's own CUB extensions (oracle/cub_ref.py: its
+    compute_exclusive_cumsum.cu and sort_keys.cu built as they are) against
+    this library's scan and sorts on the same GPU, on the step's sizes: the
+    vertex-count scan (S * G + 1 int32, in place) and the fused-layout keys of
+    the step's cameras at the reference's 16x16 tiles (stable signed 64-bit
+    pair sort). Device time per call, CUDA events, median of ``repeats``."""
+    import torch
+
+    from meshtryoshka_gb300 import _native as nt
+    from meshtryoshka_gb300 import pipeline
+    from meshtryoshka_gb300 import triangle_extraction as te
+    from meshtryoshka_gb300 import triangle_rasterization as tr
+    from oracle import cub_ref
+
+    try:
+        modules = cub_ref.load()
+    except Exception as exc:  # a build failure is reported, not fatal
+        return {"unavailable": f"reference CUB extensions did not build: {type(exc).__name__}: {exc}"[:300]}
+    if modules is None:
+        return {"unavailable": "reference CUB sources not staged (no reference checkout where this was built)"}
+    ref_scan, ref_sort = modules
+    device = w.grid_sdf.device
+    stream = torch.cuda.current_stream(device)
+    lib = nt.library()
+
+    def timed(fn, prepare):
+        times = []
+        for i in range(repeats + 3):
+            prepare()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            if i >= 3:
+                times.append(a.elapsed_time(b))
+        return statistics.median(times)
+
+    with torch.no_grad():
+        v = w.voxels
+        counts = te.count_triangle_vertices(w.grid_sdf, v.lower_corners, w.level_sets)
+        tri = te.tessellate_voxels(w.grid_sdf, v.vertices, w.grid_sh, v.neighbors, v.lower_corners, v.upper_corners,
+                                   v.indices, w.level_sets)
+        verts = pipeline.uncontract_stand_in(tri.vertices)
+        b = w.extrinsics.shape[0]
+        grid = tr.TileGrid((16, 16), w.image_shape, b, w.level_sets.numel())
+        kd = tr.create_key_defines(("camera", 6), ("tile", 20), ("depth", 32), ("shell", 6))
+        xy, depth = tr.project_vertices(verts, w.extrinsics, w.intrinsics)
+        bounds = tr.bound_triangles(xy, depth, tri.faces, grid, 0.2)
+        paired = tr.generate_keys(depth, tri.faces, tri.face_boundaries, bounds.tile_minima, bounds.tile_maxima,
+                                  bounds.num_tiles_overlapped, grid, kd)
+    n = counts.numel()
+    k = paired.keys.numel()
+    x = torch.empty_like(counts)
+    ws_ptr, ws_bytes = nt.workspace(device).get(lib.mt_scan_workspace_bytes(n))
+    refill = lambda: x.copy_(counts)  # noqa: E731
+    out = {"scan_elements": n, "sort_keys": k}
+    out["reference_scan_ms"] = timed(lambda: ref_scan.compute_exclusive_cumsum(x), refill)
+    out["ours_scan_ms"] = timed(lambda: nt.call("mt_exclusive_scan_i32", x.data_ptr(), n, ws_ptr, ws_bytes,
+                                                nt.stream(device)), refill)
+    want = x.clone()
+    ref_scan.compute_exclusive_cumsum(want.copy_(counts))
+    nt.call("mt_exclusive_scan_i32", x.copy_(counts).data_ptr(), n, ws_ptr, ws_bytes, nt.stream(device))
+    out["scan_identical"] = bool(torch.equal(x, want))
+    keys, idx = paired.keys.contiguous(), paired.triangle_indices.contiguous()
+    out["reference_sort_ms"] = timed(lambda: ref_sort.sort_keys(keys, idx, k), lambda: None)
+    ours = {}
+    out["ours_radix_sort_ms"] = timed(lambda: ours.update(p=tr.sort_keys(paired, grid)), lambda: None)
+    out["ours_tile_sort_and_delineate_ms"] = timed(
+        lambda: ours.update(t=tr._sort_and_delineate(paired, grid, kd, False)), lambda: None)
+    rk, rt = ref_sort.sort_keys(keys, idx, k)
+    out["sort_identical"] = bool(torch.equal(rk, ours["p"].keys) and torch.equal(rt, ours["p"].triangle_indices)
+                                 and torch.equal(rk, ours["t"][0].keys))
+    out["note"] = ("the reference sort is followed by its delineate_tiles kernel (Slang, not runnable here); the "
+                   "tile sort produces the sorted keys and the tile ranges in one entry point")
+    return out
+
+
 SERVE_RATES = (50, 200, 500, 1000, 2000)
+SERVE_REQUESTS = 2000
 
 
-def run_serving(device, seconds):
+def run_serving(device, requests_per_rate=SERVE_REQUESTS):
     """Serving sweep: four resident scenes (mid layout at 256^3 x2 and 128^3,
     large layout at 512^3; SH degree 3, 8 shells), Poisson arrivals at each
-    rate for `seconds`, 80 % render-only and 20 % render + gradient, images of
-    256-1920 x 256-1080 px. Continuous
-    batching (serving.Server) against the plain per-request form at the same
-    arrival times; p50 / p99 latency and throughput for both."""
+    rate for ``requests_per_rate`` requests, 80 % render-only and 20 % render
+    + gradient, images of 256-1920 x 256-1080 px. Continuous batching
+    (serving.Server) against the plain per-request form at the same arrival
+    times; p50 / p99 latency and throughput for both, and the server's peak
+    estimated bytes in flight against its budget."""
     import torch
 
     from meshtryoshka_gb300 import serving
@@ -690,26 +854,30 @@ def run_serving(device, seconds):
     torch.cuda.synchronize(device)
     rows = []
     for rate in SERVE_RATES:
-        window = max(seconds, 200.0 / rate)  # at least ~200 requests per rate for the p99
-        requests = serving.poisson_requests(scenes, float(rate), window, seed=4 + rate)
-        batched = serving.latency_summary(serving.Server(scenes).run(requests))
+        requests = serving.poisson_requests(scenes, float(rate), requests_per_rate / rate, seed=4 + rate)
+        server = serving.Server(scenes)
+        batched = serving.latency_summary(server.run(requests))
         torch.cuda.synchronize(device)
         plain = serving.latency_summary(serving.run_plain(scenes, requests))
         rows.append({"rate_rps": rate, "batched": batched, "plain": plain,
-                     "p99_ratio_plain_over_batched": plain["p99_ms"] / batched["p99_ms"]})
+                     "p99_ratio_plain_over_batched": plain["p99_ms"] / batched["p99_ms"],
+                     "peak_inflight_gb": server.peak_inflight_bytes / 1e9, "hbm_budget_gb": server.hbm_budget / 1e9})
         del requests
         torch.cuda.empty_cache()
     return {
         "workload": "4 resident scenes (mid layout at 256^3 x2 and 128^3, large layout at 512^3; 8 shells, SH deg "
-                    "3); Poisson arrivals, "
-                    f"max({seconds} s, 200 requests) per rate; 80 % render, 20 % render+gradient (MSE vs U[0,1] "
-                    "target); images 256-1920 x 256-1080, fov 40-70",
+                    f"3); Poisson arrivals, {requests_per_rate} requests per rate; 80 % render, 20 % render+gradient "
+                    "(MSE vs U[0,1] target); images 256-1920 x 256-1080, fov 40-70",
         "rates": rows,
     }
 
 
 def main():
     args = parse()
+    if args.steps is None:
+        args.steps = 5 if args.impl == "reference" else 200
+    if args.warmup is None:
+        args.warmup = 3 if args.impl == "reference" else 5
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -604,7 +604,9 @@ MT_API int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, i
  * gradients). Batches for K keys never exceed
  * K * ceil(tile_h * tile_w / 32) / 32 + camera_tiles * ceil(tile_h * tile_w / 32).
  * camera_tiles: the total tiles over cameras (B * rows * cols for a uniform
- * grid).
+ * grid). cta_threads (not in the reference, which runs one tile of
+ * TILE_H x TILE_W threads per CTA): 128, 256 or 512 threads per CTA of
+ * persistent warps (0 = 256); the results do not depend on it.
  * ---------------------------------------------------------------------- */
 MT_API size_t mt_composite_hit_bits_bytes(int64_t camera_tiles, int32_t tile_h, int32_t tile_w,
                                           int64_t batches);
@@ -618,13 +620,20 @@ MT_API int mt_intersect_and_composite_forward(
     const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
     uint32_t* warp_masks, uint64_t* work_counter, float* out, const float* target,
     const float* background, float loss_scale, float* loss_sum, void* hit_bits, size_t hit_bits_bytes,
-    mt_stream_t stream);
+    int32_t cta_threads, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
  * same keys. ssaa (1 = none): with ssaa > 1 (uniform cameras, H and W
  * multiples of ssaa) target is the factor written by mt_ssaa_loss and every
- * sub-pixel takes 1 / ssaa^2 of its output pixel's d L / d image. exact_adjoint = 0 reproduces the reference's gradient routing
+ * sub-pixel takes 1 / ssaa^2 of its output pixel's d L / d image.
+ * staging (not in the reference; NULL = off), 128-byte aligned, of at least
+ * mt_composite_staging_bytes(B, V) bytes: the backward packs every (camera,
+ * vertex) into a 32-byte record there, and each warp brings the vertex
+ * records of its next batch of triangles into shared memory with bulk copies
+ * (cp.async.bulk on an mbarrier) while it composites the current batch;
+ * same gradients. A bounded wait that gives up leaves MT_ERR_DEVICE_TIMEOUT
+ * in the staging status word. exact_adjoint = 0 reproduces the reference's gradient routing
  * (the outer hit's deferred gradient is scattered with the current hit's
  * barycentric weights); 1 uses the outer hit's own weights. */
 MT_API int mt_intersect_and_composite_backward(
@@ -638,7 +647,12 @@ MT_API int mt_intersect_and_composite_backward(
     const float* target, const float* background, float loss_scale,
     const float* grad_loss, int32_t ssaa, float* grad_colors, float* grad_signed_distances,
     float* grad_sharpness, int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
-    mt_stream_t stream);
+    void* staging, size_t staging_bytes, int32_t cta_threads, mt_stream_t stream);
+
+/* Bytes of the backward's optional staging scratch for B cameras and V
+ * vertices: a 128-byte header (a device status word at byte 0) and one
+ * 32-byte record (x, y, r, g, b, signed distance) per (camera, vertex). */
+MT_API size_t mt_composite_staging_bytes(int32_t B, int64_t V);
 
 /* MSE epilogue with SSAA (not in the reference, where the trainer applies
  * triangle_rasterization/__init__.py:274-287 and the loss as tensor ops):

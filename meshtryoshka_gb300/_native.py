@@ -99,14 +99,15 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_intersect_and_composite_forward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
-         c_float, P, P, c_size_t, P],
+         c_float, P, P, c_size_t, I32, P],
     ),
     "mt_composite_hit_bits_bytes": (c_size_t, [I64, I32, I32, I64]),
     "mt_intersect_and_composite_backward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P,
-         c_float, P, I32, P, P, P, I32, P, c_size_t, P],
+         c_float, P, I32, P, P, P, I32, P, c_size_t, P, c_size_t, I32, P],
     ),
+    "mt_composite_staging_bytes": (c_size_t, [I32, I64]),
     "mt_ssaa_loss": (I32, [P, I32, I32, I32, I32, P, P, c_float, P, P, P]),
     "mt_intersect": (I32, [P, I64, P, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, P]),
     "mt_interpolate": (I32, [P, P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),

@@ -1,12 +1,15 @@
-"""Tile-shape autotuning for the fused training step.
+"""Tile-shape and threads-per-CTA autotuning for the fused training step.
 
 Times the CUDA-graph training step (``graph.CapturedTrainingStep``) of a
-workload for each candidate tile shape (8x8, 16x16, 32x32 by default) with
-CUDA events and keeps the fastest; results are cached per workload shape so
-a trainer or server tunes once per scene/camera configuration. Every
-candidate renders the same images (the tile shape only changes the work
-decomposition), so tuning never changes results beyond atomic summation
-order in the gradients.
+workload for each candidate (tile height, tile width, threads per CTA of the
+compositing kernels) with CUDA events and keeps the fastest; results are
+cached per workload shape so a trainer or server tunes once per scene/camera
+configuration. The reference fixes one tile of TILE_H x TILE_W threads per
+CTA at compile time (triangle_rasterization/intersect_and_composite.py:11-21);
+here the tile (8, 16 or 32 pixels a side) sets the key lists and the CTA size
+(128, 256 or 512 threads of persistent warps) the launch. Every candidate
+renders the same images (both only change the work decomposition), so tuning
+never changes results beyond atomic summation order in the gradients.
 """
 
 from __future__ import annotations
@@ -17,7 +20,7 @@ import torch
 
 from . import graph, pipeline
 
-CANDIDATES = ((8, 8), (16, 16), (32, 32))
+CANDIDATES = ((8, 8, 128), (8, 8, 256), (8, 8, 512), (16, 8, 256), (16, 16, 256), (16, 16, 512), (32, 32, 256))
 _CACHE: dict = {}
 
 

@@ -43,6 +43,7 @@
 // The sharpness gradient is warp-reduced before one global atomic per warp.
 
 #include <atomic>
+#include <type_traits>
 
 #include "bary.cuh"
 #include "mt_common.cuh"
@@ -131,6 +132,59 @@ struct CompositeGrads {
   int exact;
 };
 
+// ---------------------------------------------------------------------------
+// Bulk-copy staging of the backward's triangles. Each (camera, vertex) is one
+// 32-byte record (x, y, r, g, b, signed distance, 0, 0) in a packed array;
+// while a warp composites one batch, the three records of every triangle of
+// its next batch are on their way into the warp's shared memory through
+// cp.async.bulk (one 32-byte copy per vertex), completing on the warp's
+// mbarrier. The waits are bounded: a wait that gives up records
+// MT_ERR_DEVICE_TIMEOUT and the warp stops.
+// ---------------------------------------------------------------------------
+struct alignas(16) VertexRecord {
+  float x, y, r, g, b, sdf, pad0, pad1;
+};
+constexpr int kWaitPolls = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase of parity `parity`; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+  for (int i = 0; i < kWaitPolls; ++i) {
+    if (mbar_test_wait(bar, parity)) return true;
+    __nanosleep(20);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy_to_shared(void* dst, const void* src, uint32_t bytes,
+                                                    unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
 // Per-warp shared-memory region.
 struct WarpForward {
   TriGeom geo[kBatch];
@@ -148,6 +202,19 @@ struct WarpBackward {
   int3 vids[kRing];
   float gslot[kRing][13];  // 12 used; stride 13 keeps lanes on distinct banks
   int queue[kQueue];
+};
+
+// The staged backward's region: the same, plus the next batch's vertex
+// records and their mbarrier.
+struct WarpBackwardStaged : WarpBackward {
+  VertexRecord stage[kBatch][3];
+  unsigned long long bar;
+  unsigned long long pad;
+};
+
+struct Staging {
+  const VertexRecord* records;  // [B, V] (NULL: no staging)
+  int* status;                  // device status word
 };
 
 __device__ __forceinline__ uint64_t field(uint64_t key, int off, int len) {
@@ -448,11 +515,11 @@ struct Pixel {
 
 // Work is a list of (camera, tile, warp-in-tile) items, warp-in-tile
 // fastest, cameras in order; warps are independent, so CTAs are containers of
-// kWarpsPerCta warps that each pull items from a device counter until the
-// list is exhausted (persistent warps: any camera sizes and tile loads in one
-// launch). Every tile size runs with the same 256-thread CTAs.
-constexpr int kWarpsPerCta = 8;
-constexpr int kCtaThreads = 32 * kWarpsPerCta;
+// 4, 8 or 16 warps (the caller's choice: 128, 256 or 512 threads per CTA,
+// where the reference runs one tile of TILE_H x TILE_W threads per CTA) that
+// each pull items from a device counter until the list is exhausted
+// (persistent warps: any camera sizes and tile loads in one launch).
+constexpr int kDefaultWarpsPerCta = 8;
 
 __device__ __forceinline__ int tile_warps(const CompositeArgs& a) { return (a.tile_h * a.tile_w + 31) / 32; }
 
@@ -623,7 +690,8 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   return sq;
 }
 
-__global__ void __launch_bounds__(kCtaThreads, 4)
+template <int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 32 / kWarps)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
                              unsigned long long* __restrict__ counter, float* __restrict__ loss_sum,
                              HitStore hs) {
@@ -689,9 +757,12 @@ __device__ __forceinline__ void flush_half(const CompositeArgs& a, const Composi
   __syncwarp();
 }
 
-__device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
-                                              const CompositeGrads& gr, WarpBackward& ws, const Pixel& px, int lane,
-                                              int64_t item, const HitStore& hs) {
+// Returns false when a staged wait gave up (the warp then stops).
+template <bool kStaged, typename WS>
+__device__ __forceinline__ bool backward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
+                                              const CompositeGrads& gr, WS& ws, const Pixel& px, int lane,
+                                              int64_t item, const HitStore& hs, const Staging& st,
+                                              uint32_t& phase) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
   const int cam = px.cam;
@@ -760,24 +831,90 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
   int queued = 0;
   int batch = 0;
   const int64_t hit_base = hs.batches ? (int64_t)hs.item_base[item] : -1;
-  while (__any_sync(0xffffffffu, active)) {
+  // Staged form: the next batch is formed one step ahead and its vertex
+  // records are in flight while the current batch composites.
+  int nb_next = 0, shell_next = 0;
+  bool stored_next = false;
+  uint32_t hits_next = 0, needed_next = 0;
+  int3 vid_next = make_int3(0, 0, 0);
+  auto form_next = [&](int b) {
     queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
-    const int nb = min(queued, kBatch);
-    if (nb == 0) break;
+    nb_next = min(queued, kBatch);
+    if (nb_next == 0) return;
+    stored_next = hit_base >= 0 && hit_base + b < hs.capacity;
+    hits_next = stored_next ? __ldcs(hs.batches + (hit_base + b) * 32 + lane) : 0u;
+    needed_next = stored_next ? __reduce_or_sync(0xffffffffu, hits_next) : 0xffffffffu;
+    const bool mine = lane < nb_next && ((needed_next >> lane) & 1u);
+    if (mine) {
+      const int64_t k = start + ws.queue[lane];
+      const int32_t f = __ldg(a.tri + k);
+      const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
+      vid_next = make_int3(__ldg(a.faces + 3 * (int64_t)f), __ldg(a.faces + 3 * (int64_t)f + 1),
+                           __ldg(a.faces + 3 * (int64_t)f + 2));
+      shell_next = (int)field(key, a.shell_off, a.shell_len);
+    }
+    const uint32_t copies = __popc(__ballot_sync(0xffffffffu, mine));
+    if constexpr (kStaged) {
+      if (lane == 0) mbar_arrive_expect_tx(&ws.bar, copies * 3 * (uint32_t)sizeof(VertexRecord));
+      __syncwarp();
+      if (mine) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const VertexRecord* r = st.records + (int64_t)cam * a.V;
+        bulk_copy_to_shared(&ws.stage[lane][0], r + vid_next.x, sizeof(VertexRecord), &ws.bar);
+        bulk_copy_to_shared(&ws.stage[lane][1], r + vid_next.y, sizeof(VertexRecord), &ws.bar);
+        bulk_copy_to_shared(&ws.stage[lane][2], r + vid_next.z, sizeof(VertexRecord), &ws.bar);
+      }
+    }
+    pop(ws.queue, queued, nb_next, lane);
+    queued -= nb_next;
+  };
+  if constexpr (kStaged) form_next(0);
+  while (__any_sync(0xffffffffu, active)) {
+    int nb;
+    bool stored;
+    uint32_t hits;
     const int half = batch & 1;
-    // The half being overwritten held batch - 2: flush it first.
-    if (batch >= 2) flush_half(a, gr, cam, ws, half, lane);
-    // The forward's hit bits for this batch when it stored them (the same
-    // walk, so the same bits); otherwise the test phase runs again. With
-    // stored bits only the triangles that some pixel of the warp hits are
-    // gathered (the other slots are never read).
-    const bool stored = hit_base >= 0 && hit_base + batch < hs.capacity;
-    uint32_t hits = stored ? __ldcs(hs.batches + (hit_base + batch) * 32 + lane) : 0u;
-    const uint32_t needed = stored ? __reduce_or_sync(0xffffffffu, hits) : 0xffffffffu;
-    if (lane < nb && ((needed >> lane) & 1u))
-      ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
-    pop(ws.queue, queued, nb, lane);
-    queued -= nb;
+    if constexpr (kStaged) {
+      nb = nb_next;
+      if (nb == 0) break;
+      stored = stored_next;
+      hits = hits_next;
+      const uint32_t needed = needed_next;
+      if (!mbar_wait(&ws.bar, phase & 1u)) {
+        if (lane == 0) set_device_error(st.status, MT_ERR_DEVICE_TIMEOUT);
+        return false;
+      }
+      ++phase;
+      if (batch >= 2) flush_half(a, gr, cam, ws, half, lane);
+      if (lane < nb && ((needed >> lane) & 1u)) {
+        const VertexRecord ra = ws.stage[lane][0], rb = ws.stage[lane][1], rc = ws.stage[lane][2];
+        TriGeom g;
+        setup_geometry(ra.x, ra.y, rb.x, rb.y, rc.x, rc.y, g);
+        g.shell = shell_next;
+        ws.geo[lane] = g;
+        ws.attr[lane] = TriAttr{{ra.r, ra.g, ra.b}, {rb.r, rb.g, rb.b}, {rc.r, rc.g, rc.b}, ra.sdf, rb.sdf, rc.sdf};
+        ws.vids[half * kBatch + lane] = vid_next;
+      }
+      __syncwarp();
+      form_next(batch + 1);  // the next batch's copies overlap this batch's compositing
+    } else {
+      queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
+      nb = min(queued, kBatch);
+      if (nb == 0) break;
+      // The half being overwritten held batch - 2: flush it first.
+      if (batch >= 2) flush_half(a, gr, cam, ws, half, lane);
+      // The forward's hit bits for this batch when it stored them (the same
+      // walk, so the same bits); otherwise the test phase runs again. With
+      // stored bits only the triangles that some pixel of the warp hits are
+      // gathered (the other slots are never read).
+      stored = hit_base >= 0 && hit_base + batch < hs.capacity;
+      hits = stored ? __ldcs(hs.batches + (hit_base + batch) * 32 + lane) : 0u;
+      const uint32_t needed = stored ? __reduce_or_sync(0xffffffffu, hits) : 0xffffffffu;
+      if (lane < nb && ((needed >> lane) & 1u))
+        ws.vids[half * kBatch + lane] = gather(a, cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
+      pop(ws.queue, queued, nb, lane);
+      queued -= nb;
+    }
     if (!stored && active) hits = batch_hits(ws.geo, nb, px.fx, px.fy, last_shell, ws.saved, lane);
     if (active) {
       int n = 0;
@@ -859,6 +996,17 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
     __syncwarp();
     ++batch;
   }
+  if constexpr (kStaged) {
+    // A batch formed ahead whose copies are still in flight: let them land
+    // before the stage is reused.
+    if (nb_next > 0) {
+      if (!mbar_wait(&ws.bar, phase & 1u)) {
+        if (lane == 0) set_device_error(st.status, MT_ERR_DEVICE_TIMEOUT);
+        return false;
+      }
+      ++phase;
+    }
+  }
   // The last hit's deferred gradient, with its own weights.
   if (px.in_image && last_shell != -1) {
     if (prev_batch >= batch - 2)
@@ -876,17 +1024,40 @@ __device__ __forceinline__ void backward_item(const CompositeArgs& a, const uint
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   if (lane == 0 && x != 0.f) atomicAdd(gr.grad_sharpness, x);
   __syncwarp();
+  return true;
 }
 
-__global__ void __launch_bounds__(kCtaThreads)
+template <bool kStaged>
+using WarpBackwardOf = typename std::conditional<kStaged, WarpBackwardStaged, WarpBackward>::type;
+
+// The unstaged form keeps to 80 registers (24 warps per SM) at every CTA size.
+template <bool kStaged, int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, kStaged ? 1 : (24 / kWarps > 0 ? 24 / kWarps : 1))
     composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr,
-                              unsigned long long* __restrict__ counter, HitStore hs) {
+                              unsigned long long* __restrict__ counter, HitStore hs, Staging st) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
-  WarpBackward& ws = reinterpret_cast<WarpBackward*>(smem_f4)[threadIdx.x >> 5];
+  WarpBackwardOf<kStaged>& ws = reinterpret_cast<WarpBackwardOf<kStaged>*>(smem_f4)[threadIdx.x >> 5];
+  uint32_t phase = 0;
+  if constexpr (kStaged) {
+    if (lane == 0) mbar_init(&ws.bar);
+    __syncwarp();
+  }
   const int64_t items = total_items(a);
   for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
-    backward_item(a, masks, gr, ws, pixel_of(a, item), lane, item, hs);
+    if (!backward_item<kStaged>(a, masks, gr, ws, pixel_of(a, item), lane, item, hs, st, phase)) return;
+}
+
+// Packed (camera, vertex) records for the staged backward.
+__global__ void pack_vertex_records_kernel(const float* __restrict__ xy, const float* __restrict__ colors,
+                                           const float* __restrict__ sdf, int64_t V, int B,
+                                           VertexRecord* __restrict__ out) {
+  const int64_t n = (int64_t)B * V;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = o % V;
+    const float2 p = reinterpret_cast<const float2*>(xy)[o];
+    out[o] = VertexRecord{p.x, p.y, colors[3 * o], colors[3 * o + 1], colors[3 * o + 2], __ldg(sdf + v), 0.f, 0.f};
+  }
 }
 
 // The MSE epilogue with SSAA (triangle_rasterization/__init__.py:274-287
@@ -945,9 +1116,15 @@ int check_args(const CompositeArgs& a) {
   return MT_OK;
 }
 
+// Warps per CTA for a requested threads-per-CTA (128, 256 or 512; anything
+// else, 0 included, gives the default 256).
+int cta_warps(int32_t threads) {
+  return threads == 128 ? 4 : threads == 512 ? 16 : kDefaultWarpsPerCta;
+}
+
 // Persistent grid: as many CTAs as fit on the device at once (queried once
 // per kernel and device), but no more than there are work items for.
-template <auto Kernel>
+template <auto Kernel, int kWarps>
 int persistent_ctas(const CompositeArgs& a, size_t smem, int64_t& ctas) {
   static std::atomic<int> resident[64];
   int device = 0;
@@ -956,13 +1133,13 @@ int persistent_ctas(const CompositeArgs& a, size_t smem, int64_t& ctas) {
   if (r == 0) {
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MT_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, kCtaThreads, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, 32 * kWarps, smem) != cudaSuccess)
       return MT_ERR_CUDA;
     r = max(1, sms * max(per_sm, 1));
     resident[device].store(r, std::memory_order_release);
   }
   const int64_t warps = a.total_tiles * ((a.tile_h * a.tile_w + 31) / 32);
-  const int64_t needed = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
+  const int64_t needed = (warps + kWarps - 1) / kWarps;
   ctas = needed < (int64_t)r ? needed : (int64_t)r;
   return MT_OK;
 }
@@ -1031,6 +1208,11 @@ using namespace mt;
 
 extern "C" {
 
+size_t mt_composite_staging_bytes(int32_t B, int64_t V) {
+  if (B <= 0 || V <= 0) return 0;
+  return 128 + (size_t)B * (size_t)V * sizeof(VertexRecord);
+}
+
 size_t mt_composite_hit_bits_bytes(int64_t camera_tiles, int32_t tile_h, int32_t tile_w, int64_t batches) {
   if (camera_tiles <= 0 || tile_h <= 0 || tile_w <= 0 || batches <= 0) return 0;
   if (batches > 0x7fffffff) batches = 0x7fffffff;
@@ -1047,7 +1229,8 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
                                        uint64_t* work_counter, float* out, const float* target,
                                        const float* background, float loss_scale, float* loss_sum,
-                                       void* hit_bits, size_t hit_bits_bytes, mt_stream_t stream) {
+                                       void* hit_bits, size_t hit_bits_bytes, int32_t cta_threads,
+                                       mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
@@ -1071,17 +1254,25 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
     warp_mask_kernel<<<grid_stride_blocks(K, 256), 256, 0, s>>>(a, K, num_keys, warp_masks);
     MT_CHECK_LAUNCH();
   }
-  const size_t smem = sizeof(WarpForward) * kWarpsPerCta;
-  rc = set_smem<composite_forward_kernel>(smem);
-  if (rc != MT_OK) return rc;
-  int64_t ctas = 0;
-  rc = persistent_ctas<composite_forward_kernel>(a, smem, ctas);
-  if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
-  composite_forward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hs);
-  MT_CHECK_LAUNCH();
-  return MT_OK;
+  auto launch = [&](auto warps) -> int {
+    constexpr int kW = decltype(warps)::value;
+    const size_t smem = sizeof(WarpForward) * kW;
+    int r = set_smem<composite_forward_kernel<kW>>(smem);
+    if (r != MT_OK) return r;
+    int64_t ctas = 0;
+    r = persistent_ctas<composite_forward_kernel<kW>, kW>(a, smem, ctas);
+    if (r != MT_OK) return r;
+    composite_forward_kernel<kW><<<(unsigned)ctas, 32 * kW, smem, s>>>(
+        a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hs);
+    MT_CHECK_LAUNCH();
+    return MT_OK;
+  };
+  switch (cta_warps(cta_threads)) {
+    case 4: return launch(std::integral_constant<int, 4>{});
+    case 16: return launch(std::integral_constant<int, 16>{});
+    default: return launch(std::integral_constant<int, 8>{});
+  }
 }
 
 int mt_intersect_and_composite_backward(const float* xy, const float* colors, const float* signed_distances,
@@ -1096,6 +1287,7 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         int32_t ssaa, float* grad_colors, float* grad_signed_distances,
                                         float* grad_sharpness,
                                         int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
+                                        void* staging, size_t staging_bytes, int32_t cta_threads,
                                         mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
@@ -1117,18 +1309,44 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   HitStore hs;
   rc = make_hit_store(a, const_cast<void*>(hit_bits), hit_bits_bytes, hs);
   if (rc != MT_OK) return rc;
-  const size_t smem = sizeof(WarpBackward) * kWarpsPerCta;
   cudaStream_t s = as_stream(stream);
-  rc = set_smem<composite_backward_kernel>(smem);
-  if (rc != MT_OK) return rc;
-  int64_t ctas = 0;
-  rc = persistent_ctas<composite_backward_kernel>(a, smem, ctas);
-  if (rc != MT_OK) return rc;
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
-  composite_backward_kernel<<<(unsigned)ctas, kCtaThreads, smem, s>>>(
-      a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hs);
-  MT_CHECK_LAUNCH();
-  return MT_OK;
+  const bool staged = staging != nullptr && staging_bytes >= mt_composite_staging_bytes(B, V);
+  Staging st{nullptr, nullptr};
+  if (staged) {
+    MT_REQUIRE((reinterpret_cast<uintptr_t>(staging) & 127) == 0);
+    st = Staging{reinterpret_cast<const VertexRecord*>(static_cast<char*>(staging) + 128),
+                 static_cast<int*>(staging)};
+    const int64_t n = (int64_t)B * V;
+    if (n > 0) {
+      pack_vertex_records_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(
+          xy, colors, signed_distances, V, B, const_cast<VertexRecord*>(st.records));
+      MT_CHECK_LAUNCH();
+    }
+  }
+  auto launch = [&](auto staged_c, auto warps) -> int {
+    constexpr bool kS = decltype(staged_c)::value;
+    constexpr int kW = decltype(warps)::value;
+    const size_t smem = sizeof(WarpBackwardOf<kS>) * kW;
+    int r = set_smem<composite_backward_kernel<kS, kW>>(smem);
+    if (r != MT_OK) return r;
+    int64_t ctas = 0;
+    r = persistent_ctas<composite_backward_kernel<kS, kW>, kW>(a, smem, ctas);
+    if (r != MT_OK) return r;
+    composite_backward_kernel<kS, kW><<<(unsigned)ctas, 32 * kW, smem, s>>>(
+        a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hs, st);
+    MT_CHECK_LAUNCH();
+    return MT_OK;
+  };
+  const int warps = cta_warps(cta_threads);
+  if (staged) {
+    if (warps == 4) return launch(std::true_type{}, std::integral_constant<int, 4>{});
+    if (warps == 16) return launch(std::true_type{}, std::integral_constant<int, 16>{});
+    return launch(std::true_type{}, std::integral_constant<int, 8>{});
+  }
+  if (warps == 4) return launch(std::false_type{}, std::integral_constant<int, 4>{});
+  if (warps == 16) return launch(std::false_type{}, std::integral_constant<int, 16>{});
+  return launch(std::false_type{}, std::integral_constant<int, 8>{});
 }
 
 int mt_ssaa_loss(const float* raw, int32_t B, int32_t H, int32_t W, int32_t ssaa, const float* background,

@@ -127,9 +127,9 @@ int launch_scan(const TI* in, TO* out, int64_t n, void* ws, size_t ws_bytes, cud
   if (ws_bytes < mt_scan_workspace_bytes(n)) return MT_ERR_WORKSPACE_TOO_SMALL;
   char* base = static_cast<char*>(ws);
   // Status word is cumulative across calls sharing a workspace: only the
-  // counter and descriptors are reset here.
-  if (cudaMemsetAsync(base + 4, 0, 4, stream) != cudaSuccess) return MT_ERR_CUDA;
-  if (cudaMemsetAsync(base + kScanHeader, 0, (size_t)tiles * 8, stream) != cudaSuccess) return MT_ERR_CUDA;
+  // counter and the descriptors are reset here, in one fill (with the unused
+  // header bytes between them).
+  if (cudaMemsetAsync(base + 4, 0, kScanHeader - 4 + (size_t)tiles * 8, stream) != cudaSuccess) return MT_ERR_CUDA;
   uint32_t* counter = reinterpret_cast<uint32_t*>(base + 4);
   uint64_t* desc = reinterpret_cast<uint64_t*>(base + kScanHeader);
   int* status = reinterpret_cast<int*>(base);

@@ -242,7 +242,7 @@ class Server:
     max_gradient_batch: int = 4  # render + gradient requests per batch (one shared tessellation)
     hbm_budget: int = 8 << 30  # estimated device bytes of the batches in flight (Scene.request_bytes)
     overlap_backlog: int = 1  # queued requests needed to start a batch while another is in flight
-    tile_shape: tuple[int, int] = (16, 16)
+    tile_shape: tuple[int, int] = (8, 8)  # the render path's fastest tile here (images do not depend on it)
     batches: int = field(default=0, init=False)
     peak_inflight_bytes: int = field(default=0, init=False)
 

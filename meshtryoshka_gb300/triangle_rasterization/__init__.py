@@ -109,12 +109,27 @@ class TileGrid:
     # camera-local tile index and tile ranges keep the [B, rows*cols, 2] shape
     # of the largest grid.
     camera_shapes: tuple[tuple[int, int], ...] | None = None
+    # Not in the reference: threads per CTA of the compositing kernels'
+    # persistent warps (128, 256 or 512; the reference runs one tile of
+    # TILE_H x TILE_W threads per CTA). A third element of ``tile_shape``
+    # sets it: (height, width, threads). Results do not depend on it.
+    cta_threads: int = 256
+
+    def __post_init__(self):
+        shape = tuple(int(x) for x in self.tile_shape)
+        if len(shape) == 3:
+            object.__setattr__(self, "cta_threads", shape[2])
+            shape = shape[:2]
+        if len(shape) != 2 or self.cta_threads not in (128, 256, 512):
+            raise ValueError(f"tile_shape must be (height, width) or (height, width, 128 | 256 | 512 threads), "
+                             f"not {self.tile_shape}")
+        object.__setattr__(self, "tile_shape", shape)
 
     @staticmethod
     def for_cameras(tile_shape, camera_shapes, num_shells) -> "TileGrid":
         shapes = tuple((int(h), int(w)) for h, w in camera_shapes)
         image = (max(h for h, _ in shapes), max(w for _, w in shapes))
-        return TileGrid(tuple(tile_shape), image, len(shapes), num_shells, shapes)
+        return TileGrid(tuple(tile_shape), image, len(shapes), num_shells, shapes)  # cta_threads from tile_shape
 
     @property
     def grid_shape(self) -> tuple[int, int]:
@@ -504,6 +519,18 @@ def evaluate_spherical_harmonics(vertices: Tensor, spherical_harmonics: Tensor, 
 # mode's 12 * num_shells B per pixel at 8 shells; 0 turns the store off.
 HIT_BITS_BYTES_PER_PIXEL = 16
 
+# Compositing backward with its triangles' vertex records staged into shared
+# memory by bulk copies (cp.async.bulk on an mbarrier), the next batch's while
+# the current one composites (not in the reference; same gradients).
+STAGED_BACKWARD = False
+
+
+def _staging(b: int, v: int, device) -> Tensor | None:
+    if not STAGED_BACKWARD:
+        return None
+    nbytes = int(nt.library().mt_composite_staging_bytes(b, v))
+    return torch.zeros((nbytes,), dtype=torch.uint8, device=device) if nbytes else None
+
 
 def _hit_bits(ctx, grid: TileGrid, num_keys: int, device) -> Tensor | None:
     """The hit-bit store for the forward and its backward (only when a
@@ -548,7 +575,7 @@ class IntersectAndComposite(torch.autograd.Function):
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
-                    0.0, None, nt.ptr(hits), _numel(hits), nt.stream(device))
+                    0.0, None, nt.ptr(hits), _numel(hits), grid.cta_threads, nt.stream(device))
             note(composite=out)
             ctx.hits = hits
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
@@ -570,12 +597,14 @@ class IntersectAndComposite(torch.autograd.Function):
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
             counter = torch.empty((1,), dtype=torch.int64, device=device)
+            staging = _staging(b, v, device)
             nt.call("mt_intersect_and_composite_backward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, 1, nt.ptr(grad_colors), nt.ptr(grad_sdf),
-                    nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), _numel(ctx.hits), nt.stream(device))
+                    nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), _numel(ctx.hits),
+                    nt.ptr(staging), _numel(staging), grid.cta_threads, nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
 
@@ -624,7 +653,8 @@ class IntersectCompositeLoss(torch.autograd.Function):
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out),
                     nt.ptr(target) if in_kernel else None, nt.ptr(background) if in_kernel else None, scale,
-                    loss.data_ptr() if in_kernel else None, nt.ptr(hits), _numel(hits), nt.stream(device))
+                    loss.data_ptr() if in_kernel else None, nt.ptr(hits), _numel(hits), grid.cta_threads,
+                    nt.stream(device))
             factor = target
             if not in_kernel:
                 factor = torch.empty_like(target)
@@ -651,13 +681,15 @@ class IntersectCompositeLoss(torch.autograd.Function):
             h, w = grid.image_shape
             rows, cols = grid.grid_shape
             counter = torch.empty((1,), dtype=torch.int64, device=device)
+            staging = _staging(b, v, device)
             nt.call("mt_intersect_and_composite_backward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), keys.numel(), nt.ptr(bounds), b,
                     num_shells, rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(), ssaa,
                     nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp), int(mode == "exact"),
-                    nt.ptr(ctx.hits), _numel(ctx.hits), nt.stream(device))
+                    nt.ptr(ctx.hits), _numel(ctx.hits), nt.ptr(staging), _numel(staging), grid.cta_threads,
+                    nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None, None, None, None)
 

@@ -613,3 +613,67 @@ def test_backward_with_and_without_stored_hit_bits(cuda_device, name, monkeypatc
     _close_grad(s1, s0, 1e-5)
     assert abs(h1 - h0) <= 1e-5 * max(abs(h0), 1e-12)
     assert np.abs(c0).max() > 0
+
+
+@pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside", "dense"])
+@pytest.mark.parametrize("budget", [16, 1, 0])
+def test_staged_backward_matches_unstaged(cuda_device, name, budget, monkeypatch):
+    """The backward whose vertex records arrive by bulk copies into shared
+    memory gives the gradients of the plain backward (up to the order of the
+    compositing atomics), with all, some or none of the hit bits stored."""
+    d = cuda_device
+    monkeypatch.setattr(tr, "HIT_BITS_BYTES_PER_PIXEL", budget)
+    scene = make_scene(**(DENSE if name == "dense" else SCENES[name]))
+    grid, kd, xy, depth, bounds, paired, sorted_, tb = _front(scene, d)
+    colors_np = oracle.evaluate_spherical_harmonics(scene.vertices, scene.sh, scene.extrinsics, scene.sh_degree)
+    b, s, t = grid.num_cameras, grid.num_shells, grid.num_tiles_per_image
+    g = None
+    grads = []
+    for staged in (False, True):
+        monkeypatch.setattr(tr, "STAGED_BACKWARD", staged)
+        colors = _t(colors_np, d).requires_grad_(True)
+        sdf = _t(scene.sdf, d).requires_grad_(True)
+        sharp = torch.tensor(scene.sharpness, device=d).requires_grad_(True)
+        out = tr.intersect_and_composite(xy, colors, sdf, _t(scene.faces, d), sharp, sorted_.keys,
+                                         sorted_.triangle_indices, tb.view(b, t, 2), s, grid, kd)
+        if g is None:
+            g = _t(np.random.default_rng(4).normal(0, 1, tuple(out.shape)).astype(np.float32), d)
+        out.backward(g)
+        grads.append((_n(colors.grad), _n(sdf.grad), float(sharp.grad)))
+    (c0, s0, h0), (c1, s1, h1) = grads
+    _close_grad(c1, c0, 1e-5)
+    _close_grad(s1, s0, 1e-5)
+    assert abs(h1 - h0) <= 1e-5 * max(abs(h0), 1e-12)
+    assert np.abs(c0).max() > 0
+
+
+def test_staged_backward_in_the_fused_loss_matches_oracle(cuda_device, monkeypatch):
+    monkeypatch.setattr(tr, "STAGED_BACKWARD", True)
+    scene = make_scene(**SCENES["three_cams_odd"])
+    _check_fused_backward(scene, cuda_device, "reference", (16, 16))
+
+
+@pytest.mark.parametrize("name", ["three_cams_odd", "multi_inside"])
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (16, 8)])
+def test_threads_per_cta_leave_results_unchanged(cuda_device, name, tile):
+    """The compositing kernels' CTA size (128, 256 or 512 threads of
+    persistent warps, the third element of tile_shape) only changes the
+    launch: identical images, the same gradients up to atomic order."""
+    scene = make_scene(**SCENES[name])
+    results = []
+    for threads in (256, 128, 512):
+        inputs = _fused_inputs(scene, cuda_device)
+        image = tr.render(**inputs, tile_shape=(*tile, threads), mode="fused")
+        g = _t(np.random.default_rng(7).normal(0, 1, tuple(image.shape)).astype(np.float32), cuda_device)
+        (image * g).sum().backward()
+        results.append((_n(image), _n(inputs["signed_distances"].grad), _n(inputs["spherical_harmonics"].grad)))
+    for img, gs, gh in results[1:]:
+        np.testing.assert_array_equal(img, results[0][0])
+        _close_grad(gs, results[0][1], 1e-5)
+        _close_grad(gh, results[0][2], 1e-5)
+
+
+def test_tile_grid_rejects_other_thread_counts():
+    with pytest.raises(ValueError):
+        tr.TileGrid((8, 8, 96), (64, 64), 1, 3)
+    assert tr.TileGrid((8, 8, 512), (64, 64), 1, 3).tile_shape == (8, 8)
