@@ -778,10 +778,14 @@ def run_reference_cub(w, repeats=20):
     lib = nt.library()
 
     def timed(fn, prepare):
+        # A device-side sleep ahead of the start event keeps the host's
+        # enqueue overhead (pybind for the reference, ctypes here) out of the
+        # device time of both.
         times = []
         for i in range(repeats + 3):
             prepare()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda._sleep(200_000)
             a.record(stream)
             fn()
             b.record(stream)

@@ -163,7 +163,12 @@ KERNELS_PER_CALL = {
 
 class LaunchRecorder:
     """Counts library kernel launches and optionally times every entry point
-    with CUDA events on the stream it was enqueued on."""
+    with CUDA events on the stream it was enqueued on. A timed call is
+    preceded by a short device-side sleep on that stream, so that the start
+    event fires only once the host has enqueued the call's kernels: the
+    recorded time is device time, without the host's enqueue overhead."""
+
+    SLEEP_CYCLES = 200_000  # about 0.1 ms at 2 GHz, more than one call's host overhead
 
     def __init__(self, timed: bool = False):
         self.launches = 0
@@ -201,6 +206,7 @@ def call(name: str, *args, launches: int | None = None) -> None:
         if rec.timed:
             start = torch.cuda.Event(enable_timing=True)
             end = torch.cuda.Event(enable_timing=True)
+            torch.cuda._sleep(rec.SLEEP_CYCLES)
             start.record()
     status = getattr(lib, name)(*args)
     if rec is not None and rec.timed:
