@@ -93,7 +93,7 @@ MT_API int mt_test_lookback_timeout(int32_t spin_limit, int64_t* prefix_out, voi
  * result as mt_exclusive_scan_i32, for callers that cannot allocate device
  * memory for scratch: a plain C/C++ host with no device allocator of its own,
  * or code whose host framework forbids new device allocations. Its scratch is
- * a fixed 131,328-byte __device__ array inside this library, resident on
+ * a fixed 87,640-byte __device__ array inside this library, resident on
  * every GPU that loads it until the process exits. Limits: n <=
  * mt_exclusive_scan_i32_static_max_elements() (2^26); larger n returns
  * MT_ERR_TOO_LARGE. All calls on a device share the array, so calls whose

@@ -54,7 +54,7 @@ namespace {
 constexpr int kBatch = 32;   // triangles gathered per warp batch
 constexpr int kQueue = 64;   // queued key offsets per warp
 constexpr int kRing = 64;    // gradient slots per warp (two batches)
-constexpr int kSavedFwd = 4;  // hits per lane per batch whose (u, v, w) the test phase keeps (forward)
+constexpr int kSavedFwd = 2;  // hits per pixel per batch whose samples the test phase keeps (forward)
 constexpr int kSavedBwd = 3;  // same, backward (its shared memory is tighter)
 // Hit-bit store (bytes): [0, 8) batch allocator, [8, 8 + 4 items) first
 // stored batch of each work item (int32, -1 = none), then from a 128-byte
@@ -82,10 +82,24 @@ struct alignas(16) TriAttr {
   float sa, sb, sc;
 };
 
+// The samples of up to K hits per pixel of a batch (the interpolated
+// signed distance's CDF and the interpolated colour), tagged with their
+// triangle: the forward's test phase solves pairs in dealt order, so a
+// pixel's hits arrive in no particular order. They depend on the hit alone,
+// not on the pixel's compositing state, so the lanes that solve the hits
+// compute them (all lanes busy) and the per-pixel compositing loop only
+// blends them.
+template <int K>
+struct TaggedSamples {
+  int tri[K][32];
+  float cdf[K][32];
+  float rgb[3][K][32];
+};
+
 // A (pixel, triangle) pair of the forward's test phase whose numerators
 // passed the fast reject; its divisions and acceptance test are pending.
 struct alignas(16) Candidate {
-  int id;  // pixel lane | triangle << 5 | the lane's candidate ordinal << 10
+  int id;  // pixel lane | triangle << 5
   float un, vn, wn;
 };
 constexpr int kCandRing = 64;  // ring of pending candidates per warp (solved 32 at a time)
@@ -189,10 +203,12 @@ __device__ __forceinline__ void bulk_copy_to_shared(void* dst, const void* src, 
 struct WarpForward {
   TriGeom geo[kBatch];
   TriAttr attr[kBatch];
-  SavedHits<kSavedFwd> saved;
+  TaggedSamples<kSavedFwd> saved;
   Candidate cand[kCandRing];
-  uint32_t rejected[32];  // per lane: candidates that failed the full test
+  uint32_t hitw[32];  // per pixel: bit i = triangle i of the batch is a hit
+  int nsaved[32];     // per pixel: hits solved in the batch (the first kSavedFwd are kept)
   int queue[kQueue];
+  uint8_t owner[32];  // test phase: triangle whose pairs start at each position of the current 32
 };
 
 struct WarpBackward {
@@ -336,6 +352,51 @@ __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int6
   }
 }
 
+// A sorted key's triangle: its vertex ids and its shell.
+struct TriRef {
+  int32_t ia, ib, ic;
+  int shell;
+};
+
+// Sorted key k -> its face -> the face's vertex ids (two levels of dependent
+// loads).
+__device__ __forceinline__ TriRef locate(const CompositeArgs& a, int64_t k) {
+  const int32_t f = __ldg(a.tri + k);
+  const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
+  return TriRef{__ldg(a.faces + 3 * (int64_t)f), __ldg(a.faces + 3 * (int64_t)f + 1),
+                __ldg(a.faces + 3 * (int64_t)f + 2), (int)field(key, a.shell_off, a.shell_len)};
+}
+
+// Stages a located triangle into batch slot `slot` (its projected corners
+// into `corners` when given): geometry and per-vertex colours and signed
+// distances.
+__device__ __forceinline__ void fetch(const CompositeArgs& a, int cam, const TriRef& r, TriGeom* geo, TriAttr* attr,
+                                      int slot, float2* corners = nullptr) {
+  const float2* xy = reinterpret_cast<const float2*>(a.xy) + (int64_t)cam * a.V;
+  const float2 pa = __ldg(xy + r.ia), pb = __ldg(xy + r.ib), pc = __ldg(xy + r.ic);
+  TriGeom g;
+  setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
+  g.shell = r.shell;
+  geo[slot] = g;
+  if (corners) {
+    corners[0] = pa;
+    corners[1] = pb;
+    corners[2] = pc;
+  }
+  const float* col = a.colors + (int64_t)cam * a.V * 3;
+  TriAttr t;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    t.ca[c] = __ldg(col + 3 * (int64_t)r.ia + c);
+    t.cb[c] = __ldg(col + 3 * (int64_t)r.ib + c);
+    t.cc[c] = __ldg(col + 3 * (int64_t)r.ic + c);
+  }
+  t.sa = __ldg(a.sdf + r.ia);
+  t.sb = __ldg(a.sdf + r.ib);
+  t.sc = __ldg(a.sdf + r.ic);
+  attr[slot] = t;
+}
+
 // Gathers triangle `k` of the sorted list into batch slot `slot`; returns its
 // vertex ids.
 __device__ __forceinline__ int3 gather(const CompositeArgs& a, int cam, int64_t k, TriGeom* geo, TriAttr* attr,
@@ -422,73 +483,211 @@ __device__ __forceinline__ uint32_t batch_hits(const TriGeom* geo, int nb, float
   return hits;
 }
 
+// ---------------------------------------------------------------------------
+// The forward's test phase, dealt over (pixel, triangle) pairs.
+//
+// A staged triangle can only be accepted at pixel centres inside its
+// conservative accept box (bary.cuh: cull_box; outside it the fast reject
+// fires). Its span is the set of the warp's pixels whose centres lie in that
+// box that no barycentric numerator provably rejects (edge_span): with 8x4
+// warp blocks, up to 4 rows of consecutive columns, one byte per row (first
+// column | count << 3); for other tile shapes every pixel of the warp (4
+// "rows" of 8 lanes). The pairs of all spans of a batch are numbered
+// triangle by triangle and dealt 32 at a time, one per lane, so that the warp
+// evaluates the barycentric numerators only where a hit is possible instead
+// of every lane testing every staged triangle.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kFullSpan = 0x40404040u;  // 4 rows, columns 0..7
+
+__device__ __forceinline__ uint32_t span_row(uint32_t span, int r) { return (span >> (8 * r)) & 0xffu; }
+
+__device__ __forceinline__ int span_count(uint32_t span) {
+  return (int)(((span >> 3) & 15u) + ((span >> 11) & 15u) + ((span >> 19) & 15u) + ((span >> 27) & 15u));
+}
+
+// Span of a staged triangle over the 8x4 block whose first pixel centre is
+// (bx, by), row by row: the columns of a row inside the accept box that none
+// of the three barycentric numerators provably rejects. edge_excludes applied
+// to a single pixel centre p says that numerator j rejects p when
+//   a qx + b qy + 2E (sx |qx| + sy |qy|) < thr,  q = p - P_j.
+// On a row (qy fixed) this reads g(qx) = a qx + 2E sx |qx| < R with
+// R = thr - b qy - 2E sy |qy|. When |a| > 2E sx, g is monotonic, so the
+// columns that survive form a ray bounded at the root of g(qx) = R (on the
+// side of zero that the sign of R selects), which is widened here by a
+// padding far above the rounding of this computation. Otherwise (an edge
+// within a few ulps of horizontal) g <= 4E sx |qx|, and the edge removes the
+// whole row when that bound stays below R at the row's farthest column.
+// Triangles without an exact fast reject (open accept box) span every pixel.
+__device__ __forceinline__ uint32_t edge_span(const TriGeom& g, const CullBox& box, float bx, float by) {
+  if (!(box.x0 > -__int_as_float(0x7f800000))) return kFullSpan;
+  constexpr float k2E = 0x1p-18f;  // 2 x 32 u, as in edge_excludes for one point
+  const TriangleBounds3 tb = triangle_bounds(g);
+  const EdgeBound eb[3] = {tb.v, tb.w, tb.u};
+  float slack[3], inv_lo[3], inv_hi[3];  // 2E sx, 1 / (a - 2E sx), 1 / (a + 2E sx)
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    slack[j] = k2E * eb[j].sx;
+    inv_lo[j] = __frcp_rn(eb[j].a - slack[j]);
+    inv_hi[j] = __frcp_rn(eb[j].a + slack[j]);
+  }
+  uint32_t span = 0u;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float y = by + (float)r;
+    if (!(y >= box.y0 && y <= box.y1)) continue;
+    float xl = box.x0, xu = box.x1;
+    bool empty = false;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const EdgeBound& e = eb[j];
+      const float qy = y - e.py;
+      const float R = g.thr - (e.b * qy + k2E * e.sy * fabsf(qy));
+      if (e.a > slack[j]) {  // g increasing: columns at or right of the root survive
+        const float q = R * (R <= 0.0f ? inv_lo[j] : inv_hi[j]);
+        xl = fmaxf(xl, e.px + q - (0.0625f + 0x1p-16f * (fabsf(e.px) + fabsf(q))));
+      } else if (e.a < -slack[j]) {  // g decreasing: columns at or left of the root survive
+        const float q = R * (R <= 0.0f ? inv_hi[j] : inv_lo[j]);
+        xu = fminf(xu, e.px + q + (0.0625f + 0x1p-16f * (fabsf(e.px) + fabsf(q))));
+      } else {
+        const float qf = fmaxf(fabsf(bx - e.px), fabsf(bx + 7.0f - e.px));
+        empty = empty || 2.02f * slack[j] * qf < R;
+      }
+    }
+    if (empty) continue;
+    const int c0 = max((int)ceilf(fmaxf(xl - bx, -1.0f)), 0);
+    const int c1 = min((int)floorf(fminf(xu - bx, 8.0f)), 7);
+    if (c0 <= c1) span |= ((uint32_t)c0 | ((uint32_t)(c1 - c0 + 1) << 3)) << (8 * r);
+  }
+  return span;
+}
+
+// Pixel lane of pair k (< span_count) of a span.
+__device__ __forceinline__ int span_pixel(uint32_t span, int k) {
+  const int n0 = (int)((span >> 3) & 15u), n1 = (int)((span >> 11) & 15u), n2 = (int)((span >> 19) & 15u);
+  const int t1 = n0, t2 = n0 + n1, t3 = n0 + n1 + n2;
+  const int row = (k >= t1) + (k >= t2) + (k >= t3);
+  const int before = row == 0 ? 0 : row == 1 ? t1 : row == 2 ? t2 : t3;
+  return 8 * row + (int)(span_row(span, row) & 7u) + (k - before);
+}
+
 // Solves `count` (<= 32) pending candidates starting at ring position
-// `head`, one per lane: the divisions and the acceptance test of hit_test. A
-// rejected candidate sets its triangle's bit in its pixel's `rejected` word;
-// an accepted one among its pixel's first K candidates keeps its (u, v, w).
-template <int K>
-__device__ __forceinline__ void solve_candidates(WarpForward& ws, int head, int count, int lane) {
+// `head`, one per lane: the divisions and the acceptance test of hit_test. An
+// accepted candidate sets its triangle's bit in its pixel's hit word and, if
+// it is among the first kSavedFwd hits solved for that pixel, keeps its
+// samples (sample_of) tagged with the triangle.
+__device__ __forceinline__ void sample_of(const TriAttr& t, float u, float v, float w, float s, float& cdf,
+                                          float (&rgb)[3]) {
+  float e;
+  cdf = sdf_to_cdf(interp(u, v, w, t.sa, t.sb, t.sc), s, e);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) rgb[c] = interp(u, v, w, t.ca[c], t.cb[c], t.cc[c]);
+}
+
+__device__ __forceinline__ void solve_candidates(WarpForward& ws, int head, int count, float s, int lane) {
   if (lane < count) {
     const Candidate c = ws.cand[(head + lane) & (kCandRing - 1)];
-    const int pl = c.id & 31, i = (c.id >> 5) & 31, n = c.id >> 10;
+    const int pl = c.id & 31, i = c.id >> 5;
     float u, v, w;
     if (solve_and_accept(c.un, c.vn, c.wn, ws.geo[i].dd, u, v, w)) {
-      if (n < K) {
-        ws.saved.u[n][pl] = u;
-        ws.saved.v[n][pl] = v;
-        ws.saved.w[n][pl] = w;
+      atomicOr(&ws.hitw[pl], 1u << i);
+      const int n = atomicAdd(&ws.nsaved[pl], 1);
+      if (n < kSavedFwd) {
+        float cdf, rgb[3];
+        sample_of(ws.attr[i], u, v, w, s, cdf, rgb);
+        ws.saved.tri[n][pl] = i;
+        ws.saved.cdf[n][pl] = cdf;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ws.saved.rgb[k][n][pl] = rgb[k];
       }
-    } else {
-      atomicOr(&ws.rejected[pl], 1u << i);
     }
   }
 }
 
-// Test phase of a batch with the divisions dealt across the warp. Every lane
-// evaluates the numerators of every staged triangle (the whole warp busy);
-// the (pixel, triangle) pairs that pass the fast reject are queued in a ring
-// and solved 32 at a time, one per lane, instead of by the few lanes whose
-// pixels a triangle covers while the others idle. Triangles of shells the
-// pixel has already passed are skipped, as in batch_hits. Returns the lane's
-// candidate bits (bit i: triangle i passed the fast reject) and sets `hits`
-// to those that passed the full test: the decisions and (u, v, w) of
-// hit_test, the (u, v, w) kept by candidate ordinal.
-__device__ __forceinline__ uint32_t dealt_batch_hits(WarpForward& ws, int nb, float fx, float fy, int last_shell,
-                                                     bool active, int lane, uint32_t& hits) {
+// Test phase of a batch. `span` is the span of the lane's staged triangle (0
+// for lanes at or past the batch); `blocked`: 8x4 warp blocks, whose first
+// pixel centre is (bx, by); s: the sharpness. Returns the pixel's hit bits: bit i = triangle i
+// passes the exact hit test (hit_test's decision) and its shell is above
+// `last_shell`; pixels that are not active have none.
+__device__ __forceinline__ uint32_t span_batch_hits(WarpForward& ws, uint32_t span, bool blocked, float bx, float by,
+                                                    float fx, float fy, int last_shell, bool active, float s,
+                                                    int lane) {
   const uint32_t lt = lanemask_lt();
-  ws.rejected[lane] = 0u;
-  uint32_t cand = 0;
-  int n = 0, head = 0, tail = 0;
-  for (int i = 0; i < nb; ++i) {
-    const TriGeom g = load_geom(&ws.geo[i]);
-    float un, vn, wn;
-    numerators(g, fx, fy, un, vn, wn);
-    const bool pass = active && g.shell > last_shell && numerators_pass(g, un, vn, wn);
-    const uint32_t m = __ballot_sync(0xffffffffu, pass);
-    if (pass) {
-      ws.cand[(tail + __popc(m & lt)) & (kCandRing - 1)] = Candidate{lane | (i << 5) | (n << 10), un, vn, wn};
-      cand |= 1u << i;
-      ++n;
+  ws.hitw[lane] = 0u;
+  ws.nsaved[lane] = 0;
+  // Pairs before this lane's triangle (exclusive scan of the span sizes);
+  // lanes past the batch have no pairs, so their offset is the total.
+  const int cnt = span_count(span);
+  int inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, inc, 31);
+  const int off = inc - cnt;
+  const int ls = active ? last_shell : 0x7fffffff;  // an inactive pixel passes nothing
+  int head = 0, tail = 0;
+  for (int base = 0; base < total; base += 32) {
+    // Each triangle with pairs among [base, base + 32) marks where its first
+    // one there falls; the pair's triangle is the last mark at or before it.
+    const bool here = cnt > 0 && off < base + 32 && off + cnt > base;
+    const int first = max(off, base) - base;
+    __syncwarp();
+    if (here) ws.owner[first] = (uint8_t)lane;
+    const uint32_t starts = __reduce_or_sync(0xffffffffu, here ? 1u << first : 0u);
+    __syncwarp();
+    const int i = ws.owner[31 - __clz(starts & (0xffffffffu >> (31 - lane)))];
+    const int q = base + lane;
+    const int p = span_pixel(__shfl_sync(0xffffffffu, span, i), q - __shfl_sync(0xffffffffu, off, i)) & 31;
+    const float qx = __shfl_sync(0xffffffffu, fx, p), qy = __shfl_sync(0xffffffffu, fy, p);
+    const float px = blocked ? bx + (float)(p & 7) : qx, py = blocked ? by + (float)(p >> 3) : qy;
+    const int pls = __shfl_sync(0xffffffffu, ls, p);
+    bool pass = false;
+    float un = 0.f, vn = 0.f, wn = 0.f;
+    if (q < total) {
+      const TriGeom g = load_geom(&ws.geo[i]);
+      numerators(g, px, py, un, vn, wn);
+      pass = g.shell > pls && numerators_pass(g, un, vn, wn);
     }
+    const uint32_t m = __ballot_sync(0xffffffffu, pass);
+    if (pass) ws.cand[(tail + __popc(m & lt)) & (kCandRing - 1)] = Candidate{p | (i << 5), un, vn, wn};
     tail += __popc(m);
     if (tail - head >= 32) {  // at most 63 pending: one round empties below 32
       __syncwarp();
-      solve_candidates<kSavedFwd>(ws, head, 32, lane);
+      solve_candidates(ws, head, 32, s, lane);
       head += 32;
       __syncwarp();
     }
   }
   if (tail > head) {
     __syncwarp();
-    solve_candidates<kSavedFwd>(ws, head, tail - head, lane);
+    solve_candidates(ws, head, tail - head, s, lane);
   }
   __syncwarp();
-  hits = cand & ~ws.rejected[lane];
-  return cand;
+  return ws.hitw[lane];
+}
+
+// Samples of the pixel's hit on triangle i (g) of the batch: kept by the
+// forward's test phase (ns tagged entries), or formed again.
+__device__ __forceinline__ void hit_samples(const WarpForward& ws, int ns, int i, int lane, const TriGeom& g,
+                                            float fx, float fy, float s, float& cdf, float (&rgb)[3]) {
+  int slot = -1;
+#pragma unroll
+  for (int n = 0; n < kSavedFwd; ++n)
+    if (n < ns && ws.saved.tri[n][lane] == i) slot = n;
+  if (slot >= 0) {
+    cdf = ws.saved.cdf[slot][lane];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rgb[k] = ws.saved.rgb[k][slot][lane];
+  } else {
+    float u, v, w;
+    hit_test(g, fx, fy, u, v, w);
+    sample_of(ws.attr[i], u, v, w, s, cdf, rgb);
+  }
 }
 
 // (u, v, w) of the lane's n-th hit in the batch (triangle g): kept by the
-// test phase, or solved again.
+// backward's test phase, or solved again.
 template <int K>
 __device__ __forceinline__ void hit_weights(const SavedHits<K>& saved, int n, int lane, const TriGeom& g, float fx,
                                             float fy, float& u, float& v, float& w) {
@@ -626,38 +825,50 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   int queued = 0;
   int batch = 0;
   const int64_t hit_base = hs.batches ? reserve_hit_batches(hs, masks, start, end, px.wt, item, lane) : -1;
+  // With 8x4 warp blocks a triangle's span is the part of its accept box on
+  // the block (lane 0 holds the block's first pixel); otherwise every pixel.
+  const bool blocked = (a.tile_w & 7) == 0 && (a.tile_h & 3) == 0;
+  const float bx = __shfl_sync(0xffffffffu, px.fx, 0), by = __shfl_sync(0xffffffffu, px.fy, 0);
+  // Each batch's triangles are located (sorted key -> face -> vertex ids)
+  // one batch ahead, while the previous batch is tested and composited, so
+  // that staging a batch waits on one level of dependent loads only.
+  queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
+  int nb = min(queued, kBatch);
+  TriRef ref{0, 0, 0, 0};
+  if (lane < nb) ref = locate(a, start + ws.queue[lane]);
   while (__any_sync(0xffffffffu, active)) {
-    queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
-    const int nb = min(queued, kBatch);
     if (nb == 0) break;
-    if (lane < nb) gather(a, px.cam, start + ws.queue[lane], ws.geo, ws.attr, lane);
+    uint32_t span = 0u;
+    if (lane < nb) {
+      float2 c[3];
+      fetch(a, px.cam, ref, ws.geo, ws.attr, lane, c);
+      if (blocked) {
+        const TriGeom& g = ws.geo[lane];
+        span = edge_span(g, cull_box(g, c[0].x, c[0].y, c[1].x, c[1].y, c[2].x, c[2].y), bx, by);
+      } else {
+        span = kFullSpan;
+      }
+    }
     pop(ws.queue, queued, nb, lane);
     queued -= nb;
-    uint32_t hits = 0;
-    uint32_t cand = dealt_batch_hits(ws, nb, px.fx, px.fy, last_shell, active, lane, hits);
+    queued = refill(masks, start, end, next, queued, ws.queue, px.wt, lane);
+    const int nb_next = min(queued, kBatch);
+    if (lane < nb_next) ref = locate(a, start + ws.queue[lane]);
+    uint32_t hits = span_batch_hits(ws, span, blocked, bx, by, px.fx, px.fy, last_shell, active, s, lane);
     if (hit_base >= 0 && hit_base + batch < hs.capacity) __stcs(hs.batches + (hit_base + batch) * 32 + lane, hits);
     ++batch;
     if (active) {
-      int n = 0;
-      while (cand) {
-        const int i = __ffs(cand) - 1;
-        cand &= cand - 1;
-        const int k = n++;  // candidate ordinal: the index of kept (u, v, w)
-        if (!((hits >> i) & 1u)) continue;
+      const int ns = min(ws.nsaved[lane], kSavedFwd);
+      while (hits) {
+        const int i = __ffs(hits) - 1;
+        hits &= hits - 1;
         const TriGeom& g = ws.geo[i];
         if (g.shell <= last_shell) continue;
-        float u, v, w;
-        hit_weights(ws.saved, k, lane, g, px.fx, px.fy, u, v, w);
-        const TriAttr& t = ws.attr[i];
-        const float sdf_in = interp(u, v, w, t.sa, t.sb, t.sc);
-        float e_in;
-        const float inner_cdf = sdf_to_cdf(sdf_in, s, e_in);
+        float inner_cdf, rgb[3];
+        hit_samples(ws, ns, i, lane, g, px.fx, px.fy, s, inner_cdf, rgb);
         const float alpha = clamp01(alpha_raw(outer_cdf, inner_cdf));
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float rgb = interp(u, v, w, t.ca[c], t.cb[c], t.cc[c]);
-          acc[c] = over(acc[c], rgb, T_, alpha);
-        }
+        for (int c = 0; c < 3; ++c) acc[c] = over(acc[c], rgb[c], T_, alpha);
         T_ = __fmul_rn(T_, __fsub_rn(1.0f, alpha));
         outer_cdf = inner_cdf;
         last_shell = g.shell;
@@ -667,6 +878,7 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
         }
       }
     }
+    nb = nb_next;
     __syncwarp();
   }
   float sq = 0.0f;

@@ -4,11 +4,21 @@
 // (triangle_extraction/compute_exclusive_cumsum.cu:8-39) and the int64
 // torch.cumsum of triangle_rasterization/generate_keys.py:48.
 //
-// One kernel per scan: tiles of 256 threads x 16 items are claimed in launch
-// order through an atomic counter, so every predecessor of a tile has already
-// started when the tile looks back, and the look-back always terminates. The
-// wait is still bounded: after kSpinLimit polls a tile records
-// MT_ERR_DEVICE_TIMEOUT in the workspace status word and stops waiting.
+// One kernel per scan. Tiles of 256 threads x 48 elements (24 for 64-bit
+// results) are claimed in launch order through an atomic counter, so every
+// predecessor of a tile has already started when the tile looks back, and
+// the look-back always terminates. The wait is still bounded: after
+// kSpinLimit polls a tile records MT_ERR_DEVICE_TIMEOUT in the workspace
+// status word and stops waiting.
+//
+// Each warp owns a run of consecutive elements of its tile and moves them
+// with 16-byte vector accesses in warp-contiguous rounds (round r, lane l:
+// the vector at 16 (32 r + l) bytes of the run), so every load and store
+// instruction of the warp covers one contiguous 512-byte span, with
+// streaming cache hints (the data is touched once). The scan runs in that
+// striped order: within each vector, across the lanes of a round (warp
+// shuffles), across the rounds, across the CTA's warps, then across tiles
+// (look-back by one warp).
 //
 // Workspace layout: [0,4) status, [4,8) tile counter, [256, 256+8*tiles)
 // tile descriptors. Descriptor = (inclusive-or-aggregate value << 2) | flag.
@@ -22,99 +32,97 @@ namespace mt {
 namespace {
 
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;
-constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr size_t kScanHeader = 256;
 
-// Loads kScanItems consecutive elements owned by this thread.
-template <typename TI, typename TO, bool kVector>
-__device__ __forceinline__ void load_items(const TI* in, int64_t first, int64_t n, TO (&x)[kScanItems]) {
-  if (kVector && first + kScanItems <= n) {
-    constexpr int kPer = 16 / sizeof(TI);
-    const int4* p = reinterpret_cast<const int4*>(in + first);
-#pragma unroll
-    for (int v = 0; v < kScanItems / kPer; ++v) {
-      int4 w = p[v];
-      const TI* e = reinterpret_cast<const TI*>(&w);
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) x[v * kPer + k] = (TO)e[k];
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) x[k] = (first + k < n) ? (TO)in[first + k] : (TO)0;
-  }
+// Elements per thread: 48, or 24 when the results are 64-bit (registers).
+template <typename TO>
+constexpr int scan_items() {
+  return sizeof(TO) == 4 ? 48 : 24;
 }
 
-template <typename TO, bool kVector>
-__device__ __forceinline__ void store_items(TO* out, int64_t first, int64_t n, const TO (&x)[kScanItems]) {
-  if (kVector && first + kScanItems <= n) {
-    constexpr int kPer = 16 / sizeof(TO);
-    int4* p = reinterpret_cast<int4*>(out + first);
-#pragma unroll
-    for (int v = 0; v < kScanItems / kPer; ++v) {
-      int4 w;
-      TO* e = reinterpret_cast<TO*>(&w);
-#pragma unroll
-      for (int k = 0; k < kPer; ++k) e[k] = x[v * kPer + k];
-      p[v] = w;
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
-      if (first + k < n) out[first + k] = x[k];
-  }
-}
+// The smallest tile of any scan here: workspaces are sized by it.
+constexpr int kScanTileMin = kScanThreads * 24;
 
 template <typename TI, typename TO, bool kInclusive, bool kVector>
 __global__ void __launch_bounds__(kScanThreads)
     scan_kernel(const TI* in, TO* out, int64_t n, uint32_t* counter, uint64_t* desc, int* status) {
+  constexpr int kItems = scan_items<TO>();
+  constexpr int V = 16 / (int)sizeof(TI);  // elements per 16-byte vector
+  constexpr int R = kItems / V;            // vectors per thread
+  constexpr int kWarps = kScanThreads / 32;
   __shared__ uint32_t s_tile;
-  __shared__ TO s_warp[kScanThreads / 32];
+  __shared__ TO s_warp[kWarps];
   __shared__ TO s_prefix;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(counter, 1u);
   __syncthreads();
   const int64_t tile = s_tile;
-  const int64_t first = tile * kScanTile + (int64_t)tid * kScanItems;
-
-  TO x[kScanItems];
-  load_items<TI, TO, kVector>(in, first, n, x);
-
-  // Thread-local inclusive scan.
+  const int64_t seg = tile * (kScanThreads * kItems) + (int64_t)warp * (32 * kItems);
+  const bool full = kVector && seg + 32 * kItems <= n;
+  TO x[R][V];
 #pragma unroll
-  for (int k = 1; k < kScanItems; ++k) x[k] += x[k - 1];
-  const TO thread_total = x[kScanItems - 1];
+  for (int r = 0; r < R; ++r) {
+    const int64_t first = seg + (int64_t)(32 * r + lane) * V;
+    if (full) {
+      const int4 w = __ldcs(reinterpret_cast<const int4*>(in + first));
+      const TI* e = reinterpret_cast<const TI*>(&w);
+#pragma unroll
+      for (int v = 0; v < V; ++v) x[r][v] = (TO)e[v];
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v) x[r][v] = (first + v < n) ? (TO)in[first + v] : (TO)0;
+    }
+  }
 
-  // Block-wide scan of the thread totals.
-  TO inc = warp_inclusive_sum(thread_total);
-  if (lane == 31) s_warp[warp] = inc;
+  // Within each vector, then across the lanes of each round, then across
+  // the rounds.
+  TO lane_excl[R];
+  TO warp_total = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+#pragma unroll
+    for (int v = 1; v < V; ++v) x[r][v] += x[r][v - 1];
+    const TO inc = warp_inclusive_sum(x[r][V - 1]);
+    lane_excl[r] = inc - x[r][V - 1] + warp_total;
+    warp_total += __shfl_sync(0xffffffffu, inc, 31);
+  }
+  if (lane == 0) s_warp[warp] = warp_total;
   __syncthreads();
   if (warp == 0) {
-    TO w = (lane < kScanThreads / 32) ? s_warp[lane] : (TO)0;
-    TO wi = warp_inclusive_sum(w);
-    if (lane < kScanThreads / 32) s_warp[lane] = wi - w;  // exclusive per warp
-    const TO block_total = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
-
+    const TO w = lane < kWarps ? s_warp[lane] : (TO)0;
+    const TO wi = warp_inclusive_sum(w);
+    if (lane < kWarps) s_warp[lane] = wi - w;  // exclusive per warp
+    const TO block_total = __shfl_sync(0xffffffffu, wi, kWarps - 1);
     const TO prefix = lookback_prefix<TO>(desc, tile, block_total, status);
     if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
+  const TO offset = s_prefix + s_warp[warp];
 
-  const TO offset = s_prefix + s_warp[warp] + (inc - thread_total);
-  if (kInclusive) {
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) x[k] += offset;
-  } else {
-    TO prev = offset;
+  for (int r = 0; r < R; ++r) {
+    const int64_t first = seg + (int64_t)(32 * r + lane) * V;
+    const TO base = lane_excl[r] + offset;
+    TO y[V];
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-      TO cur = x[k] + offset;
-      x[k] = prev;
-      prev = cur;
+    for (int v = 0; v < V; ++v) y[v] = kInclusive ? base + x[r][v] : (v == 0 ? base : base + x[r][v - 1]);
+    if (full) {
+      constexpr int kOut = 16 / (int)sizeof(TO);  // results per 16-byte store
+#pragma unroll
+      for (int v = 0; v < V; v += kOut) {
+        int4 w;
+        TO* e = reinterpret_cast<TO*>(&w);
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) e[k] = y[v + k];
+        __stcs(reinterpret_cast<int4*>(out + first + v), w);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        if (first + v < n) out[first + v] = y[v];
     }
   }
-  store_items<TO, kVector>(out, first, n, x);
 }
 
 template <typename TI, typename TO, bool kInclusive>
@@ -122,8 +130,9 @@ int launch_scan(const TI* in, TO* out, int64_t n, void* ws, size_t ws_bytes, cud
   MT_REQUIRE(n >= 0);
   if (n == 0) return MT_OK;
   MT_REQUIRE(in != nullptr && out != nullptr && ws != nullptr);
-  const int64_t tiles = (n + kScanTile - 1) / kScanTile;
-  MT_REQUIRE(tiles < (int64_t)0xffffffff);
+  constexpr int64_t kTile = (int64_t)kScanThreads * scan_items<TO>();
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  MT_REQUIRE(tiles < (int64_t)0x7fffffff);
   if (ws_bytes < mt_scan_workspace_bytes(n)) return MT_ERR_WORKSPACE_TOO_SMALL;
   char* base = static_cast<char*>(ws);
   // Status word is cumulative across calls sharing a workspace: only the
@@ -163,7 +172,7 @@ extern "C" {
 
 size_t mt_scan_workspace_bytes(int64_t n) {
   if (n < 0) n = 0;
-  const int64_t tiles = (n + mt::kScanTile - 1) / mt::kScanTile;
+  const int64_t tiles = (n + mt::kScanTileMin - 1) / mt::kScanTileMin;
   return mt::kScanHeader + (size_t)(tiles > 0 ? tiles : 1) * 8;
 }
 
@@ -210,7 +219,7 @@ int mt_test_lookback_timeout(int32_t spin_limit, int64_t* prefix_out, void* ws, 
 // Limits and sharing rules:
 //   * at most kStaticScanMaxElements (2^26 = 67,108,864) elements per call;
 //     larger sizes are rejected with MT_ERR_TOO_LARGE before any work;
-//   * the array (131,328 bytes) is resident on every GPU that loads this
+//   * the array (87,640 bytes) is resident on every GPU that loads this
 //     library, until the process exits;
 //   * every call on a device shares the same array and re-initialises the
 //     parts that must start at zero, so calls whose work overlaps on the GPU
@@ -230,7 +239,7 @@ namespace {
 
 constexpr int64_t kStaticScanMaxElements = (int64_t)1 << 26;
 constexpr size_t kStaticScanBytes =
-    kScanHeader + (size_t)((kStaticScanMaxElements + kScanTile - 1) / kScanTile) * 8;
+    kScanHeader + (size_t)((kStaticScanMaxElements + kScanTileMin - 1) / kScanTileMin) * 8;
 constexpr int kStaticScanMaxContexts = 64;
 
 static __device__ __align__(256) unsigned char g_static_scan_scratch[kStaticScanBytes];

@@ -88,6 +88,29 @@ def test_exclusive_cumsum_unaligned_view(cuda_device):
     assert int(base[0]) == 7
 
 
+@pytest.mark.parametrize("n", [1, 511, 4097, 1_000_003])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_scan_i64_and_widening(cuda_device, n, offset):
+    """The int64 exclusive scan and the int32 -> int64 inclusive scan (keys'
+    offsets), with sums past 2^31, on 16-byte aligned and unaligned views."""
+    from meshtryoshka_gb300 import _native as nt
+
+    rng = np.random.default_rng(n + 3 * offset)
+    lib = nt.library()
+    ws_ptr, ws_bytes = nt.workspace(cuda_device).get(lib.mt_scan_workspace_bytes(n))
+    stream = nt.stream(cuda_device)
+    x64 = rng.integers(0, 1 << 40, n).astype(np.int64)
+    base64 = _t(np.concatenate((np.zeros(offset, np.int64), x64)), cuda_device)
+    view64 = base64[offset:]
+    nt.call("mt_exclusive_scan_i64", view64.data_ptr(), n, ws_ptr, ws_bytes, stream)
+    np.testing.assert_array_equal(_n(view64), np.concatenate(([0], np.cumsum(x64)[:-1])))
+    x32 = rng.integers(0, 1 << 30, n).astype(np.int32)
+    base32 = _t(np.concatenate((np.zeros(offset, np.int32), x32)), cuda_device)
+    out = torch.empty(n + offset, dtype=torch.int64, device=cuda_device)[offset:]
+    nt.call("mt_inclusive_scan_i32_to_i64", base32[offset:].data_ptr(), out.data_ptr(), n, ws_ptr, ws_bytes, stream)
+    np.testing.assert_array_equal(_n(out), np.cumsum(x32.astype(np.int64)))
+
+
 def _sphere_scene(n, levels, sh_coeffs=4, seed=0):
     coords = -1 + (np.arange(n) + 0.5) * 2 / n
     z, y, x = np.meshgrid(coords, coords, coords, indexing="ij")
