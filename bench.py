@@ -619,10 +619,10 @@ def run_large(device, steps):
     w = pipeline.build_workload("large", device)
     out = {}
     for mode in ("fused", "explicit"):
-        def step(mode=mode):
+        def step(mode=mode, defer_sh=False):
             w.grid_sdf.grad = None
             w.grid_sh.grad = None
-            pipeline.training_step(w, mode)
+            pipeline.training_step(w, mode, defer_sh=defer_sh)
 
         step()
         torch.cuda.synchronize(device)
@@ -647,20 +647,38 @@ def run_large(device, steps):
             torch.cuda.synchronize(device)
             out[mode]["peak_hbm_gb_without_hit_bits"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
             tr.HIT_BITS_BYTES_PER_PIXEL = budget
+        # The same step with vertex colours from the grid SH (no [C, V, 3]
+        # rows, which dominate the peaks above): the two modes then differ by
+        # the explicit mode's per-shell buffers.
+        step(defer_sh=True)
+        torch.cuda.synchronize(device)
+        w.grid_sdf.grad = None
+        w.grid_sh.grad = None
+        torch.cuda.empty_cache()
+        torch.cuda.reset_peak_memory_stats(device)
+        step(defer_sh=True)
+        torch.cuda.synchronize(device)
+        out[mode]["peak_hbm_gb_deferred_sh"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
     w.grid_sdf.grad = None
     w.grid_sh.grad = None
     with torch.no_grad():
         _, stats = pipeline.forward(w, "fused")
-    # The captured step's footprint: its capacity-sized buffers, deferred SH,
-    # the contribution list and the hit bits, from the warm-up through the
-    # capture and one replay (peak above the resident scene).
+    # The captured step's footprint: the device memory its graph holds (its
+    # private pool: capacity-sized buffers with a 1.25 margin, deferred SH,
+    # the contribution list, the hit bits) plus the library workspace it
+    # reads, above the resident scene.
+    w.grid_sdf.grad = None
+    w.grid_sh.grad = None
     torch.cuda.empty_cache()
+    reserved = torch.cuda.memory_reserved(device)
     resident = torch.cuda.memory_allocated(device)
     torch.cuda.reset_peak_memory_stats(device)
     captured = graph.CapturedTrainingStep(w, capacities=pipeline.Capacities.around(stats))
     captured()
     torch.cuda.synchronize(device)
-    out["fused"]["graph_peak_hbm_gb"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
+    out["fused"]["graph_construction_peak_hbm_gb"] = (torch.cuda.max_memory_allocated(device) - resident) / 1e9
+    torch.cuda.empty_cache()
+    out["fused"]["graph_held_hbm_gb"] = (torch.cuda.memory_reserved(device) - reserved) / 1e9
     out["fused"]["graph_ms"] = autotune.time_ms(captured, repeats=steps)
     del captured
     # The captured step at the fastest tile shape (same images; the eager and

@@ -180,12 +180,14 @@ def forward_counted(w: Workload, caps: Capacities, gradient_mode: str | None = N
 
 def forward(w: Workload, mode: str = "fused", gradient_mode: str | None = None,
             grid_sdf: Tensor | None = None, grid_sh: Tensor | None = None,
-            target: Tensor | None = None) -> tuple[Tensor, dict]:
+            target: Tensor | None = None, defer_sh: bool = False) -> tuple[Tensor, dict]:
+    """The eager step's forward in either render mode. ``defer_sh``: vertex
+    colours straight from the grid SH (no per-vertex SH rows; same values)."""
     grid_sdf = w.grid_sdf if grid_sdf is None else grid_sdf
     grid_sh = w.grid_sh if grid_sh is None else grid_sh
     target = w.target if target is None else target
     tri = te.tessellate_voxels(grid_sdf, w.voxels.vertices, grid_sh, w.voxels.neighbors, w.voxels.lower_corners,
-                               w.voxels.upper_corners, w.voxels.indices, w.level_sets)
+                               w.voxels.upper_corners, w.voxels.indices, w.level_sets, defer_sh=defer_sh)
     with torch.no_grad():
         vertices = uncontract_stand_in(tri.vertices)
     if mode == "fused" and w.fused_loss and target is w.target:

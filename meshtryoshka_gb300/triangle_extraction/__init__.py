@@ -437,6 +437,14 @@ def count_triangle_vertices(signed_distances: Tensor, lower_corners: Tensor, lev
     return counts
 
 
+# The grid SH backward forms each vertex's SH gradient once into scratch
+# (48 floats per vertex) and then gathers it per grid vertex; above this many
+# bytes of scratch (2.8 M vertices) it runs its one-pass form instead, which
+# forms a vertex's gradient once per list entry and needs no scratch (same
+# values): at the 512^3 / 16-shell scene the scratch would hold 3.5 GB.
+GRID_SH_BACKWARD_SCRATCH_LIMIT = 512 << 20
+
+
 class DeferredSH:
     """Per-vertex SH coefficients that are never formed (not in the
     reference): stands where ``Triangles.spherical_harmonics`` holds the
@@ -502,7 +510,11 @@ class GridSHColors(torch.autograd.Function):
             device = vertices.device
             grad_gsh = torch.empty(ctx.gsh_shape, dtype=torch.float32, device=device)  # fully written
             v = vertices.shape[0]
-            ws_ptr, ws_bytes = nt.workspace(device).get(nt.library().mt_grid_sh_colors_backward_workspace_bytes(v))
+            need = nt.library().mt_grid_sh_colors_backward_workspace_bytes(v)
+            if need <= GRID_SH_BACKWARD_SCRATCH_LIMIT:
+                ws_ptr, ws_bytes = nt.workspace(device).get(need)
+            else:
+                ws_ptr, ws_bytes = None, 0  # the one-pass form: no scratch
             nt.call("mt_grid_sh_colors_backward", nt.ptr(d.list_offsets), nt.ptr(d.contributions), g, v,
                     nt.ptr(vertices), c, ctx.sh_degree, nt.ptr(campos), campos.shape[0], nt.ptr(colors),
                     nt.ptr(grad_colors.contiguous()), nt.ptr(grad_gsh), nt.ptr(d.num_vertices), ws_ptr, ws_bytes,
@@ -826,6 +838,7 @@ def tessellate_voxels(
     indices: Tensor,
     level_sets: Tensor,
     t_gradient: str = "detached",
+    defer_sh: bool = False,
 ) -> Triangles:
     """Marching cubes over every level set (triangle_extraction/__init__.py:75-157).
 
@@ -837,9 +850,16 @@ def tessellate_voxels(
     vertex's edge-crossing weight t = (iso - d0) / (d1 - d0) as a function of
     its two corner SDFs (topology stays fixed); the default "detached" gives
     the reference's gradients.
+
+    ``defer_sh`` (not in the reference): ``Triangles.spherical_harmonics`` is
+    a ``DeferredSH`` instead of the [C, V, 3] rows, as in
+    ``tessellate_voxels_counted`` (same colours and gradients; the rows are
+    neither written nor read). Applies when the level sets are at most
+    ``mt_vertex_grad_list_max_shells()``.
     """
+    defer = defer_sh and level_sets.shape[0] <= nt.library().mt_vertex_grad_list_max_shells()
     triangles, _ = _tessellate(signed_distances, vertices, spherical_harmonics, neighbors, lower_corners,
-                               upper_corners, indices, level_sets, None, t_gradient=t_gradient)
+                               upper_corners, indices, level_sets, None, defer, t_gradient=t_gradient)
     return triangles
 
 

@@ -6,6 +6,8 @@ single precision, round to nearest, no fused multiply-add):
   mask kernel clears is rejected by the barycentric test's fast reject at
   every pixel centre (adversarial triangles: slivers, sub-pixel, repeated
   vertices, vertices on pixel centres, huge);
+* the compositing forward's spans (edge_span): every pixel centre of a warp
+  block that escapes the fast reject lies in its triangle's span;
 * tile bounds with power-of-two tiles: division by 2^k equals multiplication
   by 2^-k for every float32, and the shifted integer division agrees with
   C's truncating one under max(., 0);
@@ -49,7 +51,7 @@ def _setup(p1, p2, p3):
     fast = dd > f32(2.0 ** -20) and dd < INF
     thr = -f32(dd * f32(2.0 ** -100)) if fast else -INF
     return dict(p1=p1, p2=p2, e12=(e12x, e12y), e13=(e13x, e13y), d1212=d1212, d1213=d1213, d1313=d1313,
-                d1223=d1223, d1323=d1323, thr=thr)
+                d1223=d1223, d1323=d1323, thr=thr, dd=dd)
 
 
 def _numerators(g, px, py):
@@ -150,6 +152,94 @@ def test_excluded_blocks_are_fast_rejected_everywhere():
                 rejected = (un < g["thr"]) | (vn < g["thr"]) | (wn < g["thr"])
                 assert rejected.all(), (p, bx, by)
     assert checked > 10000 and excluded > checked // 4  # the exclusion is exercised
+
+
+def _cull_box(g, p):
+    """The accept box of the warp culling (bary.cuh: cull_box); None when open."""
+    xmin, xmax = f32(p[:, 0].min()), f32(p[:, 0].max())
+    ymin, ymax = f32(p[:, 1].min()), f32(p[:, 1].max())
+    ext = max(f32(xmax - xmin), f32(ymax - ymin))
+    if not ext < 8192 or not all(abs(v) < 1e6 for v in (xmin, xmax, ymin, ymax)) or not g["thr"] > -INF:
+        return None
+    e23 = (f32(p[2, 0] - p[1, 0]), f32(p[2, 1] - p[1, 1]))
+    l23 = _dot2(e23[0], e23[1], e23[0], e23[1])
+    worst = max(f32(g["d1212"] * g["d1313"]), f32(g["d1212"] * l23), f32(g["d1313"] * l23))
+    if not g["dd"] >= f32(f32(1e-4) * worst):
+        return None
+    m = f32(f32(1) + f32(f32(1e-3) * ext))
+    return (f32(xmin - m), f32(xmax + m), f32(ymin - m), f32(ymax + m))
+
+
+def _edge_span(g, box, bx, by):
+    """composite.cu edge_span: per row of the 8x4 block, the surviving column
+    range (or None)."""
+    if box is None:
+        return [(0, 7)] * 4
+    k2e = f32(2.0 ** -18)
+    e12, e13 = g["e12"], g["e13"]
+    edges = []
+    for A, C, P, eX, eY in ((g["d1313"], g["d1213"], g["p1"], e12, e13), (g["d1212"], g["d1213"], g["p1"], e13, e12),
+                            (g["d1223"], g["d1323"], g["p2"], e13, e12)):
+        a = f32(f32(A * eX[0]) - f32(C * eY[0]))
+        b = f32(f32(A * eX[1]) - f32(C * eY[1]))
+        sx = f32(abs(f32(A * eX[0])) + abs(f32(C * eY[0])))
+        sy = f32(abs(f32(A * eX[1])) + abs(f32(C * eY[1])))
+        slack = f32(k2e * sx)
+        with np.errstate(divide="ignore", over="ignore"):
+            edges.append((a, b, sy, P, slack, f32(f32(1) / f32(a - slack)), f32(f32(1) / f32(a + slack))))
+    rows = []
+    for r in range(4):
+        y = f32(by + f32(r))
+        if not (box[2] <= y <= box[3]):
+            rows.append(None)
+            continue
+        xl, xu, empty = box[0], box[1], False
+        for a, b, sy, P, slack, inv_lo, inv_hi in edges:
+            qy = f32(y - P[1])
+            rr = f32(g["thr"] - f32(f32(b * qy) + f32(f32(k2e * sy) * abs(qy))))
+            with np.errstate(over="ignore", invalid="ignore"):
+                if a > slack:
+                    q = f32(rr * (inv_lo if rr <= 0 else inv_hi))
+                    pad = f32(f32(0.0625) + f32(f32(2.0 ** -16) * f32(abs(P[0]) + abs(q))))
+                    xl = np.fmax(xl, f32(f32(P[0] + q) - pad))
+                elif a < -slack:
+                    q = f32(rr * (inv_hi if rr <= 0 else inv_lo))
+                    pad = f32(f32(0.0625) + f32(f32(2.0 ** -16) * f32(abs(P[0]) + abs(q))))
+                    xu = np.fmin(xu, f32(f32(P[0] + q) + pad))
+                else:
+                    qf = max(abs(f32(bx - P[0])), abs(f32(f32(bx + f32(7)) - P[0])))
+                    empty = empty or f32(f32(f32(2.02) * slack) * qf) < rr
+        c0 = max(int(np.ceil(np.fmax(f32(xl - bx), f32(-1)))), 0)
+        c1 = min(int(np.floor(np.fmin(f32(xu - bx), f32(8)))), 7)
+        rows.append(None if empty or c0 > c1 else (c0, c1))
+    return rows
+
+
+def test_forward_spans_hold_every_pixel_that_escapes_the_fast_reject():
+    rng = np.random.default_rng(3)
+    lx, ly = np.meshgrid(np.arange(8), np.arange(4))
+    passing = in_span = 0
+    for p in _triangles(rng, 1500):
+        g = _setup(p[0], p[1], p[2])
+        box = _cull_box(g, p)
+        lo = np.floor(p.min(0)).astype(int) - 9
+        hi = np.floor(p.max(0)).astype(int) + 9
+        for bx in range(lo[0] - lo[0] % 8, hi[0] + 1, 8):
+            for by in range(lo[1] - lo[1] % 4, hi[1] + 1, 4):
+                px = (bx + lx + 0.5).astype(f32).ravel()
+                py = (by + ly + 0.5).astype(f32).ravel()
+                un, vn, wn = _numerators(g, px, py)
+                escapes = ~((un < g["thr"]) | (vn < g["thr"]) | (wn < g["thr"]))
+                if not escapes.any():
+                    continue
+                rows = _edge_span(g, box, f32(bx + 0.5), f32(by + 0.5))
+                covered = np.array([rows[k // 8] is not None and rows[k // 8][0] <= k % 8 <= rows[k // 8][1]
+                                    for k in range(32)])
+                assert not (escapes & ~covered).any(), (p, bx, by, rows)
+                passing += int(escapes.sum())
+                in_span += int(covered.sum())
+    print(f"pixel centres escaping the fast reject {passing}, in spans {in_span}")
+    assert passing > 10000 and in_span < 8 * passing  # exercised, and the spans are tight
 
 
 def test_power_of_two_tile_division_is_a_multiply():

@@ -172,6 +172,32 @@ def test_deferred_sh_matches_rows_bit_for_bit(cuda_device, config):
     assert float(out[True][1].abs().max()) > 0
 
 
+def test_grid_sh_backward_without_scratch_matches_two_pass(cuda_device, monkeypatch):
+    """The one-pass grid SH backward (taken when the two-pass form's scratch
+    would exceed its limit) gives the two-pass form's bits."""
+    w = pipeline.build_workload("small", cuda_device)
+    args = (w.voxels.vertices, None, w.voxels.neighbors, w.voxels.lower_corners, w.voxels.upper_corners,
+            w.voxels.indices, w.level_sets)
+    with torch.no_grad():
+        _, stats = pipeline.forward(w)
+    caps = pipeline.Capacities.around(stats)
+    grads = []
+    for limit in (te.GRID_SH_BACKWARD_SCRATCH_LIMIT, 0):
+        monkeypatch.setattr(te, "GRID_SH_BACKWARD_SCRATCH_LIMIT", limit)
+        gsh = w.grid_sh.detach().clone().requires_grad_(True)
+        a = list(args)
+        a[1] = gsh
+        tri, counts = te.tessellate_voxels_counted(w.grid_sdf.detach(), *a, caps.vertices, caps.faces, defer_sh=True)
+        verts = pipeline.uncontract_stand_in(tri.vertices.detach())
+        colors = tr.evaluate_spherical_harmonics(verts, tri.spherical_harmonics, w.extrinsics, w.sh_degree)
+        dcol = torch.randn(colors.shape, generator=torch.Generator(device=cuda_device).manual_seed(9),
+                           device=cuda_device)
+        dcol[:, int(counts.num_vertices):] = 0
+        grads.append(torch.autograd.grad(colors, gsh, dcol)[0])
+    torch.testing.assert_close(grads[1], grads[0], rtol=0, atol=0)
+    assert float(grads[0].abs().max()) > 0
+
+
 def test_captured_step_input_set_with_other_cameras(cuda_device):
     """A batch with other cameras in set 1 (more keys): the step detects an
     overflow if there is one, re-captures with capacities measured over every
