@@ -620,7 +620,7 @@ MT_API int mt_intersect_and_composite_forward(
     const int32_t* layout, const int64_t* cameras, int64_t camera_tiles,
     uint32_t* warp_masks, uint64_t* work_counter, float* out, const float* target,
     const float* background, float loss_scale, float* loss_sum, void* hit_bits, size_t hit_bits_bytes,
-    int32_t cta_threads, mt_stream_t stream);
+    int32_t* tile_order, size_t tile_order_bytes, int32_t cta_threads, mt_stream_t stream);
 
 /* Backward: accumulates (+=) into grad_colors [B,V,3], grad_signed_distances
  * [V], grad_sharpness [1]. warp_masks as written by the forward call on the
@@ -647,7 +647,19 @@ MT_API int mt_intersect_and_composite_backward(
     const float* target, const float* background, float loss_scale,
     const float* grad_loss, int32_t ssaa, float* grad_colors, float* grad_signed_distances,
     float* grad_sharpness, int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
-    void* staging, size_t staging_bytes, int32_t cta_threads, mt_stream_t stream);
+    void* staging, size_t staging_bytes, const int32_t* tile_order, size_t tile_order_bytes,
+    int32_t cta_threads, mt_stream_t stream);
+
+/* Bytes of the optional tile order of the compositing kernels (not in the
+ * reference, whose CTAs take tiles in grid order): int32 bucket counts and
+ * cursors, then one global tile index per tile (camera_tiles of them). With
+ * a tile order the forward sorts the tiles by descending key count (buckets
+ * of 8 keys) and its persistent warps take the tiles' work items in that
+ * order, so the few expensive tiles start first instead of last; the
+ * backward, given the same buffer after the forward on the same keys, takes
+ * the items in the same order. NULL: launch order. Results do not depend on
+ * the order (the gradients' atomic sums may round in another order). */
+MT_API size_t mt_composite_tile_order_bytes(int64_t camera_tiles);
 
 /* Bytes of the backward's optional staging scratch for B cameras and V
  * vertices: a 128-byte header (a device status word at byte 0) and one

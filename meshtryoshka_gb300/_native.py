@@ -99,13 +99,14 @@ _SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "mt_intersect_and_composite_forward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P,
-         c_float, P, P, c_size_t, I32, P],
+         c_float, P, P, c_size_t, P, c_size_t, I32, P],
     ),
     "mt_composite_hit_bits_bytes": (c_size_t, [I64, I32, I32, I64]),
+    "mt_composite_tile_order_bytes": (c_size_t, [I64]),
     "mt_intersect_and_composite_backward": (
         I32,
         [P, P, P, I64, P, P, P, P, I64, P, I32, I32, I32, I32, I32, I32, I32, I32, P, P, I64, P, P, P, P, P, P,
-         c_float, P, I32, P, P, P, I32, P, c_size_t, P, c_size_t, I32, P],
+         c_float, P, I32, P, P, P, I32, P, c_size_t, P, c_size_t, P, c_size_t, I32, P],
     ),
     "mt_composite_staging_bytes": (c_size_t, [I32, I64]),
     "mt_ssaa_loss": (I32, [P, I32, I32, I32, I32, P, P, c_float, P, P, P]),
@@ -153,7 +154,7 @@ KERNELS_PER_CALL = {
     "mt_create_voxels": 1,
     "mt_create_triangle_vertices": 2,  # vertices + source records, SH rows (1 without the rows)
     "mt_create_triangle_vertices_backward": 5,  # corner inverse, count, scan, list + grads, SH gather
-    "mt_intersect_and_composite_forward": 2,  # warp masks, composite
+    "mt_intersect_and_composite_forward": 4,  # warp masks, tile-order histogram and scatter, composite
     "mt_sort_keys_by_tile": 7,  # count, scan, tile ranges, scatter, tiny / medium / small / large bin sorts
     "mt_bound_and_generate_keys": 3,  # rectangles + chunk counts, chunk scan, keys
     "mt_build_vertex_grad_list": 4,  # corner inverse, count, scan, fill

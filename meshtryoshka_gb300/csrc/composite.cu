@@ -772,6 +772,73 @@ __device__ __forceinline__ int64_t next_item(unsigned long long* counter, int la
   return (int64_t)__shfl_sync(0xffffffffu, item, 0);
 }
 
+// ---------------------------------------------------------------------------
+// Longest-first order of the work. A work item's cost grows with its tile's
+// key count, and a few tiles (silhouettes, overlapping objects) hold many
+// times the mean; handed out in launch order they start last and the launch
+// waits on them. The tile order sorts the tiles (over all cameras) by
+// descending key count, in buckets of 8 keys (a counting sort: histogram,
+// then a scatter at each bucket's offset), and the persistent warps claim
+// the tiles' items in that order (the warps of a tile consecutively). Only
+// the processing order changes: every item computes what it computed before.
+//
+// Buffer (int32): [0, 256) bucket sizes, [256, 512) bucket cursors, then one
+// global tile index per tile.
+// ---------------------------------------------------------------------------
+constexpr int kOrderBuckets = 256;
+constexpr int kOrderHeader = 2 * kOrderBuckets;
+
+__device__ __forceinline__ int order_bucket(const CompositeArgs& a, int64_t gt) {
+  int64_t bi = gt;  // index of the tile's range in `bounds`
+  if (a.cameras != nullptr) {
+    int lo = 0, hi = a.B - 1;  // last camera whose first tile <= gt
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(a.cameras + 6 * mid + 4) <= gt) lo = mid; else hi = mid - 1;
+    }
+    bi = (int64_t)lo * a.rows * a.cols + (gt - __ldg(a.cameras + 6 * lo + 4));
+  }
+  const int64_t keys = __ldg(a.bounds + 2 * bi + 1) - __ldg(a.bounds + 2 * bi);
+  return kOrderBuckets - 1 - (int)min(max(keys, (int64_t)0) >> 3, (int64_t)(kOrderBuckets - 1));
+}
+
+__global__ void order_histogram_kernel(CompositeArgs a, int32_t* __restrict__ order) {
+  __shared__ int hist[kOrderBuckets];
+  for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gt < a.total_tiles;
+       gt += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&hist[order_bucket(a, gt)], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x)
+    if (hist[i]) atomicAdd(order + i, hist[i]);
+}
+
+__global__ void order_scatter_kernel(CompositeArgs a, int32_t* __restrict__ order) {
+  __shared__ int base[kOrderBuckets];
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int i = 0; i < kOrderBuckets; ++i) {
+      base[i] = run;
+      run += order[i];
+    }
+  }
+  __syncthreads();
+  for (int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gt < a.total_tiles;
+       gt += (int64_t)gridDim.x * blockDim.x) {
+    const int b = order_bucket(a, gt);
+    order[kOrderHeader + base[b] + atomicAdd(order + kOrderBuckets + b, 1)] = (int32_t)gt;
+  }
+}
+
+// The work item the claim `u` stands for (launch order without an order).
+__device__ __forceinline__ int64_t ordered_item(const CompositeArgs& a, const int32_t* __restrict__ order,
+                                                int64_t u) {
+  if (order == nullptr) return u;
+  const int tw = (a.tile_h * a.tile_w + 31) / 32;
+  return (int64_t)__ldg(order + kOrderHeader + u / tw) * tw + u % tw;
+}
+
 // Background blend and clip of the render entry points (images[:, :3] +
 // images[:, 3:4] * background, then clip to [0, 1]); `inside` is clip's
 // pass-through test (inclusive, as torch's clamp backward).
@@ -906,14 +973,16 @@ template <int kWarps>
 __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps)
     composite_forward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, float* __restrict__ out,
                              unsigned long long* __restrict__ counter, float* __restrict__ loss_sum,
-                             HitStore hs) {
+                             HitStore hs, const int32_t* __restrict__ order) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   float sq = 0.0f;
-  for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
+  for (int64_t u = next_item(counter, lane); u < items; u = next_item(counter, lane)) {
+    const int64_t item = ordered_item(a, order, u);
     sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs);
+  }
   if (a.target) {  // one atomic per warp for the whole launch
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
@@ -1246,7 +1315,8 @@ using WarpBackwardOf = typename std::conditional<kStaged, WarpBackwardStaged, Wa
 template <bool kStaged, int kWarps>
 __global__ void __launch_bounds__(32 * kWarps, kStaged ? 1 : (24 / kWarps > 0 ? 24 / kWarps : 1))
     composite_backward_kernel(CompositeArgs a, const uint32_t* __restrict__ masks, CompositeGrads gr,
-                              unsigned long long* __restrict__ counter, HitStore hs, Staging st) {
+                              unsigned long long* __restrict__ counter, HitStore hs, Staging st,
+                              const int32_t* __restrict__ order) {
   extern __shared__ float4 smem_f4[];
   const int lane = threadIdx.x & 31;
   WarpBackwardOf<kStaged>& ws = reinterpret_cast<WarpBackwardOf<kStaged>*>(smem_f4)[threadIdx.x >> 5];
@@ -1256,8 +1326,10 @@ __global__ void __launch_bounds__(32 * kWarps, kStaged ? 1 : (24 / kWarps > 0 ? 
     __syncwarp();
   }
   const int64_t items = total_items(a);
-  for (int64_t item = next_item(counter, lane); item < items; item = next_item(counter, lane))
+  for (int64_t u = next_item(counter, lane); u < items; u = next_item(counter, lane)) {
+    const int64_t item = ordered_item(a, order, u);
     if (!backward_item<kStaged>(a, masks, gr, ws, pixel_of(a, item), lane, item, hs, st, phase)) return;
+  }
 }
 
 // Packed (camera, vertex) records for the staged backward.
@@ -1420,6 +1492,11 @@ using namespace mt;
 
 extern "C" {
 
+size_t mt_composite_tile_order_bytes(int64_t camera_tiles) {
+  if (camera_tiles < 0) camera_tiles = 0;
+  return ((size_t)mt::kOrderHeader + (size_t)camera_tiles) * sizeof(int32_t);
+}
+
 size_t mt_composite_staging_bytes(int32_t B, int64_t V) {
   if (B <= 0 || V <= 0) return 0;
   return 128 + (size_t)B * (size_t)V * sizeof(VertexRecord);
@@ -1441,8 +1518,8 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
                                        const int64_t* cameras, int64_t camera_tiles, uint32_t* warp_masks,
                                        uint64_t* work_counter, float* out, const float* target,
                                        const float* background, float loss_scale, float* loss_sum,
-                                       void* hit_bits, size_t hit_bits_bytes, int32_t cta_threads,
-                                       mt_stream_t stream) {
+                                       void* hit_bits, size_t hit_bits_bytes, int32_t* tile_order,
+                                       size_t tile_order_bytes, int32_t cta_threads, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, nullptr,
@@ -1467,6 +1544,15 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
     MT_CHECK_LAUNCH();
   }
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
+  if (tile_order) {
+    MT_REQUIRE(tile_order_bytes >= mt_composite_tile_order_bytes(a.total_tiles));
+    if (cudaMemsetAsync(tile_order, 0, kOrderHeader * sizeof(int32_t), s) != cudaSuccess) return MT_ERR_CUDA;
+    const unsigned blocks = grid_stride_blocks(a.total_tiles, 256, 1);
+    order_histogram_kernel<<<blocks, 256, 0, s>>>(a, tile_order);
+    MT_CHECK_LAUNCH();
+    order_scatter_kernel<<<blocks, 256, 0, s>>>(a, tile_order);
+    MT_CHECK_LAUNCH();
+  }
   auto launch = [&](auto warps) -> int {
     constexpr int kW = decltype(warps)::value;
     const size_t smem = sizeof(WarpForward) * kW;
@@ -1476,7 +1562,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
     r = persistent_ctas<composite_forward_kernel<kW>, kW>(a, smem, ctas);
     if (r != MT_OK) return r;
     composite_forward_kernel<kW><<<(unsigned)ctas, 32 * kW, smem, s>>>(
-        a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hs);
+        a, warp_masks, out, reinterpret_cast<unsigned long long*>(work_counter), loss_sum, hs, tile_order);
     MT_CHECK_LAUNCH();
     return MT_OK;
   };
@@ -1499,8 +1585,8 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
                                         int32_t ssaa, float* grad_colors, float* grad_signed_distances,
                                         float* grad_sharpness,
                                         int32_t exact_adjoint, const void* hit_bits, size_t hit_bits_bytes,
-                                        void* staging, size_t staging_bytes, int32_t cta_threads,
-                                        mt_stream_t stream) {
+                                        void* staging, size_t staging_bytes, const int32_t* tile_order,
+                                        size_t tile_order_bytes, int32_t cta_threads, mt_stream_t stream) {
   MT_REQUIRE(layout != nullptr && K >= 0 && camera_tiles >= 0);
   CompositeArgs a = make_args(xy, colors, signed_distances, V, faces, sharpness, sorted_keys, sorted_triangles,
                               tile_boundaries, B, num_shells, rows, cols, tile_h, tile_w, H, W, layout, out,
@@ -1522,6 +1608,7 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
   rc = make_hit_store(a, const_cast<void*>(hit_bits), hit_bits_bytes, hs);
   if (rc != MT_OK) return rc;
   cudaStream_t s = as_stream(stream);
+  MT_REQUIRE(tile_order == nullptr || tile_order_bytes >= mt_composite_tile_order_bytes(a.total_tiles));
   if (cudaMemsetAsync(work_counter, 0, sizeof(uint64_t), s) != cudaSuccess) return MT_ERR_CUDA;
   const bool staged = staging != nullptr && staging_bytes >= mt_composite_staging_bytes(B, V);
   Staging st{nullptr, nullptr};
@@ -1546,7 +1633,7 @@ int mt_intersect_and_composite_backward(const float* xy, const float* colors, co
     r = persistent_ctas<composite_backward_kernel<kS, kW>, kW>(a, smem, ctas);
     if (r != MT_OK) return r;
     composite_backward_kernel<kS, kW><<<(unsigned)ctas, 32 * kW, smem, s>>>(
-        a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hs, st);
+        a, warp_masks, gr, reinterpret_cast<unsigned long long*>(work_counter), hs, st, tile_order);
     MT_CHECK_LAUNCH();
     return MT_OK;
   };

@@ -532,6 +532,19 @@ def _staging(b: int, v: int, device) -> Tensor | None:
     return torch.zeros((nbytes,), dtype=torch.uint8, device=device) if nbytes else None
 
 
+# Longest-first tile order of the compositing kernels (not in the reference):
+# the tiles with the most keys are composited first, so the few expensive
+# ones do not start last and hold up the launch (same results).
+TILE_ORDER = True
+
+
+def _tile_order(grid: TileGrid, device) -> Tensor | None:
+    if not TILE_ORDER:
+        return None
+    nbytes = int(nt.library().mt_composite_tile_order_bytes(grid.camera_tiles))
+    return torch.empty((nbytes // 4,), dtype=torch.int32, device=device)
+
+
 def _hit_bits(ctx, grid: TileGrid, num_keys: int, device) -> Tensor | None:
     """The hit-bit store for the forward and its backward (only when a
     gradient will be asked for): the batches num_keys keys can form at most,
@@ -571,13 +584,16 @@ class IntersectAndComposite(torch.autograd.Function):
             out = torch.empty((grid.output_numel,) if grid.ragged else (b, 4, h, w), dtype=torch.float32,
                               device=device)
             hits = _hit_bits(ctx, grid, k, device)
+            order = _tile_order(grid, device)
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out), None, None,
-                    0.0, None, nt.ptr(hits), _numel(hits), grid.cta_threads, nt.stream(device))
+                    0.0, None, nt.ptr(hits), _numel(hits), nt.ptr(order), _numel(order), grid.cta_threads,
+                    nt.stream(device))
             note(composite=out)
             ctx.hits = hits
+            ctx.order = order
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness))
@@ -604,7 +620,8 @@ class IntersectAndComposite(torch.autograd.Function):
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), nt.ptr(grad_out), None, None, 0.0, None, 1, nt.ptr(grad_colors), nt.ptr(grad_sdf),
                     nt.ptr(grad_sharp), int(mode == "exact"), nt.ptr(ctx.hits), _numel(ctx.hits),
-                    nt.ptr(staging), _numel(staging), grid.cta_threads, nt.stream(device))
+                    nt.ptr(staging), _numel(staging), nt.ptr(ctx.order), _numel(ctx.order), grid.cta_threads,
+                    nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None)
 
@@ -647,14 +664,15 @@ class IntersectCompositeLoss(torch.autograd.Function):
             loss = torch.empty((), dtype=torch.float32, device=device)
             scale = 1.0 / target.numel()
             hits = _hit_bits(ctx, grid, k, device)
+            order = _tile_order(grid, device)
             in_kernel = ssaa == 1
             nt.call("mt_intersect_and_composite_forward", nt.ptr(xy), nt.ptr(colors), nt.ptr(sdf), v,
                     nt.ptr(faces), nt.ptr(sharp), nt.ptr(keys), nt.ptr(tri), k, nt.ptr(num_keys), nt.ptr(bounds), b,
                     int(num_shells), rows, cols, grid.tile_shape[0], grid.tile_shape[1], h, w, _layout(key_defines),
                     nt.ptr(table), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter), nt.ptr(out),
                     nt.ptr(target) if in_kernel else None, nt.ptr(background) if in_kernel else None, scale,
-                    loss.data_ptr() if in_kernel else None, nt.ptr(hits), _numel(hits), grid.cta_threads,
-                    nt.stream(device))
+                    loss.data_ptr() if in_kernel else None, nt.ptr(hits), _numel(hits), nt.ptr(order),
+                    _numel(order), grid.cta_threads, nt.stream(device))
             factor = target
             if not in_kernel:
                 factor = torch.empty_like(target)
@@ -662,6 +680,7 @@ class IntersectCompositeLoss(torch.autograd.Function):
                         loss.data_ptr(), factor.data_ptr(), nt.stream(device))
             note(composite=out, loss=loss)
             ctx.hits = hits
+            ctx.order = order
             ctx.save_for_backward(xy, colors, sdf, faces, sharp, keys, tri, bounds, masks, out, factor, background)
             ctx.meta = (int(num_shells), grid, key_defines, gradient_mode or _GRADIENT_MODE,
                         torch.is_tensor(sharpness), scale, ssaa)
@@ -688,8 +707,8 @@ class IntersectCompositeLoss(torch.autograd.Function):
                     nt.ptr(_camera_table(grid, device)), grid.camera_tiles, nt.ptr(masks), nt.ptr(counter),
                     nt.ptr(out), None, nt.ptr(target), nt.ptr(background), scale, grad_loss.data_ptr(), ssaa,
                     nt.ptr(grad_colors), nt.ptr(grad_sdf), nt.ptr(grad_sharp), int(mode == "exact"),
-                    nt.ptr(ctx.hits), _numel(ctx.hits), nt.ptr(staging), _numel(staging), grid.cta_threads,
-                    nt.stream(device))
+                    nt.ptr(ctx.hits), _numel(ctx.hits), nt.ptr(staging), _numel(staging), nt.ptr(ctx.order),
+                    _numel(ctx.order), grid.cta_threads, nt.stream(device))
             return (None, grad_colors, grad_sdf, None, grad_sharp if sharp_is_tensor else None, None, None, None,
                     None, None, None, None, None, None, None, None)
 

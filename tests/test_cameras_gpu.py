@@ -132,3 +132,28 @@ def test_uneven_workload_batched_equals_per_camera(cuda_device):
     assert abs(loss_graph - loss_plain) <= LOSS_RTOL * abs(loss_plain)
     _close(w.grid_sdf.grad, g_plain[0])
     _close(w.grid_sh.grad, g_plain[1])
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (12, 20)])
+def test_tile_order_leaves_results_unchanged(cuda_device, tile, monkeypatch):
+    """The longest-first tile order of the compositing kernels (cameras of
+    different sizes: the tile's range is found through the camera table)
+    changes only the order the work is taken in: identical images, the same
+    gradients up to the order of their atomic sums."""
+    results = []
+    for ordered in (False, True):
+        monkeypatch.setattr(tr, "TILE_ORDER", ordered)
+        ext, intr, shapes, args = _scene(cuda_device)
+        images = tr.render_cameras(ext, intr, shapes, tile_shape=tile, **args)
+        rng = np.random.default_rng(3)
+        loss = sum((img * _t(rng.normal(0, 1, tuple(img.shape)).astype(np.float32), cuda_device)).sum()
+                   for img in images)
+        loss.backward()
+        results.append(([img.detach() for img in images], args["signed_distances"].grad.clone(),
+                        args["spherical_harmonics"].grad.clone()))
+    (i0, s0, h0), (i1, s1, h1) = results
+    for a, b in zip(i0, i1):
+        assert torch.equal(a, b)
+    _close(s1, s0)
+    _close(h1, h0)
+    assert float(s0.abs().max()) > 0

@@ -677,3 +677,21 @@ def test_tile_grid_rejects_other_thread_counts():
     with pytest.raises(ValueError):
         tr.TileGrid((8, 8, 96), (64, 64), 1, 3)
     assert tr.TileGrid((8, 8, 512), (64, 64), 1, 3).tile_shape == (8, 8)
+
+
+@pytest.mark.parametrize("name", ["three_cams_odd", "dense"])
+def test_tile_order_leaves_fused_results_unchanged(cuda_device, name, monkeypatch):
+    """Longest-first tile order on or off: identical images, the same
+    gradients up to atomic order (uniform cameras, hit bits stored)."""
+    scene = make_scene(**(DENSE if name == "dense" else SCENES[name]))
+    results = []
+    for ordered in (False, True):
+        monkeypatch.setattr(tr, "TILE_ORDER", ordered)
+        inputs = _fused_inputs(scene, cuda_device)
+        image = tr.render(**inputs, tile_shape=(8, 8), mode="fused")
+        g = _t(np.random.default_rng(8).normal(0, 1, tuple(image.shape)).astype(np.float32), cuda_device)
+        (image * g).sum().backward()
+        results.append((_n(image), _n(inputs["signed_distances"].grad), _n(inputs["spherical_harmonics"].grad)))
+    np.testing.assert_array_equal(results[1][0], results[0][0])
+    _close_grad(results[1][1], results[0][1], 1e-5)
+    _close_grad(results[1][2], results[0][2], 1e-5)
