@@ -814,6 +814,8 @@ __global__ void order_histogram_kernel(CompositeArgs a, int32_t* __restrict__ or
     if (hist[i]) atomicAdd(order + i, hist[i]);
 }
 
+// Lanes of a warp with the same bucket reserve their places with one atomic
+// (most tiles of a scene can share a bucket: the empty ones).
 __global__ void order_scatter_kernel(CompositeArgs a, int32_t* __restrict__ order) {
   __shared__ int base[kOrderBuckets];
   if (threadIdx.x == 0) {
@@ -824,10 +826,17 @@ __global__ void order_scatter_kernel(CompositeArgs a, int32_t* __restrict__ orde
     }
   }
   __syncthreads();
-  for (int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gt < a.total_tiles;
-       gt += (int64_t)gridDim.x * blockDim.x) {
-    const int b = order_bucket(a, gt);
-    order[kOrderHeader + base[b] + atomicAdd(order + kOrderBuckets + b, 1)] = (int32_t)gt;
+  const int lane = threadIdx.x & 31;
+  for (int64_t first = blockIdx.x * (int64_t)blockDim.x; first < a.total_tiles;
+       first += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t gt = first + threadIdx.x;
+    const int b = gt < a.total_tiles ? order_bucket(a, gt) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(peers) - 1;
+    int slot = 0;
+    if (b >= 0 && lane == leader) slot = atomicAdd(order + kOrderBuckets + b, __popc(peers));
+    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(peers & lanemask_lt());
+    if (b >= 0) order[kOrderHeader + base[b] + slot] = (int32_t)gt;
   }
 }
 

@@ -461,11 +461,12 @@ int mt_sort_keys_by_tile_supported(const int32_t* layout, int32_t separate_shell
 
 namespace {
 
-// Helper stream and fork / join events of one (device, caller stream),
-// created on first use and kept for the process.
+// Helper streams and fork / join events of one (device, caller stream),
+// created on first use and kept for the process: the bin tiers other than
+// the tiny one sort on helper streams, concurrently with it.
 struct ForkJoin {
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
 };
 
 int fork_join_for(cudaStream_t caller, ForkJoin& out) {
@@ -477,10 +478,11 @@ int fork_join_for(cudaStream_t caller, ForkJoin& out) {
   auto it = table.find({device, caller});
   if (it == table.end()) {
     ForkJoin f;
-    if (cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming) != cudaSuccess)
-      return MT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess) return MT_ERR_CUDA;
+    for (int i = 0; i < 3; ++i)
+      if (cudaStreamCreateWithFlags(&f.side[i], cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&f.join[i], cudaEventDisableTiming) != cudaSuccess)
+        return MT_ERR_CUDA;
     it = table.emplace(std::make_pair(device, caller), f).first;
   }
   out = it->second;
@@ -532,16 +534,18 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
   bin_scatter_kernel<<<grid_stride_blocks(K, kThreads), kThreads, 0, s>>>(k64, K, num_keys, m, w.counts, w.cursors,
                                                                         idx_bits, low_mask_host, w.tmp);
   MT_CHECK_LAUNCH();
-  // Large bins on the helper stream, the rest on the caller's; as many CTAs
-  // as are resident at once, each taking listed bins in turn.
+  // The four tiers sort concurrently (large, medium and small bins on the
+  // helper streams, tiny ones on the caller's); as many CTAs as are resident
+  // at once per tier, each taking listed bins in turn.
   const size_t large_smem = 2 * (size_t)kChunk * sizeof(uint64_t);
   if (set_smem<bin_sort_large_kernel>(large_smem) != MT_OK) return MT_ERR_CUDA;
   ForkJoin fj;
   if (fork_join_for(s, fj) != MT_OK) return MT_ERR_CUDA;
-  if (cudaEventRecord(fj.fork, s) != cudaSuccess || cudaStreamWaitEvent(fj.side, fj.fork, 0) != cudaSuccess)
-    return MT_ERR_CUDA;
+  if (cudaEventRecord(fj.fork, s) != cudaSuccess) return MT_ERR_CUDA;
+  for (int i = 0; i < 3; ++i)
+    if (cudaStreamWaitEvent(fj.side[i], fj.fork, 0) != cudaSuccess) return MT_ERR_CUDA;
   const unsigned large_ctas = (unsigned)(nbins < (int64_t)kSmCount * 2 ? nbins : (int64_t)kSmCount * 2);
-  bin_sort_large_kernel<<<large_ctas, kLargeThreads, large_smem, fj.side>>>(
+  bin_sort_large_kernel<<<large_ctas, kLargeThreads, large_smem, fj.side[0]>>>(
       w.tmp, w.alt, w.lists + 3 * nbins, w.list_sizes + 3, idx_mask, k64, triangles,
       reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
   MT_CHECK_LAUNCH();
@@ -551,17 +555,18 @@ int mt_sort_keys_by_tile(const int64_t* keys, const int32_t* triangles, int64_t 
                                                              sorted_triangles);
   MT_CHECK_LAUNCH();
   const unsigned medium_ctas = (unsigned)(nbins < (int64_t)kSmCount * 22 ? nbins : (int64_t)kSmCount * 22);
-  bin_sort_cta_kernel<kMediumThreads><<<medium_ctas, kMediumThreads, 0, s>>>(
+  bin_sort_cta_kernel<kMediumThreads><<<medium_ctas, kMediumThreads, 0, fj.side[1]>>>(
       w.tmp, w.lists + nbins, w.list_sizes + 1, idx_mask, k64, triangles, reinterpret_cast<uint64_t*>(sorted_keys),
       sorted_triangles);
   MT_CHECK_LAUNCH();
   const unsigned small_ctas = (unsigned)(nbins < (int64_t)kSmCount * 11 ? nbins : (int64_t)kSmCount * 11);
-  bin_sort_cta_kernel<kSmallThreads><<<small_ctas, kSmallThreads, 0, s>>>(
+  bin_sort_cta_kernel<kSmallThreads><<<small_ctas, kSmallThreads, 0, fj.side[2]>>>(
       w.tmp, w.lists + 2 * nbins, w.list_sizes + 2, idx_mask, k64, triangles,
       reinterpret_cast<uint64_t*>(sorted_keys), sorted_triangles);
   MT_CHECK_LAUNCH();
-  if (cudaEventRecord(fj.join, fj.side) != cudaSuccess || cudaStreamWaitEvent(s, fj.join, 0) != cudaSuccess)
-    return MT_ERR_CUDA;
+  for (int i = 0; i < 3; ++i)
+    if (cudaEventRecord(fj.join[i], fj.side[i]) != cudaSuccess || cudaStreamWaitEvent(s, fj.join[i], 0) != cudaSuccess)
+      return MT_ERR_CUDA;
   return MT_OK;
 }
 
