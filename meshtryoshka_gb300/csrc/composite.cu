@@ -814,29 +814,42 @@ __global__ void order_histogram_kernel(CompositeArgs a, int32_t* __restrict__ or
     if (hist[i]) atomicAdd(order + i, hist[i]);
 }
 
-// Lanes of a warp with the same bucket reserve their places with one atomic
-// (most tiles of a scene can share a bucket: the empty ones).
-__global__ void order_scatter_kernel(CompositeArgs a, int32_t* __restrict__ order) {
+__global__ void __launch_bounds__(kOrderBuckets) order_scatter_kernel(CompositeArgs a, int32_t* __restrict__ order) {
+  // Bucket offsets: a CTA-wide exclusive scan of the bucket sizes (one per
+  // thread; the kernel runs with kOrderBuckets threads).
   __shared__ int base[kOrderBuckets];
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int i = 0; i < kOrderBuckets; ++i) {
-      base[i] = run;
-      run += order[i];
-    }
+  __shared__ int warp_sums[kOrderBuckets / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int size = order[threadIdx.x];
+  int inc = size;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
   }
+  if (lane == 31) warp_sums[warp] = inc;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
+  int before = 0;
+  for (int w = 0; w < warp; ++w) before += warp_sums[w];
+  base[threadIdx.x] = before + inc - size;
+  // Each round places the CTA's next kOrderBuckets tiles: ranks within the
+  // CTA by shared-memory counters, then one global atomic per (CTA, bucket)
+  // reserves the CTA's places (most tiles of a scene can share one bucket:
+  // the empty ones).
+  __shared__ int count[kOrderBuckets], first_slot[kOrderBuckets];
   for (int64_t first = blockIdx.x * (int64_t)blockDim.x; first < a.total_tiles;
        first += (int64_t)gridDim.x * blockDim.x) {
+    count[threadIdx.x] = 0;
+    __syncthreads();
     const int64_t gt = first + threadIdx.x;
     const int b = gt < a.total_tiles ? order_bucket(a, gt) : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, b);
-    const int leader = __ffs(peers) - 1;
-    int slot = 0;
-    if (b >= 0 && lane == leader) slot = atomicAdd(order + kOrderBuckets + b, __popc(peers));
-    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(peers & lanemask_lt());
-    if (b >= 0) order[kOrderHeader + base[b] + slot] = (int32_t)gt;
+    const int rank = b >= 0 ? atomicAdd(&count[b], 1) : 0;
+    __syncthreads();
+    const int c = count[threadIdx.x];
+    if (c > 0) first_slot[threadIdx.x] = atomicAdd(order + kOrderBuckets + threadIdx.x, c);
+    __syncthreads();
+    if (b >= 0) order[kOrderHeader + base[b] + first_slot[b] + rank] = (int32_t)gt;
+    __syncthreads();  // count and first_slot are reset by the next round
   }
 }
 
@@ -1559,7 +1572,7 @@ int mt_intersect_and_composite_forward(const float* xy, const float* colors, con
     const unsigned blocks = grid_stride_blocks(a.total_tiles, 256, 1);
     order_histogram_kernel<<<blocks, 256, 0, s>>>(a, tile_order);
     MT_CHECK_LAUNCH();
-    order_scatter_kernel<<<blocks, 256, 0, s>>>(a, tile_order);
+    order_scatter_kernel<<<blocks, kOrderBuckets, 0, s>>>(a, tile_order);
     MT_CHECK_LAUNCH();
   }
   auto launch = [&](auto warps) -> int {
