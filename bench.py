@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=2000, help="requests per arrival rate of the serving sweep")
     p.add_argument("--no-subdivision", action="store_true", help="skip the subdivision step measurement")
     p.add_argument("--no-large", action="store_true", help="skip the large-configuration step in both modes")
+    p.add_argument("--no-band", action="store_true", help="skip the band-matched variant of the step")
     p.add_argument("--tile", default=None, help="tile shape HxW for the step (default: autotuned)")
     p.add_argument("--no-reference-cub", action="store_true",
                    help="skip timing the reference's CUB scan and sort extensions")
@@ -533,6 +534,8 @@ def run_ours(args, rank, world, local):
         line["serving"] = run_serving(device, args.serve_requests)
     if not args.no_large and world == 1:
         line["large"] = run_large(device, min(args.steps, 10))
+    if not args.no_band and world == 1:
+        line["band_matched"] = run_band_matched(device, min(args.steps, 20))
     if not args.no_subdivision and world == 1:
         line["subdivision"] = run_subdivision(device, min(args.steps, 20), cpu=not args.no_cpu_baseline)
     if not args.no_reference_cub and world == 1:
@@ -702,6 +705,34 @@ def run_large(device, steps):
         "sizes": {k: stats[k] for k in ("G", "Nv", "V", "F", "K", "P")},
         "max_image_diff_fused_vs_explicit": diff,
     })
+    return out
+
+
+def run_band_matched(device, steps):
+    """The mid step on a band wide enough for its shells ("mid_band": the
+    same spheres, cameras and 8 level sets in [-0.03, 0.03] on a 4-voxel
+    band, so that every shell has faces): the captured step at the
+    autotuned tile, with its sizes."""
+    import torch
+
+    from meshtryoshka_gb300 import autotune, pipeline
+
+    w = pipeline.build_workload("mid_band", device)
+    tile, tile_ms = autotune.tune_tile_shape(w, candidates=((8, 8, 128), (8, 8, 256), (16, 8, 256)),
+                                             repeats=steps)
+    with torch.no_grad():
+        _, stats = pipeline.forward(w, "fused")
+    h, wd = w.image_shape
+    cfg = w.config
+    out = {
+        "workload": f"mid_band: {cfg.resolution}^3, {cfg.band_voxels:g}-voxel band around {cfg.num_spheres} spheres, "
+                    f"SH deg {cfg.sh_degree}, {len(cfg.level_sets)} shells in [-0.03, 0.03], "
+                    f"{w.extrinsics.shape[0]}x{h}x{wd}, fused fwd+bwd training step",
+        "sizes": {k: int(stats[k]) for k in ("G", "Nv", "V", "F", "K", "P")},
+        "tile": list(tile),
+        "graph_ms": tile_ms[tile],
+        "tile_ms": {"x".join(str(x) for x in k): v for k, v in tile_ms.items()},
+    }
     return out
 
 

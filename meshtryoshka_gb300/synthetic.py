@@ -60,6 +60,12 @@ CONFIGS: dict[str, SceneConfig] = {
     # 256^3, union of 8 spheres, SH degree 3, 8 shells, 4 x 800^2 cameras.
     "mid": SceneConfig("mid", 256, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8), 50.0,
                        "orbit", 4, (800, 800), 50.0),
+    # The mid scene with a band wide enough for its shells: a 4-voxel band
+    # (|sdf| < 0.031 at the voxel centres) holds all 8 level sets in
+    # [-0.03, 0.03], where the 2-voxel band of "mid" leaves two shells empty
+    # and two nearly empty.
+    "mid_band": SceneConfig("mid_band", 256, 8, 0.6, (0.1, 0.3), None, 4.0, 0.001, 3, _even(-0.03, 0.03, 8), 50.0,
+                            "orbit", 4, (800, 800), 50.0),
     # The mid scene seen by 32 cameras of uneven resolution (200-1600 px per
     # side, fov 40-70 degrees) placed on the mid scene's orbit.
     "uneven": SceneConfig("uneven", 256, 8, 0.6, (0.1, 0.3), None, 2.0, 0.001, 3, _even(-0.03, 0.03, 8), 50.0,

@@ -130,8 +130,11 @@ def _captured(w: pipeline.Workload, gradient_mode=None):
     return step, float(loss)
 
 
-def test_captured_mid_step_matches_oracle(cuda_device):
-    w = pipeline.build_workload("mid", cuda_device)
+@pytest.mark.parametrize("config", ["mid", "mid_band"])
+def test_captured_mid_step_matches_oracle(cuda_device, config):
+    """The timed step (and its band-matched variant, whose 4-voxel band
+    gives every one of the 8 shells faces) against the oracle."""
+    w = pipeline.build_workload(config, cuda_device)
     w.tile_shape = TILE
     step, loss = _captured(w)
     rec = step.records[0]
