@@ -992,60 +992,74 @@ __global__ void __launch_bounds__(kShThreads)
 // grid vertex x), sums x's list entries of rows 8h .. 8h + 7 (96 contiguous
 // bytes per entry) weighted, in list order. The same bits as the one-pass
 // kernel, with each vertex's gradient formed once instead of once per entry.
-__global__ void vertex_sh_grad_kernel(const float* __restrict__ verts, int64_t V, const int32_t* __restrict__ count,
-                                      int n_coeff, const float* __restrict__ campos, int B,
-                                      const float* __restrict__ colors, const float* __restrict__ dcolors,
-                                      float4* __restrict__ out) {
+constexpr int kShGradThreads = 128;
+
+__global__ void __launch_bounds__(kShGradThreads)
+    vertex_sh_grad_kernel(const float* __restrict__ verts, int64_t V, const int32_t* __restrict__ count,
+                          int n_coeff, const float* __restrict__ campos, int B, const float* __restrict__ colors,
+                          const float* __restrict__ dcolors, float4* __restrict__ out) {
+  // Each round, the CTA's kShGradThreads consecutive vertices form their
+  // rows in shared memory, then write them as one contiguous block (full
+  // 128-byte lines, where each thread's own 192-byte row would be written
+  // 16 bytes at a time at a 192-byte stride).
+  __shared__ float4 s_rows[kShGradThreads * 12];
   const int64_t n = count ? min((int64_t)max(*count, 0), V) : V;
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const float px = __ldg(verts + 3 * v), py = __ldg(verts + 3 * v + 1), pz = __ldg(verts + 3 * v + 2);
-    float d[16][3];
+  for (int64_t v0 = (int64_t)blockIdx.x * kShGradThreads; v0 < n; v0 += (int64_t)gridDim.x * kShGradThreads) {
+    const int64_t v = v0 + threadIdx.x;
+    if (v < n) {
+      const float px = __ldg(verts + 3 * v), py = __ldg(verts + 3 * v + 1), pz = __ldg(verts + 3 * v + 2);
+      float d[16][3];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
-    // Cameras two at a time: both cameras' colours and colour gradients are
-    // loaded together, then the cameras are added in order.
-    for (int b0 = 0; b0 < B; b0 += 2) {
-      float col[2][3], dcol[2][3];
+      for (int k = 0; k < 16; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
+      // Cameras two at a time: both cameras' colours and colour gradients
+      // are loaded together, then the cameras are added in order.
+      for (int b0 = 0; b0 < B; b0 += 2) {
+        float col[2][3], dcol[2][3];
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const bool in = b0 + j < B;
-        const int64_t ob = ((int64_t)(b0 + j) * V + v) * 3;
+        for (int j = 0; j < 2; ++j) {
+          const bool in = b0 + j < B;
+          const int64_t ob = ((int64_t)(b0 + j) * V + v) * 3;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          col[j][c] = in ? __ldg(colors + ob + c) : 0.0f;
-          dcol[j][c] = in ? __ldg(dcolors + ob + c) : 0.0f;
+          for (int c = 0; c < 3; ++c) {
+            col[j][c] = in ? __ldg(colors + ob + c) : 0.0f;
+            dcol[j][c] = in ? __ldg(dcolors + ob + c) : 0.0f;
+          }
         }
-      }
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        float g[3];
-        bool any = false;
+        for (int j = 0; j < 2; ++j) {
+          float g[3];
+          bool any = false;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          g[c] = col[j][c] > 0.0f ? dcol[j][c] : 0.0f;
-          any |= g[c] != 0.0f;
-        }
-        if (!any) continue;  // also every camera past B (its g is zero)
-        float dx, dy, dz;
-        view_dir_at(px, py, pz, campos + 3 * (b0 + j), dx, dy, dz);
-        float basis[16];
-        sh_basis(dx, dy, dz, n_coeff, basis);
+          for (int c = 0; c < 3; ++c) {
+            g[c] = col[j][c] > 0.0f ? dcol[j][c] : 0.0f;
+            any |= g[c] != 0.0f;
+          }
+          if (!any) continue;  // also every camera past B (its g is zero)
+          float dx, dy, dz;
+          view_dir_at(px, py, pz, campos + 3 * (b0 + j), dx, dy, dz);
+          float basis[16];
+          sh_basis(dx, dy, dz, n_coeff, basis);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          if (k < n_coeff) {
+          for (int k = 0; k < 16; ++k) {
+            if (k < n_coeff) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+              for (int c = 0; c < 3; ++c) d[k][c] += basis[k] * g[c];
+            }
           }
         }
       }
-    }
-    float4* o = out + v * 12;
+      float4* row = s_rows + threadIdx.x * 12;
 #pragma unroll
-    for (int q = 0; q < 12; ++q) {
-      const int j = 4 * q;
-      o[q] = make_float4(d[j / 3][j % 3], d[(j + 1) / 3][(j + 1) % 3], d[(j + 2) / 3][(j + 2) % 3],
-                         d[(j + 3) / 3][(j + 3) % 3]);
+      for (int q = 0; q < 12; ++q) {
+        const int j = 4 * q;
+        row[q] = make_float4(d[j / 3][j % 3], d[(j + 1) / 3][(j + 1) % 3], d[(j + 2) / 3][(j + 2) % 3],
+                             d[(j + 3) / 3][(j + 3) % 3]);
+      }
     }
+    __syncthreads();
+    const int64_t rows = min((int64_t)kShGradThreads, n - v0);
+    for (int i = threadIdx.x; i < rows * 12; i += kShGradThreads) out[v0 * 12 + i] = s_rows[i];
+    __syncthreads();  // s_rows is written again by the next round
   }
 }
 
@@ -1760,7 +1774,7 @@ int mt_grid_sh_colors_backward(const int32_t* list_offsets, const int32_t* list,
   if (workspace && workspace_bytes >= mt_grid_sh_colors_backward_workspace_bytes(V) && Bn > 0) {
     float4* dsh = reinterpret_cast<float4*>(static_cast<char*>(workspace) + 256);
     MT_REQUIRE((reinterpret_cast<uintptr_t>(dsh) & 15) == 0);
-    vertex_sh_grad_kernel<<<grid_stride_blocks(V, 128), 128, 0, st>>>(vertices, V, num_vertices, n, camera_positions,
+    vertex_sh_grad_kernel<<<grid_stride_blocks(V, kShGradThreads), kShGradThreads, 0, st>>>(vertices, V, num_vertices, n, camera_positions,
                                                                       Bn, out_colors, grad_colors, dsh);
     MT_CHECK_LAUNCH();
     grid_sh_gather_kernel<<<grid_stride_blocks(2 * G, 256), 256, 0, st>>>(
