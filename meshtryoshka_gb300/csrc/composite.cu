@@ -1067,6 +1067,10 @@ __device__ __forceinline__ bool backward_item(const CompositeArgs& a, const uint
                                               int64_t item, const HitStore& hs, const Staging& st,
                                               uint32_t& phase) {
   const int64_t T = (int64_t)a.rows * a.cols;
+  // A tile without keys has no hits, so nothing flows back from its pixels
+  // (most tiles of a scene: with the tile order they come last).
+  const int64_t range = 2 * ((int64_t)px.cam * T + px.tile);
+  if (__ldg(a.bounds + range) == __ldg(a.bounds + range + 1)) return true;
   const float s = *a.sharpness;
   const int cam = px.cam;
 
