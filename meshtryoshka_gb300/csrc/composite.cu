@@ -799,7 +799,8 @@ __device__ __forceinline__ int order_bucket(const CompositeArgs& a, int64_t gt) 
     bi = (int64_t)lo * a.rows * a.cols + (gt - __ldg(a.cameras + 6 * lo + 4));
   }
   const int64_t keys = __ldg(a.bounds + 2 * bi + 1) - __ldg(a.bounds + 2 * bi);
-  return kOrderBuckets - 1 - (int)min(max(keys, (int64_t)0) >> 3, (int64_t)(kOrderBuckets - 1));
+  if (keys <= 0) return kOrderBuckets - 1;  // the last bucket holds exactly the tiles without keys
+  return kOrderBuckets - 2 - (int)min((keys - 1) >> 3, (int64_t)(kOrderBuckets - 2));
 }
 
 __global__ void order_histogram_kernel(CompositeArgs a, int32_t* __restrict__ order) {
@@ -859,6 +860,19 @@ __device__ __forceinline__ int64_t ordered_item(const CompositeArgs& a, const in
   if (order == nullptr) return u;
   const int tw = (a.tile_h * a.tile_w + 31) / 32;
   return (int64_t)__ldg(order + kOrderHeader + u / tw) * tw + u % tw;
+}
+
+// With a tile order, the claims past the tiles with keys (which come last in
+// the order) stand for items without keys: cheap, so they are claimed
+// kEmptyClaim at a time. Returns the first such claim (all items without an
+// order).
+constexpr int kEmptyClaim = 8;
+
+__device__ __forceinline__ int64_t keyed_items(const CompositeArgs& a, const int32_t* __restrict__ order) {
+  const int64_t items = total_items(a);
+  if (order == nullptr) return items;
+  const int tw = (a.tile_h * a.tile_w + 31) / 32;
+  return items - (int64_t)__ldg(order + kOrderBuckets - 1) * tw;
 }
 
 // Background blend and clip of the render entry points (images[:, :3] +
@@ -1001,9 +1015,19 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps)
   WarpForward& ws = reinterpret_cast<WarpForward*>(smem_f4)[threadIdx.x >> 5];
   const int64_t items = total_items(a);
   float sq = 0.0f;
-  for (int64_t u = next_item(counter, lane); u < items; u = next_item(counter, lane)) {
-    const int64_t item = ordered_item(a, order, u);
-    sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs);
+  // Claims of one item while they land on items with keys, then of
+  // kEmptyClaim items: a claim covers [u, u + claimed).
+  const int64_t keyed = keyed_items(a, order);
+  int64_t claimed = 1;
+  for (int64_t u = next_item(counter, lane); u < items;) {
+    for (int64_t v = u; v < min(u + claimed, items); ++v) {
+      const int64_t item = ordered_item(a, order, v);
+      sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs);
+    }
+    claimed = u + claimed >= keyed ? kEmptyClaim : 1;  // the next claim lands at or past u + claimed
+    unsigned long long next = 0;
+    if (lane == 0) next = atomicAdd(counter, (unsigned long long)claimed);
+    u = (int64_t)__shfl_sync(0xffffffffu, next, 0);
   }
   if (a.target) {  // one atomic per warp for the whole launch
 #pragma unroll
@@ -1351,8 +1375,10 @@ __global__ void __launch_bounds__(32 * kWarps, kStaged ? 1 : (24 / kWarps > 0 ? 
     if (lane == 0) mbar_init(&ws.bar);
     __syncwarp();
   }
-  const int64_t items = total_items(a);
-  for (int64_t u = next_item(counter, lane); u < items; u = next_item(counter, lane)) {
+  // Items without keys pass no gradient: with a tile order they are all past
+  // `keyed` and never claimed.
+  const int64_t keyed = keyed_items(a, order);
+  for (int64_t u = next_item(counter, lane); u < keyed; u = next_item(counter, lane)) {
     const int64_t item = ordered_item(a, order, u);
     if (!backward_item<kStaged>(a, masks, gr, ws, pixel_of(a, item), lane, item, hs, st, phase)) return;
   }
