@@ -888,7 +888,6 @@ __device__ __forceinline__ const float* target_of(const CompositeArgs& a, const 
   return a.target + px.out_base / 4 * 3 + (int64_t)px.py * px.width + px.px;
 }
 
-// Returns the pixel's sum of squared errors when the epilogue is on.
 // Reserves the work item's batches in the hit-bit store: the number of keys
 // of the tile whose mask has this warp's bit, in batches of kBatch (the walk
 // forms exactly that many batches or stops earlier). Returns the item's first
@@ -909,9 +908,13 @@ __device__ __forceinline__ int64_t reserve_hit_batches(const HitStore& hs, const
   return first;
 }
 
+// Returns the pixel's sum of squared errors when the epilogue is on.
+// `keyless`: the item's tile has no keys (known from the tile order): only
+// the empty composite is written (no tile range, no hit-bit reservation: the
+// backward never takes such items).
 __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint32_t* __restrict__ masks,
                                               float* __restrict__ out, WarpForward& ws, const Pixel& px, int lane,
-                                              int64_t item, const HitStore& hs) {
+                                              int64_t item, const HitStore& hs, bool keyless = false) {
   const int64_t T = (int64_t)a.rows * a.cols;
   const float s = *a.sharpness;
 
@@ -922,12 +925,13 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   float e_dummy;
   float outer_cdf = sdf_to_cdf(1e10f, s, e_dummy);  // dummy outer sample
 
-  const int64_t start = a.bounds[2 * ((int64_t)px.cam * T + px.tile)];
-  const int64_t end = a.bounds[2 * ((int64_t)px.cam * T + px.tile) + 1];
+  const int64_t start = keyless ? 0 : a.bounds[2 * ((int64_t)px.cam * T + px.tile)];
+  const int64_t end = keyless ? 0 : a.bounds[2 * ((int64_t)px.cam * T + px.tile) + 1];
   int64_t next = start;
   int queued = 0;
   int batch = 0;
-  const int64_t hit_base = hs.batches ? reserve_hit_batches(hs, masks, start, end, px.wt, item, lane) : -1;
+  const int64_t hit_base =
+      hs.batches && !keyless ? reserve_hit_batches(hs, masks, start, end, px.wt, item, lane) : -1;
   // With 8x4 warp blocks a triangle's span is the part of its accept box on
   // the block (lane 0 holds the block's first pixel); otherwise every pixel.
   const bool blocked = (a.tile_w & 7) == 0 && (a.tile_h & 3) == 0;
@@ -1022,7 +1026,7 @@ __global__ void __launch_bounds__(32 * kWarps, 32 / kWarps)
   for (int64_t u = next_item(counter, lane); u < items;) {
     for (int64_t v = u; v < min(u + claimed, items); ++v) {
       const int64_t item = ordered_item(a, order, v);
-      sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs);
+      sq += forward_item(a, masks, out, ws, pixel_of(a, item), lane, item, hs, v >= keyed);
     }
     claimed = u + claimed >= keyed ? kEmptyClaim : 1;  // the next claim lands at or past u + claimed
     unsigned long long next = 0;
