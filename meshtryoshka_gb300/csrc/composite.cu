@@ -311,44 +311,71 @@ __device__ __forceinline__ TriangleBounds3 triangle_bounds(const TriGeom& g) {
                          edge_bound(g.d1223, g.d1323, g.p2x, g.p2y, g.e13x, g.e13y, g.e12x, g.e12y)};
 }
 
+// The warp blocks of its tile that a key's triangle (corners pa, pb, pc) may
+// cover: bit w = warp w.
+__device__ __forceinline__ uint32_t key_mask(const CompositeArgs& a, int warps, int tile, int cols_b, float2 pa,
+                                             float2 pb, float2 pc) {
+  TriGeom g;
+  setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
+  const CullBox box = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
+  const int tx = tile % cols_b, ty = tile / cols_b;
+  // Exclusion needs the fast reject, finite coordinates and a
+  // well-conditioned triangle: exactly the triangles with a finite box.
+  const bool exact_cull = box.x0 > -__int_as_float(0x7f800000);
+  const TriangleBounds3 tb = triangle_bounds(g);
+  uint32_t m = 0;
+  for (int w = 0; w < warps; ++w) {
+    float x0, x1, y0, y1;
+    warp_block_rect(w, a.tile_w, a.tile_h, tx, ty, x0, x1, y0, y1);
+    if (!box_overlaps(box, x0, x1, y0, y1)) continue;
+    if (exact_cull && (edge_excludes(tb.v, g.thr, x0, x1, y0, y1) || edge_excludes(tb.w, g.thr, x0, x1, y0, y1) ||
+                       edge_excludes(tb.u, g.thr, x0, x1, y0, y1)))
+      continue;
+    m |= 1u << w;
+  }
+  return m;
+}
+
 // One mask per sorted key: bit w = warp w of the key's tile may be covered.
 // Keys past num_keys (a device value; all K when NULL) get no mask: no tile
-// range reaches them.
+// range reaches them. Each thread takes two keys and issues their dependent
+// loads (key and triangle, face, projected corners) side by side.
 __global__ void warp_mask_kernel(CompositeArgs a, int64_t K_capacity, const int64_t* __restrict__ num_keys,
                                  uint32_t* __restrict__ masks) {
   const int warps = (a.tile_h * a.tile_w + 31) / 32;
   const int64_t K = num_keys ? min(max(*num_keys, (int64_t)0), K_capacity) : K_capacity;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < K; k += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + k);
-    const int cam = (int)field(key, a.cam_off, a.cam_len);
-    const int tile = (int)field(key, a.tile_off, a.tile_len);
-    uint32_t m = 0;
-    const int cols_b = (a.cameras && cam < a.B) ? (int)__ldg(a.cameras + 6 * cam + 1) : a.cols;
-    const int rows_b = (a.cameras && cam < a.B) ? (int)__ldg(a.cameras + 6 * cam) : a.rows;
-    if (cam < a.B && tile < rows_b * cols_b) {
-      const int32_t f = __ldg(a.tri + k);
-      const float2* xy = reinterpret_cast<const float2*>(a.xy) + (int64_t)cam * a.V;
-      const float2 pa = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f)), pb = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f + 1)),
-                   pc = __ldg(xy + __ldg(a.faces + 3 * (int64_t)f + 2));
-      TriGeom g;
-      setup_geometry(pa.x, pa.y, pb.x, pb.y, pc.x, pc.y, g);
-      const CullBox box = cull_box(g, pa.x, pa.y, pb.x, pb.y, pc.x, pc.y);
-      const int tx = tile % cols_b, ty = tile / cols_b;
-      // Exclusion needs the fast reject, finite coordinates and a
-      // well-conditioned triangle: exactly the triangles with a finite box.
-      const bool exact_cull = box.x0 > -__int_as_float(0x7f800000);
-      const TriangleBounds3 tb = triangle_bounds(g);
-      for (int w = 0; w < warps; ++w) {
-        float x0, x1, y0, y1;
-        warp_block_rect(w, a.tile_w, a.tile_h, tx, ty, x0, x1, y0, y1);
-        if (!box_overlaps(box, x0, x1, y0, y1)) continue;
-        if (exact_cull && (edge_excludes(tb.v, g.thr, x0, x1, y0, y1) || edge_excludes(tb.w, g.thr, x0, x1, y0, y1) ||
-                           edge_excludes(tb.u, g.thr, x0, x1, y0, y1)))
-          continue;
-        m |= 1u << w;
-      }
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k0 < K; k0 += 2 * stride) {
+    const int64_t kk[2] = {k0, k0 + stride};
+    int32_t f[2];
+    int cam[2], tile[2], cols_b[2];
+    bool ok[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const bool in = kk[j] < K;
+      const uint64_t key = in ? __ldg(reinterpret_cast<const unsigned long long*>(a.keys) + kk[j]) : 0ull;
+      f[j] = in ? __ldg(a.tri + kk[j]) : 0;
+      cam[j] = (int)field(key, a.cam_off, a.cam_len);
+      tile[j] = (int)field(key, a.tile_off, a.tile_len);
+      cols_b[j] = (a.cameras && cam[j] < a.B) ? (int)__ldg(a.cameras + 6 * cam[j] + 1) : a.cols;
+      const int rows_b = (a.cameras && cam[j] < a.B) ? (int)__ldg(a.cameras + 6 * cam[j]) : a.rows;
+      ok[j] = in && cam[j] < a.B && tile[j] < rows_b * cols_b[j];
     }
-    masks[k] = m;
+    int32_t ids[2][3];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) ids[j][q] = ok[j] ? __ldg(a.faces + 3 * (int64_t)f[j] + q) : 0;
+    float2 p[2][3];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float2* xy = reinterpret_cast<const float2*>(a.xy) + (int64_t)(ok[j] ? cam[j] : 0) * a.V;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) p[j][q] = ok[j] ? __ldg(xy + ids[j][q]) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+      if (kk[j] < K) masks[kk[j]] = ok[j] ? key_mask(a, warps, tile[j], cols_b[j], p[j][0], p[j][1], p[j][2]) : 0u;
   }
 }
 

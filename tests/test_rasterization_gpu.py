@@ -695,3 +695,24 @@ def test_tile_order_leaves_fused_results_unchanged(cuda_device, name, monkeypatc
     np.testing.assert_array_equal(results[1][0], results[0][0])
     _close_grad(results[1][1], results[0][1], 1e-5)
     _close_grad(results[1][2], results[0][2], 1e-5)
+
+
+def test_fused_loss_with_every_tile_keyless(cuda_device):
+    """Triangles, but all of them far outside the image: every tile is
+    keyless (the backward then takes no work item): the loss is the
+    background's squared error and every gradient is zero."""
+    scene = make_scene()
+    inputs = _fused_inputs(scene, cuda_device)
+    inputs["vertices"] = inputs["vertices"] + torch.tensor([50.0, 0.0, 0.0], device=cuda_device)
+    h, w = scene.image_shape
+    target = _t(np.random.default_rng(11).uniform(0, 1, (1, 3, h, w)).astype(np.float32), cuda_device)
+    loss = tr.render_fused_loss(inputs["extrinsics"], inputs["intrinsics"], (h, w), inputs["vertices"],
+                                inputs["faces"], inputs["shell_face_boundaries"], inputs["signed_distances"],
+                                inputs["spherical_harmonics"], inputs["sh_degree"], inputs["sharpness"],
+                                inputs["background"], target, tile_shape=(8, 8))
+    loss.backward()
+    bg = torch.clamp(inputs["background"], 0, 1)[None, :, None, None].expand(1, 3, h, w)
+    want = float(((bg - target) ** 2).mean())
+    assert abs(float(loss) - want) <= 1e-5 * want
+    assert float(inputs["signed_distances"].grad.abs().max()) == 0.0
+    assert float(inputs["spherical_harmonics"].grad.abs().max()) == 0.0
