@@ -10,7 +10,8 @@ interpolate / composite chain.
 
 Gradients: the oracle's default ("reference") routing must reproduce the
 reference's two hand-written backward kernels (fused intersect-and-composite,
-explicit composite) within 1e-4 of the largest gradient magnitude.
+explicit composite) within 1e-4 of the largest gradient magnitude, and within 1e-4 relative on
+every entry whose magnitude is at least 1e-3 of the largest.
 
 When the reference tree is mounted, the fixtures are also regenerated in
 memory and must equal the committed files (gradients, which the reference
@@ -26,15 +27,23 @@ from oracle import oracle
 from tests import goldens
 
 GRAD_RTOL = 1e-4
+ENTRY_FLOOR = 1e-3
 ATOMIC_OUTPUTS = ("fused/grad_colors", "fused/grad_signed_distances", "fused/grad_sharpness",
                   "explicit/grad_shell_signed_distances", "explicit/grad_shell_colors", "explicit/grad_sharpness")
 
 
-def close_grad(got, want, rtol=GRAD_RTOL, what=""):
+def close_grad(got, want, rtol=GRAD_RTOL, what="", entry_rtol=None):
     got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
     scale = max(float(np.abs(want).max()), 1e-30)
     err = float(np.abs(got - want).max())
     assert err <= rtol * scale, f"{what}: max abs err {err:.3e} > {rtol:g} x {scale:.3e}"
+    # Per entry, relative, wherever the entry is not lost in the sum's
+    # rounding: magnitude at least 1e-3 of the largest.
+    big = np.abs(want) >= ENTRY_FLOOR * scale
+    if big.any():
+        entry_rtol = rtol if entry_rtol is None else entry_rtol
+        rel = float((np.abs(got - want)[big] / np.abs(want[big])).max())
+        assert rel <= entry_rtol, f"{what}: per-entry relative err {rel:.3e} > {entry_rtol:g}"
 
 
 @pytest.fixture(scope="module")
@@ -161,7 +170,9 @@ def test_fixtures_regenerate_from_reference():
         assert sorted(arrays) == sorted(committed), name
         for key, value in arrays.items():
             if key in ATOMIC_OUTPUTS:
-                close_grad(value, committed[key], rtol=1e-5, what=f"{name}:{key}")
+                # Two runs of the reference's atomics differ by up to ~2e-5 of
+                # an entry (summation order), so the per-entry bar is 1e-4.
+                close_grad(value, committed[key], rtol=1e-5, what=f"{name}:{key}", entry_rtol=1e-4)
             else:
                 np.testing.assert_array_equal(np.asarray(value), committed[key], err_msg=f"{name}:{key}")
 
