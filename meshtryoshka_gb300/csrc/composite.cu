@@ -915,16 +915,23 @@ __device__ __forceinline__ const float* target_of(const CompositeArgs& a, const 
   return a.target + px.out_base / 4 * 3 + (int64_t)px.py * px.width + px.px;
 }
 
-// Reserves the work item's batches in the hit-bit store: the number of keys
-// of the tile whose mask has this warp's bit, in batches of kBatch (the walk
-// forms exactly that many batches or stops earlier). Returns the item's first
-// stored batch, or -1 when nothing is stored; records it for the backward.
+// Reserves the work item's batches in the hit-bit store, in batches of
+// kBatch for a bound on the keys the warp walks (the walk forms at most that
+// many batches): with at most two warps to a tile most keys reach both (1.3
+// of 2 on a 256^3 scene at 8x8 tiles), so the tile's key count is the bound
+// and no pass over the masks is needed; with more warps to a tile, the keys
+// whose mask has this warp's bit, counted. Returns the item's first stored
+// batch, or -1 when nothing is stored; records it for the backward.
 __device__ __forceinline__ int64_t reserve_hit_batches(const HitStore& hs, const uint32_t* __restrict__ masks,
-                                                       int64_t start, int64_t end, int wt, int64_t item, int lane) {
-  int keys = 0;
-  for (int64_t k0 = start; k0 < end; k0 += 32) {
-    const int64_t k = k0 + lane;
-    keys += __popc(__ballot_sync(0xffffffffu, k < end && ((__ldg(masks + k) >> wt) & 1u)));
+                                                       int64_t start, int64_t end, int wt, int tile_warps,
+                                                       int64_t item, int lane) {
+  int keys = (int)(end - start);
+  if (tile_warps > 2) {
+    keys = 0;
+    for (int64_t k0 = start; k0 < end; k0 += 32) {
+      const int64_t k = k0 + lane;
+      keys += __popc(__ballot_sync(0xffffffffu, k < end && ((__ldg(masks + k) >> wt) & 1u)));
+    }
   }
   const unsigned long long batches = (unsigned long long)((keys + kBatch - 1) / kBatch);
   unsigned long long base = 0;
@@ -958,7 +965,9 @@ __device__ __forceinline__ float forward_item(const CompositeArgs& a, const uint
   int queued = 0;
   int batch = 0;
   const int64_t hit_base =
-      hs.batches && !keyless ? reserve_hit_batches(hs, masks, start, end, px.wt, item, lane) : -1;
+      hs.batches && !keyless
+          ? reserve_hit_batches(hs, masks, start, end, px.wt, (a.tile_h * a.tile_w + 31) / 32, item, lane)
+          : -1;
   // With 8x4 warp blocks a triangle's span is the part of its accept box on
   // the block (lane 0 holds the block's first pixel); otherwise every pixel.
   const bool blocked = (a.tile_w & 7) == 0 && (a.tile_h & 3) == 0;
@@ -1407,9 +1416,12 @@ __global__ void __launch_bounds__(32 * kWarps, kStaged ? 1 : (24 / kWarps > 0 ? 
     __syncwarp();
   }
   // Items without keys pass no gradient: with a tile order they are all past
-  // `keyed` and never claimed.
-  const int64_t keyed = keyed_items(a, order);
-  for (int64_t u = next_item(counter, lane); u < keyed; u = next_item(counter, lane)) {
+  // `keyed` and never claimed. The bound is read from shared memory at each
+  // claim: held in registers across the loop it made the kernel spill.
+  __shared__ int64_t s_keyed;
+  if (threadIdx.x == 0) s_keyed = keyed_items(a, order);
+  __syncthreads();
+  for (int64_t u = next_item(counter, lane); u < *(volatile int64_t*)&s_keyed; u = next_item(counter, lane)) {
     const int64_t item = ordered_item(a, order, u);
     if (!backward_item<kStaged>(a, masks, gr, ws, pixel_of(a, item), lane, item, hs, st, phase)) return;
   }
