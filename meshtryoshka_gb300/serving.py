@@ -2,10 +2,12 @@
 
 Not part of the reference (whose viewer renders one request at a time under
 a lock, viewer/viewer.py:53). Several scenes stay on the device: their voxel
-grids, signed distances and SH, and the tessellated mesh used by render-only
-requests. Requests arrive over time, each for one scene with its own camera
-and image size, either render-only or render + gradient of an MSE loss
-against a target image.
+grids, signed distances and SH, and their tessellated mesh, kept with its
+autograd graph as a function of the grid parameters (render-only requests
+read it detached; render + gradient requests back-propagate through it
+without tessellating again). Requests arrive over time, each for one scene
+with its own camera and image size, either render-only or render + gradient
+of an MSE loss against a target image.
 
 ``Server.run`` is the continuous-batching loop. At every turn it
 
@@ -19,18 +21,22 @@ against a target image.
   batch from the head of the queue: render-only requests of the head's scene
   (in arrival order, up to ``max_batch``) go into one ``render_cameras`` call
   for cameras of any size; render + gradient requests of the head's scene
-  (up to ``max_gradient_batch``) share one tessellation and each get the
-  gradient of their own loss; a batch starts while another is in flight once
+  (up to ``max_gradient_batch``) render from the resident tessellation and
+  each get the gradient of their own loss; a batch starts while another is in
+  flight once
   ``overlap_backlog`` requests wait;
 * launches the batch on its own CUDA stream, so batches overlap on the GPU.
 
 ``run_plain`` is the per-request form at the same arrival times: one request
-at a time, rendered and completed before the next starts.
+at a time, rendered and completed before the next starts; a render +
+gradient request tessellates the scene's parameters itself, as a training
+step does.
 
 Every request's result is the same alone and in a batch: a camera rendered
 in ``render_cameras`` equals its ``render_fused`` image bit for bit, and a
-gradient request's loss and gradient involve its own camera only (the shared
-tessellation is deterministic) (tests/test_serving_gpu.py).
+gradient request's loss and gradient involve its own camera only (the
+resident tessellation equals a fresh one: it is deterministic)
+(tests/test_serving_gpu.py).
 """
 
 from __future__ import annotations
@@ -60,6 +66,10 @@ class Scene:
     sharpness: Tensor  # []
     background: Tensor  # [3]
     mesh: tuple = ()  # (vertices, faces, shell face boundaries, sdf, sh) for render-only requests
+    # (grid sdf leaf, grid sh leaf, vertices, triangles): the resident
+    # tessellation as a function of the grid parameters, its autograd graph
+    # kept for the render + gradient requests.
+    grad_mesh: tuple = ()
     # Tessellated [0, 1]^3 vertices -> renderer positions (None: the 2 v - 1
     # stand-in of the synthetic scenes; a checkpoint scene uses its
     # contraction's inverse, as the reference's model does).
@@ -105,10 +115,18 @@ class Scene:
         return positions.detach().contiguous(), tri
 
     def refresh_mesh(self) -> None:
-        """Re-tessellates the cached mesh (after the scene's parameters change)."""
-        with torch.no_grad():
-            vertices, tri = self.tessellate(self.grid_sdf, self.grid_sh)
-        self.mesh = (vertices, tri.faces, tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics)
+        """Re-tessellates the resident mesh (after the scene's parameters
+        change). The tessellation is kept as a function of the grid
+        parameters, its autograd graph retained, so that render + gradient
+        requests back-propagate through it without tessellating again;
+        render-only requests read its detached outputs."""
+        sdf = self.grid_sdf.detach().requires_grad_(True)
+        sh = self.grid_sh.detach().requires_grad_(True)
+        with torch.enable_grad():
+            vertices, tri = self.tessellate(sdf, sh)
+        self.grad_mesh = (sdf, sh, vertices, tri)
+        self.mesh = (vertices, tri.faces, tri.face_boundaries, tri.signed_distances.detach(),
+                     tri.spherical_harmonics.detach())
         self.keys_per_pixel = None
 
     def measure_keys_per_pixel(self, shape=(512, 512)) -> float:
@@ -132,8 +150,10 @@ class Scene:
         """Estimated device bytes a request holds while in flight: the
         compositing output and image (28 B per pixel), its tile keys (sort
         buffers and masks, 40 B per key), and for a gradient request also the
-        tessellation with its autograd state, the grid gradients, the target
-        and the hit-bit store (16 B per pixel)."""
+        backward's tessellation-sized buffers (gradients of the vertices,
+        signed distances and SH rows, counted at the size of the tessellation
+        itself, which is resident), the grid gradients, the target and the
+        hit-bit store (16 B per pixel)."""
         kpp = self.measure_keys_per_pixel()
         p = r.pixels
         total = 28 * p + int(40 * kpp * p)
@@ -194,22 +214,20 @@ def render_alone(scene: Scene, r: Request, tile_shape=(16, 16)) -> Completed:
 
 
 def render_gradient_batch(scene: Scene, batch: list[Request], tile_shape=(16, 16)) -> list[Completed]:
-    """Render + gradient requests of one scene: one tessellation of the
-    scene's parameters shared by every request, then per request its render,
-    its MSE and the gradient of that loss alone (the same results as each
-    request alone: the tessellation is deterministic)."""
-    if len(batch) == 1:
-        return [render_alone(scene, batch[0], tile_shape)]
-    sdf = scene.grid_sdf.detach().requires_grad_(True)
-    sh = scene.grid_sh.detach().requires_grad_(True)
-    vertices, tri = scene.tessellate(sdf, sh)
+    """Render + gradient requests of one scene over its resident
+    tessellation (``Scene.grad_mesh``, built once per parameter state): per
+    request its render, its MSE and the gradient of that loss alone, back
+    through the retained tessellation graph (the same results as each
+    request alone, which tessellates again: the tessellation is
+    deterministic)."""
+    sdf, sh, vertices, tri = scene.grad_mesh
     out = []
-    for i, r in enumerate(batch):
+    for r in batch:
         image = tr.render_fused(r.extrinsics[None], r.intrinsics[None], r.shape, vertices, tri.faces,
                                 tri.face_boundaries, tri.signed_distances, tri.spherical_harmonics, scene.sh_degree,
                                 scene.sharpness, scene.background, tile_shape=tile_shape)[0]
         loss = ((image - r.target) ** 2).mean()
-        grad_sdf, grad_sh = torch.autograd.grad(loss, (sdf, sh), retain_graph=i + 1 < len(batch))
+        grad_sdf, grad_sh = torch.autograd.grad(loss, (sdf, sh), retain_graph=True)  # keep the tessellation's graph
         out.append(Completed(r, image.detach(), grad_sdf, grad_sh))
     return out
 
@@ -239,7 +257,7 @@ class Server:
     scenes: list[Scene]
     streams: int = 4  # batches in flight at once
     max_batch: int = 16  # requests per render batch
-    max_gradient_batch: int = 4  # render + gradient requests per batch (one shared tessellation)
+    max_gradient_batch: int = 4  # render + gradient requests per batch
     hbm_budget: int = 8 << 30  # estimated device bytes of the batches in flight (Scene.request_bytes)
     overlap_backlog: int = 1  # queued requests needed to start a batch while another is in flight
     tile_shape: tuple[int, int] = (8, 8)  # the render path's fastest tile here (images do not depend on it)
@@ -276,9 +294,12 @@ class Server:
             return [], 0
         return batch, used
 
-    def run(self, requests: list[Request]) -> list[Completed]:
+    def run(self, requests: list[Request], keep_results: bool = True) -> list[Completed]:
         """Serves ``requests`` (sorted by arrival) in real time; returns them
-        completed, with completion times, in completion order."""
+        completed, with completion times, in completion order. With
+        ``keep_results`` False a request's image and gradients are released
+        once it completes (delivered to a client that needs only its timing),
+        so that a long run does not hold every response on the device."""
         device = self.scenes[0].grid_sdf.device
         pool = [torch.cuda.Stream(device) for _ in range(self.streams)]
         for s in pool:
@@ -299,6 +320,8 @@ class Server:
                     t = time.perf_counter() - start
                     for c in f.results:
                         c.done = t
+                        if not keep_results:
+                            c.image = c.grad_sdf = c.grad_sh = None
                     done.extend(f.results)
                     free.append(f.stream)
                 else:
@@ -328,9 +351,11 @@ class Server:
         return done
 
 
-def run_plain(scenes: list[Scene], requests: list[Request], tile_shape=(16, 16)) -> list[Completed]:
+def run_plain(scenes: list[Scene], requests: list[Request], tile_shape=(16, 16),
+              keep_results: bool = True) -> list[Completed]:
     """The per-request form at the same arrival times: each request rendered
-    and completed before the next one starts."""
+    and completed before the next one starts (``keep_results`` as in
+    ``Server.run``)."""
     done = []
     start = time.perf_counter()
     for r in requests:
@@ -340,6 +365,8 @@ def run_plain(scenes: list[Scene], requests: list[Request], tile_shape=(16, 16))
         c = render_alone(scenes[r.scene], r, tile_shape)
         torch.cuda.synchronize()
         c.done = time.perf_counter() - start
+        if not keep_results:
+            c.image = c.grad_sdf = c.grad_sh = None
         done.append(c)
     return done
 
