@@ -76,3 +76,24 @@ def test_ragged_camera_table():
     assert table == [[5, 7, 75, 101, 0, 0], [8, 4, 128, 64, 35, 4 * 75 * 101],
                      [3, 13, 40, 200, 67, 4 * (75 * 101 + 128 * 64)]]
     assert tr._camera_table(tr.TileGrid((16, 16), (64, 64), 2, 3), "cpu") is None
+
+
+def test_compositing_buffer_sizes_without_gpu():
+    """The compositing scratch sizes (host-only calls): the hit-bit store is a
+    header (the bump counter and one int32 first batch per work item, rounded
+    to 128 bytes) plus a 128-byte line per batch; the tile order holds 512
+    int32 bucket counts and cursors plus one index per tile; the staging
+    scratch a 128-byte header plus a 32-byte record per (camera, vertex)."""
+    from meshtryoshka_gb300 import _native
+
+    lib = _native.library()
+    for tiles, th, tw, batches in ((40_000, 8, 8, 95_000), (1, 16, 16, 1), (10_001, 4, 8, 3)):
+        items = tiles * ((th * tw + 31) // 32)
+        header = (8 + 4 * items + 127) // 128 * 128
+        assert lib.mt_composite_hit_bits_bytes(tiles, th, tw, batches) == header + 128 * batches
+    assert lib.mt_composite_hit_bits_bytes(0, 8, 8, 10) == 0
+    assert lib.mt_composite_hit_bits_bytes(10, 8, 8, 0) == 0
+    assert lib.mt_composite_tile_order_bytes(40_000) == (512 + 40_000) * 4
+    assert lib.mt_composite_tile_order_bytes(0) == 512 * 4
+    assert lib.mt_composite_staging_bytes(4, 1000) == 128 + 32 * 4 * 1000
+    assert lib.mt_composite_staging_bytes(0, 1000) == 0
