@@ -1,4 +1,4 @@
-"""CPU checks of the exactness arguments behind two compositing and key
+"""CPU checks of the exactness arguments behind the compositing and key
 speed-ups, with every float32 operation emulated one by one in numpy (IEEE
 single precision, round to nearest, no fused multiply-add):
 
@@ -12,7 +12,9 @@ single precision, round to nearest, no fused multiply-add):
   by 2^-k for every float32, and the shifted integer division agrees with
   C's truncating one under max(., 0);
 * the contribution list of the vertex-interpolation backward built per grid
-  entry is the per-grid-vertex enumeration's list, written inside its bounds.
+  entry is the per-grid-vertex enumeration's list, written inside its bounds;
+* the compositing forward's hit-bit reservations cover the batches each warp
+  walks and together fit the bound the store is sized by.
 """
 
 from __future__ import annotations
@@ -361,3 +363,30 @@ def test_contribution_list_per_entry_equals_per_vertex():
         for capacity in (total, total // 2):
             per_vertex, per_entry = _lists(topology, cross, capacity)
             assert per_entry == per_vertex and len(per_vertex) > 1000
+
+
+def test_hit_bit_reservations_fit_the_store_bound():
+    """The compositing forward reserves, per (tile, warp) work item, a bound
+    on the batches the warp walks: ceil(tile keys / 32) when a tile has at
+    most two warps, else ceil(keys with the warp's mask bit / 32). The sum
+    over all items never exceeds the bound the store is sized by
+    (K * warps / 32 + items: triangle_rasterization._hit_bits and
+    mt_composite_hit_bits_bytes), and each reservation covers the batches
+    the walk forms (one per 32 keys with the warp's bit)."""
+    rng = np.random.default_rng(7)
+    for warps in (1, 2, 4, 8):
+        for _ in range(20):
+            tiles = int(rng.integers(1, 400))
+            counts = rng.choice([0, 0, 0, 1, 5, 31, 32, 33, 200, 1000], size=tiles)
+            k = int(counts.sum())
+            items = tiles * warps
+            reserved = 0
+            for n in counts:
+                masks = rng.integers(0, 1 << warps, size=int(n)) | (1 << int(rng.integers(0, warps)))
+                for wt in range(warps):
+                    own = int(((masks >> wt) & 1).sum())
+                    walked = -(-own // 32)
+                    r = -(-int(n) // 32) if warps <= 2 else walked
+                    assert r >= walked
+                    reserved += r
+            assert reserved <= k * warps // 32 + items
